@@ -1,0 +1,181 @@
+/*
+ * turbins_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * TURBINS fractional-step hot path.
+ *
+ * One context (turb_ctx) is the device-side counterpart of the reference's
+ * GVG_bag (Include/DataTypes.h:632-645): the MAC grid (MAC_grid, :573-628),
+ * the velocity, pressure and concentration vectors, and one CUDA stream.  All
+ * fields stay resident in HBM across calls; host memory is touched only by
+ * turb_field_upload / turb_field_download, which take the reference's PETSc DA
+ * layout a[(k*NY + j)*NX + i], NX = nx+1, NY = ny+1, NZ = nz+1, FP64.
+ *
+ * Every entry point returns a turb_status (0 = success).  Entry points named
+ * turb_<RefName> replace the reference routine <RefName> with the same
+ * argument meaning; the reference's struct arguments (Velocity*, Pressure*,
+ * Concentration*, MAC_grid*, Parameters*) are folded into the context.
+ * Nothing here allocates host memory that the caller must free, and no call
+ * falls back to the CPU: without a usable GB300 every call returns
+ * TURB_ERR_CUDA.
+ */
+#ifndef TURBINS_GB300_H
+#define TURBINS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TURB_OK = 0,
+    TURB_ERR_ARG = 1,            /* bad argument (size, id, NULL)           */
+    TURB_ERR_CUDA = 2,           /* CUDA runtime error / no device          */
+    TURB_ERR_NOT_CONVERGED = 3,  /* solver reached max_iter (cf. Solver.c:326-348) */
+    TURB_ERR_NAN = 4,            /* non-finite residual                     */
+    TURB_ERR_ALLOC = 5           /* device allocation failed                */
+} turb_status;
+
+/* node status codes, Include/definitions.h:93-99 */
+#define TURB_SOLID 2
+#define TURB_FLUID 3
+#define TURB_IMMERSED 5
+#define TURB_BOUNDARY 7
+#define TURB_BUFFER_SOLID 11
+
+#define TURB_SALINITY 1
+#define TURB_PARTICLE 2
+#define TURB_MAXCONC 4
+
+/* Parameters (Include/DataTypes.h:177-248), after the Input.c:405-509 rules */
+typedef struct {
+    int nx, ny, nz;              /* physical cells                            */
+    int eno_order;               /* 1..3                                       */
+    double re;                   /* Reynolds number                            */
+    int nconc;                   /* 1..TURB_MAXCONC                             */
+    double pe[TURB_MAXCONC];     /* Peclet number                               */
+    double vs0[TURB_MAXCONC];    /* settling speed after the sign flip           */
+    double alpha[TURB_MAXCONC];  /* buoyancy weights after the rescale           */
+    int ctype[TURB_MAXCONC];     /* TURB_SALINITY / TURB_PARTICLE               */
+    int sedimentation;           /* Robin top ghost for particle fractions       */
+    int wall_noslip[6];          /* velocity walls x-,x+,y-,y+,z-,z+: 1 no-slip */
+    int buoyancy;                /* subtract c at v nodes                        */
+    double vel_rtol;             /* Helmholtz relative residual (resmax)        */
+    int vel_maxit;
+    double p_rtol;               /* Poisson relative residual                    */
+    int p_maxit;
+} turb_params;
+
+/* Ghost-cell immersed-boundary stencils of one quantity (ImmersedNode,
+ * Include/DataTypes.h:520-546), linear DA indices. */
+typedef struct {
+    int n;
+    const int32_t *im;           /* [n]   immersed node                         */
+    const int32_t *nf;           /* [n]   1 or 8 fluid nodes                    */
+    const int32_t *fidx;         /* [n*8] fluid nodes                           */
+    const double *fcoef;         /* [n*8] fluid_coef                            */
+    const double *bcoef;         /* [n]   boundary_coef                         */
+} turb_ib_desc;
+
+typedef struct {
+    int nx, ny, nz;
+    const double *xc, *yc, *zc;  /* cell centres, nx+1 / ny+1 / nz+1 entries   */
+    const double *xu, *yv, *zw;  /* faces, nx+1 / ny+1 / nz+1 entries           */
+    const uint8_t *status[4];    /* u, v, w, c node status, DA layout           */
+    turb_ib_desc ib[4];          /* u, v, w, c                                  */
+} turb_grid_desc;
+
+typedef struct turb_ctx turb_ctx;
+
+/* Field identifiers for upload/download (the reference Vec each mirrors). */
+enum {
+    TURB_F_U = 0, TURB_F_V, TURB_F_W,               /* Velocity.G_data          */
+    TURB_F_PHI, TURB_F_DPX, TURB_F_DPY, TURB_F_DPZ, /* Pressure.G_data, G_dp_d* */
+    TURB_F_PB, TURB_F_DIV,                          /* Pressure.G_b, G_divergence */
+    TURB_F_UBC, TURB_F_VBC, TURB_F_WBC,             /* Velocity.G_data_bc       */
+    TURB_F_CONV_U, TURB_F_CONV_V, TURB_F_CONV_W,    /* Velocity.G_conv          */
+    TURB_F_B_U, TURB_F_B_V, TURB_F_B_W,             /* Velocity.G_b             */
+    TURB_F_CTOT,                                    /* Concentration.G_c_total  */
+    TURB_F_SCRATCH0, TURB_F_SCRATCH1,               /* MAC_grid.G_dummy1/2      */
+    TURB_F_C0 = 32,                                 /* + ic: Concentration.G_data */
+    TURB_F_CCONV0 = 40,                             /* + ic: Concentration.G_conv */
+    TURB_F_CB0 = 48,                                /* + ic: Concentration.G_b   */
+    TURB_F_VP0 = 56                                 /* + ic: G_v_particle        */
+};
+
+typedef struct {
+    int vel_iters[3][2];
+    int conc_iters[TURB_MAXCONC][2];
+    int p_iters[2];
+    double p_relres[2];
+    double div_max[2];
+    int kernel_launches;         /* launches of this library's kernels         */
+} turb_step_stats;
+
+/* Pressure solver modes for turb_set_pressure_mode */
+#define TURB_PMODE_FP64 0        /* plain FP64 MG-preconditioned CG             */
+#define TURB_PMODE_MIXED 1       /* FP32 V-cycles inside FP64 flexible CG       */
+
+/* ---- context -------------------------------------------------------------
+ * Replaces Grid_create + Velocity_create + Pressure_create + Conc_create +
+ * *_setup_lsys_accounting_geometry (Grid.c:21, Velocity.c:19, Pressure.c:15,
+ * Conc.c:22, Velocity.c:329, Pressure.c:129, Conc.c:358): allocates every
+ * field (zeroed) and the solver hierarchies on the current CUDA device. */
+int turb_create(const turb_grid_desc *grid, const turb_params *params, turb_ctx **out);
+int turb_destroy(turb_ctx *ctx);
+int turb_field_upload(turb_ctx *ctx, int field, const double *host_da);
+int turb_field_download(turb_ctx *ctx, int field, double *host_da);
+int turb_set_pressure_mode(turb_ctx *ctx, int mode);
+int turb_synchronize(turb_ctx *ctx);
+const char *turb_status_string(int status);
+
+/* ---- hot-path routines (same-named reference routine in the comment) ----- */
+/* ENO_compute_convective_terms, ENO.c:103-245: one host line, run on the GPU */
+int turb_ENO_compute_convective_terms(int order, int n, const double *D0,
+                                      const double *position,
+                                      const double *velocity, double *VdQdX);
+/* Velocity_cell_center, Velocity.c:1476-1602 */
+int turb_Velocity_cell_center(turb_ctx *ctx);
+/* Velocity_transpose_velocities, Velocity.c:3341-3663; results in SCRATCH0/1 */
+int turb_Velocity_transpose_velocities(turb_ctx *ctx, char which);
+/* Conc_compute_total_concentration, Conc.c:1291-1314 */
+int turb_Conc_compute_total_concentration(turb_ctx *ctx);
+/* Conc_set_particle_v_velocity, Conc.c:734-761 */
+int turb_Conc_set_particle_v_velocity(turb_ctx *ctx, int ic);
+/* the convection driver (absent from the reference) around
+ * ENO_compute_convective_terms and Velocity_{u,v,w}_ENO_ghost_cells
+ * (Velocity.c:2124-2801): fills TURB_F_CONV_{U,V,W} */
+int turb_Velocity_convective_terms(turb_ctx *ctx, char which);
+/* the same around Conc_ENO_ghost_cells (Conc.c:1021-1220): TURB_F_CCONV0+ic */
+int turb_Conc_convective_terms(turb_ctx *ctx, int ic);
+/* Velocity_{u,v,w}_set_RHS, Velocity.c:1607-2043 (with buoyancy on v) */
+int turb_Velocity_set_RHS(turb_ctx *ctx, char which, double dt);
+/* Conc_set_RHS, Conc.c:864-992 */
+int turb_Conc_set_RHS(turb_ctx *ctx, int ic, double dt);
+/* Velocity_modify_diagonal + Velocity_solve, Velocity.c:374-443, 306-324 */
+int turb_Velocity_solve(turb_ctx *ctx, char which, double dt, int *iters);
+/* Conc_modify_diagonal + Conc_solve, Conc.c:293-354, 840-859 */
+int turb_Conc_solve(turb_ctx *ctx, int ic, double dt, int *iters);
+/* Pressure_set_RHS, Pressure.c:171-276 */
+int turb_Pressure_set_RHS(turb_ctx *ctx, double dt);
+/* Pressure_solve, Pressure.c:443-458 (GMRES+BoomerAMG replaced by MG-CG) */
+int turb_Pressure_solve(turb_ctx *ctx, int *iters, double *relres);
+/* Pressure_project_velocity, Pressure.c:280-439 */
+int turb_Pressure_project_velocity(turb_ctx *ctx, double dt);
+/* Pressure_compute_velocity_divergence, Pressure.c:462-586 */
+int turb_Pressure_compute_velocity_divergence(turb_ctx *ctx, double *div_max);
+/* Velocity_store_old_data / Conc_store_old_data, Velocity.c:297, Conc.c:997 */
+int turb_store_old_data(turb_ctx *ctx);
+/* Velocity_rk_average / Conc_rk_average, Velocity.c:2047, Conc.c:1007 */
+int turb_rk_average(turb_ctx *ctx, double old_frac, double new_frac);
+/* one TVD-RK2 step of the restated driver (the absent main loop) */
+int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
+
+/* operator hooks used by the parity tests: y = A x on device fields */
+int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);
+int turb_pressure_apply(turb_ctx *ctx, int field_x, int field_y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

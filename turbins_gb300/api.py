@@ -1,0 +1,280 @@
+"""Python host binding of libturbgpu.so (the C ABI of include/turbins_gb300.h).
+
+The host side mirrors the reference's routine interface: one ``Context``
+holds what the reference spreads over GVG_bag, MAC_grid, Velocity, Pressure
+and Concentration; its methods carry the reference routine names
+(``Velocity_cell_center``, ``Pressure_solve`` ...) and raise ``TurbError``
+where the reference would stop (PETScErrAct) or warn (Solver_is_converged).
+There is no CPU fallback: without the CUDA library or a GPU every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import workload as W
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "lib", "libturbgpu.so")
+MAXC = 4
+
+F_U, F_V, F_W, F_PHI, F_DPX, F_DPY, F_DPZ, F_PB, F_DIV = range(9)
+F_UBC, F_VBC, F_WBC, F_CONV_U, F_CONV_V, F_CONV_W, F_B_U, F_B_V, F_B_W, F_CTOT, F_SCRATCH0, F_SCRATCH1 = range(9, 21)
+F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
+PMODE_FP64, PMODE_MIXED = 0, 1
+
+STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
+          5: "device allocation failed"}
+
+
+class TurbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (status %d)" % (msg, code))
+        self.code = code
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class _Params(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("eno_order", C.c_int),
+                ("re", C.c_double), ("nconc", C.c_int), ("pe", C.c_double * MAXC),
+                ("vs0", C.c_double * MAXC), ("alpha", C.c_double * MAXC), ("ctype", C.c_int * MAXC),
+                ("sedimentation", C.c_int), ("wall_noslip", C.c_int * 6), ("buoyancy", C.c_int),
+                ("vel_rtol", C.c_double), ("vel_maxit", C.c_int), ("p_rtol", C.c_double),
+                ("p_maxit", C.c_int)]
+
+
+class _IbDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("im", _ip), ("nf", _ip), ("fidx", _ip), ("fcoef", _dp), ("bcoef", _dp)]
+
+
+class _GridDesc(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)] + \
+        [(n, _dp) for n in ("xc", "yc", "zc", "xu", "yv", "zw")] + \
+        [("status", _u8p * 4), ("ib", _IbDesc * 4)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("vel_iters", (C.c_int * 2) * 3), ("conc_iters", (C.c_int * 2) * MAXC),
+                ("p_iters", C.c_int * 2), ("p_relres", C.c_double * 2), ("div_max", C.c_double * 2),
+                ("kernel_launches", C.c_int)]
+
+    def as_dict(self, nconc=1):
+        return dict(vel_iters=[list(self.vel_iters[i]) for i in range(3)],
+                    conc_iters=[list(self.conc_iters[i]) for i in range(nconc)],
+                    p_iters=list(self.p_iters), p_relres=list(self.p_relres),
+                    div_max=list(self.div_max), kernel_launches=self.kernel_launches)
+
+
+_lib = None
+
+
+def load_library():
+    """Load the in-tree CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise TurbError(2, "libturbgpu.so not built (run turbins_gb300.build.build())")
+        L = C.CDLL(LIBPATH)
+        L.turb_status_string.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc, what):
+    if rc != 0:
+        msg = load_library().turb_status_string(rc).decode()
+        raise TurbError(rc, "%s: %s" % (what, msg))
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def params_struct(p: W.Params):
+    cp = _Params()
+    cp.nx, cp.ny, cp.nz = p.nx, p.ny, p.nz
+    cp.eno_order = p.eno_order
+    cp.re = p.re
+    cp.nconc = p.nconc
+    for i in range(p.nconc):
+        cp.pe[i] = p.pe[i]
+        cp.vs0[i] = p.vs0[i]
+        cp.alpha[i] = p.alpha[i]
+        cp.ctype[i] = p.ctype[i]
+    cp.sedimentation = p.sedimentation
+    for i in range(6):
+        cp.wall_noslip[i] = p.wall_noslip[i]
+    cp.buoyancy = p.buoyancy
+    cp.vel_rtol, cp.vel_maxit = p.vel_rtol, p.vel_maxit
+    cp.p_rtol, cp.p_maxit = p.p_rtol, p.p_maxit
+    return cp
+
+
+class Context:
+    """Device-resident state of one case (turb_ctx)."""
+
+    def __init__(self, grid: W.Grid, params: W.Params):
+        L = load_library()
+        self.lib = L
+        self.grid = grid
+        self.params = params
+        keep = []
+        gd = _GridDesc()
+        gd.nx, gd.ny, gd.nz = grid.nx, grid.ny, grid.nz
+        for n in ("xc", "yc", "zc", "xu", "yv", "zw"):
+            a = np.ascontiguousarray(getattr(grid, n), dtype=np.float64)
+            keep.append(a)
+            setattr(gd, n, _ptr(a))
+        for qi, q in enumerate("uvwc"):
+            st = np.ascontiguousarray(grid.status[q], dtype=np.uint8)
+            keep.append(st)
+            gd.status[qi] = _ptr(st, _u8p)
+            ib = grid.ib.get(q)
+            if ib is not None and ib["n"] > 0:
+                arrs = [np.ascontiguousarray(ib["im"], dtype=np.int32), np.ascontiguousarray(ib["nf"], dtype=np.int32),
+                        np.ascontiguousarray(ib["fidx"], dtype=np.int32),
+                        np.ascontiguousarray(ib["fcoef"], dtype=np.float64),
+                        np.ascontiguousarray(ib["bcoef"], dtype=np.float64)]
+                keep.extend(arrs)
+                gd.ib[qi].n = int(ib["n"])
+                gd.ib[qi].im, gd.ib[qi].nf, gd.ib[qi].fidx = _ptr(arrs[0], _ip), _ptr(arrs[1], _ip), _ptr(arrs[2], _ip)
+                gd.ib[qi].fcoef, gd.ib[qi].bcoef = _ptr(arrs[3]), _ptr(arrs[4])
+            else:
+                gd.ib[qi].n = 0
+        self._cp = params_struct(params)
+        self.ctx = C.c_void_p()
+        _check(L.turb_create(C.byref(gd), C.byref(self._cp), C.byref(self.ctx)), "turb_create")
+        del keep
+
+    def close(self):
+        if self.ctx:
+            self.lib.turb_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- transfer -------------------------------------------------------------
+    def upload(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.size == self.grid.npts
+        _check(self.lib.turb_field_upload(self.ctx, field, _ptr(a)), "upload")
+
+    def download(self, field):
+        a = np.empty(self.grid.shape)
+        _check(self.lib.turb_field_download(self.ctx, field, _ptr(a)), "download")
+        return a
+
+    def load_state(self, s):
+        for k, f in (("u", F_U), ("v", F_V), ("w", F_W), ("phi", F_PHI), ("dpx", F_DPX), ("dpy", F_DPY),
+                     ("dpz", F_DPZ)):
+            if k in s:
+                self.upload(f, s[k])
+        for i in range(self.params.nconc):
+            self.upload(F_C0 + i, s["c%d" % i])
+
+    def state(self):
+        out = {k: self.download(f) for k, f in (("u", F_U), ("v", F_V), ("w", F_W), ("phi", F_PHI), ("dpx", F_DPX),
+                                                 ("dpy", F_DPY), ("dpz", F_DPZ), ("pb", F_PB))}
+        for i in range(self.params.nconc):
+            out["c%d" % i] = self.download(F_C0 + i)
+        return out
+
+    def set_pressure_mode(self, mode):
+        _check(self.lib.turb_set_pressure_mode(self.ctx, mode), "set_pressure_mode")
+
+    def synchronize(self):
+        _check(self.lib.turb_synchronize(self.ctx), "synchronize")
+
+    # -- reference routines -----------------------------------------------------
+    def Velocity_cell_center(self):
+        _check(self.lib.turb_Velocity_cell_center(self.ctx), "Velocity_cell_center")
+
+    def Velocity_transpose_velocities(self, which):
+        _check(self.lib.turb_Velocity_transpose_velocities(self.ctx, C.c_char(which.encode())),
+               "Velocity_transpose_velocities")
+
+    def Conc_compute_total_concentration(self):
+        _check(self.lib.turb_Conc_compute_total_concentration(self.ctx), "Conc_compute_total_concentration")
+
+    def Conc_set_particle_v_velocity(self, ic):
+        _check(self.lib.turb_Conc_set_particle_v_velocity(self.ctx, ic), "Conc_set_particle_v_velocity")
+
+    def Velocity_convective_terms(self, which):
+        _check(self.lib.turb_Velocity_convective_terms(self.ctx, C.c_char(which.encode())), "convective_terms")
+
+    def Conc_convective_terms(self, ic):
+        _check(self.lib.turb_Conc_convective_terms(self.ctx, ic), "Conc_convective_terms")
+
+    def Velocity_set_RHS(self, which, dt):
+        _check(self.lib.turb_Velocity_set_RHS(self.ctx, C.c_char(which.encode()), C.c_double(dt)), "set_RHS")
+
+    def Conc_set_RHS(self, ic, dt):
+        _check(self.lib.turb_Conc_set_RHS(self.ctx, ic, C.c_double(dt)), "Conc_set_RHS")
+
+    def Velocity_solve(self, which, dt):
+        it = C.c_int()
+        _check(self.lib.turb_Velocity_solve(self.ctx, C.c_char(which.encode()), C.c_double(dt), C.byref(it)),
+               "Velocity_solve")
+        return it.value
+
+    def Conc_solve(self, ic, dt):
+        it = C.c_int()
+        _check(self.lib.turb_Conc_solve(self.ctx, ic, C.c_double(dt), C.byref(it)), "Conc_solve")
+        return it.value
+
+    def Pressure_set_RHS(self, dt):
+        _check(self.lib.turb_Pressure_set_RHS(self.ctx, C.c_double(dt)), "Pressure_set_RHS")
+
+    def Pressure_solve(self):
+        it = C.c_int()
+        rr = C.c_double()
+        _check(self.lib.turb_Pressure_solve(self.ctx, C.byref(it), C.byref(rr)), "Pressure_solve")
+        return it.value, rr.value
+
+    def Pressure_project_velocity(self, dt):
+        _check(self.lib.turb_Pressure_project_velocity(self.ctx, C.c_double(dt)), "Pressure_project_velocity")
+
+    def Pressure_compute_velocity_divergence(self):
+        d = C.c_double()
+        _check(self.lib.turb_Pressure_compute_velocity_divergence(self.ctx, C.byref(d)), "divergence")
+        return d.value
+
+    def store_old_data(self):
+        _check(self.lib.turb_store_old_data(self.ctx), "store_old_data")
+
+    def rk_average(self, old_frac=0.5, new_frac=0.5):
+        _check(self.lib.turb_rk_average(self.ctx, C.c_double(old_frac), C.c_double(new_frac)), "rk_average")
+
+    def helmholtz_apply(self, which, ic, dt, fx, fy):
+        _check(self.lib.turb_helmholtz_apply(self.ctx, C.c_char(which.encode()), ic, C.c_double(dt), fx, fy),
+               "helmholtz_apply")
+
+    def pressure_apply(self, fx, fy):
+        _check(self.lib.turb_pressure_apply(self.ctx, fx, fy), "pressure_apply")
+
+    def step(self, dt):
+        st = StepStats()
+        _check(self.lib.turb_step(self.ctx, C.c_double(dt), C.byref(st)), "turb_step")
+        return st.as_dict(self.params.nconc)
+
+
+def ENO_compute_convective_terms(order, D0, P, V):
+    """ENO.c:103-245 on one host line, computed on the GPU."""
+    L = load_library()
+    D0 = np.ascontiguousarray(D0, dtype=np.float64)
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    out = np.zeros(len(D0))
+    _check(L.turb_ENO_compute_convective_terms(order, len(D0), _ptr(D0), _ptr(P), _ptr(V), _ptr(out)),
+           "ENO_compute_convective_terms")
+    return out

@@ -1,0 +1,206 @@
+// k_mg.cu -- pressure Poisson solve: geometric-multigrid-preconditioned CG.
+//
+// Replaces GMRES(20) + hypre BoomerAMG (Solver.c:90-265) for the system of
+// Pressure_form_LHS_matrix (Pressure.c:691-936).  CG runs in FP64 on the
+// volume-weighted form S = W A (W = cell volume), which is symmetric; the
+// corner pin of Pressure.c:864-868 is kept as an extra diagonal term.  The
+// preconditioner is one V-cycle: red-black Gauss-Seidel smoothing (2 pre, 2
+// post, reversed colour order on the way up so the cycle is symmetric),
+// restriction by summing children, piecewise-constant prolongation (its
+// transpose), rediscretised coarse operators built from the coarse cell
+// widths (so coarsening follows the y stretching), semi-coarsening of the
+// directions whose mean spacing is more than twice the finest, and a dense
+// inverse on the coarsest (<= 64 cells) level.  The V-cycle is templated on
+// its precision: FP64 (plain method) or FP32 inside the FP64 CG (mixed).
+#include "turb_internal.cuh"
+#include "turb_kernels.cuh"
+#include "turb_mg.cuh"
+
+namespace {
+
+template <typename T>
+struct LevelT {
+    int nx, ny, nz;
+    const T *dx, *dy, *dz, *rfx, *rfy, *rfz;
+    T pin;
+};
+
+template <typename T>
+__device__ __forceinline__ LevelT<T> lev_of(const MgDevLevel &L);
+
+template <>
+__device__ __forceinline__ LevelT<double> lev_of<double>(const MgDevLevel &L)
+{
+    LevelT<double> o{L.nx, L.ny, L.nz, L.dxd, L.dyd, L.dzd, L.rfxd, L.rfyd, L.rfzd, L.pin};
+    return o;
+}
+template <>
+__device__ __forceinline__ LevelT<float> lev_of<float>(const MgDevLevel &L)
+{
+    LevelT<float> o{L.nx, L.ny, L.nz, L.dxf, L.dyf, L.dzf, L.rfxf, L.rfyf, L.rfzf, (float)L.pin};
+    return o;
+}
+
+// S x - evaluated as  diag*x_p - sum f*x_nb ; returns (offsum, diag)
+template <typename T>
+__device__ __forceinline__ void s_row(const LevelT<T> &L, const T *__restrict__ x, int i, int j, int k,
+                                      T &off, T &dg)
+{
+    long long nx = L.nx, nxy = (long long)L.nx * L.ny;
+    long long c = ((long long)k * L.ny + j) * nx + i;
+    T dyz = L.dy[j] * L.dz[k], dxz = L.dx[i] * L.dz[k], dxy = L.dx[i] * L.dy[j];
+    T o = 0, d = 0, f;
+    if (i > 0) { f = dyz * L.rfx[i]; d += f; o += f * x[c - 1]; }
+    if (i < L.nx - 1) { f = dyz * L.rfx[i + 1]; d += f; o += f * x[c + 1]; }
+    if (j > 0) { f = dxz * L.rfy[j]; d += f; o += f * x[c - nx]; }
+    if (j < L.ny - 1) { f = dxz * L.rfy[j + 1]; d += f; o += f * x[c + nx]; }
+    if (k > 0) { f = dxy * L.rfz[k]; d += f; o += f * x[c - nxy]; }
+    if (k < L.nz - 1) { f = dxy * L.rfz[k + 1]; d += f; o += f * x[c + nxy]; }
+    if (i == L.nx - 1 && j == L.ny - 1 && k == L.nz - 1) d += L.pin;
+    off = o;
+    dg = d;
+}
+
+template <typename T>
+__global__ void k_invdiag(MgDevLevel Ld, T *__restrict__ invd)
+{
+    LevelT<T> L = lev_of<T>(Ld);
+    long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(c % L.nx), j = (int)((c / L.nx) % L.ny), k = (int)(c / ((long long)L.nx * L.ny));
+        T dyz = L.dy[j] * L.dz[k], dxz = L.dx[i] * L.dz[k], dxy = L.dx[i] * L.dy[j], d = 0;
+        if (i > 0) d += dyz * L.rfx[i];
+        if (i < L.nx - 1) d += dyz * L.rfx[i + 1];
+        if (j > 0) d += dxz * L.rfy[j];
+        if (j < L.ny - 1) d += dxz * L.rfy[j + 1];
+        if (k > 0) d += dxy * L.rfz[k];
+        if (k < L.nz - 1) d += dxy * L.rfz[k + 1];
+        if (i == L.nx - 1 && j == L.ny - 1 && k == L.nz - 1) d += L.pin;
+        invd[c] = T(1) / d;
+    }
+}
+
+// red-black Gauss-Seidel half sweep; zero_init: x taken as 0 on entry (first
+// sweep of a cycle, colour 0 only)
+template <typename T>
+__global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restrict__ b, const T *__restrict__ invd,
+                       T *__restrict__ x)
+{
+    LevelT<T> L = lev_of<T>(Ld);
+    int nh = (L.nx + 1) >> 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long nrow = (long long)L.ny * L.nz;
+    if (t >= nrow * nh) return;
+    int i2 = (int)(t % nh);
+    long long row = t / nh;
+    int j = (int)(row % L.ny), k = (int)(row / L.ny);
+    int i = 2 * i2 + ((j + k + color) & 1);
+    if (i >= L.nx) return;
+    long long c = ((long long)k * L.ny + j) * L.nx + i;
+    if (zero_init) { x[c] = b[c] * invd[c]; return; }
+    T off, dg;
+    s_row<T>(L, x, i, j, k, off, dg);
+    x[c] = (b[c] + off) * invd[c];
+}
+
+template <typename T>
+__global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r)
+{
+    LevelT<T> L = lev_of<T>(Ld);
+    long long n = (long long)L.nx * L.ny * L.nz;
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    int i = (int)(c % L.nx), j = (int)((c / L.nx) % L.ny), k = (int)(c / ((long long)L.nx * L.ny));
+    T off, dg;
+    s_row<T>(L, x, i, j, k, off, dg);
+    r[c] = b[c] - (dg * x[c] - off);
+}
+
+template <typename T>
+__global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ rf, T *__restrict__ bc)
+{
+    long long n = (long long)Lc.nx * Lc.ny * Lc.nz;
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    int I = (int)(c % Lc.nx), J = (int)((c / Lc.nx) % Lc.ny), K = (int)(c / ((long long)Lc.nx * Lc.ny));
+    int ni = Lf.cx ? 2 : 1, nj = Lf.cy ? 2 : 1, nk = Lf.cz ? 2 : 1;
+    int i0 = Lf.cx ? 2 * I : I, j0 = Lf.cy ? 2 * J : J, k0 = Lf.cz ? 2 * K : K;
+    T s = 0;
+    for (int kk = 0; kk < nk; kk++)
+        for (int jj = 0; jj < nj; jj++)
+            for (int ii = 0; ii < ni; ii++)
+                s += rf[((long long)(k0 + kk) * Lf.ny + (j0 + jj)) * Lf.nx + (i0 + ii)];
+    bc[c] = s;
+}
+
+template <typename T>
+__global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc, T *__restrict__ xf)
+{
+    long long n = (long long)Lf.nx * Lf.ny * Lf.nz;
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    int i = (int)(c % Lf.nx), j = (int)((c / Lf.nx) % Lf.ny), k = (int)(c / ((long long)Lf.nx * Lf.ny));
+    int I = Lf.cx ? i >> 1 : i, J = Lf.cy ? j >> 1 : j, K = Lf.cz ? k >> 1 : k;
+    xf[c] += xc[((long long)K * Lc.ny + J) * Lc.nx + I];
+}
+
+template <typename T>
+__global__ void k_coarse(int n, const double *__restrict__ ainv, const T *__restrict__ b, T *__restrict__ x)
+{
+    int r = threadIdx.x;
+    if (r >= n) return;
+    double s = 0.0;
+    for (int c = 0; c < n; c++) s += ainv[r * n + c] * (double)b[c];
+    x[r] = (T)s;
+}
+
+inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace
+
+template <typename T>
+void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd)
+{
+    k_invdiag<T><<<1024, 256, 0, s>>>(L, invd);
+}
+
+// One V-cycle from level l: input b[l], output x[l] (x starts at zero).
+template <typename T>
+void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
+{
+    const MgDevLevel &L = H.lev[l];
+    long long n = (long long)L.nx * L.ny * L.nz;
+    if (l == H.nl - 1) {
+        k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
+        return;
+    }
+    long long nrb = (long long)L.ny * L.nz * ((L.nx + 1) >> 1);
+    unsigned g = nblk(nrb, 256);
+    for (int it = 0; it < npre; it++) {
+        // the first colour-0 half sweep takes x = 0 (it reads no neighbours);
+        // every colour-1 point is then rewritten from colour-0 values only
+        k_rbgs<T><<<g, 256, 0, s>>>(L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
+        k_rbgs<T><<<g, 256, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+    }
+    k_resid<T><<<nblk(n, 256), 256, 0, s>>>(L, H.b[l], H.x[l], H.r[l]);
+    const MgDevLevel &C = H.lev[l + 1];
+    long long nc = (long long)C.nx * C.ny * C.nz;
+    k_restrict<T><<<nblk(nc, 256), 256, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
+    mg_vcycle<T>(s, H, l + 1, npre, npost);
+    k_prolong<T><<<nblk(n, 256), 256, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+    for (int it = 0; it < npost; it++) {
+        k_rbgs<T><<<g, 256, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+        k_rbgs<T><<<g, 256, 0, s>>>(L, 0, 0, H.b[l], H.invd[l], H.x[l]);
+    }
+}
+
+int mg_vcycle_launches(int nl, int npre, int npost)
+{
+    // per non-coarsest level: 2*npre + resid + restrict + prolong + 2*npost; coarsest: 1
+    return (nl - 1) * (2 * npre + 3 + 2 * npost) + 1;
+}
+
+template void mg_setup_invdiag<double>(cudaStream_t, const MgDevLevel &, double *);
+template void mg_setup_invdiag<float>(cudaStream_t, const MgDevLevel &, float *);
+template void mg_vcycle<double>(cudaStream_t, const MgHier<double> &, int, int, int);
+template void mg_vcycle<float>(cudaStream_t, const MgHier<float> &, int, int, int);

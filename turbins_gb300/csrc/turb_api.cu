@@ -1,0 +1,1190 @@
+// turb_api.cu -- the C ABI (include/turbins_gb300.h): context set-up, host
+// tables, field transfer and the per-step driver.  All arithmetic of the hot
+// path runs in the kernels of k_*.cu; the host only builds the 1-D tables of
+// grid-only quantities (with the reference's own expressions, so device
+// roundings match) and sequences launches on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/turbins_gb300.h"
+#include "turb_internal.cuh"
+#include "turb_kernels.cuh"
+#include "turb_mg.cuh"
+
+static char g_errmsg[512] = "";
+
+int turb_set_cuda_error(cudaError_t e, const char *file, int line)
+{
+    snprintf(g_errmsg, sizeof(g_errmsg), "%s (%s:%d)", cudaGetErrorString(e), file, line);
+    return TURB_ERR_CUDA;
+}
+
+// extra launchers defined at the end of this file
+void launch_pressure_apply(cudaStream_t s, const Dims &d, const uint8_t *st, const Geo &g, double dEta, double dXi,
+                           double dPhi, const double *x, double *y);
+
+namespace {
+
+struct DevBuf {
+    std::vector<void *> ptrs;
+    cudaError_t err = cudaSuccess;
+    template <typename T>
+    T *alloc(size_t n)
+    {
+        void *p = nullptr;
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e != cudaSuccess) { err = e; return nullptr; }
+        cudaMemset(p, 0, n * sizeof(T));
+        ptrs.push_back(p);
+        return (T *)p;
+    }
+    template <typename T>
+    T *upload(const std::vector<T> &h)
+    {
+        T *p = alloc<T>(h.size());
+        if (p && !h.empty()) cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+        return p;
+    }
+    void release()
+    {
+        for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+}  // namespace
+
+struct turb_ctx {
+    Dims d;
+    turb_params prm;
+    cudaStream_t s = nullptr;
+    DevBuf mem;
+    std::vector<double> xc, yc, zc, xu, yv, zw, mxc, myc, mzc, mxu, myv, mzw;
+    double dEta, dXi, dPhi;
+    Geo geo;
+    double *fld[64] = {nullptr};
+    double *old[3 + TURB_MAXCONC] = {nullptr};
+    double *jtmp = nullptr;
+    uint8_t *st[4] = {nullptr};
+    IbDev ib[4];
+    Interp2 icx, icy, icz, iyv;
+    TransW tw;
+    EnoTab eno[4][3];
+    EnoTab eno_cy[TURB_MAXCONC];
+    HelmTab helm[3], helm_c[TURB_MAXCONC];
+    const double *pcx, *pcy, *pcz;
+    ProjArgs proj;
+    // pressure
+    int pmode = TURB_PMODE_MIXED;
+    MgHier<double> H64;
+    MgHier<float> H32;
+    double *px, *pbw, *pr, *pz, *pp, *pq, *pro;
+    PcgScal *sc;
+    double *part, *dscal;
+    double *hscal = nullptr;   // pinned host scalars
+    long long nparts = 0;
+    long long launches = 0;
+};
+
+namespace {
+
+inline long long da_to_pitched(const Dims &d, long long L)
+{
+    long long i = L % d.NX, t = L / d.NX, j = t % d.NY, k = t / d.NY;
+    return d.at((int)i, (int)j, (int)k);
+}
+
+// Grid_compute_metric_coefficients, Grid.c:595-708
+void metrics(turb_ctx *c)
+{
+    int NX = c->d.NX, NY = c->d.NY, NZ = c->d.NZ;
+    c->dEta = 1.0 / (double)c->d.nx;
+    c->dXi = 1.0 / (double)c->d.ny;
+    c->dPhi = 1.0 / (double)c->d.nz;
+    auto &xc = c->xc, &yc = c->yc, &zc = c->zc, &xu = c->xu, &yv = c->yv, &zw = c->zw;
+    c->mxc.assign(NX, 0.0); c->myc.assign(NY, 0.0); c->mzc.assign(NZ, 0.0);
+    c->mxu.assign(NX, 0.0); c->myv.assign(NY, 0.0); c->mzw.assign(NZ, 0.0);
+    for (int i = 1; i < NX - 1; i++) c->mxu[i] = c->dEta / (xc[i] - xc[i - 1]);
+    c->mxu[0] = 0.5 * c->dEta / (xc[0] - xu[0]);
+    c->mxu[NX - 1] = 0.5 * c->dEta / (xu[NX - 1] - xc[NX - 2]);
+    for (int i = 1; i < NY - 1; i++) c->myv[i] = c->dXi / (yc[i] - yc[i - 1]);
+    c->myv[0] = 0.5 * c->dXi / (yc[0] - yv[0]);
+    c->myv[NY - 1] = 0.5 * c->dXi / (yv[NY - 1] - yc[NY - 2]);
+    for (int i = 1; i < NZ - 1; i++) c->mzw[i] = c->dPhi / (zc[i] - zc[i - 1]);
+    c->mzw[0] = 0.5 * c->dPhi / (zc[0] - zw[0]);
+    c->mzw[NZ - 1] = 0.5 * c->dPhi / (zw[NZ - 1] - zc[NZ - 2]);
+    for (int i = 0; i < NX - 1; i++) c->mxc[i] = c->dEta / (xu[i + 1] - xu[i]);
+    c->mxc[NX - 1] = c->dEta / (xc[NX - 1] - xc[NX - 2]);
+    for (int i = 0; i < NY - 1; i++) c->myc[i] = c->dXi / (yv[i + 1] - yv[i]);
+    c->myc[NY - 1] = c->dXi / (yc[NY - 1] - yc[NY - 2]);
+    for (int i = 0; i < NZ - 1; i++) c->mzc[i] = c->dPhi / (zc[i + 1] - zc[i]);
+    c->mzc[NZ - 1] = c->dPhi / (zc[NZ - 1] - zc[NZ - 2]);
+}
+
+Interp2 mk_interp2(DevBuf &m, int n, const std::vector<double> &X0, const std::vector<double> &X1,
+                   const std::vector<double> &XQ, int first)
+{
+    std::vector<double> dx(n, 1.0), dq(n, 0.0);
+    std::vector<uint8_t> fl(n, 0);
+    for (int t = first; t < n; t++) {
+        dx[t] = X1[t] - X0[t];
+        dq[t] = XQ[t] - X0[t];
+        fl[t] = std::fabs(X1[t] - X0[t]) < 1.0e-8;
+    }
+    Interp2 o;
+    o.dx = m.upload(dx);
+    o.dq = m.upload(dq);
+    o.flat = m.upload(fl);
+    return o;
+}
+
+// W0 = |(xq - X0) * (1/(X1 - X0))|, W1 = 1 - W0 (MyMath.c:63-72)
+W2 mk_w2(DevBuf &m, int n, int first, int last, const std::vector<double> &X0, const std::vector<double> &X1,
+         const std::vector<double> &XQ)
+{
+    std::vector<double> w0(n, 0.0), w1(n, 0.0);
+    for (int t = first; t <= last; t++) {
+        double a = 1.0 / (X1[t] - X0[t]);
+        w0[t] = std::fabs((XQ[t] - X0[t]) * a);
+        w1[t] = 1.0 - w0[t];
+    }
+    W2 o;
+    o.w0 = m.upload(w0);
+    o.w1 = m.upload(w1);
+    return o;
+}
+
+struct GhostRule {
+    int wall;      // 1: node on the wall (normal component), 0: mirror
+    double pos;    // wall coordinate
+    double mult;
+};
+
+// ENO line tables (positions and ghost rules of the *_ENO_ghost_cells routines)
+EnoTab mk_eno(DevBuf &m, int r, const std::vector<double> &pos, int s0, int e0, GhostRule lo, GhostRule hi)
+{
+    int nb = e0 - s0 + 1 + 2 * r;
+    std::vector<double> P(nb, 0.0);
+    for (int b = r; b < nb - r; b++) P[b] = pos[b - r + s0];
+    EnoTab T;
+    T.r = r; T.s0 = s0; T.e0 = e0; T.nb = nb;
+    for (int t = 0; t < 6; t++) { T.gsrc[t] = 0; T.gm[t] = 0.0; }
+    for (int ex = 0; ex < r; ex++) {
+        int gi = ex;
+        if (lo.wall) {
+            int ii = 2 * r - ex - 2;
+            if (ex == r - 1) { P[gi] = lo.pos; T.gsrc[ex] = 0; }
+            else { P[gi] = 2.0 * lo.pos - P[ii]; T.gsrc[ex] = lo.mult == 0.0 ? 0 : 1; T.gm[ex] = lo.mult; }
+        } else {
+            int ii = 2 * r - ex - 1;
+            P[gi] = 2.0 * lo.pos - P[ii];
+            T.gsrc[ex] = 1; T.gm[ex] = lo.mult;
+        }
+    }
+    for (int ex = 0; ex < r; ex++) {
+        int gi = nb - ex - 1;
+        if (hi.wall) {
+            int ii = nb - 2 * r + ex + 1;
+            if (ex == r - 1) { P[gi] = hi.pos; T.gsrc[3 + ex] = 0; }
+            else { P[gi] = 2.0 * hi.pos - P[ii]; T.gsrc[3 + ex] = hi.mult == 0.0 ? 0 : 2; T.gm[3 + ex] = hi.mult; }
+        } else {
+            int ii = nb - 2 * r + ex;
+            P[gi] = 2.0 * hi.pos - P[ii];
+            T.gsrc[3 + ex] = 2; T.gm[3 + ex] = hi.mult;
+        }
+    }
+    std::vector<double> h1(nb, 1.0), h2(nb, 1.0), h3(nb, 1.0), g2(2 * nb, 0.0), g3(3 * nb, 0.0);
+    for (int b = 0; b < nb - 1; b++) h1[b] = P[b + 1] - P[b];
+    for (int b = 1; b < nb - 1; b++) h2[b] = P[b + 1] - P[b - 1];
+    for (int b = 1; b < nb - 2; b++) h3[b] = P[b + 2] - P[b - 1];
+    for (int c = 1; c < nb - 1; c++) {
+        double xi = P[c];
+        g2[2 * c + 0] = (xi - P[c - 1]) + (xi - P[c]);
+        g2[2 * c + 1] = (xi - P[c]) + (xi - P[c + 1]);
+        for (int t = 0; t < 3; t++) {
+            int ks = c - 2 + t;
+            if (ks < 0 || ks + 2 >= nb) continue;
+            double a = P[ks], bb = P[ks + 1], e = P[ks + 2];
+            g3[3 * c + t] = (xi - a) * (xi - bb) + (xi - bb) * (xi - e) + (xi - a) * (xi - e);
+        }
+    }
+    T.h1 = m.upload(h1);
+    T.h2 = m.upload(h2);
+    T.h3 = m.upload(h3);
+    T.g2 = m.upload(g2);
+    T.g3 = m.upload(g3);
+    return T;
+}
+
+double slip(int noslip) { return noslip ? -1.0 : 1.0; }
+
+void build_eno(turb_ctx *c)
+{
+    int r = c->prm.eno_order, nx = c->d.nx, ny = c->d.ny, nz = c->d.nz;
+    const int *ns = c->prm.wall_noslip;
+    auto M = [](double p, double mult) { return GhostRule{0, p, mult}; };
+    auto Wl = [](double p, double mult) { return GhostRule{1, p, mult}; };
+    double x0 = c->xu[0], x1 = c->xu[nx], y0 = c->yv[0], y1 = c->yv[ny], z0 = c->zw[0], z1 = c->zw[nz];
+    // u: Velocity.c:2124-2352
+    c->eno[0][0] = mk_eno(c->mem, r, c->xu, 1, nx - 1, Wl(x0, -1.0), Wl(x1, 0.0));
+    c->eno[0][1] = mk_eno(c->mem, r, c->yc, 0, ny - 1, M(y0, slip(ns[2])), M(y1, slip(ns[3])));
+    c->eno[0][2] = mk_eno(c->mem, r, c->zc, 0, nz - 1, M(z0, slip(ns[4])), M(z1, slip(ns[5])));
+    // v: Velocity.c:2356-2575
+    c->eno[1][0] = mk_eno(c->mem, r, c->xc, 0, nx - 1, M(x0, slip(ns[0])), M(x1, slip(ns[1])));
+    c->eno[1][1] = mk_eno(c->mem, r, c->yv, 1, ny - 1, Wl(y0, 0.0), Wl(y1, 0.0));
+    c->eno[1][2] = mk_eno(c->mem, r, c->zc, 0, nz - 1, M(z0, slip(ns[4])), M(z1, slip(ns[5])));
+    // w: Velocity.c:2579-2801
+    c->eno[2][0] = mk_eno(c->mem, r, c->xc, 0, nx - 1, M(x0, slip(ns[0])), M(x1, slip(ns[1])));
+    c->eno[2][1] = mk_eno(c->mem, r, c->yc, 0, ny - 1, M(y0, slip(ns[2])), M(y1, slip(ns[3])));
+    c->eno[2][2] = mk_eno(c->mem, r, c->zw, 1, nz - 1, Wl(z0, 0.0), Wl(z1, 0.0));
+    // c: Conc.c:1021-1220 (Neumann; Robin top for particles with sedimentation;
+    // salinity top ghosts take the Neumann value, the reference leaves them unset)
+    c->eno[3][0] = mk_eno(c->mem, r, c->xc, 0, nx - 1, M(x0, 1.0), M(x1, 1.0));
+    c->eno[3][1] = mk_eno(c->mem, r, c->yc, 0, ny - 1, M(y0, 1.0), M(y1, 1.0));
+    c->eno[3][2] = mk_eno(c->mem, r, c->zc, 0, nz - 1, M(z0, 1.0), M(z1, 1.0));
+    for (int ic = 0; ic < c->prm.nconc; ic++) {
+        EnoTab T = c->eno[3][1];
+        if (c->prm.ctype[ic] == TURB_PARTICLE && c->prm.sedimentation) {
+            double coef = 2.0 / (c->prm.pe[ic] * c->dXi) * c->myv[ny];
+            double Vs = std::fabs(c->prm.vs0[ic]);
+            double f = (coef - Vs) / (coef + Vs);
+            for (int ex = 0; ex < r; ex++) T.gm[3 + ex] = f;
+        }
+        c->eno_cy[ic] = T;
+    }
+}
+
+// separable 1-D tables of the Helmholtz rows (Velocity.c:449-1474, Conc.c:390-730)
+HelmTab mk_helm(turb_ctx *c, int q, int ic)
+{
+    int nx = c->d.nx, ny = c->d.ny, nz = c->d.nz, NX = c->d.NX, NY = c->d.NY, NZ = c->d.NZ;
+    const int *ns = c->prm.wall_noslip;
+    double coefRe = q == 3 ? c->prm.pe[ic] : c->prm.re;
+    double Cx = -1.0 / (coefRe * c->dEta * c->dEta), Cy = -1.0 / (coefRe * c->dXi * c->dXi),
+           Cz = -1.0 / (coefRe * c->dPhi * c->dPhi);
+    std::vector<double> apx(NX, 0.0), apy(NY, 0.0), apz(NZ, 0.0), aw(NX, 0.0), ae(NX, 0.0), as(NY, 0.0),
+        an(NY, 0.0), ab(NZ, 0.0), af(NZ, 0.0);
+    auto wallfold = [](double a, int noslip) { return noslip ? -a : a; };
+    // x
+    for (int i = 0; i < NX; i++) {
+        double px, ex, wx;
+        if (q == 0) {
+            if (i < 1 || i > nx - 1) continue;
+            px = c->mxu[i]; ex = c->mxc[i]; wx = c->mxc[i - 1];
+        } else {
+            if (i > nx - 1) continue;
+            px = c->mxc[i]; ex = c->mxu[i + 1]; wx = c->mxu[i];
+        }
+        double a_w = Cx * px * wx, a_e = Cx * px * ex;
+        apx[i] = -Cx * px * (ex + wx);
+        if (q == 0) {
+            aw[i] = (i - 1 >= 1) ? a_w : 0.0;
+            ae[i] = (i + 1 <= nx - 1) ? a_e : 0.0;
+        } else {
+            aw[i] = i > 0 ? a_w : 0.0;
+            ae[i] = i < nx - 1 ? a_e : 0.0;
+            if (i == 0) apx[i] += q == 3 ? a_w : wallfold(a_w, ns[0]);
+            if (i == nx - 1) apx[i] += q == 3 ? a_e : wallfold(a_e, ns[1]);
+        }
+    }
+    // y
+    for (int j = 0; j < NY; j++) {
+        double py, ny_, sy;
+        if (q == 1) {
+            if (j < 1 || j > ny - 1) continue;
+            py = c->myv[j]; ny_ = c->myc[j]; sy = c->myc[j - 1];
+        } else {
+            if (j > ny - 1) continue;
+            py = c->myc[j]; ny_ = c->myv[j + 1]; sy = c->myv[j];
+        }
+        double a_s = Cy * py * sy, a_n = Cy * py * ny_;
+        apy[j] = -Cy * py * (ny_ + sy);
+        if (q == 1) {
+            as[j] = (j - 1 >= 1) ? a_s : 0.0;
+            an[j] = (j + 1 <= ny - 1) ? a_n : 0.0;
+        } else {
+            as[j] = j > 0 ? a_s : 0.0;
+            an[j] = j < ny - 1 ? a_n : 0.0;
+            if (j == 0) apy[j] += q == 3 ? a_s : wallfold(a_s, ns[2]);
+            if (j == ny - 1) {
+                if (q == 3) {
+                    double cf = a_n;
+                    if (c->prm.ctype[ic] == TURB_PARTICLE) {
+                        double b = 2.0 / (coefRe * c->dXi) * ny_;
+                        cf = a_n * (b - std::fabs(c->prm.vs0[ic])) / (b + std::fabs(c->prm.vs0[ic]));
+                    }
+                    apy[j] += cf;
+                } else {
+                    apy[j] += wallfold(a_n, ns[3]);
+                }
+            }
+        }
+    }
+    // z
+    for (int k = 0; k < NZ; k++) {
+        double pz, fz, bz;
+        if (q == 2) {
+            if (k < 1 || k > nz - 1) continue;
+            pz = c->mzw[k]; bz = c->mzc[k - 1]; fz = c->mzc[k];
+        } else {
+            if (k > nz - 1) continue;
+            pz = c->mzc[k]; bz = c->mzw[k]; fz = c->mzw[k + 1];
+        }
+        double a_b = Cz * pz * bz, a_f = Cz * pz * fz;
+        apz[k] = -Cz * pz * (bz + fz);
+        if (q == 2) {
+            ab[k] = (k - 1 >= 1) ? a_b : 0.0;
+            af[k] = (k + 1 <= nz - 1) ? a_f : 0.0;
+        } else {
+            ab[k] = k > 0 ? a_b : 0.0;
+            af[k] = k < nz - 1 ? a_f : 0.0;
+            if (k == 0) apz[k] += q == 3 ? a_b : wallfold(a_b, ns[4]);
+            if (k == nz - 1) apz[k] += q == 3 ? a_f : wallfold(a_f, ns[5]);
+        }
+    }
+    HelmTab h;
+    h.apx = c->mem.upload(apx); h.apy = c->mem.upload(apy); h.apz = c->mem.upload(apz);
+    h.aw = c->mem.upload(aw); h.ae = c->mem.upload(ae); h.as = c->mem.upload(as); h.an = c->mem.upload(an);
+    h.ab = c->mem.upload(ab); h.af = c->mem.upload(af);
+    h.ap_solid = -Cx * c->mxc[0] - Cy * c->myc[0] - Cz * c->mzc[0];
+    h.q = q;
+    return h;
+}
+
+IbDev mk_ib(turb_ctx *c, int q, const turb_ib_desc &ib, double aps)
+{
+    IbDev o;
+    o.n = ib.n;
+    std::vector<int32_t> im(ib.n), cnt(ib.n), col((size_t)ib.n * 8, 0);
+    std::vector<double> val((size_t)ib.n * 8, 0.0), dg(ib.n);
+    for (int t = 0; t < ib.n; t++) {
+        long long L = ib.im[t];
+        double self = 1.0;
+        int n = 0;
+        for (int g = 0; g < ib.nf[t]; g++)
+            if (ib.fidx[t * 8 + g] == ib.im[t]) self += ib.fcoef[t * 8 + g];
+        for (int g = 0; g < ib.nf[t]; g++) {
+            double cf = ib.fcoef[t * 8 + g];
+            if (ib.fidx[t * 8 + g] != ib.im[t] && std::fabs(cf) >= 1.0e-8) {
+                col[(size_t)t * 8 + n] = (int32_t)da_to_pitched(c->d, ib.fidx[t * 8 + g]);
+                val[(size_t)t * 8 + n] = aps * cf;
+                n++;
+            }
+        }
+        im[t] = (int32_t)da_to_pitched(c->d, L);
+        cnt[t] = n;
+        dg[t] = aps * self;
+    }
+    (void)q;
+    o.im = c->mem.upload(im);
+    o.cnt = c->mem.upload(cnt);
+    o.col = c->mem.upload(col);
+    o.val = c->mem.upload(val);
+    o.diag = c->mem.upload(dg);
+    return o;
+}
+
+// multigrid hierarchy (same coarsening rule as the CPU oracle)
+struct HostLev {
+    int nx, ny, nz, cx = 0, cy = 0, cz = 0;
+    std::vector<double> D[3], F[3];
+    double pin;
+};
+
+std::vector<HostLev> mg_host(turb_ctx *c)
+{
+    std::vector<HostLev> L(1);
+    HostLev &l0 = L[0];
+    l0.nx = c->d.nx; l0.ny = c->d.ny; l0.nz = c->d.nz;
+    const std::vector<double> *mc[3] = {&c->mxc, &c->myc, &c->mzc}, *mf[3] = {&c->mxu, &c->myv, &c->mzw};
+    double de[3] = {c->dEta, c->dXi, c->dPhi};
+    int n0[3] = {l0.nx, l0.ny, l0.nz};
+    for (int a = 0; a < 3; a++) {
+        l0.D[a].resize(n0[a]);
+        l0.F[a].resize(n0[a] + 1);
+        for (int i = 0; i < n0[a]; i++) l0.D[a][i] = de[a] / (*mc[a])[i];
+        for (int i = 0; i <= n0[a]; i++) l0.F[a][i] = de[a] / (*mf[a])[i];
+    }
+    l0.pin = l0.D[1][l0.ny - 1] * l0.D[2][l0.nz - 1] / l0.F[0][l0.nx];
+    for (int lev = 0; lev < TURB_MG_MAXLEV - 1; lev++) {
+        HostLev f = L[lev];
+        int nn[3] = {f.nx, f.ny, f.nz};
+        double h[3];
+        for (int a = 0; a < 3; a++) {
+            double s = 0.0;
+            for (double v : f.D[a]) s += v;
+            h[a] = s / nn[a];
+        }
+        double hmin = std::min(h[0], std::min(h[1], h[2]));
+        long long ncell = (long long)f.nx * f.ny * f.nz;
+        int cc[3];
+        for (int a = 0; a < 3; a++) cc[a] = (nn[a] % 2 == 0) && nn[a] >= 2 && h[a] <= 2.0 * hmin;
+        if (ncell <= 64 || !(cc[0] || cc[1] || cc[2])) break;
+        L[lev].cx = cc[0]; L[lev].cy = cc[1]; L[lev].cz = cc[2];
+        HostLev g;
+        int gn[3];
+        for (int a = 0; a < 3; a++) {
+            gn[a] = cc[a] ? nn[a] / 2 : nn[a];
+            g.D[a].resize(gn[a]);
+            g.F[a].resize(gn[a] + 1);
+            for (int i = 0; i < gn[a]; i++) g.D[a][i] = cc[a] ? f.D[a][2 * i] + f.D[a][2 * i + 1] : f.D[a][i];
+            if (cc[a]) {
+                g.F[a][0] = 0.5 * g.D[a][0];
+                for (int i = 1; i < gn[a]; i++) g.F[a][i] = 0.5 * (g.D[a][i - 1] + g.D[a][i]);
+                g.F[a][gn[a]] = 0.5 * g.D[a][gn[a] - 1];
+            } else {
+                g.F[a] = f.F[a];
+            }
+        }
+        g.nx = gn[0]; g.ny = gn[1]; g.nz = gn[2];
+        g.pin = f.pin;
+        L.push_back(g);
+    }
+    return L;
+}
+
+int build_mg(turb_ctx *c)
+{
+    std::vector<HostLev> L = mg_host(c);
+    int nl = (int)L.size();
+    c->H64.nl = c->H32.nl = nl;
+    for (int l = 0; l < nl; l++) {
+        HostLev &h = L[l];
+        MgDevLevel m;
+        m.nx = h.nx; m.ny = h.ny; m.nz = h.nz;
+        m.cx = h.cx; m.cy = h.cy; m.cz = h.cz;
+        m.pin = h.pin;
+        std::vector<double> rf[3];
+        std::vector<float> Df[3], rff[3];
+        for (int a = 0; a < 3; a++) {
+            rf[a].resize(h.F[a].size());
+            rff[a].resize(h.F[a].size());
+            for (size_t i = 0; i < h.F[a].size(); i++) { rf[a][i] = 1.0 / h.F[a][i]; rff[a][i] = (float)rf[a][i]; }
+            Df[a].resize(h.D[a].size());
+            for (size_t i = 0; i < h.D[a].size(); i++) Df[a][i] = (float)h.D[a][i];
+        }
+        m.dxd = c->mem.upload(h.D[0]); m.dyd = c->mem.upload(h.D[1]); m.dzd = c->mem.upload(h.D[2]);
+        m.rfxd = c->mem.upload(rf[0]); m.rfyd = c->mem.upload(rf[1]); m.rfzd = c->mem.upload(rf[2]);
+        m.dxf = c->mem.upload(Df[0]); m.dyf = c->mem.upload(Df[1]); m.dzf = c->mem.upload(Df[2]);
+        m.rfxf = c->mem.upload(rff[0]); m.rfyf = c->mem.upload(rff[1]); m.rfzf = c->mem.upload(rff[2]);
+        c->H64.lev[l] = m;
+        c->H32.lev[l] = m;
+        long long n = (long long)h.nx * h.ny * h.nz;
+        if (l > 0) {
+            c->H64.x[l] = c->mem.alloc<double>(n);
+            c->H64.b[l] = c->mem.alloc<double>(n);
+        }
+        c->H64.r[l] = c->mem.alloc<double>(n);
+        c->H64.invd[l] = c->mem.alloc<double>(n);
+        c->H32.x[l] = c->mem.alloc<float>(n);
+        c->H32.b[l] = c->mem.alloc<float>(n);
+        c->H32.r[l] = c->mem.alloc<float>(n);
+        c->H32.invd[l] = c->mem.alloc<float>(n);
+        if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+        mg_setup_invdiag<double>(c->s, m, c->H64.invd[l]);
+        mg_setup_invdiag<float>(c->s, m, c->H32.invd[l]);
+    }
+    // dense inverse of the coarsest operator (Gauss-Jordan, partial pivoting)
+    HostLev &h = L[nl - 1];
+    int n = h.nx * h.ny * h.nz;
+    if (n > 256) return TURB_ERR_ARG;
+    std::vector<double> A((size_t)n * n, 0.0), I((size_t)n * n, 0.0);
+    auto id = [&](int i, int j, int k) { return (k * h.ny + j) * h.nx + i; };
+    for (int k = 0; k < h.nz; k++)
+        for (int j = 0; j < h.ny; j++)
+            for (int i = 0; i < h.nx; i++) {
+                int r = id(i, j, k);
+                double dyz = h.D[1][j] * h.D[2][k], dxz = h.D[0][i] * h.D[2][k], dxy = h.D[0][i] * h.D[1][j];
+                double d = 0.0, f;
+                if (i > 0) { f = dyz / h.F[0][i]; d += f; A[(size_t)r * n + id(i - 1, j, k)] = -f; }
+                if (i < h.nx - 1) { f = dyz / h.F[0][i + 1]; d += f; A[(size_t)r * n + id(i + 1, j, k)] = -f; }
+                if (j > 0) { f = dxz / h.F[1][j]; d += f; A[(size_t)r * n + id(i, j - 1, k)] = -f; }
+                if (j < h.ny - 1) { f = dxz / h.F[1][j + 1]; d += f; A[(size_t)r * n + id(i, j + 1, k)] = -f; }
+                if (k > 0) { f = dxy / h.F[2][k]; d += f; A[(size_t)r * n + id(i, j, k - 1)] = -f; }
+                if (k < h.nz - 1) { f = dxy / h.F[2][k + 1]; d += f; A[(size_t)r * n + id(i, j, k + 1)] = -f; }
+                if (i == h.nx - 1 && j == h.ny - 1 && k == h.nz - 1) d += h.pin;
+                A[(size_t)r * n + r] = d;
+            }
+    for (int i = 0; i < n; i++) I[(size_t)i * n + i] = 1.0;
+    for (int col = 0; col < n; col++) {
+        int piv = col;
+        for (int r = col + 1; r < n; r++)
+            if (std::fabs(A[(size_t)r * n + col]) > std::fabs(A[(size_t)piv * n + col])) piv = r;
+        if (piv != col)
+            for (int t = 0; t < n; t++) {
+                std::swap(A[(size_t)piv * n + t], A[(size_t)col * n + t]);
+                std::swap(I[(size_t)piv * n + t], I[(size_t)col * n + t]);
+            }
+        double dv = A[(size_t)col * n + col];
+        for (int t = 0; t < n; t++) { A[(size_t)col * n + t] /= dv; I[(size_t)col * n + t] /= dv; }
+        for (int r = 0; r < n; r++) {
+            if (r == col) continue;
+            double f = A[(size_t)r * n + col];
+            if (f == 0.0) continue;
+            for (int t = 0; t < n; t++) {
+                A[(size_t)r * n + t] -= f * A[(size_t)col * n + t];
+                I[(size_t)r * n + t] -= f * I[(size_t)col * n + t];
+            }
+        }
+    }
+    c->H64.coarse_inv = c->H32.coarse_inv = c->mem.upload(I);
+    long long n0 = (long long)c->d.nx * c->d.ny * c->d.nz;
+    c->px = c->mem.alloc<double>(n0);
+    c->pbw = c->mem.alloc<double>(n0);
+    c->pr = c->mem.alloc<double>(n0);
+    c->pz = c->mem.alloc<double>(n0);
+    c->pp = c->mem.alloc<double>(n0);
+    c->pq = c->mem.alloc<double>(n0);
+    c->pro = c->mem.alloc<double>(n0);
+    c->H64.x[0] = c->pz;   // FP64 V-cycle writes z directly
+    c->H64.b[0] = c->pr;   // and reads r directly
+    c->sc = c->mem.alloc<PcgScal>(1);
+    return c->mem.err == cudaSuccess ? TURB_OK : TURB_ERR_ALLOC;
+}
+
+int qidx(char which)
+{
+    switch (which) {
+    case 'u': return 0;
+    case 'v': return 1;
+    case 'w': return 2;
+    case 'c': return 3;
+    default: return -1;
+    }
+}
+
+int check_launch(turb_ctx *c)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    (void)c;
+    return TURB_OK;
+}
+
+int fetch_scalars(turb_ctx *c, int n)
+{
+    TURB_CHECK(cudaMemcpyAsync(c->hscal, c->dscal, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *turb_status_string(int status)
+{
+    switch (status) {
+    case TURB_OK: return "ok";
+    case TURB_ERR_ARG: return "bad argument";
+    case TURB_ERR_CUDA: return g_errmsg[0] ? g_errmsg : "CUDA error";
+    case TURB_ERR_NOT_CONVERGED: return "solver did not converge";
+    case TURB_ERR_NAN: return "non-finite residual";
+    case TURB_ERR_ALLOC: return "device allocation failed";
+    default: return "unknown status";
+    }
+}
+
+int turb_create(const turb_grid_desc *g, const turb_params *p, turb_ctx **out)
+{
+    if (!g || !p || !out) return TURB_ERR_ARG;
+    *out = nullptr;
+    if (g->nx < 4 || g->ny < 4 || g->nz < 4 || p->nconc < 1 || p->nconc > TURB_MAXCONC || p->eno_order < 1 ||
+        p->eno_order > 3 || g->nx != p->nx || g->ny != p->ny || g->nz != p->nz)
+        return TURB_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        snprintf(g_errmsg, sizeof(g_errmsg), "no CUDA device");
+        return TURB_ERR_CUDA;
+    }
+    turb_ctx *c = new turb_ctx();
+    c->prm = *p;
+    Dims &d = c->d;
+    d.nx = g->nx; d.ny = g->ny; d.nz = g->nz;
+    d.NX = d.nx + 1; d.NY = d.ny + 1; d.NZ = d.nz + 1;
+    d.PX = (d.NX + 7) / 8 * 8;
+    d.plane = (long long)d.PX * d.NY;
+    d.n = d.plane * d.NZ;
+    c->xc.assign(g->xc, g->xc + d.NX); c->yc.assign(g->yc, g->yc + d.NY); c->zc.assign(g->zc, g->zc + d.NZ);
+    c->xu.assign(g->xu, g->xu + d.NX); c->yv.assign(g->yv, g->yv + d.NY); c->zw.assign(g->zw, g->zw + d.NZ);
+    metrics(c);
+    if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) { delete c; return TURB_ERR_CUDA; }
+    DevBuf &m = c->mem;
+    c->geo.xc = m.upload(c->xc); c->geo.yc = m.upload(c->yc); c->geo.zc = m.upload(c->zc);
+    c->geo.xu = m.upload(c->xu); c->geo.yv = m.upload(c->yv); c->geo.zw = m.upload(c->zw);
+    c->geo.mxc = m.upload(c->mxc); c->geo.myc = m.upload(c->myc); c->geo.mzc = m.upload(c->mzc);
+    c->geo.mxu = m.upload(c->mxu); c->geo.myv = m.upload(c->myv); c->geo.mzw = m.upload(c->mzw);
+    // fields
+    int ids[] = {TURB_F_U, TURB_F_V, TURB_F_W, TURB_F_PHI, TURB_F_DPX, TURB_F_DPY, TURB_F_DPZ, TURB_F_PB,
+                 TURB_F_DIV, TURB_F_UBC, TURB_F_VBC, TURB_F_WBC, TURB_F_CONV_U, TURB_F_CONV_V, TURB_F_CONV_W,
+                 TURB_F_B_U, TURB_F_B_V, TURB_F_B_W, TURB_F_CTOT, TURB_F_SCRATCH0, TURB_F_SCRATCH1};
+    for (int id : ids) c->fld[id] = m.alloc<double>(d.n);
+    for (int ic = 0; ic < p->nconc; ic++) {
+        c->fld[TURB_F_C0 + ic] = m.alloc<double>(d.n);
+        c->fld[TURB_F_CCONV0 + ic] = m.alloc<double>(d.n);
+        c->fld[TURB_F_CB0 + ic] = m.alloc<double>(d.n);
+        c->fld[TURB_F_VP0 + ic] = m.alloc<double>(d.n);
+        c->old[3 + ic] = m.alloc<double>(d.n);
+    }
+    for (int q = 0; q < 3; q++) c->old[q] = m.alloc<double>(d.n);
+    c->jtmp = m.alloc<double>(d.n);
+    // status (DA layout in, pitched on the device)
+    for (int q = 0; q < 4; q++) {
+        std::vector<uint8_t> h((size_t)d.n, (uint8_t)T_BOUNDARY);
+        for (int k = 0; k < d.NZ; k++)
+            for (int j = 0; j < d.NY; j++)
+                for (int i = 0; i < d.NX; i++) h[(size_t)d.at(i, j, k)] = g->status[q][((size_t)k * d.NY + j) * d.NX + i];
+        c->st[q] = m.upload(h);
+    }
+    // tables
+    int nx = d.nx, ny = d.ny, nz = d.nz;
+    {
+        std::vector<double> x0(d.NX), x1(d.NX), xq(d.NX);
+        for (int i = 0; i < nx; i++) { x0[i] = c->xu[i]; x1[i] = c->xu[i + 1]; xq[i] = c->xc[i]; }
+        c->icx = mk_interp2(m, d.NX, x0, x1, xq, 0);
+        std::vector<double> y0(d.NY), y1(d.NY), yq(d.NY);
+        for (int j = 0; j < ny; j++) { y0[j] = c->yv[j]; y1[j] = c->yv[j + 1]; yq[j] = c->yc[j]; }
+        c->icy = mk_interp2(m, d.NY, y0, y1, yq, 0);
+        std::vector<double> z0(d.NZ), z1(d.NZ), zq(d.NZ);
+        for (int k = 0; k < nz; k++) { z0[k] = c->zw[k]; z1[k] = c->zw[k + 1]; zq[k] = c->zc[k]; }
+        c->icz = mk_interp2(m, d.NZ, z0, z1, zq, 0);
+        std::vector<double> v0(d.NY, 0.0), v1(d.NY, 1.0), vq(d.NY, 0.0);
+        for (int j = 1; j < d.NY; j++) { v0[j] = c->yc[j - 1]; v1[j] = c->yc[j]; vq[j] = c->yv[j]; }
+        c->iyv = mk_interp2(m, d.NY, v0, v1, vq, 1);
+    }
+    {
+        std::vector<double> a0(d.NX + 1, 0.0), a1(d.NX + 1, 1.0), aq(d.NX + 1, 0.0);
+        for (int i = 1; i <= nx - 1; i++) { a0[i] = c->xc[i - 1]; a1[i] = c->xc[i]; aq[i] = c->xu[i]; }
+        c->tw.xu = mk_w2(m, d.NX, 1, nx - 1, a0, a1, aq);
+        for (int i = 0; i <= nx - 1; i++) { a0[i] = c->xu[i]; a1[i] = c->xu[i + 1]; aq[i] = c->xc[i]; }
+        c->tw.xc = mk_w2(m, d.NX, 0, nx - 1, a0, a1, aq);
+        std::vector<double> b0(d.NY + 1, 0.0), b1(d.NY + 1, 1.0), bq(d.NY + 1, 0.0);
+        for (int j = 0; j <= ny - 1; j++) { b0[j] = c->yv[j]; b1[j] = c->yv[j + 1]; bq[j] = c->yc[j]; }
+        c->tw.yc = mk_w2(m, d.NY, 0, ny - 1, b0, b1, bq);
+        for (int j = 1; j <= ny - 1; j++) { b0[j] = c->yc[j - 1]; b1[j] = c->yc[j]; bq[j] = c->yv[j]; }
+        c->tw.yv = mk_w2(m, d.NY, 1, ny - 1, b0, b1, bq);
+        std::vector<double> e0(d.NZ + 1, 0.0), e1(d.NZ + 1, 1.0), eq(d.NZ + 1, 0.0);
+        for (int k = 0; k <= nz - 1; k++) { e0[k] = c->zw[k]; e1[k] = c->zw[k + 1]; eq[k] = c->zc[k]; }
+        c->tw.zc = mk_w2(m, d.NZ, 0, nz - 1, e0, e1, eq);
+        for (int k = 1; k <= nz - 1; k++) { e0[k] = c->zc[k - 1]; e1[k] = c->zc[k]; eq[k] = c->zw[k]; }
+        c->tw.zw = mk_w2(m, d.NZ, 1, nz - 1, e0, e1, eq);
+    }
+    build_eno(c);
+    for (int q = 0; q < 3; q++) c->helm[q] = mk_helm(c, q, 0);
+    for (int ic = 0; ic < p->nconc; ic++) c->helm_c[ic] = mk_helm(c, 3, ic);
+    for (int q = 0; q < 4; q++) {
+        double aps = q < 3 ? c->helm[q].ap_solid : c->helm_c[0].ap_solid;
+        turb_ib_desc e = g->ib[q];
+        if (e.n < 0 || (e.n > 0 && (!e.im || !e.nf || !e.fidx || !e.fcoef))) { m.release(); delete c; return TURB_ERR_ARG; }
+        c->ib[q] = mk_ib(c, q, e, aps);
+    }
+    {
+        double a_dEta = 1.0 / c->dEta, a_dXi = 1.0 / c->dXi, a_dPhi = 1.0 / c->dPhi;
+        std::vector<double> cx(d.NX), cy(d.NY), cz(d.NZ), cyv(d.NY), czw(d.NZ);
+        for (int i = 0; i < d.NX; i++) cx[i] = c->mxc[i] * a_dEta;
+        for (int j = 0; j < d.NY; j++) { cy[j] = c->myc[j] * a_dXi; cyv[j] = a_dXi * c->myv[j]; }
+        for (int k = 0; k < d.NZ; k++) { cz[k] = c->mzc[k] * a_dPhi; czw[k] = c->mzw[k] * a_dPhi; }
+        c->pcx = m.upload(cx); c->pcy = m.upload(cy); c->pcz = m.upload(cz);
+        c->proj.su = c->st[0]; c->proj.sv = c->st[1]; c->proj.sw = c->st[2];
+        c->proj.mxu = c->geo.mxu; c->proj.cyv = m.upload(cyv); c->proj.czw = m.upload(czw);
+        c->proj.a_dEta = a_dEta;
+    }
+    c->nparts = std::max<long long>(std::max(helm_parts(d), divergence_parts(d)), (long long)pcg_nparts() * 2);
+    c->part = m.alloc<double>(c->nparts + 4096);
+    c->dscal = m.alloc<double>(16);
+    if (m.err != cudaSuccess) { m.release(); cudaStreamDestroy(c->s); delete c; return TURB_ERR_ALLOC; }
+    int rc = build_mg(c);
+    if (rc != TURB_OK) { m.release(); cudaStreamDestroy(c->s); delete c; return rc; }
+    if (cudaMallocHost(&c->hscal, 16 * sizeof(double)) != cudaSuccess) { m.release(); delete c; return TURB_ERR_ALLOC; }
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) { m.release(); delete c; return TURB_ERR_CUDA; }
+    *out = c;
+    return TURB_OK;
+}
+
+int turb_destroy(turb_ctx *c)
+{
+    if (!c) return TURB_ERR_ARG;
+    cudaStreamSynchronize(c->s);
+    c->mem.release();
+    if (c->hscal) cudaFreeHost(c->hscal);
+    cudaStreamDestroy(c->s);
+    delete c;
+    return TURB_OK;
+}
+
+static double *field_ptr(turb_ctx *c, int f)
+{
+    if (f < 0 || f >= 64) return nullptr;
+    return c->fld[f];
+}
+
+int turb_field_upload(turb_ctx *c, int field, const double *h)
+{
+    if (!c || !h) return TURB_ERR_ARG;
+    double *p = field_ptr(c, field);
+    if (!p) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    TURB_CHECK(cudaMemcpy2DAsync(p, (size_t)d.PX * 8, h, (size_t)d.NX * 8, (size_t)d.NX * 8,
+                                 (size_t)d.NY * d.NZ, cudaMemcpyHostToDevice, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_field_download(turb_ctx *c, int field, double *h)
+{
+    if (!c || !h) return TURB_ERR_ARG;
+    double *p = field_ptr(c, field);
+    if (!p) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    TURB_CHECK(cudaMemcpy2DAsync(h, (size_t)d.NX * 8, p, (size_t)d.PX * 8, (size_t)d.NX * 8,
+                                 (size_t)d.NY * d.NZ, cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_set_pressure_mode(turb_ctx *c, int mode)
+{
+    if (!c || (mode != TURB_PMODE_FP64 && mode != TURB_PMODE_MIXED)) return TURB_ERR_ARG;
+    c->pmode = mode;
+    return TURB_OK;
+}
+
+int turb_synchronize(turb_ctx *c)
+{
+    if (!c) return TURB_ERR_ARG;
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_ENO_compute_convective_terms(int order, int n, const double *D0, const double *P, const double *V,
+                                      double *out)
+{
+    if (order < 1 || order > 3 || n < 2 * order + 2 || !D0 || !P || !V || !out) return TURB_ERR_ARG;
+    double *buf = nullptr;
+    TURB_CHECK(cudaMalloc(&buf, sizeof(double) * 4 * (size_t)n));
+    cudaMemcpy(buf, D0, sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(buf + n, P, sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(buf + 2 * n, V, sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(buf + 3 * n, out, sizeof(double) * n, cudaMemcpyHostToDevice);
+    int rc = launch_eno_line(order, n, buf, buf + n, buf + 2 * n, buf + 3 * n, 0);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, buf + 3 * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (rc) return TURB_ERR_ARG;
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    return TURB_OK;
+}
+
+int turb_Velocity_cell_center(turb_ctx *c)
+{
+    if (!c) return TURB_ERR_ARG;
+    launch_cell_center(c->s, c->d, c->icx, c->icy, c->icz, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W],
+                       c->fld[TURB_F_UBC], c->fld[TURB_F_VBC], c->fld[TURB_F_WBC]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Velocity_transpose_velocities(turb_ctx *c, char which)
+{
+    int q = qidx(which);
+    if (!c || q < 0 || q > 2) return TURB_ERR_ARG;
+    launch_transpose(c->s, c->d, q, c->st[q], c->tw, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W],
+                     c->fld[TURB_F_SCRATCH0], c->fld[TURB_F_SCRATCH1]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Conc_compute_total_concentration(turb_ctx *c)
+{
+    if (!c) return TURB_ERR_ARG;
+    ConcPtrs cp;
+    ConcW cw;
+    for (int i = 0; i < 4; i++) { cp.p[i] = i < c->prm.nconc ? c->fld[TURB_F_C0 + i] : nullptr; cw.v[i] = c->prm.alpha[i]; }
+    launch_total_conc(c->s, c->d.n, c->prm.nconc, cp, cw, c->fld[TURB_F_CTOT]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Conc_set_particle_v_velocity(turb_ctx *c, int ic)
+{
+    if (!c || ic < 0 || ic >= c->prm.nconc) return TURB_ERR_ARG;
+    double sh = c->prm.ctype[ic] == TURB_PARTICLE ? c->prm.vs0[ic] : 0.0;
+    if (c->prm.ctype[ic] == TURB_PARTICLE)
+        launch_shift(c->s, c->d.n, c->fld[TURB_F_VBC], sh, c->fld[TURB_F_VP0 + ic]);
+    else
+        cudaMemcpyAsync(c->fld[TURB_F_VP0 + ic], c->fld[TURB_F_VBC], c->d.n * 8, cudaMemcpyDeviceToDevice, c->s);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+static AdvSrc adv_of(int kind, const double *a, W2 wx, W2 wy, double shift = 0.0)
+{
+    AdvSrc s;
+    s.kind = kind;
+    s.a = a;
+    s.wx = wx;
+    s.wy = wy;
+    s.shift = shift;
+    return s;
+}
+
+int turb_Velocity_convective_terms(turb_ctx *c, char which)
+{
+    int q = qidx(which);
+    if (!c || q < 0 || q > 2) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    int nx = d.nx, ny = d.ny, nz = d.nz;
+    int i0 = q == 0 ? 1 : 0, j0 = q == 1 ? 1 : 0, k0 = q == 2 ? 1 : 0;
+    const double *u = c->fld[TURB_F_U], *v = c->fld[TURB_F_V], *w = c->fld[TURB_F_W];
+    const double *self = q == 0 ? u : q == 1 ? v : w;
+    double *conv = c->fld[TURB_F_CONV_U + q];
+    W2 z{nullptr, nullptr};
+    AdvSrc ax, ay, az;
+    if (q == 0) {
+        ax = adv_of(0, u, z, z);
+        ay = adv_of(2, v, c->tw.xu, c->tw.yc);
+        az = adv_of(3, w, c->tw.xu, c->tw.zc);
+    } else if (q == 1) {
+        ax = adv_of(4, u, c->tw.xc, c->tw.yv);
+        ay = adv_of(0, v, z, z);
+        az = adv_of(5, w, c->tw.zc, c->tw.yv);
+    } else {
+        ax = adv_of(6, u, c->tw.xc, c->tw.zw);
+        ay = adv_of(7, v, c->tw.zw, c->tw.yc);
+        az = adv_of(0, w, z, z);
+    }
+    cudaMemsetAsync(conv, 0, d.n * 8, c->s);
+    launch_eno_pass(c->s, d, 0, c->eno[q][0], self, ax, j0, ny - 1, k0, nz - 1, 1, conv);
+    launch_eno_pass(c->s, d, 1, c->eno[q][1], self, ay, i0, nx - 1, k0, nz - 1, 0, conv);
+    launch_eno_pass(c->s, d, 2, c->eno[q][2], self, az, i0, nx - 1, j0, ny - 1, 0, conv);
+    c->launches += 3;
+    return check_launch(c);
+}
+
+int turb_Conc_convective_terms(turb_ctx *c, int ic)
+{
+    if (!c || ic < 0 || ic >= c->prm.nconc) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    W2 z{nullptr, nullptr};
+    double *conv = c->fld[TURB_F_CCONV0 + ic];
+    const double *cf = c->fld[TURB_F_C0 + ic];
+    AdvSrc ax = adv_of(0, c->fld[TURB_F_UBC], z, z);
+    AdvSrc ay = c->prm.ctype[ic] == TURB_PARTICLE ? adv_of(1, c->fld[TURB_F_VBC], z, z, c->prm.vs0[ic])
+                                                  : adv_of(0, c->fld[TURB_F_VBC], z, z);
+    AdvSrc az = adv_of(0, c->fld[TURB_F_WBC], z, z);
+    cudaMemsetAsync(conv, 0, d.n * 8, c->s);
+    launch_eno_pass(c->s, d, 0, c->eno[3][0], cf, ax, 0, d.ny - 1, 0, d.nz - 1, 1, conv);
+    launch_eno_pass(c->s, d, 1, c->eno_cy[ic], cf, ay, 0, d.nx - 1, 0, d.nz - 1, 0, conv);
+    launch_eno_pass(c->s, d, 2, c->eno[3][2], cf, az, 0, d.nx - 1, 0, d.ny - 1, 0, conv);
+    c->launches += 3;
+    return check_launch(c);
+}
+
+int turb_Velocity_set_RHS(turb_ctx *c, char which, double dt)
+{
+    int q = qidx(which);
+    if (!c || q < 0 || q > 2 || !(dt > 0.0)) return TURB_ERR_ARG;
+    const double *ct = c->prm.nconc > 1 ? c->fld[TURB_F_CTOT] : c->fld[TURB_F_C0];
+    launch_rhs_vel(c->s, c->d, q, c->st[q], 1.0 / dt, c->fld[TURB_F_U + q], c->fld[TURB_F_CONV_U + q],
+                   c->fld[TURB_F_DPX + q], ct, c->prm.buoyancy, c->iyv, c->fld[TURB_F_B_U + q]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Conc_set_RHS(turb_ctx *c, int ic, double dt)
+{
+    if (!c || ic < 0 || ic >= c->prm.nconc || !(dt > 0.0)) return TURB_ERR_ARG;
+    launch_rhs_conc(c->s, c->d.n, c->st[3], 1.0 / dt, c->fld[TURB_F_C0 + ic], c->fld[TURB_F_CCONV0 + ic],
+                    c->fld[TURB_F_CB0 + ic]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+static int helm_solve(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int *iters)
+{
+    const Dims &d = c->d;
+    const HelmTab &h = q < 3 ? c->helm[q] : c->helm_c[ic];
+    const IbDev &ib = c->ib[q];
+    double a_dt = 1.0 / dt;
+    double *b = c->fld[fb];
+    launch_norm2(c->s, d.n, b, c->part, norm_parts(), c->dscal);
+    int rc = fetch_scalars(c, 1);
+    if (rc) return rc;
+    double nb = std::sqrt(c->hscal[0]);
+    long long hp = helm_parts(d);
+    long long np = hp + (ib.n > 0 ? (ib.n + 255) / 256 : 0);
+    int it = 0;
+    c->launches += 2;
+    for (;;) {
+        double *x = c->fld[fx];
+        launch_helm_jacobi(c->s, d, h, c->st[q], a_dt, b, x, c->jtmp, ib, c->part, hp);
+        launch_sum_final(c->s, np, c->part, c->dscal);
+        c->launches += 2 + (ib.n > 0);
+        rc = fetch_scalars(c, 1);
+        if (rc) return rc;
+        double nr = std::sqrt(c->hscal[0]);
+        if (!std::isfinite(nr)) { if (iters) *iters = it; return TURB_ERR_NAN; }
+        if (nr <= c->prm.vel_rtol * nb) break;
+        if (it >= c->prm.vel_maxit) { if (iters) *iters = it; return TURB_ERR_NOT_CONVERGED; }
+        // the non-immersed and immersed rows of jtmp are all written: swap
+        std::swap(c->fld[fx], c->jtmp);
+        it++;
+    }
+    if (iters) *iters = it;
+    return TURB_OK;
+}
+
+int turb_Velocity_solve(turb_ctx *c, char which, double dt, int *iters)
+{
+    int q = qidx(which);
+    if (!c || q < 0 || q > 2 || !(dt > 0.0)) return TURB_ERR_ARG;
+    return helm_solve(c, q, 0, TURB_F_U + q, TURB_F_B_U + q, dt, iters);
+}
+
+int turb_Conc_solve(turb_ctx *c, int ic, double dt, int *iters)
+{
+    if (!c || ic < 0 || ic >= c->prm.nconc || !(dt > 0.0)) return TURB_ERR_ARG;
+    return helm_solve(c, 3, ic, TURB_F_C0 + ic, TURB_F_CB0 + ic, dt, iters);
+}
+
+int turb_helmholtz_apply(turb_ctx *c, char which, int ic, double dt, int fx, int fy)
+{
+    int q = qidx(which);
+    if (!c || q < 0 || !(dt > 0.0) || !field_ptr(c, fx) || !field_ptr(c, fy)) return TURB_ERR_ARG;
+    if (q == 3 && (ic < 0 || ic >= c->prm.nconc)) return TURB_ERR_ARG;
+    launch_helm_apply(c->s, c->d, q < 3 ? c->helm[q] : c->helm_c[ic], c->st[q], 1.0 / dt, c->fld[fx], c->fld[fy],
+                      c->ib[q]);
+    c->launches += 2;
+    return check_launch(c);
+}
+
+int turb_Pressure_set_RHS(turb_ctx *c, double dt)
+{
+    if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
+    launch_pressure_rhs(c->s, c->d, c->st[3], c->pcx, c->pcy, c->pcz, 1.0 / dt, c->fld[TURB_F_U],
+                        c->fld[TURB_F_V], c->fld[TURB_F_W], c->fld[TURB_F_PB]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
+{
+    if (!c) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    const MgDevLevel &L0 = c->H64.lev[0];
+    long long n0 = (long long)L0.nx * L0.ny * L0.nz;
+    cudaStream_t s = c->s;
+    PcgScal *sc = c->sc;
+    double *dsc = reinterpret_cast<double *>(sc);   // bb rr rz zr_old rz_old pq alpha beta
+    pcg_gather(s, d, L0, c->fld[TURB_F_PHI], c->fld[TURB_F_PB], c->px, c->pbw);
+    pcg_dot(s, n0, c->pbw, c->pbw, c->part);
+    pcg_reduce(s, c->part, 1, dsc + 0);
+    pcg_resid(s, L0, c->pbw, c->px, c->pr, c->part);
+    pcg_reduce(s, c->part, 1, dsc + 1);
+    c->launches += 5;
+    TURB_CHECK(cudaMemcpyAsync(c->hscal, dsc, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    TURB_CHECK(cudaStreamSynchronize(s));
+    double nb = std::sqrt(c->hscal[0]), nr = std::sqrt(c->hscal[1]);
+    double tol = c->prm.p_rtol * nb;
+    int it = 0, restart = 1, status = TURB_OK;
+    const int npre = 2, npost = 2;
+    int vl = mg_vcycle_launches(c->H64.nl, npre, npost);
+    for (;;) {
+        if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
+        if (nr <= tol || it >= c->prm.p_maxit) {
+            pcg_resid(s, L0, c->pbw, c->px, c->pr, c->part);
+            pcg_reduce(s, c->part, 1, dsc + 1);
+            c->launches += 2;
+            TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+            TURB_CHECK(cudaStreamSynchronize(s));
+            nr = std::sqrt(c->hscal[1]);
+            if (nr <= tol) break;
+            if (it >= c->prm.p_maxit) { status = TURB_ERR_NOT_CONVERGED; break; }
+            restart = 1;
+        }
+        if (c->pmode == TURB_PMODE_FP64) {
+            mg_vcycle<double>(s, c->H64, 0, npre, npost);
+            c->launches += vl;
+        } else {
+            pcg_to_float(s, n0, c->pr, c->H32.b[0]);
+            mg_vcycle<float>(s, c->H32, 0, npre, npost);
+            pcg_to_double(s, n0, c->H32.x[0], c->pz);
+            c->launches += vl + 2;
+        }
+        pcg_dot2(s, n0, c->pr, c->pz, c->pro, c->part);
+        pcg_reduce(s, c->part, 2, dsc + 2);   // rz and z.r_old
+        c->launches += 2;
+        if (!restart) { pcg_scalars(s, sc, 0); c->launches += 1; }
+        pcg_pupdate(s, n0, c->pz, c->pp, sc, restart);
+        pcg_apply(s, L0, c->pp, c->pq, c->part);
+        pcg_reduce(s, c->part, 1, dsc + 5);
+        pcg_scalars(s, sc, 1);
+        pcg_xrupdate(s, n0, c->px, c->pr, c->pro, c->pp, c->pq, sc, c->part);
+        pcg_reduce(s, c->part, 1, dsc + 1);
+        c->launches += 6;
+        TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+        TURB_CHECK(cudaStreamSynchronize(s));
+        nr = std::sqrt(c->hscal[1]);
+        restart = 0;
+        it++;
+    }
+    pcg_scatter(s, d, L0, c->px, c->fld[TURB_F_PHI]);
+    c->launches += 1;
+    if (iters) *iters = it;
+    if (relres) *relres = nb > 0.0 ? nr / nb : 0.0;
+    int rc = check_launch(c);
+    return rc ? rc : status;
+}
+
+int turb_pressure_apply(turb_ctx *c, int fx, int fy)
+{
+    if (!c || !field_ptr(c, fx) || !field_ptr(c, fy)) return TURB_ERR_ARG;
+    launch_pressure_apply(c->s, c->d, c->st[3], c->geo, c->dEta, c->dXi, c->dPhi, c->fld[fx], c->fld[fy]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Pressure_project_velocity(turb_ctx *c, double dt)
+{
+    if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
+    ProjArgs a = c->proj;
+    a.dt = dt;
+    a.coef = dt / c->prm.re;
+    launch_project(c->s, c->d, a, c->fld[TURB_F_PHI], c->fld[TURB_F_PB], c->fld[TURB_F_U], c->fld[TURB_F_V],
+                   c->fld[TURB_F_W], c->fld[TURB_F_DPX], c->fld[TURB_F_DPY], c->fld[TURB_F_DPZ]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Pressure_compute_velocity_divergence(turb_ctx *c, double *div_max)
+{
+    if (!c) return TURB_ERR_ARG;
+    launch_divergence(c->s, c->d, c->st[3], c->geo.mxc, c->geo.myc, c->geo.mzc, 1.0 / c->dEta, 1.0 / c->dXi,
+                      1.0 / c->dPhi, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W], c->fld[TURB_F_DIV],
+                      c->part, c->dscal);
+    c->launches += 2;
+    int rc = check_launch(c);
+    if (rc) return rc;
+    if (div_max) {
+        rc = fetch_scalars(c, 1);
+        if (rc) return rc;
+        *div_max = c->hscal[0];
+    }
+    return TURB_OK;
+}
+
+int turb_store_old_data(turb_ctx *c)
+{
+    if (!c) return TURB_ERR_ARG;
+    size_t b = c->d.n * 8;
+    for (int q = 0; q < 3; q++)
+        TURB_CHECK(cudaMemcpyAsync(c->old[q], c->fld[TURB_F_U + q], b, cudaMemcpyDeviceToDevice, c->s));
+    for (int ic = 0; ic < c->prm.nconc; ic++)
+        TURB_CHECK(cudaMemcpyAsync(c->old[3 + ic], c->fld[TURB_F_C0 + ic], b, cudaMemcpyDeviceToDevice, c->s));
+    return TURB_OK;
+}
+
+int turb_rk_average(turb_ctx *c, double old_frac, double new_frac)
+{
+    if (!c) return TURB_ERR_ARG;
+    for (int q = 0; q < 3; q++) launch_axpby(c->s, c->d.n, old_frac, c->old[q], new_frac, c->fld[TURB_F_U + q]);
+    for (int ic = 0; ic < c->prm.nconc; ic++)
+        launch_axpby(c->s, c->d.n, old_frac, c->old[3 + ic], new_frac, c->fld[TURB_F_C0 + ic]);
+    c->launches += 3 + c->prm.nconc;
+    return check_launch(c);
+}
+
+#define STEP_TRY(x)                      \
+    do {                                 \
+        int rc_ = (x);                   \
+        if (rc_ != TURB_OK) return rc_;  \
+    } while (0)
+
+int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
+{
+    if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
+    turb_step_stats local;
+    if (!st) st = &local;
+    memset(st, 0, sizeof(*st));
+    long long l0 = c->launches;
+    STEP_TRY(turb_store_old_data(c));
+    for (int stage = 0; stage < 2; stage++) {
+        STEP_TRY(turb_Velocity_cell_center(c));
+        if (c->prm.nconc > 1) STEP_TRY(turb_Conc_compute_total_concentration(c));
+        STEP_TRY(turb_Velocity_convective_terms(c, 'u'));
+        STEP_TRY(turb_Velocity_convective_terms(c, 'v'));
+        STEP_TRY(turb_Velocity_convective_terms(c, 'w'));
+        for (int ic = 0; ic < c->prm.nconc; ic++) STEP_TRY(turb_Conc_convective_terms(c, ic));
+        STEP_TRY(turb_Velocity_set_RHS(c, 'u', dt));
+        STEP_TRY(turb_Velocity_set_RHS(c, 'v', dt));
+        STEP_TRY(turb_Velocity_set_RHS(c, 'w', dt));
+        STEP_TRY(turb_Velocity_solve(c, 'u', dt, &st->vel_iters[0][stage]));
+        STEP_TRY(turb_Velocity_solve(c, 'v', dt, &st->vel_iters[1][stage]));
+        STEP_TRY(turb_Velocity_solve(c, 'w', dt, &st->vel_iters[2][stage]));
+        for (int ic = 0; ic < c->prm.nconc; ic++) {
+            STEP_TRY(turb_Conc_set_RHS(c, ic, dt));
+            STEP_TRY(turb_Conc_solve(c, ic, dt, &st->conc_iters[ic][stage]));
+        }
+        STEP_TRY(turb_Pressure_set_RHS(c, dt));
+        STEP_TRY(turb_Pressure_solve(c, &st->p_iters[stage], &st->p_relres[stage]));
+        STEP_TRY(turb_Pressure_project_velocity(c, dt));
+        STEP_TRY(turb_Pressure_compute_velocity_divergence(c, &st->div_max[stage]));
+    }
+    STEP_TRY(turb_rk_average(c, 0.5, 0.5));
+    st->kernel_launches = (int)(c->launches - l0);
+    return TURB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// unweighted pressure operator (Pressure_form_LHS_matrix rows), for parity
+// tests of the operator the MG-CG solves
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void k_pressure_apply(Dims d, const uint8_t *__restrict__ st, Geo g, double dEta, double dXi, double dPhi,
+                                 const double *__restrict__ x, double *__restrict__ y)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int k = blockIdx.y;
+    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
+    if (j >= d.NY) return;
+    long long p = d.at(i, j, k);
+    double Cx = -1.0 / (dEta * dEta), Cy = -1.0 / (dXi * dXi), Cz = -1.0 / (dPhi * dPhi);
+    if (st[p] == T_BOUNDARY) {
+        double aps = -Cx * g.mxc[0] - Cy * g.myc[0] - Cz * g.mzc[0];
+        y[p] = aps * x[p];
+        return;
+    }
+    int NI = d.nx, NJ = d.ny, NK = d.nz;
+    double px = g.mxc[i], py = g.myc[j], pz = g.mzc[k];
+    double ex = g.mxu[i + 1], wx = g.mxu[i], ny_ = g.myv[j + 1], sy = g.myv[j], fz = g.mzw[k + 1], bz = g.mzw[k];
+    double ap = -Cx * px * (ex + wx) - Cy * py * (ny_ + sy) - Cz * pz * (bz + fz);
+    double aw = Cx * px * wx, ae = Cx * px * ex, an = Cy * py * ny_, as = Cy * py * sy, ab = Cz * pz * bz,
+           af = Cz * pz * fz, acc = 0.0;
+    if (k > 0) acc += ab * x[p - d.plane]; else ap += ab;
+    if (j > 0) acc += as * x[p - d.PX]; else ap += as;
+    if (i > 0) acc += aw * x[p - 1]; else ap += aw;
+    if (i < NI - 1) acc += ae * x[p + 1];
+    else if (!(i == NI - 1 && j == NJ - 1 && k == NK - 1)) ap += ae;
+    if (j < NJ - 1) acc += an * x[p + d.PX]; else ap += an;
+    if (k < NK - 1) acc += af * x[p + d.plane]; else ap += af;
+    y[p] = acc + ap * x[p];
+}
+}  // namespace
+
+void launch_pressure_apply(cudaStream_t s, const Dims &d, const uint8_t *st, const Geo &g, double dEta, double dXi,
+                           double dPhi, const double *x, double *y)
+{
+    long long nij = (long long)d.NX * d.NY;
+    dim3 gr((unsigned)((nij + 255) / 256), d.NZ);
+    k_pressure_apply<<<gr, 256, 0, s>>>(d, st, g, dEta, dXi, dPhi, x, y);
+}

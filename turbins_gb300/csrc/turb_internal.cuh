@@ -1,0 +1,99 @@
+// turb_internal.cuh -- device-side data layout shared by the kernels.
+//
+// Field layout in HBM: the DA order of the reference, [k][j][i] with i
+// fastest, with the i-row padded to a pitch PX = round_up(NX, 8) doubles so
+// that every row starts on a 64-byte boundary (TMA/vector friendly).  A field
+// holds PX*NY*NZ doubles; the pad columns stay zero.  The pressure multigrid
+// works on compact per-level arrays of the physical cells (nx*ny*nz).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define T_SOLID 2
+#define T_FLUID 3
+#define T_IMMERSED 5
+#define T_BOUNDARY 7
+#define T_BUFFER_SOLID 11
+
+struct Dims {
+    int nx, ny, nz;      // physical cells
+    int NX, NY, NZ;      // DA points (cells + 1)
+    int PX;              // padded row pitch (doubles)
+    long long plane;     // PX*NY
+    long long n;         // PX*NY*NZ
+    __host__ __device__ long long at(int i, int j, int k) const
+    {
+        return ((long long)k * NY + j) * PX + i;
+    }
+};
+
+// 1-D grid arrays on the device (coordinates and metrics of Grid.c:595-708)
+struct Geo {
+    const double *xc, *yc, *zc, *xu, *yv, *zw;
+    const double *mxc, *myc, *mzc, *mxu, *myv, *mzw;
+};
+
+// Two-point interpolation table (MyMath.c:13-43): node value at xq from
+// (x0, x1): dx = x1 - x0, dq = xq - x0, flat = |dx| < 1e-8.
+struct Interp2 {
+    const double *dx, *dq;
+    const uint8_t *flat;
+};
+
+// Four-point bilinear weights of MyMath.c:54-74 along one direction:
+// W0 = |(xq - X0) / (X1 - X0)| (as a_D * (xq - X0)), W1 = 1 - W0.
+struct W2 {
+    const double *w0, *w1;
+};
+
+// ENO line tables of one (quantity, direction): buffer index b in [0, nb),
+// interior node m = b - r + s0 for b in [r, nb - r).  Denominators and the
+// stencil-position factors depend only on the grid and are built on the host
+// with the reference's own expressions (ENO.c:159-244, ghost positions of the
+// *_ENO_ghost_cells routines), so device results round identically.
+struct EnoTab {
+    int r, s0, e0, nb;
+    const double *h1;    // P[b+1]-P[b]
+    const double *h2;    // P[b+1]-P[b-1]
+    const double *h3;    // P[b+2]-P[b-1]
+    const double *g2;    // [nb*2]: k=b-1, k=b  -> (x_i-x_k)+(x_i-x_k1)
+    const double *g3;    // [nb*3]: kstar=b-2,b-1,b -> three-product sum
+    int gsrc[6];         // ghost b<r: [0..r), ghost b>=nb-r: [3..3+r) by ex
+    double gm[6];        // 0: zero, 1: m*q[s0], 2: m*q[e0]
+};
+
+struct IbDev {
+    int n;
+    const int32_t *im;   // linear index in the pitched layout
+    const int32_t *cnt;  // number of off-diagonal entries kept
+    const int32_t *col;  // [n*8] pitched indices of kept off-diagonal entries
+    const double *val;   // [n*8] ap_solid * fluid_coef
+    const double *diag;  // [n]   ap_solid * (1 + sum of self coefficients)
+};
+
+// 1-D coefficient tables of one Helmholtz operator (separable rows of the
+// *_form_LHS_matrix routines, wall folding included)
+struct HelmTab {
+    const double *apx, *apy, *apz;   // ap = apx[i] + apy[j] + apz[k]
+    const double *aw, *ae, *as, *an, *ab, *af;   // 0 where the entry is absent
+    double ap_solid;
+    int q;                           // 0 u, 1 v, 2 w, 3 c
+};
+
+// Multigrid level (compact nx*ny*nz layout)
+struct MgLevel {
+    int nx, ny, nz;
+    long long n;
+    int cx, cy, cz;          // coarsened into the next level along x/y/z
+    const double *rfx, *rfy, *rfz;  // 1/face distance [n+1]
+    const double *dx, *dy, *dz;     // widths
+    double pin;                     // corner east-face coefficient
+};
+
+#define TURB_CHECK(x)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (x);                                                  \
+        if (e_ != cudaSuccess) return turb_set_cuda_error(e_, __FILE__, __LINE__); \
+    } while (0)
+
+int turb_set_cuda_error(cudaError_t e, const char *file, int line);

@@ -1,0 +1,48 @@
+// turb_mg.cuh -- multigrid hierarchy descriptors (device pointers).
+#pragma once
+#include "turb_internal.cuh"
+
+#define TURB_MG_MAXLEV 24
+
+struct MgDevLevel {
+    int nx, ny, nz;
+    int cx, cy, cz;                                   // coarsened into next level
+    const double *dxd, *dyd, *dzd, *rfxd, *rfyd, *rfzd;
+    const float *dxf, *dyf, *dzf, *rfxf, *rfyf, *rfzf;
+    double pin;
+};
+
+template <typename T>
+struct MgHier {
+    int nl;
+    MgDevLevel lev[TURB_MG_MAXLEV];
+    T *x[TURB_MG_MAXLEV], *b[TURB_MG_MAXLEV], *r[TURB_MG_MAXLEV], *invd[TURB_MG_MAXLEV];
+    const double *coarse_inv;
+};
+
+template <typename T>
+void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd);
+template <typename T>
+void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost);
+int mg_vcycle_launches(int nl, int npre, int npost);
+
+// FP64 CG vector kernels on the compact level-0 layout (k_pcg.cu)
+struct PcgScal {
+    double bb, rr, rz, zr_old, rz_old, pq, alpha, beta;   // slot order is used by the reductions
+};
+void pcg_gather(cudaStream_t s, const Dims &d, const MgDevLevel &L0, const double *phi_da, const double *pb_da,
+                double *x, double *bw);
+void pcg_scatter(cudaStream_t s, const Dims &d, const MgDevLevel &L0, const double *x, double *phi_da);
+void pcg_resid(cudaStream_t s, const MgDevLevel &L0, const double *bw, const double *x, double *r, double *part);
+void pcg_apply(cudaStream_t s, const MgDevLevel &L0, const double *p, double *q, double *part);
+void pcg_dot(cudaStream_t s, long long n, const double *a, const double *b, double *part);
+void pcg_dot2(cudaStream_t s, long long n, const double *r, const double *z, const double *rold, double *part);
+void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst);
+void pcg_pupdate(cudaStream_t s, long long n, const double *z, double *p, const PcgScal *sc, int first);
+void pcg_xrupdate(cudaStream_t s, long long n, double *x, double *r, double *rold, const double *p,
+                  const double *q, const PcgScal *sc, double *part);
+void pcg_scalars(cudaStream_t s, PcgScal *sc, int what);
+void pcg_to_float(cudaStream_t s, long long n, const double *a, float *b);
+void pcg_to_double(cudaStream_t s, long long n, const float *a, double *b);
+void pcg_copy(cudaStream_t s, long long n, const double *a, double *b);
+int pcg_nparts();
