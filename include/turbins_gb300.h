@@ -171,6 +171,26 @@ int turb_rk_average(turb_ctx *ctx, double old_frac, double new_frac);
 /* one TVD-RK2 step of the restated driver (the absent main loop) */
 int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
 
+/* ---- measurement ---------------------------------------------------------
+ * CUDA-event timing per kernel group on the context stream (enable resets the
+ * accumulators; read synchronizes and returns ms and launches per group). */
+#define TURB_PROF_ENO_X 0      /* x-direction ENO passes                        */
+#define TURB_PROF_ENO_YZ 1     /* y/z-direction ENO passes                      */
+#define TURB_PROF_JACOBI 2     /* Helmholtz Jacobi sweeps                       */
+#define TURB_PROF_MG 3         /* multigrid V-cycles (all levels)               */
+#define TURB_PROF_PCG 4        /* FP64 CG vector kernels and reductions         */
+#define TURB_PROF_NGROUPS 5
+int turb_profile_enable(turb_ctx *ctx, int on);
+int turb_profile_read(turb_ctx *ctx, double *ms, long long *launches);
+/* events 0..7 on the context stream; elapsed waits for event b */
+int turb_event_record(turb_ctx *ctx, int slot);
+int turb_event_elapsed(turb_ctx *ctx, int a, int b, double *ms);
+/* number of this library's kernel launches issued by ctx so far */
+int turb_kernel_launches(turb_ctx *ctx, long long *n);
+/* page-lock caller memory for the host-buffer transfers */
+int turb_host_register(void *ptr, size_t bytes);
+int turb_host_unregister(void *ptr);
+
 /* operator hooks used by the parity tests: y = A x on device fields */
 int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);
 int turb_pressure_apply(turb_ctx *ctx, int field_x, int field_y);

@@ -1,0 +1,297 @@
+/*
+ * ref_harness.c -- drives the reference's own routines, compiled unmodified
+ * against the single-rank PETSc shim, on caller-supplied arrays (TEST
+ * INFRASTRUCTURE ONLY).  Linked with the reference sources into
+ * oracle/_ref/libturbins_ref.so by oracle/refbuild.py; used to pin the CPU
+ * oracle (turb_oracle.c) and to generate tests/golden fixtures.
+ *
+ * Arrays are DA-ordered doubles of (nx+1)(ny+1)(nz+1) points.  The harness
+ * builds the MAC_grid by hand (coordinates + the reference's
+ * Grid_compute_metric_coefficients), fills the status vectors and the
+ * ImmersedNode stencils, and creates the Velocity / Pressure / Concentration
+ * objects with the reference's *_create routines.
+ */
+#include "definitions.h"
+#include "DataTypes.h"
+#include "ENO.h"
+#include "Grid.h"
+#include "Immersed.h"
+#include "Velocity.h"
+#include "Conc.h"
+#include "Pressure.h"
+#include <string.h>
+
+typedef struct {
+    MAC_grid *g;
+    Parameters *p;
+    Velocity *u, *v, *w;
+    Pressure *pr;
+    Concentration *c[4];
+    ENO_Scheme *eno;
+    long n;
+} ref_case;
+
+static void vset(Vec v, const double *a, long n) { memcpy(shim_vec_data(v), a, sizeof(double) * n); }
+static void vget(Vec v, double *a, long n) { memcpy(a, shim_vec_data(v), sizeof(double) * n); }
+
+ref_case *ref_create(int nx, int ny, int nz, const double *xc, const double *yc, const double *zc,
+                     const double *xu, const double *yv, const double *zw, const unsigned char *st_u,
+                     const unsigned char *st_v, const unsigned char *st_w, const unsigned char *st_c,
+                     int eno_order, double re, int nconc, const double *pe, const double *vs0,
+                     const double *alpha, const int *ctype, int sedimentation)
+{
+    ref_case *r = (ref_case *)calloc(1, sizeof(ref_case));
+    Parameters *p = (Parameters *)calloc(1, sizeof(Parameters));
+    MAC_grid *g = (MAC_grid *)calloc(1, sizeof(MAC_grid));
+    int NX = nx + 1, NY = ny + 1, NZ = nz + 1, i;
+    long n = (long)NX * NY * NZ, t;
+    const unsigned char *st[4] = {st_u, st_v, st_w, st_c};
+    Vec *gs[4], *ls[4];
+    double ***sp[4];
+    r->g = g; r->p = p; r->n = n;
+    p->NX = nx; p->NY = ny; p->NZ = nz;
+    p->Re = re; p->NConc = nconc; p->ENO_scheme_order = eno_order;
+    p->Pe = (double *)calloc(4, sizeof(double)); p->Phi = (double *)calloc(4, sizeof(double));
+    p->Conc_alpha = (double *)calloc(4, sizeof(double)); p->V_s0 = (double *)calloc(4, sizeof(double));
+    p->conc_type = (int *)calloc(4, sizeof(int));
+    for (i = 0; i < nconc; i++) {
+        p->Pe[i] = pe[i]; p->V_s0[i] = vs0[i]; p->Conc_alpha[i] = alpha[i]; p->conc_type[i] = ctype[i];
+    }
+    p->sedimentation = (short)sedimentation;
+    p->viscosity_type = CONSTANT_VISCOSITY;
+    p->resmax = 1e-12;
+    p->xmin = xu[0]; p->ymin = yv[0]; p->zmin = zw[0];
+    /* grid */
+    g->NX = NX; g->NY = NY; g->NZ = NZ; g->NT = NX * NY * NZ;
+    g->NI = NX - 1; g->NJ = NY - 1; g->NK = NZ - 1;
+    g->dEta = 1.0 / (double)nx; g->dXi = 1.0 / (double)ny; g->dPhi = 1.0 / (double)nz;
+    g->G_Is = g->G_Js = g->G_Ks = 0; g->G_Ie = NX; g->G_Je = NY; g->G_Ke = NZ;
+    g->L_Is = g->L_Js = g->L_Ks = 0; g->L_Ie = NX; g->L_Je = NY; g->L_Ke = NZ;
+    DACreate3d(PCW, DA_NONPERIODIC, DA_STENCIL_STAR, NX, NY, NZ, 1, 1, 1, 1, eno_order, 0, 0, 0, &g->DA_3D);
+    DACreate3d(PCW, DA_NONPERIODIC, DA_STENCIL_BOX, NX, NY, NZ, 1, 1, 1, 1, 3, 0, 0, 0, &g->DA_3D_BOX);
+    DACreate3d(PCW, DA_NONPERIODIC, DA_STENCIL_STAR, NX, NY, NZ, 1, 1, 1, 1, 1, 0, 0, 0, &g->DA_3D_Lsys);
+#define A1(name, len) g->name = (double *)calloc((size_t)(len), sizeof(double))
+    A1(xc, NX); A1(yc, NY); A1(zc, NZ); A1(xu, NX); A1(yu, NY); A1(zu, NZ); A1(xv, NX); A1(yv, NY); A1(zv, NZ);
+    A1(xw, NX); A1(yw, NY); A1(zw, NZ); A1(metric_xc, NX); A1(metric_yc, NY); A1(metric_zc, NZ);
+    A1(metric_xu, NX); A1(metric_yv, NY); A1(metric_zw, NZ); A1(dx_c, NX); A1(dy_c, NY); A1(dz_c, NZ);
+#undef A1
+    memcpy(g->xc, xc, 8 * NX); memcpy(g->yc, yc, 8 * NY); memcpy(g->zc, zc, 8 * NZ);
+    memcpy(g->xu, xu, 8 * NX); memcpy(g->yv, yv, 8 * NY); memcpy(g->zw, zw, 8 * NZ);
+    /* aliases of Grid_import_grid_from_file, Grid.c:1366-1378 */
+    memcpy(g->xv, xc, 8 * NX); memcpy(g->xw, xc, 8 * NX); memcpy(g->yu, yc, 8 * NY);
+    memcpy(g->yw, yc, 8 * NY); memcpy(g->zu, zc, 8 * NZ); memcpy(g->zv, zc, 8 * NZ);
+    Grid_compute_metric_coefficients(g, 'u');
+    Grid_compute_metric_coefficients(g, 'v');
+    Grid_compute_metric_coefficients(g, 'w');
+    Grid_compute_metric_coefficients(g, 'c');
+    gs[0] = &g->G_u_status; gs[1] = &g->G_v_status; gs[2] = &g->G_w_status; gs[3] = &g->G_c_status;
+    ls[0] = &g->L_u_status; ls[1] = &g->L_v_status; ls[2] = &g->L_w_status; ls[3] = &g->L_c_status;
+    for (i = 0; i < 4; i++) {
+        double *a;
+        DACreateGlobalVector(g->DA_3D_BOX, gs[i]);
+        *ls[i] = *gs[i];
+        a = shim_vec_data(*gs[i]);
+        for (t = 0; t < n; t++) a[t] = (double)st[i][t];
+    }
+    DAVecGetArray(g->DA_3D_BOX, g->L_u_status, (void ***)&g->u_status);
+    DAVecGetArray(g->DA_3D_BOX, g->L_v_status, (void ***)&g->v_status);
+    DAVecGetArray(g->DA_3D_BOX, g->L_w_status, (void ***)&g->w_status);
+    DAVecGetArray(g->DA_3D_BOX, g->L_c_status, (void ***)&g->c_status);
+    (void)sp;
+    DACreateGlobalVector(g->DA_3D, &g->lsys_diagonal);
+    DACreateGlobalVector(g->DA_3D, &g->G_dummy1); g->L_dummy1 = g->G_dummy1;
+    DACreateGlobalVector(g->DA_3D, &g->G_dummy2); g->L_dummy2 = g->G_dummy2;
+    r->u = Velocity_create(g, p, 'u');
+    r->v = Velocity_create(g, p, 'v');
+    r->w = Velocity_create(g, p, 'w');
+    r->pr = Pressure_create(g, p);
+    for (i = 0; i < nconc; i++) r->c[i] = Conc_create(g, p, i);
+    r->eno = ENO_create(p);
+    return r;
+}
+
+/* immersed stencils of quantity q: im/fidx are DA linear indices */
+void ref_set_immersed(ref_case *r, char q, int n, const int *im, const int *nf, const int *fidx,
+                      const double *fcoef, const double *bcoef)
+{
+    MAC_grid *g = r->g;
+    Immersed *I;
+    int NX = g->NX, NY = g->NY, t, k;
+    I = Immersed_create(g, q);
+    if (q == 'u') g->u_immersed = I;
+    else if (q == 'v') g->v_immersed = I;
+    else if (q == 'w') g->w_immersed = I;
+    else g->c_immersed = I;
+    Immersed_set_q_immersed_indices(g, q);
+    Immersed_set_q_immersed_boundary_condition(g, q);
+    for (t = 0; t < n; t++) {
+        int ii = im[t] % NX, jj = (im[t] / NX) % NY, kk = im[t] / (NX * NY);
+        int gi = Immersed_get_ib_global_index(I, ii, jj, kk);
+        ImmersedNode *nd = Immersed_get_ib_node(I, gi);
+        nd->n_fluid = nf[t];
+        nd->boundary_coef = bcoef[t];
+        for (k = 0; k < nf[t]; k++) {
+            int f = fidx[t * 8 + k];
+            nd->fluid_index[k].x_index = f % NX;
+            nd->fluid_index[k].y_index = (f / NX) % NY;
+            nd->fluid_index[k].z_index = f / (NX * NY);
+            nd->fluid_coef[k] = fcoef[t * 8 + k];
+        }
+    }
+}
+
+void ref_eno_line(ref_case *r, int order, int n, const double *D0, const double *P, const double *V, double *out)
+{
+    /* a scheme sized for this line (ENO_create sizes its buffers from NX/NY/NZ) */
+    Parameters tmp = *r->p;
+    ENO_Scheme *e;
+    tmp.NX = n; tmp.NY = 1; tmp.NZ = 1; tmp.ENO_scheme_order = order;
+    e = ENO_create(&tmp);
+    memcpy(e->D0, D0, 8 * n); memcpy(e->Position, P, 8 * n); memcpy(e->Velocity, V, 8 * n);
+    memset(e->VdQdX, 0, 8 * n);
+    ENO_compute_convective_terms(e, n);
+    memcpy(out, e->VdQdX, 8 * n);
+    ENO_destroy(e);
+}
+
+static Velocity *vel_of(ref_case *r, char q) { return q == 'u' ? r->u : q == 'v' ? r->v : r->w; }
+
+void ref_cell_center(ref_case *r, const double *u, const double *v, const double *w, double *ub, double *vb, double *wb)
+{
+    long n = r->n;
+    vset(r->u->G_data, u, n); vset(r->v->G_data, v, n); vset(r->w->G_data, w, n);
+    VecSet(r->u->G_data_bc, 0.0); VecSet(r->v->G_data_bc, 0.0); VecSet(r->w->G_data_bc, 0.0);
+    Velocity_cell_center(r->u, r->v, r->w, r->g, r->p);
+    vget(r->u->G_data_bc, ub, n); vget(r->v->G_data_bc, vb, n); vget(r->w->G_data_bc, wb, n);
+}
+
+void ref_transpose(ref_case *r, char q, const double *u, const double *v, const double *w, double *A, double *B)
+{
+    long n = r->n;
+    vset(r->u->L_data, u, n); vset(r->v->L_data, v, n); vset(r->w->L_data, w, n);
+    VecSet(r->g->G_dummy1, 0.0); VecSet(r->g->G_dummy2, 0.0);
+    Velocity_transpose_velocities(r->u, r->v, r->w, r->g, r->p, q);
+    vget(r->g->G_dummy1, A, n); vget(r->g->G_dummy2, B, n);
+}
+
+/* ghost cells of one line: buffer D0/P (length nbuf) holds the interior at
+ * [order, nbuf-order); the routine fills the ghosts in place */
+void ref_ghost_cells(ref_case *r, char q, int ic, char dir, int i0, int j0, int k0, int i1, int j1, int k1,
+                     int nbuf, double *D0, double *P)
+{
+    ENO_Scheme *e = r->eno;
+    Indices s, t;
+    s.x_index = i0; s.y_index = j0; s.z_index = k0;
+    t.x_index = i1; t.y_index = j1; t.z_index = k1;
+    memcpy(e->D0, D0, 8 * nbuf); memcpy(e->Position, P, 8 * nbuf);
+    if (q == 'u') Velocity_u_ENO_ghost_cells(e, r->u, r->g, r->p, s, t, dir);
+    else if (q == 'v') Velocity_v_ENO_ghost_cells(e, r->v, r->g, r->p, s, t, dir);
+    else if (q == 'w') Velocity_w_ENO_ghost_cells(e, r->w, r->g, r->p, s, t, dir);
+    else Conc_ENO_ghost_cells(e, r->c[ic], r->g, r->p, s, t, dir);
+    memcpy(D0, e->D0, 8 * nbuf); memcpy(P, e->Position, 8 * nbuf);
+}
+
+void ref_set_rhs_vel(ref_case *r, char q, double dt, const double *x, const double *conv, const double *dp,
+                     const double *ctot, double *b)
+{
+    long n = r->n;
+    Velocity *V = vel_of(r, q);
+    vset(V->G_data, x, n);
+    vset(V->G_conv, conv, n);
+    if (q == 'u') { vset(r->pr->G_dp_dx, dp, n); Velocity_u_set_RHS(V, r->pr, r->g, r->p, dt); }
+    else if (q == 'w') { vset(r->pr->G_dp_dz, dp, n); Velocity_w_set_RHS(V, r->pr, r->g, r->p, dt); }
+    else {
+        vset(r->pr->G_dp_dy, dp, n);
+        if (r->p->NConc > 1) vset(r->c[0]->G_c_total, ctot, n);
+        else vset(r->c[0]->G_data, ctot, n);
+        Velocity_v_set_RHS(V, r->pr, r->c, r->g, r->p, dt);
+    }
+    vget(V->G_b, b, n);
+}
+
+void ref_set_rhs_conc(ref_case *r, int ic, double dt, const double *c, const double *conv, double *b)
+{
+    long n = r->n;
+    vset(r->c[ic]->G_data, c, n);
+    vset(r->c[ic]->G_conv, conv, n);
+    Conc_set_RHS(r->c[ic], r->g, r->p, dt);
+    vget(r->c[ic]->G_b, b, n);
+}
+
+void ref_total_concentration(ref_case *r, const double *const *c, double *ct)
+{
+    long n = r->n;
+    int i;
+    for (i = 0; i < r->p->NConc; i++) vset(r->c[i]->G_data, c[i], n);
+    Conc_compute_total_concentration(r->c, r->p);
+    vget(r->c[0]->G_c_total, ct, n);
+}
+
+/* y = (LHS + 1/dt on non-immersed rows) x, assembled by the reference */
+void ref_lhs_apply(ref_case *r, char q, int ic, double dt, const double *x, double *y)
+{
+    Mat A;
+    if (q == 'c') {
+        Concentration *c = r->c[ic];
+        MatDestroy(c->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &c->A);
+        Conc_form_LHS_matrix(c, r->g, r->p);
+        Conc_modify_diagonal(c, r->g, dt, 0.0);
+        A = c->A;
+    } else {
+        Velocity *V = vel_of(r, q);
+        MatDestroy(V->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &V->A);
+        if (q == 'u') Velocity_u_form_LHS_matrix(V, r->g, r->p);
+        else if (q == 'v') Velocity_v_form_LHS_matrix(V, r->g, r->p);
+        else Velocity_w_form_LHS_matrix(V, r->g, r->p);
+        Velocity_modify_diagonal(V, r->g, r->p, dt, 0.0);
+        A = V->A;
+    }
+    shim_mat_mult(A, x, y);
+}
+
+void ref_pressure_apply(ref_case *r, const double *x, double *y)
+{
+    MatDestroy(r->pr->A);
+    DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &r->pr->A);
+    Pressure_form_LHS_matrix(r->pr, r->g);
+    shim_mat_mult(r->pr->A, x, y);
+}
+
+void ref_pressure_rhs(ref_case *r, double dt, const double *u, const double *v, const double *w, double *b)
+{
+    long n = r->n;
+    vset(r->u->L_data, u, n); vset(r->v->L_data, v, n); vset(r->w->L_data, w, n);
+    Pressure_set_RHS(r->pr, r->u, r->v, r->w, r->g, r->p, dt);
+    vget(r->pr->G_b, b, n);
+}
+
+void ref_project(ref_case *r, double dt, const double *phi, const double *pb, double *u, double *v, double *w,
+                 double *dpx, double *dpy, double *dpz)
+{
+    long n = r->n;
+    vset(r->pr->G_data, phi, n); vset(r->pr->G_b, pb, n);
+    vset(r->u->G_data, u, n); vset(r->v->G_data, v, n); vset(r->w->G_data, w, n);
+    vset(r->pr->G_dp_dx, dpx, n); vset(r->pr->G_dp_dy, dpy, n); vset(r->pr->G_dp_dz, dpz, n);
+    Pressure_project_velocity(r->pr, r->u, r->v, r->w, r->g, r->p, dt);
+    vget(r->u->G_data, u, n); vget(r->v->G_data, v, n); vget(r->w->G_data, w, n);
+    vget(r->pr->G_dp_dx, dpx, n); vget(r->pr->G_dp_dy, dpy, n); vget(r->pr->G_dp_dz, dpz, n);
+}
+
+double ref_divergence(ref_case *r, const double *u, const double *v, const double *w, double *div)
+{
+    long n = r->n;
+    double m;
+    vset(r->u->G_data, u, n); vset(r->v->G_data, v, n); vset(r->w->G_data, w, n);
+    m = Pressure_compute_velocity_divergence(r->pr, r->u, r->v, r->w, r->g, r->p);
+    vget(r->pr->G_divergence, div, n);
+    return m;
+}
+
+void ref_metrics(ref_case *r, double *mxc, double *myc, double *mzc, double *mxu, double *myv, double *mzw)
+{
+    MAC_grid *g = r->g;
+    memcpy(mxc, g->metric_xc, 8 * g->NX); memcpy(myc, g->metric_yc, 8 * g->NY); memcpy(mzc, g->metric_zc, 8 * g->NZ);
+    memcpy(mxu, g->metric_xu, 8 * g->NX); memcpy(myv, g->metric_yv, 8 * g->NY); memcpy(mzw, g->metric_zw, 8 * g->NZ);
+}

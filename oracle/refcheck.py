@@ -1,0 +1,182 @@
+"""ctypes binding of oracle/_ref/libturbins_ref.so, the reference's own
+routines compiled against the PETSc shim (TEST INFRASTRUCTURE ONLY).
+
+Used to pin the CPU oracle and to regenerate tests/golden.  Includes the
+restated line driver (the reference has none) expressed with the reference's
+own ghost-cell routines and ENO_compute_convective_terms.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import refbuild
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_ubyte)
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def available():
+    return os.path.exists(refbuild.LIB) or refbuild.available()
+
+
+class Reference:
+    def __init__(self, grid, params):
+        lib = C.CDLL(refbuild.build())
+        lib.ref_create.restype = C.c_void_p
+        lib.ref_divergence.restype = C.c_double
+        for f in ("ref_set_immersed", "ref_eno_line", "ref_cell_center", "ref_transpose", "ref_ghost_cells",
+                  "ref_set_rhs_vel", "ref_set_rhs_conc", "ref_total_concentration", "ref_lhs_apply",
+                  "ref_pressure_apply", "ref_pressure_rhs", "ref_project", "ref_divergence", "ref_metrics"):
+            getattr(lib, f).argtypes = None
+        self.lib = lib
+        self.g = grid
+        self.p = params
+        self._keep = []
+        st = [np.ascontiguousarray(grid.status[q], dtype=np.uint8) for q in "uvwc"]
+        self._keep += st
+        n = params.nconc
+        pe = np.array(list(params.pe) + [0] * 4, dtype=np.float64)[:4]
+        vs = np.array(list(params.vs0) + [0] * 4, dtype=np.float64)[:4]
+        al = np.array(list(params.alpha) + [0] * 4, dtype=np.float64)[:4]
+        ct = np.array(list(params.ctype) + [0] * 4, dtype=np.int32)[:4]
+        co = [np.ascontiguousarray(getattr(grid, k), dtype=np.float64) for k in ("xc", "yc", "zc", "xu", "yv", "zw")]
+        self._keep += co + [pe, vs, al, ct]
+        self.h = C.c_void_p(lib.ref_create(C.c_int(grid.nx), C.c_int(grid.ny), C.c_int(grid.nz),
+                                           *[_p(a) for a in co], *[_p(s, _up) for s in st],
+                                           C.c_int(params.eno_order), C.c_double(params.re), C.c_int(n), _p(pe),
+                                           _p(vs), _p(al), _p(ct, _ip), C.c_int(params.sedimentation)))
+        for q in "uvwc":
+            ib = grid.ib.get(q)
+            if ib is None:
+                continue
+            arrs = [np.ascontiguousarray(ib["im"], dtype=np.int32), np.ascontiguousarray(ib["nf"], dtype=np.int32),
+                    np.ascontiguousarray(ib["fidx"], dtype=np.int32), np.ascontiguousarray(ib["fcoef"], dtype=np.float64),
+                    np.ascontiguousarray(ib["bcoef"], dtype=np.float64)]
+            self._keep += arrs
+            lib.ref_set_immersed(self.h, C.c_char(q.encode()), C.c_int(int(ib["n"])), _p(arrs[0], _ip),
+                                 _p(arrs[1], _ip), _p(arrs[2], _ip), _p(arrs[3]), _p(arrs[4]))
+
+    def _z(self):
+        return np.zeros(self.g.shape)
+
+    def metrics(self):
+        g = self.g
+        out = [np.zeros(g.nx + 1), np.zeros(g.ny + 1), np.zeros(g.nz + 1), np.zeros(g.nx + 1), np.zeros(g.ny + 1),
+               np.zeros(g.nz + 1)]
+        self.lib.ref_metrics(self.h, *[_p(a) for a in out])
+        return dict(zip(("mxc", "myc", "mzc", "mxu", "myv", "mzw"), out))
+
+    def eno_line(self, order, D0, P, V):
+        D0, P, V = [np.ascontiguousarray(a, dtype=np.float64) for a in (D0, P, V)]
+        out = np.zeros(len(D0))
+        self.lib.ref_eno_line(self.h, C.c_int(order), C.c_int(len(D0)), _p(D0), _p(P), _p(V), _p(out))
+        return out
+
+    def cell_center(self, u, v, w):
+        a, b, c = self._z(), self._z(), self._z()
+        self.lib.ref_cell_center(self.h, _p(u), _p(v), _p(w), _p(a), _p(b), _p(c))
+        return a, b, c
+
+    def transpose(self, q, u, v, w):
+        A, B = self._z(), self._z()
+        self.lib.ref_transpose(self.h, C.c_char(q.encode()), _p(u), _p(v), _p(w), _p(A), _p(B))
+        return A, B
+
+    def set_rhs_vel(self, q, dt, x, conv, dp, ctot):
+        b = self._z()
+        self.lib.ref_set_rhs_vel(self.h, C.c_char(q.encode()), C.c_double(dt), _p(x), _p(conv), _p(dp), _p(ctot),
+                                 _p(b))
+        return b
+
+    def set_rhs_conc(self, ic, dt, c, conv):
+        b = self._z()
+        self.lib.ref_set_rhs_conc(self.h, C.c_int(ic), C.c_double(dt), _p(c), _p(conv), _p(b))
+        return b
+
+    def total_concentration(self, cs):
+        arr = (_dp * 4)()
+        for i, c in enumerate(cs):
+            arr[i] = _p(c)
+        out = self._z()
+        self.lib.ref_total_concentration(self.h, arr, _p(out))
+        return out
+
+    def lhs_apply(self, q, ic, dt, x):
+        y = self._z()
+        self.lib.ref_lhs_apply(self.h, C.c_char(q.encode()), C.c_int(ic), C.c_double(dt),
+                               _p(np.ascontiguousarray(x)), _p(y))
+        return y
+
+    def pressure_apply(self, x):
+        y = self._z()
+        self.lib.ref_pressure_apply(self.h, _p(np.ascontiguousarray(x)), _p(y))
+        return y
+
+    def pressure_rhs(self, dt, u, v, w):
+        b = self._z()
+        self.lib.ref_pressure_rhs(self.h, C.c_double(dt), _p(u), _p(v), _p(w), _p(b))
+        return b
+
+    def project(self, dt, phi, pb, u, v, w, dpx, dpy, dpz):
+        self.lib.ref_project(self.h, C.c_double(dt), _p(phi), _p(pb), _p(u), _p(v), _p(w), _p(dpx), _p(dpy), _p(dpz))
+
+    def divergence(self, u, v, w):
+        d = self._z()
+        m = self.lib.ref_divergence(self.h, _p(u), _p(v), _p(w), _p(d))
+        return m, d
+
+    # -- restated line driver around the reference's ghost and ENO routines --
+    def convection(self, q, ic, fld, vx, vy, vz):
+        """conv = Vx dq/dx + Vy dq/dy + Vz dq/dz over full box lines of
+        non-BOUNDARY nodes; ghosts filled by the reference routines."""
+        g, r = self.g, self.p.eno_order
+        nx, ny, nz = g.nx, g.ny, g.nz
+        i0 = 1 if q == "u" else 0
+        j0 = 1 if q == "v" else 0
+        k0 = 1 if q == "w" else 0
+        x, y, z = g.coords(q)
+        conv = self._z()
+        qc = C.c_char(q.encode())
+        for d, (pos, s0, e0, vel) in enumerate(((x, i0, nx - 1, vx), (y, j0, ny - 1, vy), (z, k0, nz - 1, vz))):
+            nint = e0 - s0 + 1
+            nb = nint + 2 * r
+            if d == 0:
+                lines = [(None, j, k) for k in range(k0, nz) for j in range(j0, ny)]
+            elif d == 1:
+                lines = [(i, None, k) for k in range(k0, nz) for i in range(i0, nx)]
+            else:
+                lines = [(i, j, None) for j in range(j0, ny) for i in range(i0, nx)]
+            for (i, j, k) in lines:
+                sl = (slice(k, k + 1) if k is not None else slice(s0, e0 + 1),
+                      slice(j, j + 1) if j is not None else slice(s0, e0 + 1),
+                      slice(i, i + 1) if i is not None else slice(s0, e0 + 1))
+                vals = fld[sl].ravel()
+                vv = vel[sl].ravel()
+                D0 = np.zeros(nb)
+                P = np.zeros(nb)
+                V = np.zeros(nb)
+                D0[r:r + nint] = vals
+                P[r:r + nint] = pos[s0:e0 + 1]
+                V[r:r + nint] = vv
+                # salinity top ghosts are never written by the reference:
+                # pre-fill with the Neumann value (the restated driver's choice)
+                D0[nb - r:] = vals[-1]
+                ci = (i if i is not None else s0, j if j is not None else s0, k if k is not None else s0)
+                ce = (i if i is not None else e0, j if j is not None else e0, k if k is not None else e0)
+                self.lib.ref_ghost_cells(self.h, qc, C.c_int(ic), C.c_char(b"xyz"[d:d + 1]), C.c_int(ci[0]),
+                                         C.c_int(ci[1]), C.c_int(ci[2]), C.c_int(ce[0]), C.c_int(ce[1]),
+                                         C.c_int(ce[2]), C.c_int(nb), _p(D0), _p(P))
+                out = self.eno_line(r, D0, P, V)[r:r + nint]
+                if d == 0:
+                    conv[sl] = out.reshape(conv[sl].shape)
+                else:
+                    conv[sl] = (conv[sl].ravel() + out).reshape(conv[sl].shape)
+        return conv

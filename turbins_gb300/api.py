@@ -278,3 +278,48 @@ def ENO_compute_convective_terms(order, D0, P, V):
     _check(L.turb_ENO_compute_convective_terms(order, len(D0), _ptr(D0), _ptr(P), _ptr(V), _ptr(out)),
            "ENO_compute_convective_terms")
     return out
+
+
+# ---- measurement helpers ------------------------------------------------------
+PROF_GROUPS = ("eno_x", "eno_yz", "jacobi", "mg", "pcg")
+
+
+def _ctx_method(name):
+    def f(self, *a):
+        return getattr(self.lib, name)(self.ctx, *a)
+    return f
+
+
+def profile_enable(ctx, on=True):
+    _check(ctx.lib.turb_profile_enable(ctx.ctx, 1 if on else 0), "profile_enable")
+
+
+def profile_read(ctx):
+    ms = (C.c_double * len(PROF_GROUPS))()
+    nl = (C.c_longlong * len(PROF_GROUPS))()
+    _check(ctx.lib.turb_profile_read(ctx.ctx, ms, nl), "profile_read")
+    return {g: (ms[i], nl[i]) for i, g in enumerate(PROF_GROUPS)}
+
+
+def event_record(ctx, slot):
+    _check(ctx.lib.turb_event_record(ctx.ctx, slot), "event_record")
+
+
+def event_elapsed(ctx, a, b):
+    ms = C.c_double()
+    _check(ctx.lib.turb_event_elapsed(ctx.ctx, a, b, C.byref(ms)), "event_elapsed")
+    return ms.value
+
+
+def kernel_launches(ctx):
+    n = C.c_longlong()
+    _check(ctx.lib.turb_kernel_launches(ctx.ctx, C.byref(n)), "kernel_launches")
+    return n.value
+
+
+def host_register(arr):
+    _check(load_library().turb_host_register(C.c_void_p(arr.ctypes.data), C.c_size_t(arr.nbytes)), "host_register")
+
+
+def host_unregister(arr):
+    _check(load_library().turb_host_unregister(C.c_void_p(arr.ctypes.data)), "host_unregister")

@@ -88,6 +88,14 @@ struct turb_ctx {
     double *hscal = nullptr;   // pinned host scalars
     long long nparts = 0;
     long long launches = 0;
+    // per-group CUDA-event timing (turb_profile_*)
+    int prof = 0;
+    struct Rec { int g, nl; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    double prof_ms[TURB_PROF_NGROUPS] = {0};
+    long long prof_nl[TURB_PROF_NGROUPS] = {0};
+    cudaEvent_t user_ev[8] = {nullptr};
 };
 
 namespace {
@@ -572,6 +580,53 @@ int fetch_scalars(turb_ctx *c, int n)
     return TURB_OK;
 }
 
+cudaEvent_t prof_event(turb_ctx *c)
+{
+    if (!c->pool.empty()) {
+        cudaEvent_t e = c->pool.back();
+        c->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// open a timed group on the context stream; returns a handle for prof_end
+int prof_begin(turb_ctx *c, int g)
+{
+    if (!c->prof) return -1;
+    turb_ctx::Rec r;
+    r.g = g;
+    r.nl = 0;
+    r.a = prof_event(c);
+    r.b = prof_event(c);
+    cudaEventRecord(r.a, c->s);
+    c->recs.push_back(r);
+    return (int)c->recs.size() - 1;
+}
+
+void prof_end(turb_ctx *c, int h, int nlaunch)
+{
+    if (h < 0) return;
+    cudaEventRecord(c->recs[h].b, c->s);
+    c->recs[h].nl = nlaunch;
+}
+
+void prof_collect(turb_ctx *c)
+{
+    cudaStreamSynchronize(c->s);
+    for (auto &r : c->recs) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        c->prof_ms[r.g] += ms;
+        c->prof_nl[r.g] += r.nl;
+        c->pool.push_back(r.a);
+        c->pool.push_back(r.b);
+    }
+    c->recs.clear();
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -712,6 +767,10 @@ int turb_destroy(turb_ctx *c)
 {
     if (!c) return TURB_ERR_ARG;
     cudaStreamSynchronize(c->s);
+    prof_collect(c);
+    for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->user_ev)
+        if (e) cudaEventDestroy(e);
     c->mem.release();
     if (c->hscal) cudaFreeHost(c->hscal);
     cudaStreamDestroy(c->s);
@@ -862,9 +921,13 @@ int turb_Velocity_convective_terms(turb_ctx *c, char which)
         az = adv_of(0, w, z, z);
     }
     cudaMemsetAsync(conv, 0, d.n * 8, c->s);
+    int h = prof_begin(c, TURB_PROF_ENO_X);
     launch_eno_pass(c->s, d, 0, c->eno[q][0], self, ax, j0, ny - 1, k0, nz - 1, 1, conv);
+    prof_end(c, h, 1);
+    h = prof_begin(c, TURB_PROF_ENO_YZ);
     launch_eno_pass(c->s, d, 1, c->eno[q][1], self, ay, i0, nx - 1, k0, nz - 1, 0, conv);
     launch_eno_pass(c->s, d, 2, c->eno[q][2], self, az, i0, nx - 1, j0, ny - 1, 0, conv);
+    prof_end(c, h, 2);
     c->launches += 3;
     return check_launch(c);
 }
@@ -881,9 +944,13 @@ int turb_Conc_convective_terms(turb_ctx *c, int ic)
                                                   : adv_of(0, c->fld[TURB_F_VBC], z, z);
     AdvSrc az = adv_of(0, c->fld[TURB_F_WBC], z, z);
     cudaMemsetAsync(conv, 0, d.n * 8, c->s);
+    int h = prof_begin(c, TURB_PROF_ENO_X);
     launch_eno_pass(c->s, d, 0, c->eno[3][0], cf, ax, 0, d.ny - 1, 0, d.nz - 1, 1, conv);
+    prof_end(c, h, 1);
+    h = prof_begin(c, TURB_PROF_ENO_YZ);
     launch_eno_pass(c->s, d, 1, c->eno_cy[ic], cf, ay, 0, d.nx - 1, 0, d.nz - 1, 0, conv);
     launch_eno_pass(c->s, d, 2, c->eno[3][2], cf, az, 0, d.nx - 1, 0, d.ny - 1, 0, conv);
+    prof_end(c, h, 2);
     c->launches += 3;
     return check_launch(c);
 }
@@ -925,7 +992,9 @@ static int helm_solve(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int
     c->launches += 2;
     for (;;) {
         double *x = c->fld[fx];
+        int ph = prof_begin(c, TURB_PROF_JACOBI);
         launch_helm_jacobi(c->s, d, h, c->st[q], a_dt, b, x, c->jtmp, ib, c->part, hp);
+        prof_end(c, ph, 1);
         launch_sum_final(c->s, np, c->part, c->dscal);
         c->launches += 2 + (ib.n > 0);
         rc = fetch_scalars(c, 1);
@@ -1010,15 +1079,19 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             if (it >= c->prm.p_maxit) { status = TURB_ERR_NOT_CONVERGED; break; }
             restart = 1;
         }
+        int ph = prof_begin(c, TURB_PROF_MG);
         if (c->pmode == TURB_PMODE_FP64) {
             mg_vcycle<double>(s, c->H64, 0, npre, npost);
             c->launches += vl;
+            prof_end(c, ph, vl);
         } else {
             pcg_to_float(s, n0, c->pr, c->H32.b[0]);
             mg_vcycle<float>(s, c->H32, 0, npre, npost);
             pcg_to_double(s, n0, c->H32.x[0], c->pz);
             c->launches += vl + 2;
+            prof_end(c, ph, vl + 2);
         }
+        ph = prof_begin(c, TURB_PROF_PCG);
         pcg_dot2(s, n0, c->pr, c->pz, c->pro, c->part);
         pcg_reduce(s, c->part, 2, dsc + 2);   // rz and z.r_old
         c->launches += 2;
@@ -1030,6 +1103,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         pcg_xrupdate(s, n0, c->px, c->pr, c->pro, c->pp, c->pq, sc, c->part);
         pcg_reduce(s, c->part, 1, dsc + 1);
         c->launches += 6;
+        prof_end(c, ph, 8 + (restart ? 0 : 1));
         TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
         TURB_CHECK(cudaStreamSynchronize(s));
         nr = std::sqrt(c->hscal[1]);
@@ -1100,6 +1174,62 @@ int turb_rk_average(turb_ctx *c, double old_frac, double new_frac)
         launch_axpby(c->s, c->d.n, old_frac, c->old[3 + ic], new_frac, c->fld[TURB_F_C0 + ic]);
     c->launches += 3 + c->prm.nconc;
     return check_launch(c);
+}
+
+int turb_profile_enable(turb_ctx *c, int on)
+{
+    if (!c) return TURB_ERR_ARG;
+    prof_collect(c);
+    for (int g = 0; g < TURB_PROF_NGROUPS; g++) { c->prof_ms[g] = 0.0; c->prof_nl[g] = 0; }
+    c->prof = on ? 1 : 0;
+    return TURB_OK;
+}
+
+int turb_profile_read(turb_ctx *c, double *ms, long long *nlaunch)
+{
+    if (!c || !ms || !nlaunch) return TURB_ERR_ARG;
+    prof_collect(c);
+    for (int g = 0; g < TURB_PROF_NGROUPS; g++) { ms[g] = c->prof_ms[g]; nlaunch[g] = c->prof_nl[g]; }
+    return TURB_OK;
+}
+
+int turb_event_record(turb_ctx *c, int slot)
+{
+    if (!c || slot < 0 || slot >= 8) return TURB_ERR_ARG;
+    if (!c->user_ev[slot]) TURB_CHECK(cudaEventCreate(&c->user_ev[slot]));
+    TURB_CHECK(cudaEventRecord(c->user_ev[slot], c->s));
+    return TURB_OK;
+}
+
+int turb_event_elapsed(turb_ctx *c, int a, int b, double *ms)
+{
+    if (!c || !ms || a < 0 || b < 0 || a >= 8 || b >= 8 || !c->user_ev[a] || !c->user_ev[b]) return TURB_ERR_ARG;
+    TURB_CHECK(cudaEventSynchronize(c->user_ev[b]));
+    float f = 0.0f;
+    TURB_CHECK(cudaEventElapsedTime(&f, c->user_ev[a], c->user_ev[b]));
+    *ms = f;
+    return TURB_OK;
+}
+
+int turb_kernel_launches(turb_ctx *c, long long *n)
+{
+    if (!c || !n) return TURB_ERR_ARG;
+    *n = c->launches;
+    return TURB_OK;
+}
+
+int turb_host_register(void *p, size_t bytes)
+{
+    if (!p || !bytes) return TURB_ERR_ARG;
+    TURB_CHECK(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+    return TURB_OK;
+}
+
+int turb_host_unregister(void *p)
+{
+    if (!p) return TURB_ERR_ARG;
+    TURB_CHECK(cudaHostUnregister(p));
+    return TURB_OK;
 }
 
 #define STEP_TRY(x)                      \
