@@ -116,6 +116,10 @@ typedef struct {
 #define TURB_PMODE_FP64 0        /* plain FP64 MG-preconditioned CG             */
 #define TURB_PMODE_MIXED 1       /* FP32 V-cycles inside FP64 flexible CG       */
 
+/* Helmholtz (implicit viscous / diffusive) solver modes */
+#define TURB_HMODE_FP64 0        /* FP64 point-Jacobi iteration                 */
+#define TURB_HMODE_MIXED 1       /* FP64 defect correction, FP32 inner sweeps   */
+
 /* ---- context -------------------------------------------------------------
  * Replaces Grid_create + Velocity_create + Pressure_create + Conc_create +
  * *_setup_lsys_accounting_geometry (Grid.c:21, Velocity.c:19, Pressure.c:15,
@@ -126,6 +130,8 @@ int turb_destroy(turb_ctx *ctx);
 int turb_field_upload(turb_ctx *ctx, int field, const double *host_da);
 int turb_field_download(turb_ctx *ctx, int field, double *host_da);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);
+/* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
+int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 int turb_synchronize(turb_ctx *ctx);
 const char *turb_status_string(int status);
 
@@ -176,10 +182,11 @@ int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
  * accumulators; read synchronizes and returns ms and launches per group). */
 #define TURB_PROF_ENO_X 0      /* x-direction ENO passes                        */
 #define TURB_PROF_ENO_YZ 1     /* y/z-direction ENO passes                      */
-#define TURB_PROF_JACOBI 2     /* Helmholtz Jacobi sweeps                       */
+#define TURB_PROF_JACOBI 2     /* Helmholtz FP64 sweeps / FP64 residuals        */
 #define TURB_PROF_MG 3         /* multigrid V-cycles (all levels)               */
 #define TURB_PROF_PCG 4        /* FP64 CG vector kernels and reductions         */
-#define TURB_PROF_NGROUPS 5
+#define TURB_PROF_INNER32 5    /* FP32 inner sweeps of the Helmholtz correction */
+#define TURB_PROF_NGROUPS 6
 int turb_profile_enable(turb_ctx *ctx, int on);
 int turb_profile_read(turb_ctx *ctx, double *ms, long long *launches);
 /* events 0..7 on the context stream; elapsed waits for event b */

@@ -863,28 +863,101 @@ static void mg_coarse_solve(mg_lev *L)
     }
 }
 
-/* restriction: sum of the (up to 8) children; prolongation: its transpose */
-static void mg_restrict(const mg_lev *f, const double *rf, const mg_lev *c, double *bc)
+/* restriction and prolongation.  mode 0: sum of the (up to 8) children and
+ * its transpose (piecewise constant); mode 1: linear interpolation between
+ * coarse cell centres along each coarsened direction (positions from the
+ * cell widths, so it follows the stretching) and its transpose. */
+static int g_mg_mode = 1;
+static int g_npre = 2, g_npost = 2;
+void to_set_mg_options(int mode, int npre, int npost) { g_mg_mode = mode; g_npre = npre; g_npost = npost; }
+
+static void centres(const double *D, int n, double *X)
 {
-    int i, j, k;
-    memset(bc, 0, sizeof(double) * (size_t)c->nx * c->ny * c->nz);
+    int i;
+    X[0] = 0.5 * D[0];
+    for (i = 1; i < n; i++) X[i] = X[i - 1] + 0.5 * (D[i - 1] + D[i]);
+}
+
+/* 1-D prolongation weights of fine index i: coarse (I0, I1), weights (w0, w1) */
+static void pw(const double *xf, const double *xc, int nc, int coarsened, int i, int *I0, int *I1,
+               double *w0, double *w1)
+{
+    int I;
+    if (!coarsened) { *I0 = *I1 = i; *w0 = 1.0; *w1 = 0.0; return; }
+    I = i / 2;
+    if (g_mg_mode == 0) { *I0 = *I1 = I; *w0 = 1.0; *w1 = 0.0; return; }
+    if (xf[i] < xc[I]) {
+        if (I == 0) { *I0 = *I1 = 0; *w0 = 1.0; *w1 = 0.0; return; }
+        *I0 = I - 1; *I1 = I;
+    } else {
+        if (I == nc - 1) { *I0 = *I1 = I; *w0 = 1.0; *w1 = 0.0; return; }
+        *I0 = I; *I1 = I + 1;
+    }
+    *w1 = (xf[i] - xc[*I0]) / (xc[*I1] - xc[*I0]);
+    *w0 = 1.0 - *w1;
+}
+
+typedef struct { int *I0, *I1; double *w0, *w1; } pw_tab;
+
+static void pw_build(const double *Df, int nf, const double *Dc, int nc, int coarsened, pw_tab *t)
+{
+    double *xf = malloc(sizeof(double) * nf), *xc = malloc(sizeof(double) * nc);
+    int i;
+    centres(Df, nf, xf);
+    centres(Dc, nc, xc);
+    t->I0 = malloc(sizeof(int) * nf); t->I1 = malloc(sizeof(int) * nf);
+    t->w0 = malloc(sizeof(double) * nf); t->w1 = malloc(sizeof(double) * nf);
+    for (i = 0; i < nf; i++) pw(xf, xc, nc, coarsened, i, &t->I0[i], &t->I1[i], &t->w0[i], &t->w1[i]);
+    free(xf); free(xc);
+}
+
+static void pw_free(pw_tab *t) { free(t->I0); free(t->I1); free(t->w0); free(t->w1); }
+
+static void mg_transfer(const mg_lev *f, const mg_lev *c, double *xf, double *xc, int restrict_)
+{
+    pw_tab tx, ty, tz;
+    int i, j, k, a, b, d;
+    pw_build(f->DX, f->nx, c->DX, c->nx, f->cx, &tx);
+    pw_build(f->DY, f->ny, c->DY, c->ny, f->cy, &ty);
+    pw_build(f->DZ, f->nz, c->DZ, c->nz, f->cz, &tz);
+    if (restrict_) memset(xc, 0, sizeof(double) * (size_t)c->nx * c->ny * c->nz);
     for (k = 0; k < f->nz; k++)
         for (j = 0; j < f->ny; j++)
-            for (i = 0; i < f->nx; i++)
-                bc[LI(c, f->cx ? i / 2 : i, f->cy ? j / 2 : j, f->cz ? k / 2 : k)] += rf[LI(f, i, j, k)];
+            for (i = 0; i < f->nx; i++) {
+                size_t pf = LI(f, i, j, k);
+                double acc = 0.0;
+                for (d = 0; d < 2; d++) {
+                    int K = d ? tz.I1[k] : tz.I0[k];
+                    double wz = d ? tz.w1[k] : tz.w0[k];
+                    if (wz == 0.0) continue;
+                    for (b = 0; b < 2; b++) {
+                        int J = b ? ty.I1[j] : ty.I0[j];
+                        double wy = b ? ty.w1[j] : ty.w0[j];
+                        if (wy == 0.0) continue;
+                        for (a = 0; a < 2; a++) {
+                            int I = a ? tx.I1[i] : tx.I0[i];
+                            double wx = a ? tx.w1[i] : tx.w0[i], w = wx * wy * wz;
+                            if (wx == 0.0) continue;
+                            if (restrict_) xc[LI(c, I, J, K)] += w * xf[pf];
+                            else acc += w * xc[LI(c, I, J, K)];
+                        }
+                    }
+                }
+                if (!restrict_) xf[pf] += acc;
+            }
+    pw_free(&tx); pw_free(&ty); pw_free(&tz);
+}
+
+static void mg_restrict(const mg_lev *f, const double *rf, const mg_lev *c, double *bc)
+{
+    mg_transfer(f, c, (double *)rf, bc, 1);
 }
 
 static void mg_prolong_add(const mg_lev *f, double *xf, const mg_lev *c, const double *xc)
 {
-    int i, j, k;
-    for (k = 0; k < f->nz; k++)
-        for (j = 0; j < f->ny; j++)
-            for (i = 0; i < f->nx; i++)
-                xf[LI(f, i, j, k)] += xc[LI(c, f->cx ? i / 2 : i, f->cy ? j / 2 : j, f->cz ? k / 2 : k)];
+    mg_transfer(f, c, xf, (double *)xc, 0);
 }
 
-#define MG_NPRE 2
-#define MG_NPOST 2
 
 static void mg_vcycle(mg_hier *H, int lev)
 {
@@ -893,13 +966,13 @@ static void mg_vcycle(mg_hier *H, int lev)
     int s;
     if (lev == H->nl - 1) { mg_coarse_solve(L); return; }
     memset(L->x, 0, nc * sizeof(double));
-    for (s = 0; s < MG_NPRE; s++) { mg_rbgs(L, L->x, L->b, 0); mg_rbgs(L, L->x, L->b, 1); }
+    for (s = 0; s < g_npre; s++) { mg_rbgs(L, L->x, L->b, 0); mg_rbgs(L, L->x, L->b, 1); }
     mg_apply(L, L->x, L->r);
     for (t = 0; t < nc; t++) L->r[t] = L->b[t] - L->r[t];
     mg_restrict(L, L->r, &H->L[lev + 1], H->L[lev + 1].b);
     mg_vcycle(H, lev + 1);
     mg_prolong_add(L, L->x, &H->L[lev + 1], H->L[lev + 1].x);
-    for (s = 0; s < MG_NPOST; s++) { mg_rbgs(L, L->x, L->b, 1); mg_rbgs(L, L->x, L->b, 0); }
+    for (s = 0; s < g_npost; s++) { mg_rbgs(L, L->x, L->b, 1); mg_rbgs(L, L->x, L->b, 0); }
 }
 
 int to_pressure_solve(const to_grid *g, const to_params *p, const double *b,

@@ -119,6 +119,7 @@ typedef struct {
     double div_max[2];
 } to_step_stats;
 
+void to_set_mg_options(int mode, int npre, int npost);
 int to_step(const to_grid *g, const to_params *p, to_state *s, double dt,
             to_step_stats *stats);
 

@@ -201,10 +201,14 @@ def test_pressure_solve(api, oracle_mod, name, mk, mode):
 
 
 @pytest.mark.parametrize("name,mk", CASES[:3])
-def test_helmholtz_solve(api, oracle_mod, name, mk):
+@pytest.mark.parametrize("hmode", [0, 1])
+def test_helmholtz_solve(api, oracle_mod, name, mk, hmode):
+    """FP64 Jacobi and FP64-residual/FP32-inner defect correction both reach
+    the discrete solution of the oracle's BiCGStab (KSPIBCGS)."""
     case = mk()
     s = _cases.random_state(case, seed=13)
     ctx, orc, _ = _pair(case, api, oracle_mod, s)
+    ctx.set_helmholtz_mode(hmode, 6)
     dt = case.dt
     for q, f, fb in (("u", api.F_U, api.F_B_U), ("v", api.F_V, api.F_B_V), ("w", api.F_W, api.F_B_W)):
         b = s[q] / dt + 0.1
@@ -215,6 +219,17 @@ def test_helmholtz_solve(api, oracle_mod, name, mk):
         case.params.vel_rtol = 1e-14
         orc2 = type(orc)(case.grid, case.params)
         xr, itr, rr = orc2.helmholtz_solve(q, 0, dt, b, s[q], method=0)
+        assert np.abs(x - xr).max() <= 1e-10 * max(1.0, np.abs(xr).max())
+        case.params.vel_rtol = 1e-12
+    for ic in range(case.params.nconc):
+        b = s["c%d" % ic] / dt
+        b[case.grid.status["c"] != 3] = 0.0
+        ctx.upload(api.F_CB0 + ic, b)
+        ctx.Conc_solve(ic, dt)
+        x = ctx.download(api.F_C0 + ic)
+        case.params.vel_rtol = 1e-14
+        orc2 = type(orc)(case.grid, case.params)
+        xr, itr, rr = orc2.helmholtz_solve("c", ic, dt, b, s["c%d" % ic], method=0)
         assert np.abs(x - xr).max() <= 1e-10 * max(1.0, np.abs(xr).max())
         case.params.vel_rtol = 1e-12
 
@@ -239,3 +254,26 @@ def test_step_matches_oracle(api, oracle_mod, name, mk):
     for k in ("u", "v", "w"):
         assert np.abs(g[k] - so[k]).max() <= 1e-7 * vscale, k
     assert np.abs(g["c0"] - so["c0"]).max() <= 1e-9 * np.abs(so["c0"]).max()
+
+
+def test_failure_paths(api, oracle_mod):
+    """Non-convergence and non-finite input come back as status codes; the
+    context stays usable afterwards."""
+    case = _cases.bump_small()
+    ctx, orc, s = _pair(case, api, oracle_mod, _cases.random_state(case, seed=17))
+    case.params.p_maxit = 1
+    ctx2 = api.Context(case.grid, case.params)
+    ctx2.load_state(s)
+    ctx2.Pressure_set_RHS(case.dt)
+    with pytest.raises(api.TurbError) as e:
+        ctx2.Pressure_solve()
+    assert e.value.code == 3
+    b = np.zeros(case.grid.shape)
+    b[3, 3, 3] = np.nan
+    ctx.upload(api.F_B_U, b)
+    with pytest.raises(api.TurbError) as e:
+        ctx.Velocity_solve("u", case.dt)
+    assert e.value.code == 4
+    ctx.load_state(s)
+    st = ctx.step(case.dt)
+    assert max(st["div_max"]) <= 1e-10

@@ -24,6 +24,7 @@ F_U, F_V, F_W, F_PHI, F_DPX, F_DPY, F_DPZ, F_PB, F_DIV = range(9)
 F_UBC, F_VBC, F_WBC, F_CONV_U, F_CONV_V, F_CONV_W, F_B_U, F_B_V, F_B_W, F_CTOT, F_SCRATCH0, F_SCRATCH1 = range(9, 21)
 F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
 PMODE_FP64, PMODE_MIXED = 0, 1
+HMODE_FP64, HMODE_MIXED = 0, 1
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed"}
@@ -192,6 +193,9 @@ class Context:
     def set_pressure_mode(self, mode):
         _check(self.lib.turb_set_pressure_mode(self.ctx, mode), "set_pressure_mode")
 
+    def set_helmholtz_mode(self, mode, inner_sweeps=6):
+        _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")
+
     def synchronize(self):
         _check(self.lib.turb_synchronize(self.ctx), "synchronize")
 
@@ -281,13 +285,7 @@ def ENO_compute_convective_terms(order, D0, P, V):
 
 
 # ---- measurement helpers ------------------------------------------------------
-PROF_GROUPS = ("eno_x", "eno_yz", "jacobi", "mg", "pcg")
-
-
-def _ctx_method(name):
-    def f(self, *a):
-        return getattr(self.lib, name)(self.ctx, *a)
-    return f
+PROF_GROUPS = ("eno_x", "eno_yz", "jacobi", "mg", "pcg", "inner32")
 
 
 def profile_enable(ctx, on=True):

@@ -117,22 +117,50 @@ __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restr
 }
 
 template <typename T>
+__device__ __forceinline__ const T *rw_of(const Xfer1D &t);
+template <>
+__device__ __forceinline__ const double *rw_of<double>(const Xfer1D &t) { return t.rwd; }
+template <>
+__device__ __forceinline__ const float *rw_of<float>(const Xfer1D &t) { return t.rwf; }
+template <typename T>
+__device__ __forceinline__ const T *pw0_of(const Xfer1D &t);
+template <>
+__device__ __forceinline__ const double *pw0_of<double>(const Xfer1D &t) { return t.w0d; }
+template <>
+__device__ __forceinline__ const float *pw0_of<float>(const Xfer1D &t) { return t.w0f; }
+template <typename T>
+__device__ __forceinline__ const T *pw1_of(const Xfer1D &t);
+template <>
+__device__ __forceinline__ const double *pw1_of<double>(const Xfer1D &t) { return t.w1d; }
+template <>
+__device__ __forceinline__ const float *pw1_of<float>(const Xfer1D &t) { return t.w1f; }
+
+// restriction = transpose of the linear prolongation (gather over <= 4 fine
+// cells per coarsened direction)
+template <typename T>
 __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ rf, T *__restrict__ bc)
 {
     long long n = (long long)Lc.nx * Lc.ny * Lc.nz;
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     int I = (int)(c % Lc.nx), J = (int)((c / Lc.nx) % Lc.ny), K = (int)(c / ((long long)Lc.nx * Lc.ny));
-    int ni = Lf.cx ? 2 : 1, nj = Lf.cy ? 2 : 1, nk = Lf.cz ? 2 : 1;
-    int i0 = Lf.cx ? 2 * I : I, j0 = Lf.cy ? 2 * J : J, k0 = Lf.cz ? 2 * K : K;
+    const T *rwx = rw_of<T>(Lf.tx), *rwy = rw_of<T>(Lf.ty), *rwz = rw_of<T>(Lf.tz);
+    int nxx = Lf.tx.rcnt[I], nyy = Lf.ty.rcnt[J], nzz = Lf.tz.rcnt[K];
     T s = 0;
-    for (int kk = 0; kk < nk; kk++)
-        for (int jj = 0; jj < nj; jj++)
-            for (int ii = 0; ii < ni; ii++)
-                s += rf[((long long)(k0 + kk) * Lf.ny + (j0 + jj)) * Lf.nx + (i0 + ii)];
+    for (int c3 = 0; c3 < nzz; c3++) {
+        int k = Lf.tz.rf[4 * K + c3];
+        T wz = rwz[4 * K + c3];
+        for (int b = 0; b < nyy; b++) {
+            int j = Lf.ty.rf[4 * J + b];
+            T wyz = wz * rwy[4 * J + b];
+            const T *row = rf + ((long long)k * Lf.ny + j) * Lf.nx;
+            for (int a = 0; a < nxx; a++) s += wyz * rwx[4 * I + a] * row[Lf.tx.rf[4 * I + a]];
+        }
+    }
     bc[c] = s;
 }
 
+// linear prolongation (stretching-aware weights), added to the fine iterate
 template <typename T>
 __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc, T *__restrict__ xf)
 {
@@ -140,8 +168,25 @@ __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     int i = (int)(c % Lf.nx), j = (int)((c / Lf.nx) % Lf.ny), k = (int)(c / ((long long)Lf.nx * Lf.ny));
-    int I = Lf.cx ? i >> 1 : i, J = Lf.cy ? j >> 1 : j, K = Lf.cz ? k >> 1 : k;
-    xf[c] += xc[((long long)K * Lc.ny + J) * Lc.nx + I];
+    int Ix[2] = {Lf.tx.I0[i], Lf.tx.I1[i]}, Iy[2] = {Lf.ty.I0[j], Lf.ty.I1[j]}, Iz[2] = {Lf.tz.I0[k], Lf.tz.I1[k]};
+    T wx[2] = {pw0_of<T>(Lf.tx)[i], pw1_of<T>(Lf.tx)[i]};
+    T wy[2] = {pw0_of<T>(Lf.ty)[j], pw1_of<T>(Lf.ty)[j]};
+    T wz[2] = {pw0_of<T>(Lf.tz)[k], pw1_of<T>(Lf.tz)[k]};
+    T acc = 0;
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+        if (wz[d] == T(0)) continue;
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            if (wy[b] == T(0)) continue;
+            const T *row = xc + ((long long)Iz[d] * Lc.ny + Iy[b]) * Lc.nx;
+            T wyz = wz[d] * wy[b];
+#pragma unroll
+            for (int a = 0; a < 2; a++)
+                if (wx[a] != T(0)) acc += wyz * wx[a] * row[Ix[a]];
+        }
+    }
+    xf[c] += acc;
 }
 
 template <typename T>

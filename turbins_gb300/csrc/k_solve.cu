@@ -133,6 +133,107 @@ __global__ void k_sum_final(long long n, const double *__restrict__ part, double
     if (threadIdx.x == 0) *out = s;
 }
 
+// ---- mixed-precision defect correction -----------------------------------
+// outer: x <- x + e, r = b - A x in FP64 (rounded to FP32 for the inner solve)
+__global__ void k_helm_resid64(Dims d, HelmTab h, const uint8_t *__restrict__ st, double a_dt,
+                               const double *__restrict__ b, const double *__restrict__ x,
+                               const float *__restrict__ e, double *__restrict__ xn, float *__restrict__ rf,
+                               double *__restrict__ part)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int k = blockIdx.y;
+    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
+    double r2 = 0.0;
+    if (j < d.NY) {
+        long long p = d.at(i, j, k);
+        int s = st[p];
+        double xp = x[p] + (double)e[p];
+        xn[p] = xp;
+        if (s != T_IMMERSED) {
+            bool stencil = (h.q == 3) ? (s == T_FLUID) : (s == T_FLUID || s == T_BUFFER_SOLID);
+            double acc;
+            if (stencil) {
+                double dg = h.apx[i] + h.apy[j] + h.apz[k] + a_dt, c;
+                acc = dg * xp;
+                c = h.aw[i]; if (c != 0.0) acc = fma(c, x[p - 1] + (double)e[p - 1], acc);
+                c = h.ae[i]; if (c != 0.0) acc = fma(c, x[p + 1] + (double)e[p + 1], acc);
+                c = h.as[j]; if (c != 0.0) acc = fma(c, x[p - d.PX] + (double)e[p - d.PX], acc);
+                c = h.an[j]; if (c != 0.0) acc = fma(c, x[p + d.PX] + (double)e[p + d.PX], acc);
+                c = h.ab[k]; if (c != 0.0) acc = fma(c, x[p - d.plane] + (double)e[p - d.plane], acc);
+                c = h.af[k]; if (c != 0.0) acc = fma(c, x[p + d.plane] + (double)e[p + d.plane], acc);
+            } else {
+                acc = (h.ap_solid + a_dt) * xp;
+            }
+            double r = b[p] - acc;
+            rf[p] = (float)r;
+            r2 = r * r;
+        }
+    }
+    double bs = block_sum(r2);
+    if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + blockIdx.x] = bs;
+}
+
+__global__ void k_ib_resid64(IbDev ib, const double *__restrict__ b, const double *__restrict__ x,
+                             const float *__restrict__ e, float *__restrict__ rf, double *__restrict__ part)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double r2 = 0.0;
+    if (t < ib.n) {
+        long long im = ib.im[t];
+        double acc = ib.diag[t] * (x[im] + (double)e[im]);
+        int c = ib.cnt[t];
+        for (int g = 0; g < c; g++) {
+            long long q = ib.col[t * 8 + g];
+            acc += ib.val[t * 8 + g] * (x[q] + (double)e[q]);
+        }
+        double r = b[im] - acc;
+        rf[im] = (float)r;
+        r2 = r * r;
+    }
+    double bs = block_sum(r2);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+}
+
+// inner FP32 Jacobi sweep on A e = r (first sweep from e = 0)
+__global__ void k_helm_jac32(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
+                             const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
+                             int first)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int k = blockIdx.y;
+    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
+    if (j >= d.NY) return;
+    long long p = d.at(i, j, k);
+    int s = st[p];
+    if (s == T_IMMERSED) return;
+    bool stencil = (h.q == 3) ? (s == T_FLUID) : (s == T_FLUID || s == T_BUFFER_SOLID);
+    float dg = stencil ? (h.apx[i] + h.apy[j] + h.apz[k] + a_dt) : (h.ap_solid + a_dt);
+    if (first) { en[p] = r[p] / dg; return; }
+    float acc = dg * e[p], c;
+    if (stencil) {
+        c = h.aw[i]; if (c != 0.0f) acc = fmaf(c, e[p - 1], acc);
+        c = h.ae[i]; if (c != 0.0f) acc = fmaf(c, e[p + 1], acc);
+        c = h.as[j]; if (c != 0.0f) acc = fmaf(c, e[p - d.PX], acc);
+        c = h.an[j]; if (c != 0.0f) acc = fmaf(c, e[p + d.PX], acc);
+        c = h.ab[k]; if (c != 0.0f) acc = fmaf(c, e[p - d.plane], acc);
+        c = h.af[k]; if (c != 0.0f) acc = fmaf(c, e[p + d.plane], acc);
+    }
+    en[p] = e[p] + (r[p] - acc) / dg;
+}
+
+__global__ void k_ib_jac32(IbDevF ib, const float *__restrict__ r, const float *__restrict__ e,
+                           float *__restrict__ en, int first)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ib.n) return;
+    long long im = ib.im[t];
+    if (first) { en[im] = r[im] / ib.diag[t]; return; }
+    float acc = ib.diag[t] * e[im];
+    int c = ib.cnt[t];
+    for (int g = 0; g < c; g++) acc += ib.val[t * 8 + g] * e[ib.col[t * 8 + g]];
+    en[im] = e[im] + (r[im] - acc) / ib.diag[t];
+}
+
 constexpr int NPART = 1024;
 
 __global__ void k_norm2(long long n, const double *__restrict__ x, double *__restrict__ part)
@@ -153,6 +254,25 @@ long long helm_parts(const Dims &d)
 }
 
 long long norm_parts() { return NPART; }
+
+void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
+                         const double *b, const double *x, const float *e, double *xn, float *rf, const IbDev &ib,
+                         double *part, long long nparts)
+{
+    long long nij = (long long)d.NX * d.NY;
+    dim3 g((unsigned)((nij + HB - 1) / HB), d.NZ);
+    k_helm_resid64<<<g, HB, 0, s>>>(d, h, st, a_dt, b, x, e, xn, rf, part);
+    if (ib.n > 0) k_ib_resid64<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, b, x, e, rf, part + nparts);
+}
+
+void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
+                       const float *r, const float *e, float *en, const IbDevF &ib, int first)
+{
+    long long nij = (long long)d.NX * d.NY;
+    dim3 g((unsigned)((nij + HB - 1) / HB), d.NZ);
+    k_helm_jac32<<<g, HB, 0, s>>>(d, h, st, a_dt, r, e, en, first);
+    if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
+}
 
 void launch_helm_apply(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
                        const double *x, double *y, const IbDev &ib)

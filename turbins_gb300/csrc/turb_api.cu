@@ -76,6 +76,11 @@ struct turb_ctx {
     EnoTab eno[4][3];
     EnoTab eno_cy[TURB_MAXCONC];
     HelmTab helm[3], helm_c[TURB_MAXCONC];
+    HelmTabF helmf[3], helmf_c[TURB_MAXCONC];
+    IbDevF ibf[4];
+    float *hrf = nullptr, *he0 = nullptr, *he1 = nullptr;   // defect-correction buffers
+    int hmode = TURB_HMODE_MIXED;
+    int hinner = 6;
     const double *pcx, *pcy, *pcz;
     ProjArgs proj;
     // pressure
@@ -396,6 +401,40 @@ IbDev mk_ib(turb_ctx *c, int q, const turb_ib_desc &ib, double aps)
     return o;
 }
 
+HelmTabF mk_helmf(turb_ctx *c, const HelmTab &h)
+{
+    auto cp = [&](const double *dp, int n) {
+        std::vector<double> tmp(n);
+        cudaMemcpy(tmp.data(), dp, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        std::vector<float> f(tmp.begin(), tmp.end());
+        return (const float *)c->mem.upload(f);
+    };
+    HelmTabF o;
+    int NX = c->d.NX, NY = c->d.NY, NZ = c->d.NZ;
+    o.apx = cp(h.apx, NX); o.aw = cp(h.aw, NX); o.ae = cp(h.ae, NX);
+    o.apy = cp(h.apy, NY); o.as = cp(h.as, NY); o.an = cp(h.an, NY);
+    o.apz = cp(h.apz, NZ); o.ab = cp(h.ab, NZ); o.af = cp(h.af, NZ);
+    o.ap_solid = (float)h.ap_solid;
+    o.q = h.q;
+    return o;
+}
+
+IbDevF mk_ibf(turb_ctx *c, const IbDev &ib)
+{
+    IbDevF o;
+    o.n = ib.n;
+    o.im = ib.im; o.cnt = ib.cnt; o.col = ib.col;
+    std::vector<double> v((size_t)std::max(ib.n, 1) * 8, 0.0), dg(std::max(ib.n, 1), 1.0);
+    if (ib.n > 0) {
+        cudaMemcpy(v.data(), ib.val, sizeof(double) * 8 * ib.n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(dg.data(), ib.diag, sizeof(double) * ib.n, cudaMemcpyDeviceToHost);
+    }
+    std::vector<float> vf(v.begin(), v.end()), df(dg.begin(), dg.end());
+    o.val = c->mem.upload(vf);
+    o.diag = c->mem.upload(df);
+    return o;
+}
+
 // multigrid hierarchy (same coarsening rule as the CPU oracle)
 struct HostLev {
     int nx, ny, nz, cx = 0, cy = 0, cz = 0;
@@ -455,6 +494,49 @@ std::vector<HostLev> mg_host(turb_ctx *c)
     return L;
 }
 
+// linear prolongation along one direction between cell centres (positions
+// accumulated from the widths) and its transpose
+Xfer1D mk_xfer(DevBuf &m, const std::vector<double> &Df, const std::vector<double> &Dc, int coarsened)
+{
+    int nf = (int)Df.size(), nc = (int)Dc.size();
+    std::vector<double> xf(nf), xc(nc);
+    xf[0] = 0.5 * Df[0];
+    for (int i = 1; i < nf; i++) xf[i] = xf[i - 1] + 0.5 * (Df[i - 1] + Df[i]);
+    xc[0] = 0.5 * Dc[0];
+    for (int i = 1; i < nc; i++) xc[i] = xc[i - 1] + 0.5 * (Dc[i - 1] + Dc[i]);
+    std::vector<int> I0(nf), I1(nf), rcnt(nc, 0), rf(4 * (size_t)nc, 0);
+    std::vector<double> w0(nf), w1(nf), rw(4 * (size_t)nc, 0.0);
+    for (int i = 0; i < nf; i++) {
+        if (!coarsened) { I0[i] = I1[i] = i; w0[i] = 1.0; w1[i] = 0.0; continue; }
+        int I = i / 2, a, b;
+        if (xf[i] < xc[I]) {
+            if (I == 0) { I0[i] = I1[i] = 0; w0[i] = 1.0; w1[i] = 0.0; continue; }
+            a = I - 1; b = I;
+        } else {
+            if (I == nc - 1) { I0[i] = I1[i] = I; w0[i] = 1.0; w1[i] = 0.0; continue; }
+            a = I; b = I + 1;
+        }
+        I0[i] = a; I1[i] = b;
+        w1[i] = (xf[i] - xc[a]) / (xc[b] - xc[a]);
+        w0[i] = 1.0 - w1[i];
+    }
+    for (int i = 0; i < nf; i++) {
+        int Is[2] = {I0[i], I1[i]};
+        double ws[2] = {w0[i], w1[i]};
+        for (int t = 0; t < 2; t++) {
+            if (ws[t] == 0.0 || (t == 1 && Is[1] == Is[0])) continue;
+            int C = Is[t], q = rcnt[C];
+            if (q < 4) { rf[4 * (size_t)C + q] = i; rw[4 * (size_t)C + q] = ws[t]; rcnt[C] = q + 1; }
+        }
+    }
+    std::vector<float> w0f(w0.begin(), w0.end()), w1f(w1.begin(), w1.end()), rwf(rw.begin(), rw.end());
+    Xfer1D t;
+    t.I0 = m.upload(I0); t.I1 = m.upload(I1);
+    t.w0d = m.upload(w0); t.w1d = m.upload(w1); t.w0f = m.upload(w0f); t.w1f = m.upload(w1f);
+    t.rcnt = m.upload(rcnt); t.rf = m.upload(rf); t.rwd = m.upload(rw); t.rwf = m.upload(rwf);
+    return t;
+}
+
 int build_mg(turb_ctx *c)
 {
     std::vector<HostLev> L = mg_host(c);
@@ -466,6 +548,11 @@ int build_mg(turb_ctx *c)
         m.nx = h.nx; m.ny = h.ny; m.nz = h.nz;
         m.cx = h.cx; m.cy = h.cy; m.cz = h.cz;
         m.pin = h.pin;
+        if (l + 1 < nl) {
+            m.tx = mk_xfer(c->mem, h.D[0], L[l + 1].D[0], h.cx);
+            m.ty = mk_xfer(c->mem, h.D[1], L[l + 1].D[1], h.cy);
+            m.tz = mk_xfer(c->mem, h.D[2], L[l + 1].D[2], h.cz);
+        }
         std::vector<double> rf[3];
         std::vector<float> Df[3], rff[3];
         for (int a = 0; a < 3; a++) {
@@ -739,7 +826,13 @@ int turb_create(const turb_grid_desc *g, const turb_params *p, turb_ctx **out)
         turb_ib_desc e = g->ib[q];
         if (e.n < 0 || (e.n > 0 && (!e.im || !e.nf || !e.fidx || !e.fcoef))) { m.release(); delete c; return TURB_ERR_ARG; }
         c->ib[q] = mk_ib(c, q, e, aps);
+        c->ibf[q] = mk_ibf(c, c->ib[q]);
     }
+    for (int q = 0; q < 3; q++) c->helmf[q] = mk_helmf(c, c->helm[q]);
+    for (int ic = 0; ic < p->nconc; ic++) c->helmf_c[ic] = mk_helmf(c, c->helm_c[ic]);
+    c->hrf = m.alloc<float>(d.n);
+    c->he0 = m.alloc<float>(d.n);
+    c->he1 = m.alloc<float>(d.n);
     {
         double a_dEta = 1.0 / c->dEta, a_dXi = 1.0 / c->dXi, a_dPhi = 1.0 / c->dPhi;
         std::vector<double> cx(d.NX), cy(d.NY), cz(d.NZ), cyv(d.NY), czw(d.NZ);
@@ -975,7 +1068,7 @@ int turb_Conc_set_RHS(turb_ctx *c, int ic, double dt)
     return check_launch(c);
 }
 
-static int helm_solve(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int *iters)
+static int helm_solve_fp64(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int *iters)
 {
     const Dims &d = c->d;
     const HelmTab &h = q < 3 ? c->helm[q] : c->helm_c[ic];
@@ -1008,6 +1101,69 @@ static int helm_solve(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int
         it++;
     }
     if (iters) *iters = it;
+    return TURB_OK;
+}
+
+// FP64 defect correction with FP32 inner Jacobi sweeps: every outer step
+// forms x <- x + e and r = b - A x in FP64 (the convergence test is on this
+// FP64 residual), then approximately solves A e = r with hinner FP32 sweeps.
+static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int *iters)
+{
+    const Dims &d = c->d;
+    const HelmTab &h = q < 3 ? c->helm[q] : c->helm_c[ic];
+    const HelmTabF &hf = q < 3 ? c->helmf[q] : c->helmf_c[ic];
+    const IbDev &ib = c->ib[q];
+    const IbDevF &ibf = c->ibf[q];
+    double a_dt = 1.0 / dt;
+    double *b = c->fld[fb];
+    launch_norm2(c->s, d.n, b, c->part, norm_parts(), c->dscal);
+    TURB_CHECK(cudaMemsetAsync(c->he0, 0, d.n * sizeof(float), c->s));
+    int rc = fetch_scalars(c, 1);
+    if (rc) return rc;
+    double nb = std::sqrt(c->hscal[0]);
+    long long hp = helm_parts(d);
+    long long np = hp + (ib.n > 0 ? (ib.n + 255) / 256 : 0);
+    int it = 0;
+    c->launches += 2;
+    float *e = c->he0, *en = c->he1;
+    for (;;) {
+        int ph = prof_begin(c, TURB_PROF_JACOBI);
+        launch_helm_resid64(c->s, d, h, c->st[q], a_dt, b, c->fld[fx], e, c->jtmp, c->hrf, ib, c->part, hp);
+        prof_end(c, ph, 1);
+        launch_sum_final(c->s, np, c->part, c->dscal);
+        c->launches += 2 + (ib.n > 0);
+        std::swap(c->fld[fx], c->jtmp);     // x <- x + e
+        rc = fetch_scalars(c, 1);
+        if (rc) return rc;
+        double nr = std::sqrt(c->hscal[0]);
+        if (!std::isfinite(nr)) { if (iters) *iters = it; return TURB_ERR_NAN; }
+        if (nr <= c->prm.vel_rtol * nb) break;
+        if (it >= c->prm.vel_maxit) { if (iters) *iters = it; return TURB_ERR_NOT_CONVERGED; }
+        ph = prof_begin(c, TURB_PROF_INNER32);
+        for (int s = 0; s < c->hinner; s++) {
+            launch_helm_jac32(c->s, d, hf, c->st[q], (float)a_dt, c->hrf, e, en, ibf, s == 0);
+            std::swap(e, en);
+        }
+        prof_end(c, ph, c->hinner);
+        c->launches += c->hinner * (1 + (ib.n > 0));
+        it++;
+    }
+    if (iters) *iters = it;
+    return TURB_OK;
+}
+
+static int helm_solve(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int *iters)
+{
+    return c->hmode == TURB_HMODE_MIXED ? helm_solve_mixed(c, q, ic, fx, fb, dt, iters)
+                                        : helm_solve_fp64(c, q, ic, fx, fb, dt, iters);
+}
+
+int turb_set_helmholtz_mode(turb_ctx *c, int mode, int inner_sweeps)
+{
+    if (!c || (mode != TURB_HMODE_FP64 && mode != TURB_HMODE_MIXED) || inner_sweeps < 1 || inner_sweeps > 64)
+        return TURB_ERR_ARG;
+    c->hmode = mode;
+    c->hinner = inner_sweeps;
     return TURB_OK;
 }
 

@@ -80,6 +80,18 @@ struct HelmTab {
     int q;                           // 0 u, 1 v, 2 w, 3 c
 };
 
+// FP32 copies for the inner solves of the mixed-precision defect correction
+struct IbDevF {
+    int n;
+    const int32_t *im, *cnt, *col;
+    const float *val, *diag;
+};
+struct HelmTabF {
+    const float *apx, *apy, *apz, *aw, *ae, *as, *an, *ab, *af;
+    float ap_solid;
+    int q;
+};
+
 // Multigrid level (compact nx*ny*nz layout)
 struct MgLevel {
     int nx, ny, nz;

@@ -4,9 +4,22 @@
 
 #define TURB_MG_MAXLEV 24
 
+// 1-D transfer tables between a level and the next coarser one along one
+// direction: prolongation weights per fine index (two coarse cells) and the
+// transposed (restriction) lists per coarse index (up to four fine cells).
+struct Xfer1D {
+    const int *I0, *I1;
+    const double *w0d, *w1d;
+    const float *w0f, *w1f;
+    const int *rcnt, *rf;
+    const double *rwd;
+    const float *rwf;
+};
+
 struct MgDevLevel {
     int nx, ny, nz;
     int cx, cy, cz;                                   // coarsened into next level
+    Xfer1D tx, ty, tz;                                // transfer to the next level
     const double *dxd, *dyd, *dzd, *rfxd, *rfyd, *rfzd;
     const float *dxf, *dyf, *dzf, *rfxf, *rfyf, *rfzf;
     double pin;
