@@ -274,6 +274,6 @@ def test_failure_paths(api, oracle_mod):
     with pytest.raises(api.TurbError) as e:
         ctx.Velocity_solve("u", case.dt)
     assert e.value.code == 4
-    ctx.load_state(s)
+    ctx.load_state(case.state)
     st = ctx.step(case.dt)
     assert max(st["div_max"]) <= 1e-10

@@ -87,13 +87,8 @@ __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restr
                        T *__restrict__ x)
 {
     LevelT<T> L = lev_of<T>(Ld);
-    int nh = (L.nx + 1) >> 1;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long nrow = (long long)L.ny * L.nz;
-    if (t >= nrow * nh) return;
-    int i2 = (int)(t % nh);
-    long long row = t / nh;
-    int j = (int)(row % L.ny), k = (int)(row / L.ny);
+    int i2 = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (j >= L.ny) return;
     int i = 2 * i2 + ((j + k + color) & 1);
     if (i >= L.nx) return;
     long long c = ((long long)k * L.ny + j) * L.nx + i;
@@ -107,10 +102,9 @@ template <typename T>
 __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r)
 {
     LevelT<T> L = lev_of<T>(Ld);
-    long long n = (long long)L.nx * L.ny * L.nz;
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    int i = (int)(c % L.nx), j = (int)((c / L.nx) % L.ny), k = (int)(c / ((long long)L.nx * L.ny));
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= L.nx || j >= L.ny) return;
+    long long c = ((long long)k * L.ny + j) * L.nx + i;
     T off, dg;
     s_row<T>(L, x, i, j, k, off, dg);
     r[c] = b[c] - (dg * x[c] - off);
@@ -140,10 +134,9 @@ __device__ __forceinline__ const float *pw1_of<float>(const Xfer1D &t) { return 
 template <typename T>
 __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ rf, T *__restrict__ bc)
 {
-    long long n = (long long)Lc.nx * Lc.ny * Lc.nz;
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    int I = (int)(c % Lc.nx), J = (int)((c / Lc.nx) % Lc.ny), K = (int)(c / ((long long)Lc.nx * Lc.ny));
+    int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
+    if (I >= Lc.nx || J >= Lc.ny) return;
+    long long c = ((long long)K * Lc.ny + J) * Lc.nx + I;
     const T *rwx = rw_of<T>(Lf.tx), *rwy = rw_of<T>(Lf.ty), *rwz = rw_of<T>(Lf.tz);
     int nxx = Lf.tx.rcnt[I], nyy = Lf.ty.rcnt[J], nzz = Lf.tz.rcnt[K];
     T s = 0;
@@ -164,10 +157,9 @@ __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ r
 template <typename T>
 __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc, T *__restrict__ xf)
 {
-    long long n = (long long)Lf.nx * Lf.ny * Lf.nz;
-    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    int i = (int)(c % Lf.nx), j = (int)((c / Lf.nx) % Lf.ny), k = (int)(c / ((long long)Lf.nx * Lf.ny));
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= Lf.nx || j >= Lf.ny) return;
+    long long c = ((long long)k * Lf.ny + j) * Lf.nx + i;
     int Ix[2] = {Lf.tx.I0[i], Lf.tx.I1[i]}, Iy[2] = {Lf.ty.I0[j], Lf.ty.I1[j]}, Iz[2] = {Lf.tz.I0[k], Lf.tz.I1[k]};
     T wx[2] = {pw0_of<T>(Lf.tx)[i], pw1_of<T>(Lf.tx)[i]};
     T wy[2] = {pw0_of<T>(Lf.ty)[j], pw1_of<T>(Lf.ty)[j]};
@@ -200,6 +192,8 @@ __global__ void k_coarse(int n, const double *__restrict__ ainv, const T *__rest
 }
 
 inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+inline dim3 g3(int nx, int ny, int nz) { return dim3((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)nz); }
+const dim3 B38(32, 8, 1);
 
 }  // namespace
 
@@ -219,23 +213,21 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
         k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
         return;
     }
-    long long nrb = (long long)L.ny * L.nz * ((L.nx + 1) >> 1);
-    unsigned g = nblk(nrb, 256);
+    dim3 g = g3((L.nx + 1) >> 1, L.ny, L.nz);
     for (int it = 0; it < npre; it++) {
         // the first colour-0 half sweep takes x = 0 (it reads no neighbours);
         // every colour-1 point is then rewritten from colour-0 values only
-        k_rbgs<T><<<g, 256, 0, s>>>(L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
-        k_rbgs<T><<<g, 256, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+        k_rbgs<T><<<g, B38, 0, s>>>(L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
+        k_rbgs<T><<<g, B38, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
     }
-    k_resid<T><<<nblk(n, 256), 256, 0, s>>>(L, H.b[l], H.x[l], H.r[l]);
+    k_resid<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, H.b[l], H.x[l], H.r[l]);
     const MgDevLevel &C = H.lev[l + 1];
-    long long nc = (long long)C.nx * C.ny * C.nz;
-    k_restrict<T><<<nblk(nc, 256), 256, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
+    k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
     mg_vcycle<T>(s, H, l + 1, npre, npost);
-    k_prolong<T><<<nblk(n, 256), 256, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+    k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
     for (int it = 0; it < npost; it++) {
-        k_rbgs<T><<<g, 256, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
-        k_rbgs<T><<<g, 256, 0, s>>>(L, 0, 0, H.b[l], H.invd[l], H.x[l]);
+        k_rbgs<T><<<g, B38, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+        k_rbgs<T><<<g, B38, 0, s>>>(L, 0, 0, H.b[l], H.invd[l], H.x[l]);
     }
 }
 

@@ -19,90 +19,97 @@ __device__ __forceinline__ double warp_sum(double v)
 __device__ __forceinline__ void block_store(double v, double *dst)
 {
     __shared__ double sm[32];
+    int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     v = warp_sum(v);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    if ((lt & 31) == 0) sm[lt >> 5] = v;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        double r = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    if (lt < 32) {
+        double r = (lt < (nt >> 5)) ? sm[lt] : 0.0;
         r = warp_sum(r);
-        if (threadIdx.x == 0) *dst = r;
+        if (lt == 0) *dst = r;
     }
     __syncthreads();
 }
 
+constexpr int KC = 4;   // planes per thread in the 3-D stencil kernels
+__device__ __forceinline__ long long blk3() { return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x; }
+
 struct Cell {
     int i, j, k;
 };
-__device__ __forceinline__ Cell cell_of(const MgDevLevel &L, long long c)
-{
-    Cell o;
-    o.i = (int)(c % L.nx);
-    long long t = c / L.nx;
-    o.j = (int)(t % L.ny);
-    o.k = (int)(t / L.ny);
-    return o;
-}
 
+// (S x)_c in difference form: sum over present faces of f (x_c - x_nb) plus
+// the corner pin; an absent neighbour is redirected to the cell itself so
+// its difference vanishes
 __device__ __forceinline__ double s_apply(const MgDevLevel &L, const double *__restrict__ x, long long c, Cell q)
 {
     long long nx = L.nx, nxy = (long long)L.nx * L.ny;
-    double dyz = L.dyd[q.j] * L.dzd[q.k], dxz = L.dxd[q.i] * L.dzd[q.k], dxy = L.dxd[q.i] * L.dyd[q.j];
-    double o = 0.0, d = 0.0, f, xc = x[c];
-    if (q.i > 0) { f = dyz * L.rfxd[q.i]; d += f; o += f * x[c - 1]; }
-    if (q.i < L.nx - 1) { f = dyz * L.rfxd[q.i + 1]; d += f; o += f * x[c + 1]; }
-    if (q.j > 0) { f = dxz * L.rfyd[q.j]; d += f; o += f * x[c - nx]; }
-    if (q.j < L.ny - 1) { f = dxz * L.rfyd[q.j + 1]; d += f; o += f * x[c + nx]; }
-    if (q.k > 0) { f = dxy * L.rfzd[q.k]; d += f; o += f * x[c - nxy]; }
-    if (q.k < L.nz - 1) { f = dxy * L.rfzd[q.k + 1]; d += f; o += f * x[c + nxy]; }
-    if (q.i == L.nx - 1 && q.j == L.ny - 1 && q.k == L.nz - 1) d += L.pin;
-    return d * xc - o;
+    double xc = x[c];
+    double xw = x[c - (q.i > 0 ? 1 : 0)], xe = x[c + (q.i < L.nx - 1 ? 1 : 0)];
+    double xs = x[c - (q.j > 0 ? nx : 0)], xn = x[c + (q.j < L.ny - 1 ? nx : 0)];
+    double xb = x[c - (q.k > 0 ? nxy : 0)], xf = x[c + (q.k < L.nz - 1 ? nxy : 0)];
+    double sx = fma(L.rfxd[q.i], xc - xw, L.rfxd[q.i + 1] * (xc - xe));
+    double sy = fma(L.rfyd[q.j], xc - xs, L.rfyd[q.j + 1] * (xc - xn));
+    double sz = fma(L.rfzd[q.k], xc - xb, L.rfzd[q.k + 1] * (xc - xf));
+    double dx = L.dxd[q.i], dy = L.dyd[q.j], dz = L.dzd[q.k];
+    double v = fma(dy * dz, sx, fma(dx * dz, sy, (dx * dy) * sz));
+    if (q.i == L.nx - 1 && q.j == L.ny - 1 && q.k == L.nz - 1) v = fma(L.pin, xc, v);
+    return v;
 }
 
 __global__ void k_gather(Dims d, MgDevLevel L, const double *__restrict__ phi, const double *__restrict__ pb,
                          double *__restrict__ x, double *__restrict__ bw)
 {
-    long long n = (long long)L.nx * L.ny * L.nz;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        Cell q = cell_of(L, c);
-        long long p = d.at(q.i, q.j, q.k);
-        x[c] = phi[p];
-        bw[c] = (L.dxd[q.i] * L.dyd[q.j] * L.dzd[q.k]) * pb[p];
-    }
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= L.nx || j >= L.ny) return;
+    long long c = ((long long)k * L.ny + j) * L.nx + i, p = d.at(i, j, k);
+    x[c] = phi[p];
+    bw[c] = (L.dxd[i] * L.dyd[j] * L.dzd[k]) * pb[p];
 }
 
 __global__ void k_scatter(Dims d, MgDevLevel L, const double *__restrict__ x, double *__restrict__ phi)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = blockIdx.y;
-    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
-    if (j >= d.NY) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= d.NX || j >= d.NY) return;
     long long p = d.at(i, j, k);
     phi[p] = (i < L.nx && j < L.ny && k < L.nz) ? x[((long long)k * L.ny + j) * L.nx + i] : 0.0;
 }
 
+// r = W b - S x with partial |r|^2 per block (3-D launch, KC planes per thread)
 __global__ void k_resid(MgDevLevel L, const double *__restrict__ bw, const double *__restrict__ x,
                         double *__restrict__ r, double *__restrict__ part)
 {
-    long long n = (long long)L.nx * L.ny * L.nz;
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double acc = 0.0;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        double v = bw[c] - s_apply(L, x, c, cell_of(L, c));
-        r[c] = v;
-        acc += v * v;
-    }
-    block_store(acc, part + blockIdx.x);
+    if (i < L.nx && j < L.ny)
+        for (int kk = 0; kk < KC; kk++) {
+            int k = blockIdx.z * KC + kk;
+            if (k >= L.nz) break;
+            long long c = ((long long)k * L.ny + j) * L.nx + i;
+            Cell q{i, j, k};
+            double v = bw[c] - s_apply(L, x, c, q);
+            r[c] = v;
+            acc += v * v;
+        }
+    block_store(acc, part + blk3());
 }
 
+// q = S p with partial p.q per block
 __global__ void k_apply(MgDevLevel L, const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part)
 {
-    long long n = (long long)L.nx * L.ny * L.nz;
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double acc = 0.0;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        double v = s_apply(L, p, c, cell_of(L, c));
-        q[c] = v;
-        acc += p[c] * v;
-    }
-    block_store(acc, part + blockIdx.x);
+    if (i < L.nx && j < L.ny)
+        for (int kk = 0; kk < KC; kk++) {
+            int k = blockIdx.z * KC + kk;
+            if (k >= L.nz) break;
+            long long c = ((long long)k * L.ny + j) * L.nx + i;
+            Cell cc{i, j, k};
+            double v = s_apply(L, p, c, cc);
+            q[c] = v;
+            acc += p[c] * v;
+        }
+    block_store(acc, part + blk3());
 }
 
 __global__ void k_dot(long long n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ part)
@@ -126,11 +133,11 @@ __global__ void k_dot2(long long n, const double *__restrict__ r, const double *
     block_store(b, part + NP + blockIdx.x);
 }
 
-__global__ void k_reduce(const double *__restrict__ part, int nvals, double *__restrict__ dst)
+__global__ void k_reduce(const double *__restrict__ part, int nvals, int nper, double *__restrict__ dst)
 {
     for (int v = 0; v < nvals; v++) {
         double acc = 0.0;
-        for (int t = threadIdx.x; t < NP; t += blockDim.x) acc += part[v * NP + t];
+        for (int t = threadIdx.x; t < nper; t += blockDim.x) acc += part[(long long)v * nper + t];
         block_store(acc, dst + v);
     }
 }
@@ -191,27 +198,35 @@ long long ncell(const MgDevLevel &L) { return (long long)L.nx * L.ny * L.nz; }
 
 int pcg_nparts() { return NP; }
 
+static dim3 g3k(const MgDevLevel &L)
+{
+    return dim3((unsigned)((L.nx + 31) / 32), (unsigned)((L.ny + 7) / 8), (unsigned)((L.nz + KC - 1) / KC));
+}
+int pcg_stencil_parts(const MgDevLevel &L)
+{
+    dim3 g = g3k(L);
+    return (int)(g.x * g.y * g.z);
+}
+
 void pcg_gather(cudaStream_t s, const Dims &d, const MgDevLevel &L0, const double *phi_da, const double *pb_da,
                 double *x, double *bw)
 {
-    k_gather<<<NP, BS, 0, s>>>(d, L0, phi_da, pb_da, x, bw);
+    k_gather<<<dim3((L0.nx + 31) / 32, (L0.ny + 7) / 8, L0.nz), dim3(32, 8), 0, s>>>(d, L0, phi_da, pb_da, x, bw);
 }
 
 void pcg_scatter(cudaStream_t s, const Dims &d, const MgDevLevel &L0, const double *x, double *phi_da)
 {
-    long long nij = (long long)d.NX * d.NY;
-    dim3 g((unsigned)((nij + BS - 1) / BS), d.NZ);
-    k_scatter<<<g, BS, 0, s>>>(d, L0, x, phi_da);
+    k_scatter<<<dim3((d.NX + 31) / 32, (d.NY + 7) / 8, d.NZ), dim3(32, 8), 0, s>>>(d, L0, x, phi_da);
 }
 
 void pcg_resid(cudaStream_t s, const MgDevLevel &L0, const double *bw, const double *x, double *r, double *part)
 {
-    k_resid<<<NP, BS, 0, s>>>(L0, bw, x, r, part);
+    k_resid<<<g3k(L0), dim3(32, 8), 0, s>>>(L0, bw, x, r, part);
 }
 
 void pcg_apply(cudaStream_t s, const MgDevLevel &L0, const double *p, double *q, double *part)
 {
-    k_apply<<<NP, BS, 0, s>>>(L0, p, q, part);
+    k_apply<<<g3k(L0), dim3(32, 8), 0, s>>>(L0, p, q, part);
 }
 
 void pcg_dot(cudaStream_t s, long long n, const double *a, const double *b, double *part)
@@ -224,9 +239,9 @@ void pcg_dot2(cudaStream_t s, long long n, const double *r, const double *z, con
     k_dot2<<<NP, BS, 0, s>>>(n, r, z, rold, part);
 }
 
-void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst)
+void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst, int nper)
 {
-    k_reduce<<<1, 1024, 0, s>>>(part, nvals, dst);
+    k_reduce<<<1, 1024, 0, s>>>(part, nvals, nper > 0 ? nper : NP, dst);
 }
 
 void pcg_pupdate(cudaStream_t s, long long n, const double *z, double *p, const PcgScal *sc, int first)

@@ -14,62 +14,86 @@
 
 namespace {
 
-constexpr int HB = 256;   // block size of the Helmholtz sweeps
-
-struct RowOut {
-    double diag, ax;      // diagonal coefficient and (A x)_p
-};
-
-__device__ __forceinline__ RowOut helm_row(const Dims &d, const HelmTab &h, int s, double a_dt,
-                                           const double *__restrict__ x, long long p, int i, int j, int k)
-{
-    RowOut o;
-    bool stencil = (h.q == 3) ? (s == T_FLUID) : (s == T_FLUID || s == T_BUFFER_SOLID);
-    if (stencil) {
-        double dg = h.apx[i] + h.apy[j] + h.apz[k] + a_dt;
-        double acc = dg * x[p];
-        double c;
-        c = h.aw[i]; if (c != 0.0) acc = fma(c, x[p - 1], acc);
-        c = h.ae[i]; if (c != 0.0) acc = fma(c, x[p + 1], acc);
-        c = h.as[j]; if (c != 0.0) acc = fma(c, x[p - d.PX], acc);
-        c = h.an[j]; if (c != 0.0) acc = fma(c, x[p + d.PX], acc);
-        c = h.ab[k]; if (c != 0.0) acc = fma(c, x[p - d.plane], acc);
-        c = h.af[k]; if (c != 0.0) acc = fma(c, x[p + d.plane], acc);
-        o.diag = dg;
-        o.ax = acc;
-    } else {
-        double dg = h.ap_solid + a_dt;
-        o.diag = dg;
-        o.ax = dg * x[p];
-    }
-    return o;
-}
+constexpr int HBX = 32, HBY = 8, KC = 4;   // 32x8 threads over (i, j), KC planes per thread
 
 __device__ __forceinline__ double block_sum(double v)
 {
     __shared__ double sm[32];
+    int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    if ((lt & 31) == 0) sm[lt >> 5] = v;
     __syncthreads();
     double r = 0.0;
-    if (threadIdx.x < 32) {
-        r = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    if (lt < 32) {
+        r = (lt < (nt >> 5)) ? sm[lt] : 0.0;
         for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
     }
-    return r;   // valid in thread 0
+    return r;   // valid in thread (0, 0)
+}
+
+__device__ __forceinline__ long long part_index()
+{
+    return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+}
+
+// offsets of the six neighbours; an absent neighbour (coefficient 0) is
+// redirected to the point itself so that every load stays inside the field
+struct Nb {
+    long long w, e, s, n, b, f;
+};
+__device__ __forceinline__ Nb nb_of(const Dims &d, int i, int j, int k)
+{
+    Nb o;
+    o.w = i > 0 ? -1 : 0;
+    o.e = i < d.NX - 1 ? 1 : 0;
+    o.s = j > 0 ? -(long long)d.PX : 0;
+    o.n = j < d.NY - 1 ? (long long)d.PX : 0;
+    o.b = k > 0 ? -d.plane : 0;
+    o.f = k < d.NZ - 1 ? d.plane : 0;
+    return o;
+}
+
+__device__ __forceinline__ bool is_stencil(int q, int s)
+{
+    return (q == 3) ? (s == T_FLUID) : (s == T_FLUID || s == T_BUFFER_SOLID);
+}
+
+// (A x)_p and the diagonal of a non-immersed row (rows of *_form_LHS_matrix
+// plus 1/dt); coefficients are products of 1-D tables, zero where absent
+__device__ __forceinline__ double helm_ax(const Dims &d, const HelmTab &h, int s, double a_dt,
+                                          const double *__restrict__ x, long long p, int i, int j, int k,
+                                          double &dg)
+{
+    if (!is_stencil(h.q, s)) {
+        dg = h.ap_solid + a_dt;
+        return dg * x[p];
+    }
+    Nb o = nb_of(d, i, j, k);
+    dg = h.apx[i] + h.apy[j] + h.apz[k] + a_dt;
+    double acc = dg * x[p];
+    acc = fma(h.aw[i], x[p + o.w], acc);
+    acc = fma(h.ae[i], x[p + o.e], acc);
+    acc = fma(h.as[j], x[p + o.s], acc);
+    acc = fma(h.an[j], x[p + o.n], acc);
+    acc = fma(h.ab[k], x[p + o.b], acc);
+    acc = fma(h.af[k], x[p + o.f], acc);
+    return acc;
 }
 
 __global__ void k_helm_apply(Dims d, HelmTab h, const uint8_t *__restrict__ st, double a_dt,
                              const double *__restrict__ x, double *__restrict__ y)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = blockIdx.y;
-    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
-    if (j >= d.NY) return;
-    long long p = d.at(i, j, k);
-    int s = st[p];
-    if (s == T_IMMERSED) return;
-    y[p] = helm_row(d, h, s, a_dt, x, p, i, j, k).ax;
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    for (int kk = 0; kk < KC; kk++) {
+        int k = blockIdx.z * KC + kk;
+        if (k >= d.NZ) break;
+        long long p = d.at(i, j, k);
+        int s = st[p];
+        if (s == T_IMMERSED) continue;
+        double dg;
+        y[p] = helm_ax(d, h, s, a_dt, x, p, i, j, k, dg);
+    }
 }
 
 // immersed rows: y = diag*x_im + sum val*x_col
@@ -89,22 +113,23 @@ __global__ void k_helm_jacobi(Dims d, HelmTab h, const uint8_t *__restrict__ st,
                               const double *__restrict__ b, const double *__restrict__ x,
                               double *__restrict__ xn, double *__restrict__ part)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = blockIdx.y;
-    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double r2 = 0.0;
-    if (j < d.NY) {
-        long long p = d.at(i, j, k);
-        int s = st[p];
-        if (s != T_IMMERSED) {
-            RowOut o = helm_row(d, h, s, a_dt, x, p, i, j, k);
-            double r = b[p] - o.ax;
-            xn[p] = x[p] + r / o.diag;
-            r2 = r * r;
+    if (i < d.NX && j < d.NY) {
+        for (int kk = 0; kk < KC; kk++) {
+            int k = blockIdx.z * KC + kk;
+            if (k >= d.NZ) break;
+            long long p = d.at(i, j, k);
+            int s = st[p];
+            if (s == T_IMMERSED) continue;
+            double dg, ax = helm_ax(d, h, s, a_dt, x, p, i, j, k, dg);
+            double r = b[p] - ax;
+            xn[p] = x[p] + r / dg;
+            r2 = fma(r, r, r2);
         }
     }
     double bs = block_sum(r2);
-    if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + blockIdx.x] = bs;
+    if (threadIdx.x == 0 && threadIdx.y == 0) part[part_index()] = bs;
 }
 
 __global__ void k_ib_jacobi(IbDev ib, const double *__restrict__ b, const double *__restrict__ x,
@@ -134,58 +159,47 @@ __global__ void k_sum_final(long long n, const double *__restrict__ part, double
 }
 
 // ---- mixed-precision defect correction -----------------------------------
-// outer: x <- x + e, r = b - A x in FP64 (rounded to FP32 for the inner solve)
+// xn = x + e over the whole field (FP64 accumulation of the FP32 correction)
+__global__ void k_add_corr(long long n, const double *__restrict__ x, const float *__restrict__ e,
+                           double *__restrict__ xn)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+        xn[p] = x[p] + (double)e[p];
+}
+
+// r = b - A x in FP64, rounded to FP32 for the inner solve; |r|^2 partials
 __global__ void k_helm_resid64(Dims d, HelmTab h, const uint8_t *__restrict__ st, double a_dt,
                                const double *__restrict__ b, const double *__restrict__ x,
-                               const float *__restrict__ e, double *__restrict__ xn, float *__restrict__ rf,
-                               double *__restrict__ part)
+                               float *__restrict__ rf, double *__restrict__ part)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = blockIdx.y;
-    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double r2 = 0.0;
-    if (j < d.NY) {
-        long long p = d.at(i, j, k);
-        int s = st[p];
-        double xp = x[p] + (double)e[p];
-        xn[p] = xp;
-        if (s != T_IMMERSED) {
-            bool stencil = (h.q == 3) ? (s == T_FLUID) : (s == T_FLUID || s == T_BUFFER_SOLID);
-            double acc;
-            if (stencil) {
-                double dg = h.apx[i] + h.apy[j] + h.apz[k] + a_dt, c;
-                acc = dg * xp;
-                c = h.aw[i]; if (c != 0.0) acc = fma(c, x[p - 1] + (double)e[p - 1], acc);
-                c = h.ae[i]; if (c != 0.0) acc = fma(c, x[p + 1] + (double)e[p + 1], acc);
-                c = h.as[j]; if (c != 0.0) acc = fma(c, x[p - d.PX] + (double)e[p - d.PX], acc);
-                c = h.an[j]; if (c != 0.0) acc = fma(c, x[p + d.PX] + (double)e[p + d.PX], acc);
-                c = h.ab[k]; if (c != 0.0) acc = fma(c, x[p - d.plane] + (double)e[p - d.plane], acc);
-                c = h.af[k]; if (c != 0.0) acc = fma(c, x[p + d.plane] + (double)e[p + d.plane], acc);
-            } else {
-                acc = (h.ap_solid + a_dt) * xp;
-            }
-            double r = b[p] - acc;
+    if (i < d.NX && j < d.NY) {
+        for (int kk = 0; kk < KC; kk++) {
+            int k = blockIdx.z * KC + kk;
+            if (k >= d.NZ) break;
+            long long p = d.at(i, j, k);
+            int s = st[p];
+            if (s == T_IMMERSED) continue;
+            double dg, r = b[p] - helm_ax(d, h, s, a_dt, x, p, i, j, k, dg);
             rf[p] = (float)r;
-            r2 = r * r;
+            r2 = fma(r, r, r2);
         }
     }
     double bs = block_sum(r2);
-    if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + blockIdx.x] = bs;
+    if (threadIdx.x == 0 && threadIdx.y == 0) part[part_index()] = bs;
 }
 
 __global__ void k_ib_resid64(IbDev ib, const double *__restrict__ b, const double *__restrict__ x,
-                             const float *__restrict__ e, float *__restrict__ rf, double *__restrict__ part)
+                             float *__restrict__ rf, double *__restrict__ part)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     double r2 = 0.0;
     if (t < ib.n) {
         long long im = ib.im[t];
-        double acc = ib.diag[t] * (x[im] + (double)e[im]);
+        double acc = ib.diag[t] * x[im];
         int c = ib.cnt[t];
-        for (int g = 0; g < c; g++) {
-            long long q = ib.col[t * 8 + g];
-            acc += ib.val[t * 8 + g] * (x[q] + (double)e[q]);
-        }
+        for (int g = 0; g < c; g++) acc += ib.val[t * 8 + g] * x[ib.col[t * 8 + g]];
         double r = b[im] - acc;
         rf[im] = (float)r;
         r2 = r * r;
@@ -199,26 +213,30 @@ __global__ void k_helm_jac32(Dims d, HelmTabF h, const uint8_t *__restrict__ st,
                              const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
                              int first)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = blockIdx.y;
-    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
-    if (j >= d.NY) return;
-    long long p = d.at(i, j, k);
-    int s = st[p];
-    if (s == T_IMMERSED) return;
-    bool stencil = (h.q == 3) ? (s == T_FLUID) : (s == T_FLUID || s == T_BUFFER_SOLID);
-    float dg = stencil ? (h.apx[i] + h.apy[j] + h.apz[k] + a_dt) : (h.ap_solid + a_dt);
-    if (first) { en[p] = r[p] / dg; return; }
-    float acc = dg * e[p], c;
-    if (stencil) {
-        c = h.aw[i]; if (c != 0.0f) acc = fmaf(c, e[p - 1], acc);
-        c = h.ae[i]; if (c != 0.0f) acc = fmaf(c, e[p + 1], acc);
-        c = h.as[j]; if (c != 0.0f) acc = fmaf(c, e[p - d.PX], acc);
-        c = h.an[j]; if (c != 0.0f) acc = fmaf(c, e[p + d.PX], acc);
-        c = h.ab[k]; if (c != 0.0f) acc = fmaf(c, e[p - d.plane], acc);
-        c = h.af[k]; if (c != 0.0f) acc = fmaf(c, e[p + d.plane], acc);
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.NX || j >= d.NY) return;
+    for (int kk = 0; kk < KC; kk++) {
+        int k = blockIdx.z * KC + kk;
+        if (k >= d.NZ) break;
+        long long p = d.at(i, j, k);
+        int s = st[p];
+        if (s == T_IMMERSED) continue;
+        bool stencil = is_stencil(h.q, s);
+        float dg = stencil ? (h.apx[i] + h.apy[j] + h.apz[k] + a_dt) : (h.ap_solid + a_dt);
+        float inv = __frcp_rn(dg);
+        if (first) { en[p] = r[p] * inv; continue; }
+        float acc = dg * e[p];
+        if (stencil) {
+            Nb o = nb_of(d, i, j, k);
+            acc = fmaf(h.aw[i], e[p + o.w], acc);
+            acc = fmaf(h.ae[i], e[p + o.e], acc);
+            acc = fmaf(h.as[j], e[p + o.s], acc);
+            acc = fmaf(h.an[j], e[p + o.n], acc);
+            acc = fmaf(h.ab[k], e[p + o.b], acc);
+            acc = fmaf(h.af[k], e[p + o.f], acc);
+        }
+        en[p] = fmaf(r[p] - acc, inv, e[p]);
     }
-    en[p] = e[p] + (r[p] - acc) / dg;
 }
 
 __global__ void k_ib_jac32(IbDevF ib, const float *__restrict__ r, const float *__restrict__ e,
@@ -227,11 +245,18 @@ __global__ void k_ib_jac32(IbDevF ib, const float *__restrict__ r, const float *
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ib.n) return;
     long long im = ib.im[t];
-    if (first) { en[im] = r[im] / ib.diag[t]; return; }
+    float inv = __frcp_rn(ib.diag[t]);
+    if (first) { en[im] = r[im] * inv; return; }
     float acc = ib.diag[t] * e[im];
     int c = ib.cnt[t];
     for (int g = 0; g < c; g++) acc += ib.val[t * 8 + g] * e[ib.col[t * 8 + g]];
-    en[im] = e[im] + (r[im] - acc) / ib.diag[t];
+    en[im] = fmaf(r[im] - acc, inv, e[im]);
+}
+
+inline dim3 hgrid(const Dims &d)
+{
+    return dim3((unsigned)((d.NX + HBX - 1) / HBX), (unsigned)((d.NY + HBY - 1) / HBY),
+                (unsigned)((d.NZ + KC - 1) / KC));
 }
 
 constexpr int NPART = 1024;
@@ -249,37 +274,16 @@ __global__ void k_norm2(long long n, const double *__restrict__ x, double *__res
 
 long long helm_parts(const Dims &d)
 {
-    long long nij = (long long)d.NX * d.NY;
-    return ((nij + HB - 1) / HB) * d.NZ;
+    dim3 g = hgrid(d);
+    return (long long)g.x * g.y * g.z;
 }
 
 long long norm_parts() { return NPART; }
 
-void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
-                         const double *b, const double *x, const float *e, double *xn, float *rf, const IbDev &ib,
-                         double *part, long long nparts)
-{
-    long long nij = (long long)d.NX * d.NY;
-    dim3 g((unsigned)((nij + HB - 1) / HB), d.NZ);
-    k_helm_resid64<<<g, HB, 0, s>>>(d, h, st, a_dt, b, x, e, xn, rf, part);
-    if (ib.n > 0) k_ib_resid64<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, b, x, e, rf, part + nparts);
-}
-
-void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
-                       const float *r, const float *e, float *en, const IbDevF &ib, int first)
-{
-    long long nij = (long long)d.NX * d.NY;
-    dim3 g((unsigned)((nij + HB - 1) / HB), d.NZ);
-    k_helm_jac32<<<g, HB, 0, s>>>(d, h, st, a_dt, r, e, en, first);
-    if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
-}
-
 void launch_helm_apply(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
                        const double *x, double *y, const IbDev &ib)
 {
-    long long nij = (long long)d.NX * d.NY;
-    dim3 g((unsigned)((nij + HB - 1) / HB), d.NZ);
-    k_helm_apply<<<g, HB, 0, s>>>(d, h, st, a_dt, x, y);
+    k_helm_apply<<<hgrid(d), dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, x, y);
     if (ib.n > 0) k_ib_apply<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, x, y);
 }
 
@@ -288,16 +292,8 @@ void launch_helm_jacobi(cudaStream_t s, const Dims &d, const HelmTab &h, const u
                         const double *b, const double *x, double *xn, const IbDev &ib, double *part,
                         long long nparts)
 {
-    long long nij = (long long)d.NX * d.NY;
-    dim3 g((unsigned)((nij + HB - 1) / HB), d.NZ);
-    k_helm_jacobi<<<g, HB, 0, s>>>(d, h, st, a_dt, b, x, xn, part);
-    long long np = nparts;
-    if (ib.n > 0) {
-        int nbk = (ib.n + 255) / 256;
-        k_ib_jacobi<<<nbk, 256, 0, s>>>(ib, b, x, xn, part + nparts);
-        np += nbk;
-    }
-    (void)np;
+    k_helm_jacobi<<<hgrid(d), dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, b, x, xn, part);
+    if (ib.n > 0) k_ib_jacobi<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, b, x, xn, part + nparts);
 }
 
 void launch_sum_final(cudaStream_t s, long long nparts, const double *part, double *out)
@@ -310,4 +306,24 @@ void launch_norm2(cudaStream_t s, long long n, const double *x, double *part, lo
     (void)nparts;
     k_norm2<<<NPART, 256, 0, s>>>(n, x, part);
     k_sum_final<<<1, 1024, 0, s>>>(NPART, part, out);
+}
+
+void launch_add_corr(cudaStream_t s, long long n, const double *x, const float *e, double *xn)
+{
+    k_add_corr<<<1216, 256, 0, s>>>(n, x, e, xn);
+}
+
+void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
+                         const double *b, const double *x, float *rf, const IbDev &ib, double *part,
+                         long long nparts)
+{
+    k_helm_resid64<<<hgrid(d), dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, b, x, rf, part);
+    if (ib.n > 0) k_ib_resid64<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, b, x, rf, part + nparts);
+}
+
+void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
+                       const float *r, const float *e, float *en, const IbDevF &ib, int first)
+{
+    k_helm_jac32<<<hgrid(d), dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
+    if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
 }

@@ -36,14 +36,14 @@ struct Ijk {
     bool ok;
 };
 
+// 3-D launch: blocks of 32 x 8 threads over (i, j), one z-block per k
 __device__ __forceinline__ Ijk ijk_of(const Dims &d)
 {
     Ijk r;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    r.k = blockIdx.y;
-    r.j = (int)(t / d.NX);
-    r.i = (int)(t - (long long)r.j * d.NX);
-    r.ok = r.j < d.NY;
+    r.i = blockIdx.x * blockDim.x + threadIdx.x;
+    r.j = blockIdx.y * blockDim.y + threadIdx.y;
+    r.k = blockIdx.z;
+    r.ok = r.i < d.NX && r.j < d.NY;
     return r;
 }
 
@@ -203,14 +203,15 @@ __global__ void k_divergence(Dims d, const uint8_t *__restrict__ st, const doubl
     }
     // block max (values are >= 0)
     __shared__ double sm[32];
+    int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     double m = dc;
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    if ((lt & 31) == 0) sm[lt >> 5] = m;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        m = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    if (lt < 32) {
+        m = (lt < (nt >> 5)) ? sm[lt] : 0.0;
         for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + blockIdx.x] = m;
+        if (lt == 0) part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = m;
     }
 }
 
@@ -242,22 +243,22 @@ __global__ void k_axpby(long long n, double a, const double *__restrict__ x, dou
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-static inline dim3 grid_of(const Dims &d, int bs)
+static const dim3 B3(32, 8, 1);
+static inline dim3 grid_of(const Dims &d, int)
 {
-    long long nij = (long long)d.NX * d.NY;
-    return dim3((unsigned)((nij + bs - 1) / bs), (unsigned)d.NZ, 1);
+    return dim3((unsigned)((d.NX + 31) / 32), (unsigned)((d.NY + 7) / 8), (unsigned)d.NZ);
 }
 
 void launch_cell_center(cudaStream_t s, const Dims &d, Interp2 ix, Interp2 iy, Interp2 iz, const double *u,
                         const double *v, const double *w, double *ubc, double *vbc, double *wbc)
 {
-    k_cell_center<<<grid_of(d, 256), 256, 0, s>>>(d, ix, iy, iz, u, v, w, ubc, vbc, wbc);
+    k_cell_center<<<grid_of(d, 256), B3, 0, s>>>(d, ix, iy, iz, u, v, w, ubc, vbc, wbc);
 }
 
 void launch_transpose(cudaStream_t s, const Dims &d, int which, const uint8_t *st, TransW tw, const double *u,
                       const double *v, const double *w, double *A, double *B)
 {
-    k_transpose<<<grid_of(d, 256), 256, 0, s>>>(d, which, st, tw, u, v, w, A, B);
+    k_transpose<<<grid_of(d, 256), B3, 0, s>>>(d, which, st, tw, u, v, w, A, B);
 }
 
 void launch_total_conc(cudaStream_t s, long long n, int nc, ConcPtrs c, ConcW a, double *ct)
@@ -273,7 +274,7 @@ void launch_shift(cudaStream_t s, long long n, const double *x, double sh, doubl
 void launch_rhs_vel(cudaStream_t s, const Dims &d, int q, const uint8_t *st, double a_dt, const double *x,
                     const double *conv, const double *dp, const double *ct, int buoy, Interp2 iyv, double *b)
 {
-    k_rhs_vel<<<grid_of(d, 256), 256, 0, s>>>(d, q, st, a_dt, x, conv, dp, ct, buoy, iyv, b);
+    k_rhs_vel<<<grid_of(d, 256), B3, 0, s>>>(d, q, st, a_dt, x, conv, dp, ct, buoy, iyv, b);
 }
 
 void launch_rhs_conc(cudaStream_t s, long long n, const uint8_t *st, double a_dt, const double *c,
@@ -286,19 +287,19 @@ void launch_pressure_rhs(cudaStream_t s, const Dims &d, const uint8_t *st, const
                          const double *cz, double a_dt, const double *u, const double *v, const double *w,
                          double *b)
 {
-    k_pressure_rhs<<<grid_of(d, 256), 256, 0, s>>>(d, st, cx, cy, cz, a_dt, u, v, w, b);
+    k_pressure_rhs<<<grid_of(d, 256), B3, 0, s>>>(d, st, cx, cy, cz, a_dt, u, v, w, b);
 }
 
 void launch_project(cudaStream_t s, const Dims &d, ProjArgs a, const double *phi, const double *pb, double *u,
                     double *v, double *w, double *dpx, double *dpy, double *dpz)
 {
-    k_project<<<grid_of(d, 256), 256, 0, s>>>(d, a, phi, pb, u, v, w, dpx, dpy, dpz);
+    k_project<<<grid_of(d, 256), B3, 0, s>>>(d, a, phi, pb, u, v, w, dpx, dpy, dpz);
 }
 
 long long divergence_parts(const Dims &d)
 {
     dim3 g = grid_of(d, 256);
-    return (long long)g.x * g.y;
+    return (long long)g.x * g.y * g.z;
 }
 
 void launch_divergence(cudaStream_t s, const Dims &d, const uint8_t *st, const double *mxc, const double *myc,
@@ -306,8 +307,8 @@ void launch_divergence(cudaStream_t s, const Dims &d, const uint8_t *st, const d
                        const double *v, const double *w, double *div, double *part, double *out)
 {
     dim3 g = grid_of(d, 256);
-    k_divergence<<<g, 256, 0, s>>>(d, st, mxc, myc, mzc, a_dEta, a_dXi, a_dPhi, u, v, w, div, part);
-    k_max_final<<<1, 1024, 0, s>>>((long long)g.x * g.y, part, out);
+    k_divergence<<<g, B3, 0, s>>>(d, st, mxc, myc, mzc, a_dEta, a_dXi, a_dPhi, u, v, w, div, part);
+    k_max_final<<<1, 1024, 0, s>>>((long long)g.x * g.y * g.z, part, out);
 }
 
 void launch_axpby(cudaStream_t s, long long n, double a, const double *x, double b, double *y)

@@ -101,6 +101,13 @@ struct turb_ctx {
     double prof_ms[TURB_PROF_NGROUPS] = {0};
     long long prof_nl[TURB_PROF_NGROUPS] = {0};
     cudaEvent_t user_ev[8] = {nullptr};
+    // CUDA graphs: V-cycle per pressure mode, CG vector step (restart / not),
+    // FP32 inner sweeps of each Helmholtz field
+    cudaGraphExec_t g_mg[2] = {nullptr, nullptr};
+    cudaGraphExec_t g_pcg[2] = {nullptr, nullptr};
+    cudaGraphExec_t g_inner[3 + TURB_MAXCONC] = {nullptr};
+    int g_inner_n[3 + TURB_MAXCONC] = {0};
+    int use_graphs = 1;
 };
 
 namespace {
@@ -714,6 +721,27 @@ void prof_collect(turb_ctx *c)
     c->recs.clear();
 }
 
+template <typename F>
+int capture(turb_ctx *c, cudaGraphExec_t *out, F body)
+{
+    cudaGraph_t g = nullptr;
+    TURB_CHECK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaError_t e = cudaStreamEndCapture(c->s, &g);
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    return TURB_OK;
+}
+
+void free_graphs(turb_ctx *c)
+{
+    for (auto &g : c->g_mg) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto &g : c->g_pcg) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto &g : c->g_inner) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -845,6 +873,7 @@ int turb_create(const turb_grid_desc *g, const turb_params *p, turb_ctx **out)
         c->proj.a_dEta = a_dEta;
     }
     c->nparts = std::max<long long>(std::max(helm_parts(d), divergence_parts(d)), (long long)pcg_nparts() * 2);
+    c->nparts = std::max<long long>(c->nparts, (long long)((d.nx + 31) / 32) * ((d.ny + 7) / 8) * d.nz);
     c->part = m.alloc<double>(c->nparts + 4096);
     c->dscal = m.alloc<double>(16);
     if (m.err != cudaSuccess) { m.release(); cudaStreamDestroy(c->s); delete c; return TURB_ERR_ALLOC; }
@@ -861,6 +890,7 @@ int turb_destroy(turb_ctx *c)
     if (!c) return TURB_ERR_ARG;
     cudaStreamSynchronize(c->s);
     prof_collect(c);
+    free_graphs(c);
     for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
     for (cudaEvent_t e : c->user_ev)
         if (e) cudaEventDestroy(e);
@@ -1117,7 +1147,6 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
     double a_dt = 1.0 / dt;
     double *b = c->fld[fb];
     launch_norm2(c->s, d.n, b, c->part, norm_parts(), c->dscal);
-    TURB_CHECK(cudaMemsetAsync(c->he0, 0, d.n * sizeof(float), c->s));
     int rc = fetch_scalars(c, 1);
     if (rc) return rc;
     double nb = std::sqrt(c->hscal[0]);
@@ -1127,12 +1156,16 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
     c->launches += 2;
     float *e = c->he0, *en = c->he1;
     for (;;) {
+        if (it > 0) {
+            launch_add_corr(c->s, d.n, c->fld[fx], e, c->jtmp);   // x <- x + e
+            std::swap(c->fld[fx], c->jtmp);
+            c->launches += 1;
+        }
         int ph = prof_begin(c, TURB_PROF_JACOBI);
-        launch_helm_resid64(c->s, d, h, c->st[q], a_dt, b, c->fld[fx], e, c->jtmp, c->hrf, ib, c->part, hp);
+        launch_helm_resid64(c->s, d, h, c->st[q], a_dt, b, c->fld[fx], c->hrf, ib, c->part, hp);
         prof_end(c, ph, 1);
         launch_sum_final(c->s, np, c->part, c->dscal);
         c->launches += 2 + (ib.n > 0);
-        std::swap(c->fld[fx], c->jtmp);     // x <- x + e
         rc = fetch_scalars(c, 1);
         if (rc) return rc;
         double nr = std::sqrt(c->hscal[0]);
@@ -1140,10 +1173,25 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
         if (nr <= c->prm.vel_rtol * nb) break;
         if (it >= c->prm.vel_maxit) { if (iters) *iters = it; return TURB_ERR_NOT_CONVERGED; }
         ph = prof_begin(c, TURB_PROF_INNER32);
-        for (int s = 0; s < c->hinner; s++) {
-            launch_helm_jac32(c->s, d, hf, c->st[q], (float)a_dt, c->hrf, e, en, ibf, s == 0);
-            std::swap(e, en);
+        int gi = q < 3 ? q : 3 + ic;
+        auto sweeps = [&]() {
+            float *ea = c->he0, *eb = c->he1;
+            for (int t = 0; t < c->hinner; t++) {
+                launch_helm_jac32(c->s, d, hf, c->st[q], (float)a_dt, c->hrf, ea, eb, ibf, t == 0);
+                std::swap(ea, eb);
+            }
+        };
+        if (c->use_graphs) {
+            if (c->g_inner[gi] && c->g_inner_n[gi] != c->hinner) { cudaGraphExecDestroy(c->g_inner[gi]); c->g_inner[gi] = nullptr; }
+            if (!c->g_inner[gi]) { int rc2 = capture(c, &c->g_inner[gi], sweeps); if (rc2) return rc2; c->g_inner_n[gi] = c->hinner; }
+            TURB_CHECK(cudaGraphLaunch(c->g_inner[gi], c->s));
+        } else {
+            sweeps();
         }
+        // the sweeps start from he0 and alternate; the result is in he0 after
+        // an even number of sweeps
+        e = (c->hinner % 2 == 0) ? c->he0 : c->he1;
+        en = (e == c->he0) ? c->he1 : c->he0;
         prof_end(c, ph, c->hinner);
         c->launches += c->hinner * (1 + (ib.n > 0));
         it++;
@@ -1212,8 +1260,9 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     pcg_gather(s, d, L0, c->fld[TURB_F_PHI], c->fld[TURB_F_PB], c->px, c->pbw);
     pcg_dot(s, n0, c->pbw, c->pbw, c->part);
     pcg_reduce(s, c->part, 1, dsc + 0);
+    int nsp = pcg_stencil_parts(L0);
     pcg_resid(s, L0, c->pbw, c->px, c->pr, c->part);
-    pcg_reduce(s, c->part, 1, dsc + 1);
+    pcg_reduce(s, c->part, 1, dsc + 1, nsp);
     c->launches += 5;
     TURB_CHECK(cudaMemcpyAsync(c->hscal, dsc, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     TURB_CHECK(cudaStreamSynchronize(s));
@@ -1226,7 +1275,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
         if (nr <= tol || it >= c->prm.p_maxit) {
             pcg_resid(s, L0, c->pbw, c->px, c->pr, c->part);
-            pcg_reduce(s, c->part, 1, dsc + 1);
+            pcg_reduce(s, c->part, 1, dsc + 1, nsp);
             c->launches += 2;
             TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
             TURB_CHECK(cudaStreamSynchronize(s));
@@ -1235,31 +1284,49 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             if (it >= c->prm.p_maxit) { status = TURB_ERR_NOT_CONVERGED; break; }
             restart = 1;
         }
+        int pm = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
+        auto vcycle = [&]() {
+            if (pm == 0) {
+                mg_vcycle<double>(s, c->H64, 0, npre, npost);
+            } else {
+                pcg_to_float(s, n0, c->pr, c->H32.b[0]);
+                mg_vcycle<float>(s, c->H32, 0, npre, npost);
+                pcg_to_double(s, n0, c->H32.x[0], c->pz);
+            }
+        };
+        auto cgstep = [&](int rs) {
+            pcg_dot2(s, n0, c->pr, c->pz, c->pro, c->part);
+            pcg_reduce(s, c->part, 2, dsc + 2);   // rz and z.r_old
+            if (!rs) pcg_scalars(s, sc, 0);
+            pcg_pupdate(s, n0, c->pz, c->pp, sc, rs);
+            pcg_apply(s, L0, c->pp, c->pq, c->part);
+            pcg_reduce(s, c->part, 1, dsc + 5, nsp);
+            pcg_scalars(s, sc, 1);
+            pcg_xrupdate(s, n0, c->px, c->pr, c->pro, c->pp, c->pq, sc, c->part);
+            pcg_reduce(s, c->part, 1, dsc + 1);
+        };
+        int nmg = vl + (pm ? 2 : 0), ncg = 8 + (restart ? 0 : 1);
         int ph = prof_begin(c, TURB_PROF_MG);
-        if (c->pmode == TURB_PMODE_FP64) {
-            mg_vcycle<double>(s, c->H64, 0, npre, npost);
-            c->launches += vl;
-            prof_end(c, ph, vl);
+        if (c->use_graphs) {
+            if (!c->g_mg[pm]) { int rc = capture(c, &c->g_mg[pm], vcycle); if (rc) return rc; }
+            TURB_CHECK(cudaGraphLaunch(c->g_mg[pm], s));
         } else {
-            pcg_to_float(s, n0, c->pr, c->H32.b[0]);
-            mg_vcycle<float>(s, c->H32, 0, npre, npost);
-            pcg_to_double(s, n0, c->H32.x[0], c->pz);
-            c->launches += vl + 2;
-            prof_end(c, ph, vl + 2);
+            vcycle();
         }
+        prof_end(c, ph, nmg);
         ph = prof_begin(c, TURB_PROF_PCG);
-        pcg_dot2(s, n0, c->pr, c->pz, c->pro, c->part);
-        pcg_reduce(s, c->part, 2, dsc + 2);   // rz and z.r_old
-        c->launches += 2;
-        if (!restart) { pcg_scalars(s, sc, 0); c->launches += 1; }
-        pcg_pupdate(s, n0, c->pz, c->pp, sc, restart);
-        pcg_apply(s, L0, c->pp, c->pq, c->part);
-        pcg_reduce(s, c->part, 1, dsc + 5);
-        pcg_scalars(s, sc, 1);
-        pcg_xrupdate(s, n0, c->px, c->pr, c->pro, c->pp, c->pq, sc, c->part);
-        pcg_reduce(s, c->part, 1, dsc + 1);
-        c->launches += 6;
-        prof_end(c, ph, 8 + (restart ? 0 : 1));
+        if (c->use_graphs) {
+            if (!c->g_pcg[restart]) {
+                int rs = restart;
+                int rc = capture(c, &c->g_pcg[restart], [&]() { cgstep(rs); });
+                if (rc) return rc;
+            }
+            TURB_CHECK(cudaGraphLaunch(c->g_pcg[restart], s));
+        } else {
+            cgstep(restart);
+        }
+        prof_end(c, ph, ncg);
+        c->launches += nmg + ncg;
         TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
         TURB_CHECK(cudaStreamSynchronize(s));
         nr = std::sqrt(c->hscal[1]);
@@ -1439,10 +1506,8 @@ namespace {
 __global__ void k_pressure_apply(Dims d, const uint8_t *__restrict__ st, Geo g, double dEta, double dXi, double dPhi,
                                  const double *__restrict__ x, double *__restrict__ y)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int k = blockIdx.y;
-    int j = (int)(t / d.NX), i = (int)(t - (long long)j * d.NX);
-    if (j >= d.NY) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= d.NX || j >= d.NY) return;
     long long p = d.at(i, j, k);
     double Cx = -1.0 / (dEta * dEta), Cy = -1.0 / (dXi * dXi), Cz = -1.0 / (dPhi * dPhi);
     if (st[p] == T_BOUNDARY) {
@@ -1470,7 +1535,5 @@ __global__ void k_pressure_apply(Dims d, const uint8_t *__restrict__ st, Geo g, 
 void launch_pressure_apply(cudaStream_t s, const Dims &d, const uint8_t *st, const Geo &g, double dEta, double dXi,
                            double dPhi, const double *x, double *y)
 {
-    long long nij = (long long)d.NX * d.NY;
-    dim3 gr((unsigned)((nij + 255) / 256), d.NZ);
-    k_pressure_apply<<<gr, 256, 0, s>>>(d, st, g, dEta, dXi, dPhi, x, y);
+    k_pressure_apply<<<dim3((d.NX + 31) / 32, (d.NY + 7) / 8, d.NZ), dim3(32, 8), 0, s>>>(d, st, g, dEta, dXi, dPhi, x, y);
 }

@@ -59,9 +59,10 @@ void launch_helm_jacobi(cudaStream_t s, const Dims &d, const HelmTab &h, const u
                         const double *b, const double *x, double *xn, const IbDev &ib, double *part,
                         long long nparts);
 long long helm_parts(const Dims &d);
+void launch_add_corr(cudaStream_t s, long long n, const double *x, const float *e, double *xn);
 void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
-                         const double *b, const double *x, const float *e, double *xn, float *rf, const IbDev &ib,
-                         double *part, long long nparts);
+                         const double *b, const double *x, float *rf, const IbDev &ib, double *part,
+                         long long nparts);
 void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
                        const float *r, const float *e, float *en, const IbDevF &ib, int first);
 void launch_sum_final(cudaStream_t s, long long nparts, const double *part, double *out);

@@ -50,7 +50,8 @@ void pcg_resid(cudaStream_t s, const MgDevLevel &L0, const double *bw, const dou
 void pcg_apply(cudaStream_t s, const MgDevLevel &L0, const double *p, double *q, double *part);
 void pcg_dot(cudaStream_t s, long long n, const double *a, const double *b, double *part);
 void pcg_dot2(cudaStream_t s, long long n, const double *r, const double *z, const double *rold, double *part);
-void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst);
+void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst, int nper = 0);
+int pcg_stencil_parts(const MgDevLevel &L);
 void pcg_pupdate(cudaStream_t s, long long n, const double *z, double *p, const PcgScal *sc, int first);
 void pcg_xrupdate(cudaStream_t s, long long n, double *x, double *r, double *rold, const double *p,
                   const double *q, const PcgScal *sc, double *part);
