@@ -132,6 +132,10 @@ int turb_field_download(turb_ctx *ctx, int field, double *host_da);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
+/* ENO divided differences: 1 (default) divides by a grid spacing through its
+ * precomputed reciprocal with two correction steps, 0 uses IEEE division;
+ * both round to nearest, so the results are the same bits */
+int turb_set_eno_division(turb_ctx *ctx, int fast);
 int turb_synchronize(turb_ctx *ctx);
 const char *turb_status_string(int status);
 
@@ -197,6 +201,12 @@ int turb_kernel_launches(turb_ctx *ctx, long long *n);
 /* page-lock caller memory for the host-buffer transfers */
 int turb_host_register(void *ptr, size_t bytes);
 int turb_host_unregister(void *ptr);
+
+/* self-test: the ENO kernels' division by a grid spacing (reciprocal-based,
+ * two Markstein corrections) against IEEE division on nsamples operand pairs;
+ * returns the number of bitwise mismatches (and one offending (a, h)) */
+int turb_selftest_division(long long nsamples, unsigned long long seed,
+                           unsigned long long *mismatches, double *example);
 
 /* operator hooks used by the parity tests: y = A x on device fields */
 int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);

@@ -79,11 +79,23 @@ def test_cell_center_transpose_bitexact(api, oracle_mod, name, mk):
         assert same(ctx.download(api.F_SCRATCH1)[nb], B[nb])
 
 
+def test_division_selftest(api):
+    """The ENO kernels divide by grid spacings through a precomputed
+    reciprocal and two Markstein corrections; that must give the IEEE
+    quotient bit for bit (random, near-representable and near-midpoint
+    quotients, differences of nearby values)."""
+    for seed in (1, 2, 3, 4):
+        bad, ex = api.selftest_division(1 << 29, seed)
+        assert bad == 0, (bad, ex)
+
+
+@pytest.mark.parametrize("fastdiv", [1, 0])
 @pytest.mark.parametrize("name,mk", CASES)
-def test_convection_bitexact(api, oracle_mod, name, mk):
+def test_convection_bitexact(api, oracle_mod, name, mk, fastdiv):
     case = mk()
     s = _cases.random_state(case, seed=3)
     ctx, orc, _ = _pair(case, api, oracle_mod, s)
+    ctx.set_eno_division(fastdiv)
     for q, f in (("u", api.F_CONV_U), ("v", api.F_CONV_V), ("w", api.F_CONV_W)):
         ctx.Velocity_convective_terms(q)
         if q == "u":

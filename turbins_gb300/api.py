@@ -196,6 +196,9 @@ class Context:
     def set_helmholtz_mode(self, mode, inner_sweeps=6):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")
 
+    def set_eno_division(self, fast):
+        _check(self.lib.turb_set_eno_division(self.ctx, 1 if fast else 0), "set_eno_division")
+
     def synchronize(self):
         _check(self.lib.turb_synchronize(self.ctx), "synchronize")
 
@@ -321,3 +324,12 @@ def host_register(arr):
 
 def host_unregister(arr):
     _check(load_library().turb_host_unregister(C.c_void_p(arr.ctypes.data)), "host_unregister")
+
+
+def selftest_division(nsamples, seed=1):
+    """Bitwise mismatches of the ENO kernels' division against IEEE division."""
+    bad = C.c_ulonglong()
+    ex = (C.c_double * 2)()
+    _check(load_library().turb_selftest_division(C.c_longlong(nsamples), C.c_ulonglong(seed), C.byref(bad), ex),
+           "selftest_division")
+    return bad.value, (ex[0], ex[1])

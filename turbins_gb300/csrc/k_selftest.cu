@@ -1,0 +1,81 @@
+// k_selftest.cu -- on-device self-tests of arithmetic building blocks.
+// turb_selftest_division compares div_by_spacing (turb_div.cuh) with the IEEE
+// division __ddiv_rn bit for bit on random and adversarial operands.
+#include <cstdint>
+#include "../../include/turbins_gb300.h"
+#include "turb_div.cuh"
+#include "turb_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ unsigned long long mix(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// double with random mantissa and exponent in [emin, emax]
+__device__ __forceinline__ double rnd(unsigned long long r, int emin, int emax, bool sign)
+{
+    unsigned long long m = r & 0xFFFFFFFFFFFFFULL;
+    int e = emin + (int)((r >> 52) % (unsigned)(emax - emin + 1));
+    unsigned long long bits = ((unsigned long long)(e + 1023) << 52) | m;
+    if (sign && ((r >> 63) & 1)) bits |= 0x8000000000000000ULL;
+    return __longlong_as_double((long long)bits);
+}
+
+__global__ void k_selftest(long long n, unsigned long long seed, unsigned long long *bad, double *ex)
+{
+    unsigned long long nbad = 0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        unsigned long long r1 = mix(seed ^ (2 * t)), r2 = mix(seed ^ (2 * t + 1)), r3 = mix(r1 ^ r2);
+        double h = rnd(r2, -14, 3, false);               // spacings 6e-5 .. 16
+        double y = __ddiv_rn(1.0, h);
+        double a;
+        switch (r3 & 3) {
+        case 0: a = rnd(r1, -80, 80, true); break;        // generic
+        case 1: a = __dmul_rn(rnd(r1, -40, 40, true), h); break;   // a/h near a double
+        case 2: {                                         // a/h near a midpoint
+            double q = rnd(r1, -40, 40, true);
+            double qm = __dadd_rn(q, __dmul_rn(0.5, __dadd_rn(__longlong_as_double(__double_as_longlong(q) + 1), -q)));
+            a = __dmul_rn(qm, h);
+            break;
+        }
+        default: {                                        // difference of nearby values
+            double b0 = rnd(r1, -20, 20, true);
+            a = __dadd_rn(__longlong_as_double(__double_as_longlong(b0) + (long long)(r3 >> 40) % 9), -b0);
+            break;
+        }
+        }
+        double q1 = div_by_spacing(a, h, y), q2 = __ddiv_rn(a, h);
+        if (__double_as_longlong(q1) != __double_as_longlong(q2)) {
+            nbad++;
+            ex[0] = a; ex[1] = h;
+        }
+    }
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+}  // namespace
+
+extern "C" int turb_selftest_division(long long nsamples, unsigned long long seed, unsigned long long *mismatches,
+                                      double *example)
+{
+    if (nsamples <= 0 || !mismatches) return TURB_ERR_ARG;
+    unsigned long long *dbad = nullptr;
+    double *dex = nullptr;
+    TURB_CHECK(cudaMalloc(&dbad, sizeof(unsigned long long)));
+    TURB_CHECK(cudaMalloc(&dex, 2 * sizeof(double)));
+    cudaMemset(dbad, 0, sizeof(unsigned long long));
+    cudaMemset(dex, 0, 2 * sizeof(double));
+    k_selftest<<<1216, 256>>>(nsamples, seed, dbad, dex);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, dbad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && example) e = cudaMemcpy(example, dex, 2 * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(dbad);
+    cudaFree(dex);
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    return TURB_OK;
+}

@@ -235,6 +235,12 @@ EnoTab mk_eno(DevBuf &m, int r, const std::vector<double> &pos, int s0, int e0, 
     T.h1 = m.upload(h1);
     T.h2 = m.upload(h2);
     T.h3 = m.upload(h3);
+    std::vector<double> r1(nb), r2(nb), r3(nb);
+    for (int b = 0; b < nb; b++) { r1[b] = 1.0 / h1[b]; r2[b] = 1.0 / h2[b]; r3[b] = 1.0 / h3[b]; }
+    T.rh1 = m.upload(r1);
+    T.rh2 = m.upload(r2);
+    T.rh3 = m.upload(r3);
+    T.fastdiv = 1;
     T.g2 = m.upload(g2);
     T.g3 = m.upload(g3);
     return T;
@@ -1204,6 +1210,15 @@ static int helm_solve(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int
 {
     return c->hmode == TURB_HMODE_MIXED ? helm_solve_mixed(c, q, ic, fx, fb, dt, iters)
                                         : helm_solve_fp64(c, q, ic, fx, fb, dt, iters);
+}
+
+int turb_set_eno_division(turb_ctx *c, int fast)
+{
+    if (!c || (fast != 0 && fast != 1)) return TURB_ERR_ARG;
+    for (int q = 0; q < 4; q++)
+        for (int dd = 0; dd < 3; dd++) c->eno[q][dd].fastdiv = fast;
+    for (int ic = 0; ic < TURB_MAXCONC; ic++) c->eno_cy[ic].fastdiv = fast;
+    return TURB_OK;
 }
 
 int turb_set_helmholtz_mode(turb_ctx *c, int mode, int inner_sweeps)

@@ -58,6 +58,8 @@ struct EnoTab {
     const double *h3;    // P[b+2]-P[b-1]
     const double *g2;    // [nb*2]: k=b-1, k=b  -> (x_i-x_k)+(x_i-x_k1)
     const double *g3;    // [nb*3]: kstar=b-2,b-1,b -> three-product sum
+    const double *rh1, *rh2, *rh3;   // RN(1/h*) for the reciprocal-based division
+    int fastdiv;         // 1: div_by_spacing (turb_div.cuh), 0: IEEE division
     int gsrc[6];         // ghost b<r: [0..r), ghost b>=nb-r: [3..3+r) by ex
     double gm[6];        // 0: zero, 1: m*q[s0], 2: m*q[e0]
 };
