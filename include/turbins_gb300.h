@@ -132,8 +132,8 @@ int turb_field_download(turb_ctx *ctx, int field, double *host_da);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
-/* ENO divided differences: 1 (default) divides by a grid spacing through its
- * precomputed reciprocal with two correction steps, 0 uses IEEE division;
+/* ENO divided differences: 0 (default) uses IEEE division, 1 divides by a
+ * grid spacing through its precomputed reciprocal with two correction steps;
  * both round to nearest, so the results are the same bits */
 int turb_set_eno_division(turb_ctx *ctx, int fast);
 int turb_synchronize(turb_ctx *ctx);
