@@ -33,7 +33,8 @@ typedef enum {
     TURB_ERR_CUDA = 2,           /* CUDA runtime error / no device          */
     TURB_ERR_NOT_CONVERGED = 3,  /* solver reached max_iter (cf. Solver.c:326-348) */
     TURB_ERR_NAN = 4,            /* non-finite residual                     */
-    TURB_ERR_ALLOC = 5           /* device allocation failed                */
+    TURB_ERR_ALLOC = 5,          /* device allocation failed                */
+    TURB_ERR_SCRATCH_LIMIT = 6   /* grid larger than the fixed scratch of turb_velocity_divergence_noalloc */
 } turb_status;
 
 /* node status codes, Include/definitions.h:93-99 */
@@ -178,6 +179,27 @@ int turb_Pressure_compute_velocity_divergence(turb_ctx *ctx, double *div_max);
 int turb_store_old_data(turb_ctx *ctx);
 /* Velocity_rk_average / Conc_rk_average, Velocity.c:2047, Conc.c:1007 */
 int turb_rk_average(turb_ctx *ctx, double old_frac, double new_frac);
+/* No reference counterpart: the divergence check of
+ * Pressure_compute_velocity_divergence for callers that cannot allocate GPU
+ * memory (a step replayed inside a CUDA graph capture, a host under a fixed
+ * memory budget, a plugin that only receives device buffers).  Every argument
+ * is caller-owned: u, v, w (FP64, DA order with rows of `pitch` doubles),
+ * c_status (uint8), the metrics mxc/myc/mzc (nx+1/ny+1/nz+1 doubles) and the
+ * output div on the device, div_max on the host.  The only scratch is a
+ * file-scope __device__ array of TURB_NOALLOC_MAX_BLOCKS doubles (512 KB) that
+ * every GPU loading this library holds until exit; grids needing more than
+ * TURB_NOALLOC_MAX_BLOCKS blocks of 32 x 8 x 8 points return
+ * TURB_ERR_SCRATCH_LIMIT.  Nothing is allocated: the first call on a device
+ * resolves the array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (different streams, no ordering) race.  The call
+ * synchronizes `stream` (a cudaStream_t, 0 = legacy default stream). */
+#define TURB_NOALLOC_MAX_BLOCKS 65536
+int turb_velocity_divergence_noalloc(int nx, int ny, int nz, long long pitch, const double *u,
+                                     const double *v, const double *w, const uint8_t *c_status,
+                                     const double *mxc, const double *myc, const double *mzc,
+                                     double *div, double *div_max, void *stream);
+
 /* one TVD-RK2 step of the restated driver (the absent main loop) */
 int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
 

@@ -764,6 +764,7 @@ const char *turb_status_string(int status)
     case TURB_ERR_NOT_CONVERGED: return "solver did not converge";
     case TURB_ERR_NAN: return "non-finite residual";
     case TURB_ERR_ALLOC: return "device allocation failed";
+    case TURB_ERR_SCRATCH_LIMIT: return "grid larger than the static scratch of the no-allocation entry point";
     default: return "unknown status";
     }
 }
