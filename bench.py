@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--ny", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
     ap.add_argument("--pmode", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--guess", default="previous", choices=["previous", "extrapolate", "learned"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=3, help="timed steps of the plain FP64 MG-CG variant")
@@ -244,6 +245,9 @@ def main():
     ctx = api.Context(g, case.params)
     ctx.load_state(case.state)
     ctx.set_pressure_mode(api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64)
+    guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED}[a.guess]
+    if guess != api.GUESS_PREVIOUS:
+        ctx.set_pressure_guess(guess)
     dt = case.dt
     for _ in range(a.warmup):
         ctx.step(dt)
@@ -333,12 +337,13 @@ def main():
                                        % (a.nx, a.ny, a.nz),
                            "pressure": "%s MG-CG (FP64 CG, %s V-cycles), rtol 1e-10" % (
                                a.pmode, "FP32" if a.pmode == "mixed" else "FP64"),
-                           "learned_warm_start": False,
+                           "learned_warm_start": a.guess == "learned", "pressure_guess": a.guess,
                            "l2": "inputs larger than L2: each FP64 field is %.0f MB" % (npts * 8 / 1e6),
                            "parallelism": "replicas" if dist.world > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "plain_fp64": plain,
-                "solver": {"p_iters": [s["p_iters"] for s in stats], "vel_iters": stats[-1]["vel_iters"],
+                "solver": {"p_iters": [s["p_iters"] for s in stats], "guess_tried_taken": ctx.pressure_guess_stats(),
+                           "vel_iters": stats[-1]["vel_iters"],
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}
         print(json.dumps(line))
     ctx.close()

@@ -131,6 +131,17 @@ int turb_destroy(turb_ctx *ctx);
 int turb_field_upload(turb_ctx *ctx, int field, const double *host_da);
 int turb_field_download(turb_ctx *ctx, int field, double *host_da);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);
+/* Initial guess of the Poisson solve.  PREVIOUS: the last solution (the
+ * reference's nonzero initial guess, Solver.c:84).  EXTRAPOLATE: 2 p1 - p2 from
+ * the last two solutions of the same RK stage.  LEARNED: p1 + net(b, p1, p2)
+ * from the warm-start network (turb_net_*).  A candidate is used only if its
+ * initial residual is below the PREVIOUS guess's; the solve always iterates
+ * to the same FP64 tolerance. */
+#define TURB_GUESS_PREVIOUS 0
+#define TURB_GUESS_EXTRAPOLATE 1
+#define TURB_GUESS_LEARNED 2
+int turb_set_pressure_guess(turb_ctx *ctx, int mode);
+int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 0 (default) uses IEEE division, 1 divides by a

@@ -25,6 +25,7 @@ F_UBC, F_VBC, F_WBC, F_CONV_U, F_CONV_V, F_CONV_W, F_B_U, F_B_V, F_B_W, F_CTOT, 
 F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
 PMODE_FP64, PMODE_MIXED = 0, 1
 HMODE_FP64, HMODE_MIXED = 0, 1
+GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed"}
@@ -192,6 +193,14 @@ class Context:
 
     def set_pressure_mode(self, mode):
         _check(self.lib.turb_set_pressure_mode(self.ctx, mode), "set_pressure_mode")
+
+    def set_pressure_guess(self, mode):
+        _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
+
+    def pressure_guess_stats(self):
+        a, b = C.c_int(), C.c_int()
+        _check(self.lib.turb_pressure_guess_stats(self.ctx, C.byref(a), C.byref(b)), "pressure_guess_stats")
+        return a.value, b.value
 
     def set_helmholtz_mode(self, mode, inner_sweeps=6):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")

@@ -176,6 +176,13 @@ __global__ void k_xrupdate(long long n, double *__restrict__ x, double *__restri
     block_store(acc, part + blockIdx.x);
 }
 
+__global__ void k_lincomb(long long n, double a, const double *__restrict__ x, double b, const double *__restrict__ y,
+                          double *__restrict__ out)
+{
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+        out[c] = a * x[c] + b * y[c];
+}
+
 __global__ void k_f2(long long n, const double *__restrict__ a, float *__restrict__ b)
 {
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
@@ -260,3 +267,7 @@ void pcg_scalars(cudaStream_t s, PcgScal *sc, int what) { k_scalars<<<1, 32, 0, 
 void pcg_to_float(cudaStream_t s, long long n, const double *a, float *b) { k_f2<<<NP, BS, 0, s>>>(n, a, b); }
 void pcg_to_double(cudaStream_t s, long long n, const float *a, double *b) { k_d2<<<NP, BS, 0, s>>>(n, a, b); }
 void pcg_copy(cudaStream_t s, long long n, const double *a, double *b) { k_copy<<<NP, BS, 0, s>>>(n, a, b); }
+void pcg_lincomb(cudaStream_t s, long long n, double a, const double *x, double b, const double *y, double *out)
+{
+    k_lincomb<<<NP, BS, 0, s>>>(n, a, x, b, y, out);
+}

@@ -108,6 +108,15 @@ struct turb_ctx {
     cudaGraphExec_t g_inner[3 + TURB_MAXCONC] = {nullptr};
     int g_inner_n[3 + TURB_MAXCONC] = {0};
     int use_graphs = 1;
+    // pressure initial guess: history of the last two solutions per RK stage
+    int guess_mode = TURB_GUESS_PREVIOUS;
+    int stage = 0;
+    double *ph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int nh[2] = {0, 0};
+    int guess_taken = 0, guess_tried = 0;
+    // learned guess hook (k_cnn.cu): candidate = phi1 + net(b, phi1, phi2)
+    int (*learned)(turb_ctx *, const double *, const double *, const double *, double *) = nullptr;
+    void *net = nullptr;
 };
 
 namespace {
@@ -938,6 +947,22 @@ int turb_field_download(turb_ctx *c, int field, double *h)
     return TURB_OK;
 }
 
+int turb_set_pressure_guess(turb_ctx *c, int mode)
+{
+    if (!c || mode < TURB_GUESS_PREVIOUS || mode > TURB_GUESS_LEARNED) return TURB_ERR_ARG;
+    if (mode == TURB_GUESS_LEARNED && !c->learned) return TURB_ERR_ARG;
+    c->guess_mode = mode;
+    return TURB_OK;
+}
+
+int turb_pressure_guess_stats(turb_ctx *c, int *tried, int *taken)
+{
+    if (!c || !tried || !taken) return TURB_ERR_ARG;
+    *tried = c->guess_tried;
+    *taken = c->guess_taken;
+    return TURB_OK;
+}
+
 int turb_set_pressure_mode(turb_ctx *c, int mode)
 {
     if (!c || (mode != TURB_PMODE_FP64 && mode != TURB_PMODE_MIXED)) return TURB_ERR_ARG;
@@ -1283,6 +1308,35 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     TURB_CHECK(cudaMemcpyAsync(c->hscal, dsc, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     TURB_CHECK(cudaStreamSynchronize(s));
     double nb = std::sqrt(c->hscal[0]), nr = std::sqrt(c->hscal[1]);
+    // candidate initial guess from this stage's history; kept only if it
+    // lowers the initial residual below the previous-solution guess
+    int st = c->stage & 1;
+    if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2) {
+        int ok = 0;
+        if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
+            pcg_lincomb(s, n0, 2.0, c->ph[st][0], -1.0, c->ph[st][1], c->pz);
+            c->launches += 1;
+            ok = 1;
+        } else if (c->guess_mode == TURB_GUESS_LEARNED && c->learned) {
+            ok = c->learned(c, c->pbw, c->ph[st][0], c->ph[st][1], c->pz) == TURB_OK;
+        }
+        if (ok) {
+            pcg_resid(s, L0, c->pbw, c->pz, c->pq, c->part);
+            pcg_reduce(s, c->part, 1, dsc + 1, nsp);
+            c->launches += 2;
+            TURB_CHECK(cudaMemcpyAsync(c->hscal + 2, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+            TURB_CHECK(cudaStreamSynchronize(s));
+            double nrc = std::sqrt(c->hscal[2]);
+            c->guess_tried++;
+            if (nrc < nr) {
+                pcg_copy(s, n0, c->pz, c->px);
+                pcg_copy(s, n0, c->pq, c->pr);
+                c->launches += 2;
+                nr = nrc;
+                c->guess_taken++;
+            }
+        }
+    }
     double tol = c->prm.p_rtol * nb;
     int it = 0, restart = 1, status = TURB_OK;
     const int npre = 2, npost = 2;
@@ -1351,6 +1405,17 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     }
     pcg_scatter(s, d, L0, c->px, c->fld[TURB_F_PHI]);
     c->launches += 1;
+    if (status == TURB_OK && c->guess_mode != TURB_GUESS_PREVIOUS) {
+        if (!c->ph[st][0]) {
+            c->ph[st][0] = c->mem.alloc<double>(n0);
+            c->ph[st][1] = c->mem.alloc<double>(n0);
+            if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+        }
+        std::swap(c->ph[st][0], c->ph[st][1]);
+        pcg_copy(s, n0, c->px, c->ph[st][0]);
+        c->launches += 1;
+        c->nh[st] = std::min(c->nh[st] + 1, 2);
+    }
     if (iters) *iters = it;
     if (relres) *relres = nb > 0.0 ? nr / nb : 0.0;
     int rc = check_launch(c);
@@ -1486,6 +1551,7 @@ int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
     long long l0 = c->launches;
     STEP_TRY(turb_store_old_data(c));
     for (int stage = 0; stage < 2; stage++) {
+        c->stage = stage;
         STEP_TRY(turb_Velocity_cell_center(c));
         if (c->prm.nconc > 1) STEP_TRY(turb_Conc_compute_total_concentration(c));
         STEP_TRY(turb_Velocity_convective_terms(c, 'u'));

@@ -60,3 +60,4 @@ void pcg_to_float(cudaStream_t s, long long n, const double *a, float *b);
 void pcg_to_double(cudaStream_t s, long long n, const float *a, double *b);
 void pcg_copy(cudaStream_t s, long long n, const double *a, double *b);
 int pcg_nparts();
+void pcg_lincomb(cudaStream_t s, long long n, double a, const double *x, double b, const double *y, double *out);
