@@ -223,7 +223,8 @@ int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
 #define TURB_PROF_MG 3         /* multigrid V-cycles (all levels)               */
 #define TURB_PROF_PCG 4        /* FP64 CG vector kernels and reductions         */
 #define TURB_PROF_INNER32 5    /* FP32 inner sweeps of the Helmholtz correction */
-#define TURB_PROF_NGROUPS 6
+#define TURB_PROF_NET 6        /* warm-start network: inputs, forward, guard     */
+#define TURB_PROF_NGROUPS 7
 int turb_profile_enable(turb_ctx *ctx, int on);
 int turb_profile_read(turb_ctx *ctx, double *ms, long long *launches);
 /* events 0..7 on the context stream; elapsed waits for event b */
@@ -240,6 +241,63 @@ int turb_host_unregister(void *ptr);
  * returns the number of bitwise mismatches (and one offending (a, h)) */
 int turb_selftest_division(long long nsamples, unsigned long long seed,
                            unsigned long long *mismatches, double *example);
+
+/* ---- learned initial guess of the pressure solve ---------------------------
+ * No reference counterpart: the reference starts each Poisson solve from the
+ * previous pressure (Solver.c:84).  A 4-level 3-D U-Net (channels
+ * 16-32-64-128, 3x3x3 kernels, BF16 weights and activations, FP32
+ * accumulation on the tcgen05 tensor cores) on the nx x ny x nz physical
+ * cells (each a multiple of 8, at least 16) maps three channels -- the
+ * residual r1 = b - A p1 of the previous pressure p1 (scaled by its rms s),
+ * the last increment p1 - p2 (times diag A / s) and b (scaled by its rms) --
+ * to a correction delta = s diag(A)^-1 out; the candidate p1 + delta is
+ * guarded like every other guess.  Parameters are FP32 masters (Adam); the
+ * convolutions use BF16 copies.  train = 1 allocates the backward buffers. */
+typedef struct turb_net turb_net;
+typedef struct turb_snaps turb_snaps;
+int turb_net_create(int nx, int ny, int nz, int train, turb_net **out);
+int turb_net_destroy(turb_net *net);
+long long turb_net_num_params(const turb_net *net);
+int turb_net_init_params(turb_net *net, unsigned long long seed);
+int turb_net_set_params(turb_net *net, const float *host, long long count);
+int turb_net_get_params(turb_net *net, float *host, long long count);
+/* gradients of the last turb_net_backward (train nets) */
+int turb_net_get_grads(turb_net *net, float *host, long long count);
+/* in3: 3 x ncell FP32 device array (channel-major, cells x fastest);
+ * out: ncell FP32 device array; stream NULL = default stream */
+int turb_net_forward(turb_net *net, const float *in3, float *out, void *stream);
+/* gradients for d loss / d out = gout (ncell FP32 device) of the last forward */
+int turb_net_backward(turb_net *net, const float *gout, void *stream);
+int turb_net_adam(turb_net *net, float lr, void *stream);
+/* snapshot store: the network inputs of pressure solves, in3 layout */
+int turb_snaps_create(int nx, int ny, int nz, int capacity, turb_snaps **out);
+int turb_snaps_destroy(turb_snaps *snaps);
+int turb_snaps_count(const turb_snaps *snaps);
+int turb_snaps_data(turb_snaps *snaps, int index, const float **dev_ptr);
+/* record one snapshot at every pressure solve that has a two-deep history of
+ * its RK stage (NULL stops recording) */
+int turb_set_snapshot_store(turb_ctx *ctx, turb_snaps *snaps);
+/* use net for TURB_GUESS_LEARNED (grid of net = physical cells of ctx) */
+int turb_set_learned_net(turb_ctx *ctx, turb_net *net);
+/* steps of Adam on randomly drawn snapshots; loss = |r1 - A delta|^2/|r1|^2
+ * with ctx's pressure operator; mean loss over the steps */
+int turb_net_train(turb_net *net, turb_ctx *ctx, turb_snaps *snaps, int steps, float lr,
+                   unsigned long long seed, double *mean_loss);
+int turb_net_eval(turb_net *net, turb_ctx *ctx, turb_snaps *snaps, int first, int count,
+                  double *mean_loss);
+/* self-test of the tcgen05 operand descriptors: one 128 x 64 x 32 BF16 MMA
+ * from K-major (mn_major = 0) or MN-major (1) shared-memory layouts; swap = 1
+ * exchanges the LBO and SBO fields.  Returns the number of wrong results. */
+int turb_selftest_umma(int mn_major, int swap, unsigned long long *mismatches);
+/* one convolution of the network's kernels on caller device buffers
+ * (channel-blocked BF16 [C/8][Z][Y][X][8]; W FP32 [27][cout][cin]):
+ * dgrad_mode 0: out (cout ch) = relu?(conv(in) + bias); 1: out (cin ch) =
+ * data gradient of in (cout ch).  wgrad: dw (FP32 [27][cout][cin]) = weight
+ * gradient of dy (cout ch) against x (cin ch). */
+int turb_conv3_test(int X, int Y, int Z, int cin, int cout, const void *in, const float *W,
+                    const float *bias, int relu, int dgrad_mode, void *out, void *stream);
+int turb_conv3_wgrad_test(int X, int Y, int Z, int cin, int cout, const void *x, const void *dy,
+                          float *dw, void *stream);
 
 /* operator hooks used by the parity tests: y = A x on device fields */
 int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);

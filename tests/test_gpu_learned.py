@@ -1,0 +1,84 @@
+"""The learned initial guess end to end on the GPU: snapshots recorded by the
+plain solver, training with the library's own forward/backward/Adam kernels,
+and what the trained network gains over the previous-pressure guess on later
+steps of the same flow -- with the converged answer unchanged."""
+import numpy as np
+import pytest
+
+from turbins_gb300 import workload as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mods():
+    from turbins_gb300 import build
+    build.build()
+    from turbins_gb300 import api as A
+    from turbins_gb300 import net as N
+    return A, N
+
+
+def _case():
+    c = W.turbidity_bump_case(64, 32, 32)
+    c.params.eno_order = 3
+    return c
+
+
+def _run(A, case, state, steps, dt, guess, net=None):
+    ctx = A.Context(case.grid, case.params)
+    ctx.load_state(state)
+    if net is not None:
+        from turbins_gb300 import net as N
+        N.set_learned_net(ctx, net)
+    ctx.set_pressure_guess(guess)
+    iters = []
+    for _ in range(steps):
+        st = ctx.step(dt)
+        iters.append(sum(st["p_iters"]))
+        assert max(st["div_max"]) <= 1e-10
+    out = ctx.state()
+    tried, taken = ctx.pressure_guess_stats()
+    return out, iters, tried, taken
+
+
+def test_learned_guess_trains_and_gains(mods):
+    A, N = mods
+    case = _case()
+    dt = case.dt
+    nx, ny, nz = case.params.nx, case.params.ny, case.params.nz
+    ctx = A.Context(case.grid, case.params)
+    ctx.load_state(case.state)
+    train = N.Snapshots(nx, ny, nz, 160)
+    held = N.Snapshots(nx, ny, nz, 40)
+    N.set_snapshot_store(ctx, train)
+    for _ in range(60):
+        ctx.step(dt)
+    N.set_snapshot_store(ctx, held)
+    for _ in range(20):
+        ctx.step(dt)
+    N.set_snapshot_store(ctx, None)
+    assert len(train) >= 100 and len(held) >= 30
+    state = ctx.state()
+
+    net = N.Net(nx, ny, nz, train=True)
+    net.init_params(1)
+    before = net.eval_on(ctx, held, 0, len(held))
+    assert abs(before - 1.0) < 0.5          # near-zero output leaves the residual as it is
+    loss = net.train_on(ctx, train, 600, lr=1e-3, seed=7)
+    after = net.eval_on(ctx, held, 0, len(held))
+    print("held-out |r|^2 ratio before %.4f after %.4f (train %.4f)" % (before, after, loss))
+    assert after < 0.8 * before
+
+    ref, it_prev, _, _ = _run(A, case, state, 12, dt, A.GUESS_PREVIOUS)
+    got, it_learn, tried, taken = _run(A, case, state, 12, dt, A.GUESS_LEARNED, net)
+    print("PCG iterations per step: previous %s  learned %s  (guess taken %d/%d)" % (it_prev, it_learn, taken, tried))
+    assert tried > 0 and taken > 0
+    assert sum(it_learn) <= sum(it_prev)
+    # the guess changes the iteration count, not the converged answer
+    for k in ("u", "v", "w"):
+        scale = max(np.abs(ref[k]).max(), 1e-30)
+        assert np.abs(got[k] - ref[k]).max() <= 1e-7 * scale, k
+    p0, p1 = ref["phi"] - ref["phi"].mean(), got["phi"] - got["phi"].mean()
+    assert np.abs(p1 - p0).max() <= 1e-7 * np.abs(p0).max()
+    net.close()

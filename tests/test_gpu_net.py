@@ -1,0 +1,111 @@
+"""The learned pressure guess on the GPU: tcgen05 descriptor layouts, single
+convolutions (forward, data gradient, weight gradient) and the whole U-Net's
+forward output and parameter gradients against the numpy oracle
+(oracle/unet_oracle.py, run with the same BF16 roundings)."""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def netmod():
+    from turbins_gb300 import build
+    build.build()
+    from turbins_gb300 import net as N
+    return N
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
+
+
+@pytest.mark.parametrize("mn", [0, 1])
+def test_umma_descriptor_layouts(netmod, mn):
+    bad = netmod.selftest_umma(mn, 0)
+    if bad:
+        other = netmod.selftest_umma(mn, 1)
+        pytest.fail("mn_major=%d: %d wrong results (%d with LBO/SBO exchanged)" % (mn, bad, other))
+
+
+def _bf16_dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(torch.bfloat16).cuda()
+
+
+def _to_np(t):
+    return t.float().cpu().numpy().astype(np.float64)
+
+
+CONV_SHAPES = [(128, 4, 3, 16, 32), (256, 2, 2, 32, 16), (32, 8, 4, 64, 128), (8, 4, 4, 128, 64),
+               (4, 2, 2, 32, 32), (200, 3, 2, 16, 16)]
+
+
+@pytest.mark.parametrize("X,Y,Z,cin,cout", CONV_SHAPES)
+def test_conv_forward_and_dgrad(netmod, X, Y, Z, cin, cout):
+    rng = np.random.default_rng(X * 7 + cin)
+    x = U.bf16_round(rng.normal(size=(cin, Z, Y, X)))
+    W = rng.normal(0, 0.2, size=(27, cout, cin)).astype(np.float32)
+    b = rng.normal(0, 0.1, size=cout).astype(np.float32)
+    Wq = U.bf16_round(W)
+    xd = _bf16_dev(U.to_blocked(x))
+    out = torch.zeros((cout // 8, Z, Y, X, 8), dtype=torch.bfloat16, device="cuda")
+    netmod.conv3(X, Y, Z, cin, cout, xd, torch.from_numpy(W).cuda(), torch.from_numpy(b).cuda(), relu=True, out=out)
+    got = U.from_blocked(_to_np(out), cout)
+    ref = np.maximum(U.conv3(x, Wq, b.astype(np.float64)), 0.0)
+    scale = np.abs(ref).max()
+    assert np.all(np.abs(got - ref) <= 2.0 ** -8 * np.abs(ref) + 1e-5 * scale)
+    # data gradient: dy has cout channels, dx cin
+    dy = U.bf16_round(rng.normal(size=(cout, Z, Y, X)))
+    dx = torch.zeros((cin // 8, Z, Y, X, 8), dtype=torch.bfloat16, device="cuda")
+    netmod.conv3(X, Y, Z, cin, cout, _bf16_dev(U.to_blocked(dy)), torch.from_numpy(W).cuda(), dgrad=True, out=dx)
+    got = U.from_blocked(_to_np(dx), cin)
+    ref = U.conv3_dgrad(dy, Wq)
+    scale = np.abs(ref).max()
+    assert np.all(np.abs(got - ref) <= 2.0 ** -8 * np.abs(ref) + 1e-5 * scale)
+
+
+@pytest.mark.parametrize("X,Y,Z,cin,cout", [(128, 4, 3, 16, 32), (32, 8, 4, 64, 128), (4, 2, 2, 128, 64),
+                                            (16, 8, 8, 32, 16), (48, 4, 2, 16, 16)])
+def test_conv_wgrad(netmod, X, Y, Z, cin, cout):
+    rng = np.random.default_rng(X + cin * 3 + cout)
+    x = U.bf16_round(rng.normal(size=(cin, Z, Y, X)))
+    dy = U.bf16_round(rng.normal(size=(cout, Z, Y, X)))
+    dw = torch.zeros((27, cout, cin), dtype=torch.float32, device="cuda")
+    netmod.conv3_wgrad(X, Y, Z, cin, cout, _bf16_dev(U.to_blocked(x)), _bf16_dev(U.to_blocked(dy)), dw)
+    ref = U.conv3_wgrad(x, dy)
+    got = dw.cpu().numpy().astype(np.float64)
+    # FP32 sums of exact BF16 products: bounded by the sum of |terms|
+    bound = 1e-5 * U.conv3_wgrad(np.abs(x), np.abs(dy)) + 1e-6
+    assert np.all(np.abs(got - ref) <= bound)
+
+
+@pytest.mark.parametrize("dims", [(32, 16, 16), (128, 16, 16)])
+def test_net_forward_backward_vs_oracle(netmod, dims):
+    nx, ny, nz = dims
+    rng = np.random.default_rng(nx + 1)
+    p = U.init_params(3)
+    in3 = rng.normal(size=(3, nz, ny, nx))
+    gout = rng.normal(size=(nz, ny, nx))
+    net = netmod.Net(nx, ny, nz, train=True)
+    net.set_params(p)
+    din = torch.from_numpy(in3.astype(np.float32)).cuda()
+    dout = torch.zeros((nz, ny, nx), dtype=torch.float32, device="cuda")
+    net.forward(din, dout)
+    net.backward(torch.from_numpy(gout.astype(np.float32)).cuda())
+    g = net.get_grads().astype(np.float64)
+    orc = U.UNet(p, bf16=True)
+    ref_out = orc.forward(in3.astype(np.float32).astype(np.float64))
+    ref_g = orc.backward(gout.astype(np.float32).astype(np.float64))
+    assert _rel(dout.cpu().numpy(), ref_out) < 1e-2
+    offs, hw, hb, n = U.param_layout()
+    for l, (w, b) in enumerate(offs):
+        cin, cout, _ = U.LAYERS[l]
+        e_w = _rel(g[w:w + 27 * cin * cout], ref_g[w:w + 27 * cin * cout])
+        e_b = _rel(g[b:b + cout], ref_g[b:b + cout])
+        assert e_w < 3e-2 and e_b < 3e-2, (l, e_w, e_b)
+    assert _rel(g[hw:hw + 17], ref_g[hw:hw + 17]) < 1e-2
+    net.close()

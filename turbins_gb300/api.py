@@ -28,7 +28,7 @@ HMODE_FP64, HMODE_MIXED = 0, 1
 GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
-          5: "device allocation failed"}
+          5: "device allocation failed", 6: "scratch limit"}
 
 
 class TurbError(RuntimeError):
@@ -297,7 +297,7 @@ def ENO_compute_convective_terms(order, D0, P, V):
 
 
 # ---- measurement helpers ------------------------------------------------------
-PROF_GROUPS = ("eno_x", "eno_yz", "jacobi", "mg", "pcg", "inner32")
+PROF_GROUPS = ("eno_x", "eno_yz", "jacobi", "mg", "pcg", "inner32", "net")
 
 
 def profile_enable(ctx, on=True):

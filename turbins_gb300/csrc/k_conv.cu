@@ -1,0 +1,669 @@
+// k_conv.cu -- 3x3x3 convolutions (stride 1, zero padding 1) as implicit
+// GEMMs on the tcgen05 tensor cores: BF16 operands, FP32 accumulators in
+// TMEM, operands staged by TMA, one producer warp, one MMA warp and four
+// epilogue warps per CTA, persistent CTAs with a double-buffered accumulator.
+//
+// Forward (and data gradient, the same kernel on mirrored weights):
+//   out[v][co] = sum_tap sum_ci W[tap][co][ci] * in[v + off(tap)][ci]
+// GEMM view per output tile: M = 128 voxels, N = cout, K = 27 taps x cin.
+// On grids at least 128 voxels wide a tile is one x row and, per channel
+// chunk, ONE TMA box (130 x 3 x 3 voxels) feeds all 27 taps: the A operand of
+// tap (dx, dy, dz) is the same shared-memory slab at a 16-byte-granular offset.
+// Narrower grids load one 128-voxel box per tap (TMA fills the padding with
+// zeros either way).
+//
+// Weight gradient: dW[tap][co][ci] = sum_v dy[v][co] * in[v + off(tap)][ci];
+// M = (taps of a group) x cin = 128 rows, N = cout, K = voxels, both operands
+// MN-major straight from the channel-blocked layout.  Each CTA accumulates a
+// range of voxel tiles in TMEM and adds its partial sums to FP32 dW.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "tc_ptx.cuh"
+#include "turb_conv.cuh"
+
+namespace {
+
+char g_conv_err[256] = "";
+
+// barrier slots
+constexpr int FA = 0, EA = 4, FB = 8, EB = 16, AF = 24, AE = 26, WB = 28, FIN = 29, NBAR = 30;
+
+struct ConvArgs {
+    int X, Y, Z, cin, cout, kc, nkc;
+    int slab, bx, by, bz, ntx, nty, ntz, ntiles;
+    int wres, sa, sb;
+    uint32_t abytes, bbytes, astride, bstride, wbytes, a_lbo;
+    const bf16 *wpk;
+    const float *bias;
+    int relu;
+    const bf16 *skip, *mask;
+    bf16 *out;
+    const float *headw, *headb;
+    float *hout;
+    int *err;
+};
+
+__device__ __forceinline__ void fail(volatile int *abort_, int *err, int code)
+{
+    *abort_ = 1;
+    atomicExch(err, code);
+}
+
+// last fill of stage s among `n` fills of an S-stage ring, waited for so that
+// no copy is still landing when the CTA exits
+__device__ __forceinline__ void drain(uint32_t bars, int base, uint32_t n, int S, volatile int *abort_)
+{
+    for (int s = 0; s < S; s++) {
+        if ((uint32_t)s >= n) break;
+        uint32_t last = (uint32_t)s + (uint32_t)S * ((n - 1 - (uint32_t)s) / (uint32_t)S);
+        tc::mbar_wait(bars + 8 * (base + s), (last / S) & 1, abort_);
+    }
+}
+
+__global__ void __launch_bounds__(192) k_conv(const __grid_constant__ CUtensorMap mapA, ConvArgs a)
+{
+    extern __shared__ uint8_t dsm[];
+    __shared__ __align__(8) uint64_t bar[NBAR];
+    __shared__ uint32_t tslot;
+    __shared__ int abort_s;
+    volatile int *abort_ = &abort_s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t sraw = tc::smem_u32(dsm);
+    const uint32_t sA = (sraw + 1023u) & ~1023u;
+    const uint32_t nA = a.slab ? 2u : (uint32_t)a.sa;
+    const uint32_t sB = sA + nA * a.astride;
+    const uint32_t bars = tc::smem_u32(bar);
+    const uint32_t ncols = a.cout * 2 < 32 ? 32u : (uint32_t)(a.cout * 2);
+
+    if (threadIdx.x == 0) {
+        abort_s = 0;
+        for (int i = 0; i < NBAR; i++) tc::mbar_init(bars + 8 * i, (i == AE || i == AE + 1) ? 4u : 1u);
+        tc::mbar_fence_init();
+        tc::prefetch_map(&mapA);
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(tc::smem_u32(&tslot), ncols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tbase = tslot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t ua = 0, ub = 0;
+            bool ok = true;
+            if (a.wres) {
+                tc::mbar_expect_tx(bars + 8 * WB, a.wbytes);
+                tc::bulk_load(sB, a.wpk, a.wbytes, bars + 8 * WB);
+            }
+            for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x) {
+                int tx = t % a.ntx, r = t / a.ntx, ty = r % a.nty, tz = r / a.nty;
+                int x0 = tx * a.bx, y0 = ty * a.by, z0 = tz * a.bz;
+                for (int kci = 0; ok && kci < a.nkc; kci++) {
+                    int cb = kci * (a.kc >> 3);
+                    if (a.slab) {
+                        uint32_t s = ua & 1u;
+                        if (!tc::mbar_wait(bars + 8 * (EA + s), ((ua >> 1) & 1u) ^ 1u, abort_)) { ok = false; break; }
+                        tc::mbar_expect_tx(bars + 8 * (FA + s), a.abytes);
+                        tc::tma_load5(sA + s * a.astride, &mapA, 0, x0 - 1, y0 - 1, z0 - 1, cb, bars + 8 * (FA + s));
+                        ua++;
+                    }
+                    for (int tap = 0; tap < 27; tap++) {
+                        if (!a.slab) {
+                            uint32_t s = ua % (uint32_t)a.sa;
+                            if (!tc::mbar_wait(bars + 8 * (EA + s), ((ua / a.sa) & 1u) ^ 1u, abort_)) { ok = false; break; }
+                            int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
+                            tc::mbar_expect_tx(bars + 8 * (FA + s), a.abytes);
+                            tc::tma_load5(sA + s * a.astride, &mapA, 0, x0 + dx - 1, y0 + dy - 1, z0 + dz - 1, cb,
+                                          bars + 8 * (FA + s));
+                            ua++;
+                        }
+                        if (!a.wres) {
+                            uint32_t s = ub % (uint32_t)a.sb;
+                            if (!tc::mbar_wait(bars + 8 * (EB + s), ((ub / a.sb) & 1u) ^ 1u, abort_)) { ok = false; break; }
+                            tc::mbar_expect_tx(bars + 8 * (FB + s), a.bbytes);
+                            tc::bulk_load(sB + s * a.bstride, a.wpk + (size_t)(kci * 27 + tap) * a.kc * a.cout, a.bbytes,
+                                          bars + 8 * (FB + s));
+                            ub++;
+                        }
+                    }
+                }
+            }
+            if (!ok) fail(abort_, a.err, 1);
+            drain(bars, FA, ua, (int)nA, abort_);
+            if (!a.wres) drain(bars, FB, ub, a.sb, abort_);
+            if (a.wres) tc::mbar_wait(bars + 8 * WB, 0, abort_);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, a.cout, 0, 0);
+            const uint32_t b_lbo = (uint32_t)a.cout * 16u;
+            uint32_t ua = 0, ub = 0, it = 0;
+            bool ok = true;
+            if (a.wres && !tc::mbar_wait(bars + 8 * WB, 0, abort_)) ok = false;
+            for (int t = blockIdx.x; ok && t < a.ntiles; t += gridDim.x, it++) {
+                uint32_t ab = it & 1u;
+                if (!tc::mbar_wait(bars + 8 * (AE + ab), ((it >> 1) & 1u) ^ 1u, abort_)) { ok = false; break; }
+                tc::fence_after();
+                uint32_t dt = tbase + ab * (uint32_t)a.cout;
+                for (int kci = 0; ok && kci < a.nkc; kci++) {
+                    uint32_t abuf = 0, sa_slab = 0;
+                    if (a.slab) {
+                        sa_slab = ua & 1u;
+                        if (!tc::mbar_wait(bars + 8 * (FA + sa_slab), (ua >> 1) & 1u, abort_)) { ok = false; break; }
+                        abuf = sA + sa_slab * a.astride;
+                    }
+                    for (int tap = 0; tap < 27; tap++) {
+                        uint32_t s_a = 0, s_b = 0, bbuf, aoff = 0;
+                        if (!a.slab) {
+                            s_a = ua % (uint32_t)a.sa;
+                            if (!tc::mbar_wait(bars + 8 * (FA + s_a), (ua / a.sa) & 1u, abort_)) { ok = false; break; }
+                            abuf = sA + s_a * a.astride;
+                        } else {
+                            int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
+                            aoff = (uint32_t)(((dz * 3 + dy) * (a.bx + 2) + dx) * 16);
+                        }
+                        if (!a.wres) {
+                            s_b = ub % (uint32_t)a.sb;
+                            if (!tc::mbar_wait(bars + 8 * (FB + s_b), (ub / a.sb) & 1u, abort_)) { ok = false; break; }
+                            bbuf = sB + s_b * a.bstride;
+                        } else {
+                            bbuf = sB + (uint32_t)((kci * 27 + tap) * a.kc * a.cout * 2);
+                        }
+                        tc::fence_after();
+                        for (int ks = 0; ks < (a.kc >> 4); ks++) {
+                            uint64_t ad = tc::sdesc(abuf + aoff + (uint32_t)ks * 2u * a.a_lbo, a.a_lbo, 128);
+                            uint64_t bd = tc::sdesc(bbuf + (uint32_t)ks * 2u * b_lbo, b_lbo, 128);
+                            tc::mma_bf16(dt, ad, bd, idesc, (kci | tap | ks) != 0);
+                        }
+                        if (!a.wres) { tc::mma_commit(bars + 8 * (EB + s_b)); ub++; }
+                        if (!a.slab) { tc::mma_commit(bars + 8 * (EA + s_a)); ua++; }
+                    }
+                    if (ok && a.slab) { tc::mma_commit(bars + 8 * (EA + sa_slab)); ua++; }
+                }
+                if (ok) tc::mma_commit(bars + 8 * (AF + ab));
+            }
+            if (!ok) fail(abort_, a.err, 1);
+            tc::mma_commit(bars + 8 * FIN);
+            tc::mbar_wait(bars + 8 * FIN, 0, abort_);
+        }
+    } else if (warp >= 2) {
+        const int q = warp & 3, row = q * 32 + lane;
+        const int xx = row % a.bx, yy = (row / a.bx) % a.by, zz = row / (a.bx * a.by);
+        const size_t plane = (size_t)a.X * a.Y * a.Z;
+        uint32_t it = 0;
+        for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, it++) {
+            uint32_t ab = it & 1u;
+            if (!tc::mbar_wait(bars + 8 * (AF + ab), (it >> 1) & 1u, abort_)) { fail(abort_, a.err, 1); break; }
+            tc::fence_after();
+            int tx = t % a.ntx, r = t / a.ntx, ty = r % a.nty, tz = r / a.nty;
+            int gx = tx * a.bx + xx, gy = ty * a.by + yy, gz = tz * a.bz + zz;
+            bool valid = zz < a.bz && gx < a.X && gy < a.Y && gz < a.Z;
+            size_t vox = ((size_t)gz * a.Y + gy) * a.X + gx;
+            uint32_t taddr = tbase + ((uint32_t)(q * 32) << 16) + ab * (uint32_t)a.cout;
+            float hsum = 0.f;
+            for (int ch = 0; ch < (a.cout >> 4); ch++) {
+                uint32_t rr[16];
+                tc::tmem_ld16(taddr + (uint32_t)ch * 16u, rr);
+                tc::tmem_wait_ld();
+                if (!valid) continue;
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) v[j] = __uint_as_float(rr[j]);
+                if (a.bias) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) v[j] += a.bias[ch * 16 + j];
+                }
+                size_t o0 = ((size_t)(2 * ch) * plane + vox) * 8, o1 = o0 + plane * 8;
+                if (a.skip) {
+                    uint4 s0 = *reinterpret_cast<const uint4 *>(a.skip + o0);
+                    uint4 s1 = *reinterpret_cast<const uint4 *>(a.skip + o1);
+                    const bf16 *p0 = reinterpret_cast<const bf16 *>(&s0), *p1 = reinterpret_cast<const bf16 *>(&s1);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) { v[j] += __bfloat162float(p0[j]); v[8 + j] += __bfloat162float(p1[j]); }
+                }
+                if (a.relu) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.f);
+                }
+                if (a.mask) {
+                    uint4 m0 = *reinterpret_cast<const uint4 *>(a.mask + o0);
+                    uint4 m1 = *reinterpret_cast<const uint4 *>(a.mask + o1);
+                    const bf16 *p0 = reinterpret_cast<const bf16 *>(&m0), *p1 = reinterpret_cast<const bf16 *>(&m1);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        if (!(__bfloat162float(p0[j]) > 0.f)) v[j] = 0.f;
+                        if (!(__bfloat162float(p1[j]) > 0.f)) v[8 + j] = 0.f;
+                    }
+                }
+                uint4 w0, w1;
+                bf16 *q0 = reinterpret_cast<bf16 *>(&w0), *q1 = reinterpret_cast<bf16 *>(&w1);
+#pragma unroll
+                for (int j = 0; j < 8; j++) { q0[j] = __float2bfloat16_rn(v[j]); q1[j] = __float2bfloat16_rn(v[8 + j]); }
+                if (a.out) {
+                    *reinterpret_cast<uint4 *>(a.out + o0) = w0;
+                    *reinterpret_cast<uint4 *>(a.out + o1) = w1;
+                }
+                if (a.headw) {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        hsum = fmaf(a.headw[ch * 16 + j], __bfloat162float(q0[j]), hsum);
+                        hsum = fmaf(a.headw[ch * 16 + 8 + j], __bfloat162float(q1[j]), hsum);
+                    }
+                }
+            }
+            if (valid && a.hout) a.hout[vox] = hsum + *a.headb;
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(bars + 8 * (AE + ab));
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 1) tc::tmem_dealloc(tbase, ncols);
+}
+
+// ---- weight gradient --------------------------------------------------------------
+struct WgArgs {
+    int X, Y, Z, cin, cout, G, ngroups, nsplit;
+    int bx, by, bz, nb, ntx, nty, ntz, ntiles;
+    uint32_t tapbytes, bbytes, stride;
+    float *dw;
+    int *err;
+};
+
+constexpr int WG_STAGES = 3;
+
+__global__ void __launch_bounds__(192) k_wgrad(const __grid_constant__ CUtensorMap mapX,
+                                               const __grid_constant__ CUtensorMap mapD, WgArgs a)
+{
+    extern __shared__ uint8_t dsm[];
+    __shared__ __align__(8) uint64_t bar[2 * WG_STAGES + 2];
+    __shared__ uint32_t tslot;
+    __shared__ int abort_s;
+    volatile int *abort_ = &abort_s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t s0 = (tc::smem_u32(dsm) + 1023u) & ~1023u;
+    const uint32_t bars = tc::smem_u32(bar);
+    const int F = 0, E = WG_STAGES, DONE = 2 * WG_STAGES, FINB = 2 * WG_STAGES + 1;
+    const uint32_t ncols = a.cout < 32 ? 32u : (uint32_t)a.cout;
+    const int g = blockIdx.x % a.ngroups, sp = blockIdx.x / a.ngroups;
+    const int ntaps = min(a.G, 27 - g * a.G);
+
+    if (threadIdx.x == 0) {
+        abort_s = 0;
+        for (int i = 0; i < 2 * WG_STAGES + 2; i++) tc::mbar_init(bars + 8 * i, 1);
+        tc::mbar_fence_init();
+        tc::prefetch_map(&mapX);
+        tc::prefetch_map(&mapD);
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(tc::smem_u32(&tslot), ncols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tbase = tslot;
+    const uint32_t sbo = (uint32_t)a.nb * 16u;   // next 8 channels
+    const int nks = a.nb >> 4;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t u = 0;
+            bool ok = true;
+            for (int t = sp; t < a.ntiles; t += a.nsplit) {
+                int tx = t % a.ntx, r = t / a.ntx, ty = r % a.nty, tz = r / a.nty;
+                int x0 = tx * a.bx, y0 = ty * a.by, z0 = tz * a.bz;
+                uint32_t s = u % WG_STAGES;
+                if (!tc::mbar_wait(bars + 8 * (E + s), ((u / WG_STAGES) & 1u) ^ 1u, abort_)) { ok = false; break; }
+                uint32_t buf = s0 + s * a.stride;
+                tc::mbar_expect_tx(bars + 8 * (F + s), (uint32_t)ntaps * a.tapbytes + a.bbytes);
+                for (int tl = 0; tl < ntaps; tl++) {
+                    int tap = g * a.G + tl, dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
+                    tc::tma_load5(buf + (uint32_t)tl * a.tapbytes, &mapX, 0, x0 + dx - 1, y0 + dy - 1, z0 + dz - 1, 0,
+                                  bars + 8 * (F + s));
+                }
+                tc::tma_load5(buf + (uint32_t)a.G * a.tapbytes, &mapD, 0, x0, y0, z0, 0, bars + 8 * (F + s));
+                u++;
+            }
+            if (!ok) fail(abort_, a.err, 2);
+            drain(bars, F, u, WG_STAGES, abort_);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, a.cout, 1, 1);
+            uint32_t u = 0;
+            bool ok = true;
+            for (int t = sp; t < a.ntiles; t += a.nsplit) {
+                uint32_t s = u % WG_STAGES;
+                if (!tc::mbar_wait(bars + 8 * (F + s), (u / WG_STAGES) & 1u, abort_)) { ok = false; break; }
+                tc::fence_after();
+                uint32_t abuf = s0 + s * a.stride, bbuf = abuf + (uint32_t)a.G * a.tapbytes;
+                for (int ks = 0; ks < nks; ks++) {
+                    uint64_t ad = tc::sdesc(abuf + (uint32_t)ks * 256u, 128, sbo);
+                    uint64_t bd = tc::sdesc(bbuf + (uint32_t)ks * 256u, 128, sbo);
+                    tc::mma_bf16(tbase, ad, bd, idesc, (u | (uint32_t)ks) != 0);
+                }
+                tc::mma_commit(bars + 8 * (E + s));
+                u++;
+            }
+            if (!ok) fail(abort_, a.err, 2);
+            tc::mma_commit(bars + 8 * DONE);
+            tc::mma_commit(bars + 8 * FINB);
+            tc::mbar_wait(bars + 8 * FINB, 0, abort_);
+        }
+    } else if (warp >= 2) {
+        const int q = warp & 3, row = q * 32 + lane;
+        const bool have = sp < a.ntiles;
+        if (have) {
+            if (!tc::mbar_wait(bars + 8 * DONE, 0, abort_)) {
+                fail(abort_, a.err, 2);
+            } else {
+                tc::fence_after();
+                const int tl = row / a.cin, ci = row % a.cin, tap = g * a.G + tl;
+                const bool valid = tl < ntaps && !*abort_;
+                uint32_t taddr = tbase + ((uint32_t)(q * 32) << 16);
+                for (int ch = 0; ch < (a.cout >> 4); ch++) {
+                    uint32_t rr[16];
+                    tc::tmem_ld16(taddr + (uint32_t)ch * 16u, rr);
+                    tc::tmem_wait_ld();
+                    if (!valid) continue;
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        atomicAdd(a.dw + ((size_t)tap * a.cout + ch * 16 + j) * a.cin + ci, __uint_as_float(rr[j]));
+                }
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 1) tc::tmem_dealloc(tbase, ncols);
+}
+
+// ---- descriptor self-test ------------------------------------------------------------
+// One CTA: A (128 x 32) and B (64 x 32) written by the threads into shared
+// memory in a K-major or MN-major core-matrix layout, two MMAs (K = 16 each)
+// into TMEM, the result compared with an exact FP32 product (all values are
+// small multiples of 1/4, so every sum is exact).  Shared memory is sized so
+// that every read stays inside it even if the LBO and SBO fields are swapped.
+constexpr int ST_M = 128, ST_N = 64, ST_K = 32, ST_SMEM = 128 * 1024;
+
+__device__ __forceinline__ float st_a(int m, int k) { return (float)(((m * 3 + k * 7) % 9) - 4) * 0.25f; }
+__device__ __forceinline__ float st_b(int n, int k) { return (float)(((n * 5 + k * 3) % 7) - 3) * 0.5f; }
+
+__global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigned long long *bad)
+{
+    extern __shared__ uint8_t dsm[];
+    __shared__ __align__(8) uint64_t bar[1];
+    __shared__ uint32_t tslot;
+    __shared__ int abort_s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t s0 = (tc::smem_u32(dsm) + 1023u) & ~1023u;
+    uint8_t *g0 = dsm + (s0 - tc::smem_u32(dsm));
+    const uint32_t offB = 32 * 1024;
+    if (threadIdx.x == 0) {
+        abort_s = 0;
+        tc::mbar_init(tc::smem_u32(bar), 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_u32(&tslot), 64);
+        tc::tmem_relinquish();
+    }
+    for (int i = threadIdx.x; i < (ST_SMEM - 1024) / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(g0)[i] = 0u;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ST_M * ST_K; i += blockDim.x) {
+        int m = i / ST_K, k = i % ST_K;
+        uint32_t off = mn ? (uint32_t)((m / 8) * (ST_K * 16) + (k / 8) * 128 + (k % 8) * 16 + (m % 8) * 2)
+                          : (uint32_t)((k / 8) * (ST_M * 16) + (m / 8) * 128 + (m % 8) * 16 + (k % 8) * 2);
+        *reinterpret_cast<bf16 *>(g0 + off) = __float2bfloat16_rn(st_a(m, k));
+    }
+    for (int i = threadIdx.x; i < ST_N * ST_K; i += blockDim.x) {
+        int n = i / ST_K, k = i % ST_K;
+        uint32_t off = mn ? (uint32_t)((n / 8) * (ST_K * 16) + (k / 8) * 128 + (k % 8) * 16 + (n % 8) * 2)
+                          : (uint32_t)((k / 8) * (ST_N * 16) + (n / 8) * 128 + (n % 8) * 16 + (k % 8) * 2);
+        *reinterpret_cast<bf16 *>(g0 + offB + off) = __float2bfloat16_rn(st_b(n, k));
+    }
+    tc::fence_proxy_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tbase = tslot;
+    if (threadIdx.x == 0) {
+        // (K-group stride, M/N-group stride) of the layouts written above
+        uint32_t a_k = mn ? 128u : ST_M * 16u, a_m = mn ? ST_K * 16u : 128u;
+        uint32_t b_k = mn ? 128u : ST_N * 16u, b_n = mn ? ST_K * 16u : 128u;
+        uint32_t idesc = tc::idesc_bf16(ST_M, ST_N, mn, mn);
+        for (int ks = 0; ks < ST_K / 16; ks++) {
+            uint32_t aa = s0 + (uint32_t)ks * 2u * a_k, bb = s0 + offB + (uint32_t)ks * 2u * b_k;
+            uint64_t ad = swap ? tc::sdesc(aa, a_m, a_k) : tc::sdesc(aa, a_k, a_m);
+            uint64_t bd = swap ? tc::sdesc(bb, b_n, b_k) : tc::sdesc(bb, b_k, b_n);
+            tc::mma_bf16(tbase, ad, bd, idesc, ks > 0);
+        }
+        tc::mma_commit(tc::smem_u32(bar));
+    }
+    bool ok = tc::mbar_wait(tc::smem_u32(bar), 0, &abort_s);
+    tc::fence_after();
+    unsigned long long nbad = ok ? 0ull : 1000000ull;
+    int row = (warp & 3) * 32 + lane;
+    for (int ch = 0; ch < ST_N / 16; ch++) {
+        uint32_t rr[16];
+        tc::tmem_ld16(tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)ch * 16u, rr);
+        tc::tmem_wait_ld();
+        for (int j = 0; j < 16; j++) {
+            int n = ch * 16 + j;
+            float ref = 0.f;
+            for (int k = 0; k < ST_K; k++) ref += st_a(row, k) * st_b(n, k);
+            if (__uint_as_float(rr[j]) != ref) nbad++;
+        }
+    }
+    atomicAdd(bad, nbad);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_dealloc(tbase, 64);
+}
+
+// ---- weight packing ------------------------------------------------------------------
+// fwd:  wf[((kci*27 + tap)*(kc/8) + kg)*cout + n][e] = W[tap][n][kci*kc + kg*8 + e]
+// bwd:  wd[((kci*27 + tap)*(kcb/8) + kg)*cin + n][e] = W[26 - tap][kci*kcb + kg*8 + e][n]
+__global__ void k_pack(const float *__restrict__ W, int cin, int cout, int kcf, int kcb, bf16 *__restrict__ wf,
+                       bf16 *__restrict__ wd)
+{
+    long long n = 27LL * cin * cout;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        int ci = (int)(idx % cin);
+        long long t = idx / cin;
+        int co = (int)(t % cout), tap = (int)(t / cout);
+        bf16 w = __float2bfloat16_rn(W[idx]);
+        {
+            int kci = ci / kcf, r = ci % kcf, kg = r >> 3, e = r & 7;
+            long long o = ((((long long)kci * 27 + tap) * (kcf >> 3) + kg) * cout + co) * 8 + e;
+            wf[o] = w;
+        }
+        {
+            int kci = co / kcb, r = co % kcb, kg = r >> 3, e = r & 7;
+            long long o = ((((long long)kci * 27 + (26 - tap)) * (kcb >> 3) + kg) * cin + ci) * 8 + e;
+            wd[o] = w;
+        }
+    }
+}
+
+// ---- host -----------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+int get_encode()
+{
+    std::call_once(g_encode_once, []() {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    return g_encode ? 0 : 1;
+}
+
+// channel-blocked tensor [C/8][Z][Y][X][8] as a 5-D map (8, X, Y, Z, C/8)
+int make_map(CUtensorMap *m, const void *ptr, int X, int Y, int Z, int C, int b1, int b2, int b3, int b4)
+{
+    if (get_encode()) { snprintf(g_conv_err, sizeof(g_conv_err), "cuTensorMapEncodeTiled unavailable"); return 1; }
+    cuuint64_t dims[5] = {8, (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(C / 8)};
+    cuuint64_t str[4] = {16, (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16};
+    cuuint32_t box[5] = {8, (cuuint32_t)b1, (cuuint32_t)b2, (cuuint32_t)b3, (cuuint32_t)b4};
+    cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(ptr), dims, str, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        snprintf(g_conv_err, sizeof(g_conv_err), "cuTensorMapEncodeTiled failed (%d) for %dx%dx%dx%d box %d,%d,%d,%d",
+                 (int)r, X, Y, Z, C, b1, b2, b3, b4);
+        return 1;
+    }
+    return 0;
+}
+
+inline uint32_t r1024(uint32_t v) { return (v + 1023u) & ~1023u; }
+
+void tile_dims(int X, int Y, int Z, int &bx, int &by, int &bz)
+{
+    bx = X < 128 ? X : 128;
+    by = Y < 128 / bx ? Y : 128 / bx;
+    bz = Z < 128 / (bx * by) ? Z : 128 / (bx * by);
+}
+
+int blocks_per_sm(const void *fn, int threads, uint32_t smem)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) n = 1;
+    return n < 1 ? 1 : n;
+}
+
+}  // namespace
+
+const char *conv_last_error() { return g_conv_err; }
+
+ConvPlan conv_plan(int X, int Y, int Z, int cin, int cout)
+{
+    ConvPlan p{};
+    p.slab = X >= 128;
+    p.kc = cin < (p.slab ? 32 : 64) ? cin : (p.slab ? 32 : 64);
+    p.nkc = cin / p.kc;
+    if (p.slab) { p.bx = 128; p.by = 1; p.bz = 1; }
+    else tile_dims(X, Y, Z, p.bx, p.by, p.bz);
+    p.nb = p.bx * p.by * p.bz;
+    p.ntx = (X + p.bx - 1) / p.bx; p.nty = (Y + p.by - 1) / p.by; p.ntz = (Z + p.bz - 1) / p.bz;
+    p.ntiles = p.ntx * p.nty * p.ntz;
+    p.wbytes = 27u * cin * cout * 2u;
+    p.wres = p.wbytes <= 65536u;
+    p.sa = 4; p.sb = 4;
+    if (p.slab) {
+        p.abytes = 8u * (p.bx + 2) * 3u * 3u * (p.kc / 8) * 2u;
+        p.a_lbo = (uint32_t)(p.bx + 2) * 9u * 16u;
+    } else {
+        p.abytes = (uint32_t)p.nb * p.kc * 2u;
+        p.a_lbo = (uint32_t)p.nb * 16u;
+    }
+    // a stage always spans 128 rows per 8 channels so that the MMA reads stay in it
+    p.astride = r1024(p.abytes > 256u * p.kc ? p.abytes : 256u * p.kc);
+    p.bbytes = (uint32_t)p.kc * cout * 2u;
+    p.bstride = r1024(p.bbytes);
+    uint32_t na = p.slab ? 2u : (uint32_t)p.sa;
+    p.smem = na * p.astride + (p.wres ? r1024(p.wbytes) : (uint32_t)p.sb * p.bstride) + 1024u;
+    p.ncols = cout * 2 < 32 ? 32 : cout * 2;
+    return p;
+}
+
+void conv_pack_weights(cudaStream_t s, const float *W, int cin, int cout, int kc_fwd, int kc_bwd, bf16 *wf, bf16 *wd)
+{
+    long long n = 27LL * cin * cout;
+    int nb = (int)((n + 255) / 256);
+    k_pack<<<nb < 2048 ? nb : 2048, 256, 0, s>>>(W, cin, cout, kc_fwd, kc_bwd, wf, wd);
+}
+
+int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int cout, const bf16 *wpk,
+              const ConvEpi &e, int *err, int nsm)
+{
+    if (cin % 16 || cout % 16 || cout > 128 || cin > 128) { snprintf(g_conv_err, sizeof(g_conv_err), "conv channels"); return 1; }
+    ConvPlan p = conv_plan(X, Y, Z, cin, cout);
+    CUtensorMap map;
+    int rc = p.slab ? make_map(&map, in, X, Y, Z, cin, p.bx + 2, 3, 3, p.kc / 8)
+                    : make_map(&map, in, X, Y, Z, cin, p.bx, p.by, p.bz, p.kc / 8);
+    if (rc) return 1;
+    ConvArgs a{};
+    a.X = X; a.Y = Y; a.Z = Z; a.cin = cin; a.cout = cout; a.kc = p.kc; a.nkc = p.nkc;
+    a.slab = p.slab; a.bx = p.bx; a.by = p.by; a.bz = p.bz; a.ntx = p.ntx; a.nty = p.nty; a.ntz = p.ntz;
+    a.ntiles = p.ntiles; a.wres = p.wres; a.sa = p.sa; a.sb = p.sb;
+    a.abytes = p.abytes; a.bbytes = p.bbytes; a.astride = p.astride; a.bstride = p.bstride; a.wbytes = p.wbytes;
+    a.a_lbo = p.a_lbo; a.wpk = wpk;
+    a.bias = e.bias; a.relu = e.relu; a.skip = e.skip; a.mask = e.mask; a.out = e.out;
+    a.headw = e.headw; a.headb = e.headb; a.hout = e.hout; a.err = err;
+    static std::once_flag attr;
+    std::call_once(attr, []() { cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); });
+    int bps = blocks_per_sm((const void *)k_conv, 192, p.smem);
+    int tm = 512 / p.ncols;
+    if (bps > tm) bps = tm;
+    int grid = nsm * bps;
+    if (grid > p.ntiles) grid = p.ntiles;
+    k_conv<<<grid, 192, p.smem, s>>>(map, a);
+    return 0;
+}
+
+int conv3_wgrad(cudaStream_t s, const bf16 *x, const bf16 *dy, int X, int Y, int Z, int cin, int cout, float *dw,
+                int *err, int nsm)
+{
+    if (cin % 16 || cout % 16 || cout > 128 || cin > 128) { snprintf(g_conv_err, sizeof(g_conv_err), "wgrad channels"); return 1; }
+    WgArgs a{};
+    tile_dims(X, Y, Z, a.bx, a.by, a.bz);
+    a.nb = a.bx * a.by * a.bz;
+    if (a.nb % 16) { snprintf(g_conv_err, sizeof(g_conv_err), "wgrad grid below 16 voxels"); return 1; }
+    a.X = X; a.Y = Y; a.Z = Z; a.cin = cin; a.cout = cout;
+    a.G = 128 / cin; a.ngroups = (27 + a.G - 1) / a.G;
+    a.ntx = (X + a.bx - 1) / a.bx; a.nty = (Y + a.by - 1) / a.by; a.ntz = (Z + a.bz - 1) / a.bz;
+    a.ntiles = a.ntx * a.nty * a.ntz;
+    a.tapbytes = (uint32_t)a.nb * cin * 2u;
+    a.bbytes = (uint32_t)a.nb * cout * 2u;
+    // operand reads span 128 rows per 8 channels: keep that much room per stage
+    uint32_t abig = 128u * 16u * (uint32_t)(a.G * cin / 8), bbig = 128u * 16u * (uint32_t)(cout / 8);
+    uint32_t aroom = (uint32_t)a.G * a.tapbytes;
+    a.stride = r1024((aroom > abig ? aroom : abig) + (a.bbytes > bbig ? a.bbytes : bbig));
+    uint32_t smem = WG_STAGES * a.stride + 1024u;
+    CUtensorMap mx, md;
+    if (make_map(&mx, x, X, Y, Z, cin, a.bx, a.by, a.bz, cin / 8)) return 1;
+    if (make_map(&md, dy, X, Y, Z, cout, a.bx, a.by, a.bz, cout / 8)) return 1;
+    static std::once_flag attr;
+    std::call_once(attr, []() { cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); });
+    int want = 2 * nsm / a.ngroups;
+    a.nsplit = want < 1 ? 1 : want;
+    if (a.nsplit > a.ntiles) a.nsplit = a.ntiles;
+    a.dw = dw; a.err = err;
+    k_wgrad<<<a.ngroups * a.nsplit, 192, smem, s>>>(mx, md, a);
+    return 0;
+}
+
+int conv_selftest_umma(int mn_major, int swap, unsigned long long *mismatches)
+{
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return 1;
+    cudaMemset(d, 0, sizeof(*d));
+    cudaFuncSetAttribute(k_umma_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, ST_SMEM);
+    k_umma_selftest<<<1, 128, ST_SMEM>>>(mn_major, swap, d);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(*d), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) { snprintf(g_conv_err, sizeof(g_conv_err), "%s", cudaGetErrorString(e)); return 1; }
+    return 0;
+}

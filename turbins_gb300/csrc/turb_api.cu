@@ -13,6 +13,7 @@
 #include "turb_internal.cuh"
 #include "turb_kernels.cuh"
 #include "turb_mg.cuh"
+#include "turb_net.cuh"
 
 static char g_errmsg[512] = "";
 
@@ -114,9 +115,9 @@ struct turb_ctx {
     double *ph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int nh[2] = {0, 0};
     int guess_taken = 0, guess_tried = 0;
-    // learned guess hook (k_cnn.cu): candidate = phi1 + net(b, phi1, phi2)
-    int (*learned)(turb_ctx *, const double *, const double *, const double *, double *) = nullptr;
-    void *net = nullptr;
+    // learned guess (k_net.cu) and the snapshot store that training reads
+    TurbNet *net = nullptr;
+    TurbSnaps *snaps = nullptr;
 };
 
 namespace {
@@ -950,9 +951,54 @@ int turb_field_download(turb_ctx *c, int field, double *h)
 int turb_set_pressure_guess(turb_ctx *c, int mode)
 {
     if (!c || mode < TURB_GUESS_PREVIOUS || mode > TURB_GUESS_LEARNED) return TURB_ERR_ARG;
-    if (mode == TURB_GUESS_LEARNED && !c->learned) return TURB_ERR_ARG;
+    if (mode == TURB_GUESS_LEARNED && !c->net) return TURB_ERR_ARG;
     c->guess_mode = mode;
     return TURB_OK;
+}
+
+int turb_set_snapshot_store(turb_ctx *c, turb_snaps *snaps)
+{
+    if (!c) return TURB_ERR_ARG;
+    TurbSnaps *sn = reinterpret_cast<TurbSnaps *>(snaps);
+    if (sn) {
+        int nx, ny, nz;
+        snaps_dims(sn, &nx, &ny, &nz);
+        const MgDevLevel &L0 = c->H64.lev[0];
+        if (nx != L0.nx || ny != L0.ny || nz != L0.nz) return TURB_ERR_ARG;
+    }
+    c->snaps = sn;
+    return TURB_OK;
+}
+
+int turb_set_learned_net(turb_ctx *c, turb_net *net)
+{
+    if (!c) return TURB_ERR_ARG;
+    TurbNet *n = reinterpret_cast<TurbNet *>(net);
+    if (n) {
+        int nx, ny, nz;
+        net_dims(n, &nx, &ny, &nz);
+        const MgDevLevel &L0 = c->H64.lev[0];
+        if (nx != L0.nx || ny != L0.ny || nz != L0.nz) return TURB_ERR_ARG;
+    } else if (c->guess_mode == TURB_GUESS_LEARNED) {
+        c->guess_mode = TURB_GUESS_PREVIOUS;
+    }
+    c->net = n;
+    return TURB_OK;
+}
+
+int turb_net_train(turb_net *net, turb_ctx *c, turb_snaps *snaps, int steps, float lr, unsigned long long seed,
+                   double *mean_loss)
+{
+    if (!c || !net || !snaps) return TURB_ERR_ARG;
+    return net_train(reinterpret_cast<TurbNet *>(net), c->s, c->H64.lev[0], c->H64.invd[0],
+                     reinterpret_cast<TurbSnaps *>(snaps), steps, lr, seed, mean_loss);
+}
+
+int turb_net_eval(turb_net *net, turb_ctx *c, turb_snaps *snaps, int first, int count, double *mean_loss)
+{
+    if (!c || !net || !snaps) return TURB_ERR_ARG;
+    return net_eval(reinterpret_cast<TurbNet *>(net), c->s, c->H64.lev[0], c->H64.invd[0],
+                    reinterpret_cast<TurbSnaps *>(snaps), first, count, mean_loss);
 }
 
 int turb_pressure_guess_stats(turb_ctx *c, int *tried, int *taken)
@@ -1311,14 +1357,25 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     // candidate initial guess from this stage's history; kept only if it
     // lowers the initial residual below the previous-solution guess
     int st = c->stage & 1;
+    if (c->snaps && c->nh[st] >= 2) {
+        int rc = net_snapshot(c->snaps, s, L0, c->H64.invd[0], c->pr, c->pbw, c->ph[st][0], c->ph[st][1]);
+        if (rc) return rc;
+        c->launches += 5;
+    }
     if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2) {
-        int ok = 0;
+        int ok = 0, ph = -1;
         if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
             pcg_lincomb(s, n0, 2.0, c->ph[st][0], -1.0, c->ph[st][1], c->pz);
             c->launches += 1;
             ok = 1;
-        } else if (c->guess_mode == TURB_GUESS_LEARNED && c->learned) {
-            ok = c->learned(c, c->pbw, c->ph[st][0], c->ph[st][1], c->pz) == TURB_OK;
+        } else if (c->guess_mode == TURB_GUESS_LEARNED && c->net) {
+            // candidate = previous pressure + network correction of its residual
+            ph = prof_begin(c, TURB_PROF_NET);
+            int rc = net_guess(c->net, s, L0, c->H64.invd[0], c->pr, c->pbw, c->ph[st][0], c->ph[st][1], c->px,
+                               c->pz);
+            if (rc) return rc;
+            c->launches += NET_GUESS_LAUNCHES;
+            ok = 1;
         }
         if (ok) {
             pcg_resid(s, L0, c->pbw, c->pz, c->pq, c->part);
@@ -1327,6 +1384,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             TURB_CHECK(cudaMemcpyAsync(c->hscal + 2, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
             TURB_CHECK(cudaStreamSynchronize(s));
             double nrc = std::sqrt(c->hscal[2]);
+            if (ph >= 0) prof_end(c, ph, NET_GUESS_LAUNCHES + 2);
             c->guess_tried++;
             if (nrc < nr) {
                 pcg_copy(s, n0, c->pz, c->px);
@@ -1405,7 +1463,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     }
     pcg_scatter(s, d, L0, c->px, c->fld[TURB_F_PHI]);
     c->launches += 1;
-    if (status == TURB_OK && c->guess_mode != TURB_GUESS_PREVIOUS) {
+    if (status == TURB_OK && (c->guess_mode != TURB_GUESS_PREVIOUS || c->snaps)) {
         if (!c->ph[st][0]) {
             c->ph[st][0] = c->mem.alloc<double>(n0);
             c->ph[st][1] = c->mem.alloc<double>(n0);
