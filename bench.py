@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=3, help="timed steps of the plain FP64 MG-CG variant")
+    ap.add_argument("--train-seeds", type=int, default=8, help="learned guess: training runs (one bump field each)")
+    ap.add_argument("--train-steps", type=int, default=250, help="learned guess: steps per training run")
+    ap.add_argument("--train-iters", type=int, default=3000, help="learned guess: Adam steps")
+    ap.add_argument("--net-params", default=None, help="learned guess: .npy parameters instead of training")
     return ap.parse_args()
 
 
@@ -238,6 +242,17 @@ def main():
     from turbins_gb300 import api, build
     from turbins_gb300 import workload as W
     build.build()
+    learned_info, params = None, None
+    if a.guess == "learned":
+        from turbins_gb300 import learned as LN
+        if a.net_params:
+            params = np.load(a.net_params)
+            learned_info = {"params": os.path.basename(a.net_params)}
+        else:
+            tn = (max(16, a.nx // 4), max(16, a.ny // 4), max(16, a.nz // 4))
+            params, learned_info = LN.train_default(LN.multi_bump_train_case(*tn), seeds=a.train_seeds,
+                                                    steps=a.train_steps, iters=a.train_iters)
+            learned_info["train_grid"] = list(tn)
     case = W.multi_bump_case(a.nx, a.ny, a.nz)
     g = case.grid
     nc = g.nx * g.ny * g.nz
@@ -246,7 +261,10 @@ def main():
     ctx.load_state(case.state)
     ctx.set_pressure_mode(api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64)
     guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED}[a.guess]
-    if guess != api.GUESS_PREVIOUS:
+    net = None
+    if guess == api.GUESS_LEARNED:
+        net = LN.attach(ctx, params)
+    elif guess != api.GUESS_PREVIOUS:
         ctx.set_pressure_guess(guess)
     dt = case.dt
     for _ in range(a.warmup):
@@ -278,6 +296,7 @@ def main():
     plain = None
     if a.plain_steps > 0:
         ctx.set_pressure_mode(api.PMODE_FP64)
+        ctx.set_pressure_guess(api.GUESS_PREVIOUS)   # the plain method: previous-pressure guess
         ctx.step(dt)
         api.event_record(ctx, 2)
         pst = [ctx.step(dt) for _ in range(a.plain_steps)]
@@ -286,6 +305,7 @@ def main():
         plain = {"value": dist.world * nc * a.plain_steps / (pms / 1e3) / 1e6, "ms_per_step": pms / a.plain_steps,
                  "p_iters": [s["p_iters"] for s in pst], "steps": a.plain_steps}
         ctx.set_pressure_mode(api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64)
+        ctx.set_pressure_guess(guess)
     # ---- end to end through the C ABI with host buffers ---------------------
     e2e = None
     if not a.no_e2e:
@@ -341,12 +361,14 @@ def main():
                            "l2": "inputs larger than L2: each FP64 field is %.0f MB" % (npts * 8 / 1e6),
                            "parallelism": "replicas" if dist.world > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "plain_fp64": plain,
+                "clocks": clk, "plain_fp64": plain, "learned": learned_info,
                 "solver": {"p_iters": [s["p_iters"] for s in stats], "guess_tried_taken": ctx.pressure_guess_stats(),
                            "vel_iters": stats[-1]["vel_iters"],
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}
         print(json.dumps(line))
     ctx.close()
+    if net is not None:
+        net.close()
     dist.close()
 
 

@@ -142,6 +142,9 @@ int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 #define TURB_GUESS_LEARNED 2
 int turb_set_pressure_guess(turb_ctx *ctx, int mode);
 int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
+/* geometric mean over the tried candidates of |r(candidate)| / |r(previous)|
+ * (initial residuals; 1 when nothing was tried) */
+int turb_pressure_guess_ratio(turb_ctx *ctx, double *geo_mean);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 0 (default) uses IEEE division, 1 divides by a
@@ -248,8 +251,8 @@ int turb_selftest_division(long long nsamples, unsigned long long seed,
  * 16-32-64-128, 3x3x3 kernels, BF16 weights and activations, FP32
  * accumulation on the tcgen05 tensor cores) on the nx x ny x nz physical
  * cells (each a multiple of 8, at least 16) maps three channels -- the
- * residual r1 = b - A p1 of the previous pressure p1 (scaled by its rms s),
- * the last increment p1 - p2 (times diag A / s) and b (scaled by its rms) --
+ * residual r1 = b - A p1 of the previous pressure p1, the last increment
+ * p1 - p2 of the same RK stage and b, each scaled by its rms (s for r1) --
  * to a correction delta = s diag(A)^-1 out; the candidate p1 + delta is
  * guarded like every other guess.  Parameters are FP32 masters (Adam); the
  * convolutions use BF16 copies.  train = 1 allocates the backward buffers. */
@@ -263,6 +266,10 @@ int turb_net_set_params(turb_net *net, const float *host, long long count);
 int turb_net_get_params(turb_net *net, float *host, long long count);
 /* gradients of the last turb_net_backward (train nets) */
 int turb_net_get_grads(turb_net *net, float *host, long long count);
+/* forward activations of the last forward (0..17: x0 a0 p0 a1 p1 a2 p2 a3 b3
+ * c2 s2 b2 c1 s1 b1 c0 s0 b0), raw BF16 bits, channel-blocked layout; b0
+ * exists on train nets only */
+int turb_net_get_activation(turb_net *net, int which, uint16_t *host, long long count);
 /* in3: 3 x ncell FP32 device array (channel-major, cells x fastest);
  * out: ncell FP32 device array; stream NULL = default stream */
 int turb_net_forward(turb_net *net, const float *in3, float *out, void *stream);

@@ -202,6 +202,11 @@ class Context:
         _check(self.lib.turb_pressure_guess_stats(self.ctx, C.byref(a), C.byref(b)), "pressure_guess_stats")
         return a.value, b.value
 
+    def pressure_guess_ratio(self):
+        r = C.c_double()
+        _check(self.lib.turb_pressure_guess_ratio(self.ctx, C.byref(r)), "pressure_guess_ratio")
+        return r.value
+
     def set_helmholtz_mode(self, mode, inner_sweeps=6):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")
 

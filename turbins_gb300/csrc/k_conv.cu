@@ -545,6 +545,28 @@ void tile_dims(int X, int Y, int Z, int &bx, int &by, int &bz)
     bz = Z < 128 / (bx * by) ? Z : 128 / (bx * by);
 }
 
+// largest dynamic shared memory a launch of fn may request (opt-in limit
+// minus the kernel's static shared memory); set as fn's attribute once
+int dyn_smem_limit(const void *fn)
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return 0;
+    int lim = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) return 0;
+    return lim;
+}
+
+int launch_error(const char *what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return 0;
+    snprintf(g_conv_err, sizeof(g_conv_err), "%s launch: %s", what, cudaGetErrorString(e));
+    return 1;
+}
+
 int blocks_per_sm(const void *fn, int threads, uint32_t smem)
 {
     int n = 0;
@@ -611,15 +633,15 @@ int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int 
     a.a_lbo = p.a_lbo; a.wpk = wpk;
     a.bias = e.bias; a.relu = e.relu; a.skip = e.skip; a.mask = e.mask; a.out = e.out;
     a.headw = e.headw; a.headb = e.headb; a.hout = e.hout; a.err = err;
-    static std::once_flag attr;
-    std::call_once(attr, []() { cudaFuncSetAttribute(k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); });
+    static int lim = dyn_smem_limit((const void *)k_conv);
+    if ((int)p.smem > lim) { snprintf(g_conv_err, sizeof(g_conv_err), "conv needs %u B of shared memory", p.smem); return 1; }
     int bps = blocks_per_sm((const void *)k_conv, 192, p.smem);
     int tm = 512 / p.ncols;
     if (bps > tm) bps = tm;
     int grid = nsm * bps;
     if (grid > p.ntiles) grid = p.ntiles;
     k_conv<<<grid, 192, p.smem, s>>>(map, a);
-    return 0;
+    return launch_error("k_conv");
 }
 
 int conv3_wgrad(cudaStream_t s, const bf16 *x, const bf16 *dy, int X, int Y, int Z, int cin, int cout, float *dw,
@@ -644,14 +666,14 @@ int conv3_wgrad(cudaStream_t s, const bf16 *x, const bf16 *dy, int X, int Y, int
     CUtensorMap mx, md;
     if (make_map(&mx, x, X, Y, Z, cin, a.bx, a.by, a.bz, cin / 8)) return 1;
     if (make_map(&md, dy, X, Y, Z, cout, a.bx, a.by, a.bz, cout / 8)) return 1;
-    static std::once_flag attr;
-    std::call_once(attr, []() { cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); });
+    static int lim = dyn_smem_limit((const void *)k_wgrad);
+    if ((int)smem > lim) { snprintf(g_conv_err, sizeof(g_conv_err), "wgrad needs %u B of shared memory", smem); return 1; }
     int want = 2 * nsm / a.ngroups;
     a.nsplit = want < 1 ? 1 : want;
     if (a.nsplit > a.ntiles) a.nsplit = a.ntiles;
     a.dw = dw; a.err = err;
     k_wgrad<<<a.ngroups * a.nsplit, 192, smem, s>>>(mx, md, a);
-    return 0;
+    return launch_error("k_wgrad");
 }
 
 int conv_selftest_umma(int mn_major, int swap, unsigned long long *mismatches)

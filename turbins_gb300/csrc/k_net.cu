@@ -15,8 +15,8 @@
 //
 // Inputs (per cell of the compact pressure layout): the divergence residual
 // that the previous pressure leaves, r1 = W b - S p1, scaled by its rms s;
-// the last pressure increment p1 - p2 in the same units (times diag S / s);
-// and the divergence W b scaled by its rms.  Output: the correction
+// the last pressure increment p1 - p2 and the divergence W b, each scaled by
+// its own rms.  Output: the correction
 // delta = s * diag(S)^-1 * out added to the previous pressure.  Training
 // minimises |r1 - S delta|^2 / |r1|^2, the squared relative initial residual
 // of the corrected guess, i.e. exactly what the solver's guard compares.
@@ -224,17 +224,47 @@ __global__ void k_adam(long long n, float *__restrict__ p, const float *__restri
     }
 }
 
-// network inputs from the solver state (compact layout); sc[0] = |r1|^2, sc[1] = |b|^2
-__global__ void k_prep(long long n, const double *__restrict__ r1, const double *__restrict__ bw,
-                       const double *__restrict__ p1, const double *__restrict__ p2, const double *__restrict__ invd,
-                       const double *__restrict__ sc, float *__restrict__ in3)
+// partial sums of r1^2, b^2 and (p1 - p2)^2: part[k * NSUM + block]
+constexpr int NSUM = 512;
+__global__ void k_sumsq3(long long n, const double *__restrict__ r1, const double *__restrict__ bw,
+                         const double *__restrict__ p1, const double *__restrict__ p2, double *__restrict__ part)
 {
-    double rs = sqrt(sc[0] / (double)n), bs = sqrt(sc[1] / (double)n);
-    double ir = rs > 0.0 ? 1.0 / rs : 0.0, ib = bs > 0.0 ? 1.0 / bs : 0.0;
+    double a = 0.0, b = 0.0, c = 0.0;
+    GRID_STRIDE(v, n)
+    {
+        double d = p1[v] - p2[v];
+        a = fma(r1[v], r1[v], a);
+        b = fma(bw[v], bw[v], b);
+        c = fma(d, d, c);
+    }
+    __shared__ double sm[3][8];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sm[0][w] = a; sm[1][w] = b; sm[2][w] = c; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sm[threadIdx.x][i];
+        part[threadIdx.x * NSUM + blockIdx.x] = t;
+    }
+}
+
+// network inputs from the solver state (compact layout), each channel scaled
+// by its rms: sc[0] = |r1|^2, sc[1] = |b|^2, sc[2] = |p1 - p2|^2
+__global__ void k_prep(long long n, const double *__restrict__ r1, const double *__restrict__ bw,
+                       const double *__restrict__ p1, const double *__restrict__ p2, const double *__restrict__ sc,
+                       float *__restrict__ in3)
+{
+    double rs = sqrt(sc[0] / (double)n), bs = sqrt(sc[1] / (double)n), ds = sqrt(sc[2] / (double)n);
+    double ir = rs > 0.0 ? 1.0 / rs : 0.0, ib = bs > 0.0 ? 1.0 / bs : 0.0, id = ds > 0.0 ? 1.0 / ds : 0.0;
     GRID_STRIDE(v, n)
     {
         in3[v] = (float)(r1[v] * ir);
-        in3[n + v] = (float)((p1[v] - p2[v]) / invd[v] * ir);
+        in3[n + v] = (float)((p1[v] - p2[v]) * id);
         in3[2 * n + v] = (float)(bw[v] * ib);
     }
 }
@@ -336,7 +366,7 @@ int conv(TurbNet *n, cudaStream_t s, int l, const bf16 *in, const ConvEpi &e)
     const LayerDef &d = DEFS[l];
     int lv = d.lev;
     int rc = conv3_fwd(s, in, n->X[lv], n->Y[lv], n->Z[lv], d.cin, d.cout, n->wf[l], e, n->err, n->nsm);
-    return rc ? TURB_ERR_CUDA : TURB_OK;
+    return rc ? turb_set_error_text(conv_last_error()) : TURB_OK;
 }
 // data gradient of layer l: dy (cout ch) -> dx (cin ch), masked by `mask`
 int dgrad(TurbNet *n, cudaStream_t s, int l, const bf16 *dy, const bf16 *mask, bf16 *dx)
@@ -347,14 +377,14 @@ int dgrad(TurbNet *n, cudaStream_t s, int l, const bf16 *dy, const bf16 *mask, b
     e.mask = mask;
     e.out = dx;
     int rc = conv3_fwd(s, dy, n->X[lv], n->Y[lv], n->Z[lv], d.cout, d.cin, n->wd[l], e, n->err, n->nsm);
-    return rc ? TURB_ERR_CUDA : TURB_OK;
+    return rc ? turb_set_error_text(conv_last_error()) : TURB_OK;
 }
 int wgrad(TurbNet *n, cudaStream_t s, int l, const bf16 *x, const bf16 *dy)
 {
     const LayerDef &d = DEFS[l];
     int lv = d.lev;
     int rc = conv3_wgrad(s, x, dy, n->X[lv], n->Y[lv], n->Z[lv], d.cin, d.cout, n->G + n->woff[l], n->err, n->nsm);
-    if (rc) return TURB_ERR_CUDA;
+    if (rc) return turb_set_error_text(conv_last_error());
     k_chan_sum<<<dim3(nblk(n->V[lv]) < 256 ? nblk(n->V[lv]) : 256, d.cout / 8), 256, 0, s>>>(n->V[lv], dy,
                                                                                               n->G + n->boff[l]);
     return TURB_OK;
@@ -468,7 +498,8 @@ int read_err(TurbNet *n, cudaStream_t s)
     if (cudaStreamSynchronize(s) != cudaSuccess) return TURB_ERR_CUDA;
     if (h) {
         cudaMemsetAsync(n->err, 0, sizeof(int), s);
-        return TURB_ERR_CUDA;
+        return turb_set_error_text(h == 2 ? "weight-gradient kernel: barrier wait timed out"
+                                          : "convolution kernel: barrier wait timed out");
     }
     return TURB_OK;
 }
@@ -477,6 +508,7 @@ int ensure_parts(double **part, long long *have, const MgDevLevel &L0)
 {
     long long need = pcg_stencil_parts(L0);
     if (need < 2LL * pcg_nparts()) need = 2LL * pcg_nparts();
+    if (need < 3LL * NSUM) need = 3LL * NSUM;
     if (*have >= need) return TURB_OK;
     if (*part) cudaFree(*part);
     *part = nullptr;
@@ -485,13 +517,12 @@ int ensure_parts(double **part, long long *have, const MgDevLevel &L0)
     return TURB_OK;
 }
 
-// |r1|^2 and |b|^2 into sc[0], sc[1]
-void input_norms(cudaStream_t s, long long n, const double *r1, const double *bw, double *part, double *sc)
+// |r1|^2, |b|^2 and |p1 - p2|^2 into sc[0..2]
+void input_norms(cudaStream_t s, long long n, const double *r1, const double *bw, const double *p1, const double *p2,
+                 double *part, double *sc)
 {
-    pcg_dot(s, n, r1, r1, part);
-    pcg_reduce(s, part, 1, sc + 0);
-    pcg_dot(s, n, bw, bw, part);
-    pcg_reduce(s, part, 1, sc + 1);
+    k_sumsq3<<<NSUM, 256, 0, s>>>(n, r1, bw, p1, p2, part);
+    for (int k = 0; k < 3; k++) pcg_reduce(s, part + k * NSUM, 1, sc + k, NSUM);
 }
 
 // loss of the current forward output against snapshot inputs in3; gradient into n->gout when want_grad
@@ -532,8 +563,8 @@ int net_guess(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *i
     if (!n || !same_grid(n, L0)) return TURB_ERR_ARG;
     if (ensure_parts(&n->part, &n->nparts, L0)) return TURB_ERR_ALLOC;
     long long V = n->V[0];
-    input_norms(st, V, r1, bw, n->part, n->sc);
-    k_prep<<<nblk(V), 256, 0, st>>>(V, r1, bw, p1, p2, invd, n->sc, n->in3);
+    input_norms(st, V, r1, bw, p1, p2, n->part, n->sc);
+    k_prep<<<nblk(V), 256, 0, st>>>(V, r1, bw, p1, p2, n->sc, n->in3);
     NCHK(forward(n, st, n->in3, n->hout));
     k_post<<<nblk(V), 256, 0, st>>>(V, base, invd, n->hout, n->sc, out);
     if (cudaGetLastError() != cudaSuccess) return TURB_ERR_CUDA;
@@ -547,8 +578,8 @@ int net_snapshot(TurbSnaps *sn, cudaStream_t st, const MgDevLevel &L0, const dou
     if (sn->n >= sn->cap) return TURB_OK;   // store full: later solves are not recorded
     if (ensure_parts(&sn->part, &sn->nparts, L0)) return TURB_ERR_ALLOC;
     long long V = sn->V;
-    input_norms(st, V, r1, bw, sn->part, sn->sc);
-    k_prep<<<nblk(V), 256, 0, st>>>(V, r1, bw, p1, p2, invd, sn->sc, sn->data + (long long)sn->n * 3 * V);
+    input_norms(st, V, r1, bw, p1, p2, sn->part, sn->sc);
+    k_prep<<<nblk(V), 256, 0, st>>>(V, r1, bw, p1, p2, sn->sc, sn->data + (long long)sn->n * 3 * V);
     sn->n++;
     return cudaGetLastError() == cudaSuccess ? TURB_OK : TURB_ERR_CUDA;
 }
@@ -758,6 +789,21 @@ int turb_net_adam(turb_net *h, float lr, void *stream)
     return cudaStreamSynchronize(s) == cudaSuccess ? TURB_OK : TURB_ERR_CUDA;
 }
 
+// forward activations in order x0 a0 p0 a1 p1 a2 p2 a3 b3 c2 s2 b2 c1 s1 b1 c0 s0 b0,
+// copied as raw BF16 bits in the channel-blocked layout
+int turb_net_get_activation(turb_net *h, int which, uint16_t *host, long long count)
+{
+    TurbNet *n = reinterpret_cast<TurbNet *>(h);
+    if (!n || !host || which < 0 || which > 17) return TURB_ERR_ARG;
+    struct A { bf16 *p; int lev, c; };
+    const A t[18] = {{n->x0, 0, 16}, {n->a0, 0, 16}, {n->p0, 1, 16}, {n->a1, 1, 32}, {n->p1, 2, 32}, {n->a2, 2, 64},
+                     {n->p2, 3, 64}, {n->a3, 3, 128}, {n->b3, 3, 128}, {n->c2, 3, 64}, {n->s2, 2, 64}, {n->b2, 2, 64},
+                     {n->c1, 2, 32}, {n->s1, 1, 32}, {n->b1, 1, 32}, {n->c0, 1, 16}, {n->s0, 0, 16}, {n->b0, 0, 16}};
+    const A &a = t[which];
+    if (!a.p || count != n->V[a.lev] * a.c) return TURB_ERR_ARG;
+    return cudaMemcpy(host, a.p, (size_t)count * 2, cudaMemcpyDeviceToHost) == cudaSuccess ? TURB_OK : TURB_ERR_CUDA;
+}
+
 int turb_snaps_create(int nx, int ny, int nz, int capacity, turb_snaps **out)
 {
     if (!out || nx < 1 || ny < 1 || nz < 1 || capacity < 1) return TURB_ERR_ARG;
@@ -831,7 +877,7 @@ int turb_conv3_test(int X, int Y, int Z, int cin, int cout, const void *in, cons
     cudaError_t ce = cudaStreamSynchronize(s);
     if (ce == cudaSuccess) ce = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(wf); cudaFree(wd); cudaFree(err);
-    if (rc) return TURB_ERR_ARG;
+    if (rc) return turb_set_error_text(conv_last_error());
     return (ce != cudaSuccess || h) ? TURB_ERR_CUDA : TURB_OK;
 }
 
@@ -853,7 +899,7 @@ int turb_conv3_wgrad_test(int X, int Y, int Z, int cin, int cout, const void *x,
     cudaError_t ce = cudaStreamSynchronize(s);
     if (ce == cudaSuccess) ce = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(err);
-    if (rc) return TURB_ERR_ARG;
+    if (rc) return turb_set_error_text(conv_last_error());
     return (ce != cudaSuccess || h) ? TURB_ERR_CUDA : TURB_OK;
 }
 

@@ -17,6 +17,12 @@
 
 static char g_errmsg[512] = "";
 
+int turb_set_error_text(const char *msg)
+{
+    snprintf(g_errmsg, sizeof(g_errmsg), "%s", msg);
+    return TURB_ERR_CUDA;
+}
+
 int turb_set_cuda_error(cudaError_t e, const char *file, int line)
 {
     snprintf(g_errmsg, sizeof(g_errmsg), "%s (%s:%d)", cudaGetErrorString(e), file, line);
@@ -115,6 +121,7 @@ struct turb_ctx {
     double *ph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int nh[2] = {0, 0};
     int guess_taken = 0, guess_tried = 0;
+    double guess_logsum = 0.0;   // sum of log(|r candidate| / |r previous|)
     // learned guess (k_net.cu) and the snapshot store that training reads
     TurbNet *net = nullptr;
     TurbSnaps *snaps = nullptr;
@@ -1001,6 +1008,13 @@ int turb_net_eval(turb_net *net, turb_ctx *c, turb_snaps *snaps, int first, int 
                     reinterpret_cast<TurbSnaps *>(snaps), first, count, mean_loss);
 }
 
+int turb_pressure_guess_ratio(turb_ctx *c, double *geo_mean)
+{
+    if (!c || !geo_mean) return TURB_ERR_ARG;
+    *geo_mean = c->guess_tried > 0 ? std::exp(c->guess_logsum / c->guess_tried) : 1.0;
+    return TURB_OK;
+}
+
 int turb_pressure_guess_stats(turb_ctx *c, int *tried, int *taken)
 {
     if (!c || !tried || !taken) return TURB_ERR_ARG;
@@ -1386,6 +1400,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             double nrc = std::sqrt(c->hscal[2]);
             if (ph >= 0) prof_end(c, ph, NET_GUESS_LAUNCHES + 2);
             c->guess_tried++;
+            if (nr > 0.0 && nrc > 0.0 && std::isfinite(nrc)) c->guess_logsum += std::log(nrc / nr);
             if (nrc < nr) {
                 pcg_copy(s, n0, c->pz, c->px);
                 pcg_copy(s, n0, c->pq, c->pr);

@@ -9,10 +9,13 @@
 struct TurbNet;
 struct TurbSnaps;
 
+// records a message for turb_status_string(TURB_ERR_CUDA); returns TURB_ERR_CUDA
+int turb_set_error_text(const char *msg);
+
 // kernel launches of one net_guess (norms 4, inputs 1, forward 18, update 1)
 constexpr int NET_GUESS_LAUNCHES = 24;
 
-// candidate = base + s * invd * net(r1 / s, (p1 - p2) / (invd * s), b / |b|_rms),
+// candidate = base + s * invd * net(r1 / s, (p1 - p2) / |p1 - p2|_rms, b / |b|_rms),
 // s = |r1|_rms; all vectors on the compact cell layout of L0
 int net_guess(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *invd, const double *r1,
               const double *bw, const double *p1, const double *p2, const double *base, double *out);

@@ -1,0 +1,152 @@
+"""Training and use of the learned initial guess of the pressure solve.
+
+Snapshots come from the plain solver (previous-pressure guess) on small runs
+of the same physics; the network is trained on the GPU by the library's own
+kernels (turb_net_train: tcgen05 forward and backward, Adam) and is then
+attached to a solver context of any size whose cell counts are multiples of
+8.  The solver keeps a network guess only when it lowers the initial residual
+below the previous pressure's, so the converged answer never depends on it.
+
+    python -m turbins_gb300.learned --infer 256 128 128      # training + inference report
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import api as A
+from . import net as N
+from . import workload as W
+
+
+def record(case_fn, seeds, steps, capacity=None):
+    """Run case_fn(seed) for `steps` steps per seed with the plain solver and
+    keep the network inputs of every pressure solve.  Returns (store, ctx),
+    ctx being a context on the same grid (its pressure operator defines the
+    training loss)."""
+    store, ctx = None, None
+    for seed in seeds:
+        case = case_fn(seed)
+        p = case.params
+        if store is None:
+            store = N.Snapshots(p.nx, p.ny, p.nz, capacity or 2 * steps * len(seeds))
+        if ctx is not None:
+            ctx.close()
+        ctx = A.Context(case.grid, case.params)
+        ctx.load_state(case.state)
+        N.set_snapshot_store(ctx, store)
+        for _ in range(steps):
+            ctx.step(case.dt)
+        N.set_snapshot_store(ctx, None)
+    return store, ctx
+
+
+def train(store, ctx, iters=3000, lr=1e-3, seed=0, init_seed=1):
+    """Adam on randomly drawn snapshots (lr for 70% of the steps, lr/4 after);
+    returns (net, mean loss of the last phase)."""
+    nx, ny, nz = ctx.params.nx, ctx.params.ny, ctx.params.nz
+    net = N.Net(nx, ny, nz, train=True)
+    net.init_params(init_seed)
+    n1 = int(0.7 * iters)
+    net.train_on(ctx, store, n1, lr=lr, seed=seed)
+    loss = net.train_on(ctx, store, iters - n1, lr=lr / 4, seed=seed + 1)
+    return net, loss
+
+
+def attach(ctx, params):
+    """Network of ctx's size carrying `params`, used as the LEARNED guess."""
+    p = ctx.params
+    net = N.Net(p.nx, p.ny, p.nz, train=False)
+    net.set_params(params)
+    N.set_learned_net(ctx, net)
+    ctx.set_pressure_guess(A.GUESS_LEARNED)
+    return net
+
+
+def multi_bump_train_case(nx=128, ny=64, nz=64):
+    """Training runs for the 512x256x256 multi-bump step: the same physics and
+    x spacing on a quarter-length domain, one bump field per seed."""
+    return lambda seed: W.multi_bump_case(nx, ny, nz, seed=100 + seed, lx=32.0 * nx / 512.0)
+
+
+def turbidity_train_case(nx=128, ny=64, nz=64):
+    """Training runs for the single-bump turbidity current: one lock-noise seed each."""
+    return lambda seed: W.turbidity_bump_case(nx, ny, nz, seed=seed)
+
+
+def train_default(case_fn, seeds=8, steps=250, iters=3000, lr=1e-3):
+    t0 = time.perf_counter()
+    store, ctx = record(case_fn, range(seeds), steps)
+    t1 = time.perf_counter()
+    net, loss = train(store, ctx, iters=iters, lr=lr)
+    t2 = time.perf_counter()
+    info = dict(snapshots=len(store), record_s=t1 - t0, train_s=t2 - t1, iters=iters, train_loss=loss)
+    params = net.get_params()
+    net.close()
+    store.close()
+    ctx.close()
+    return params, info
+
+
+def compare(case, params, steps, pmode=A.PMODE_MIXED):
+    """Per-step PCG iterations and pressure-solve time with the previous-pressure
+    guess and with the learned guess, from the same initial state."""
+    out = {}
+    for name in ("previous", "learned"):
+        ctx = A.Context(case.grid, case.params)
+        ctx.load_state(case.state)
+        ctx.set_pressure_mode(pmode)
+        net = attach(ctx, params) if name == "learned" else None
+        for _ in range(2):
+            ctx.step(case.dt)   # history for the guess
+        A.profile_enable(ctx, True)
+        its = []
+        for _ in range(steps):
+            st = ctx.step(case.dt)
+            its.append(list(st["p_iters"]))
+        prof = A.profile_read(ctx)
+        tried, taken = ctx.pressure_guess_stats()
+        out[name] = dict(p_iters=its, mean_iters=float(np.mean(its)), residual_ratio=ctx.pressure_guess_ratio(),
+                         solve_ms_per_step=sum(prof[g][0] for g in ("mg", "pcg", "net")) / steps,
+                         net_ms_per_step=prof["net"][0] / steps, guess_tried=tried, guess_taken=taken)
+        if net is not None:
+            net.close()
+        ctx.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--infer", type=int, nargs=3, default=[256, 128, 128])
+    ap.add_argument("--train", type=int, nargs=3, default=[128, 64, 64])
+    ap.add_argument("--seeds", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=250)
+    ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--compare-steps", type=int, default=20)
+    ap.add_argument("--warm-steps", type=int, default=200, help="steps before the comparison window")
+    ap.add_argument("--physics", choices=["turbidity", "multi"], default="turbidity")
+    ap.add_argument("--save", default=None)
+    a = ap.parse_args()
+    tx, ty, tz = a.train
+    mk = turbidity_train_case(tx, ty, tz) if a.physics == "turbidity" else multi_bump_train_case(tx, ty, tz)
+    params, info = train_default(mk, seeds=a.seeds, steps=a.steps, iters=a.iters)
+    if a.save:
+        np.save(a.save, params)
+    nx, ny, nz = a.infer
+    case = W.turbidity_bump_case(nx, ny, nz) if a.physics == "turbidity" else \
+        W.multi_bump_case(nx, ny, nz, lx=32.0 * nx / 512.0)
+    ctx = A.Context(case.grid, case.params)
+    ctx.load_state(case.state)
+    for _ in range(a.warm_steps):
+        ctx.step(case.dt)
+    case.state = ctx.state()
+    ctx.close()
+    res = compare(case, params, a.compare_steps)
+    print(json.dumps(dict(train=info, infer=[nx, ny, nz], physics=a.physics, warm_steps=a.warm_steps, **res)))
+
+
+if __name__ == "__main__":
+    main()

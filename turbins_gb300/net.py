@@ -70,6 +70,22 @@ class Net:
                "turb_net_get_grads")
         return g
 
+    ACTS = ("x0", "a0", "p0", "a1", "p1", "a2", "p2", "a3", "b3", "c2", "s2", "b2", "c1", "s1", "b1", "c0", "s0", "b0")
+    ACT_SHAPE = dict(x0=(0, 16), a0=(0, 16), p0=(1, 16), a1=(1, 32), p1=(2, 32), a2=(2, 64), p2=(3, 64), a3=(3, 128),
+                     b3=(3, 128), c2=(3, 64), s2=(2, 64), b2=(2, 64), c1=(2, 32), s1=(1, 32), b1=(1, 32), c0=(1, 16),
+                     s0=(0, 16), b0=(0, 16))
+
+    def activation(self, name):
+        """Forward activation as float64 [C, Z, Y, X] (BF16 values)."""
+        lev, c = self.ACT_SHAPE[name]
+        nx, ny, nz = (d >> lev for d in self.dims)
+        raw = np.zeros((c // 8, nz, ny, nx, 8), dtype=np.uint16)
+        _check(self.lib.turb_net_get_activation(self.h, self.ACTS.index(name),
+                                                raw.ctypes.data_as(C.POINTER(C.c_uint16)), C.c_longlong(raw.size)),
+               "turb_net_get_activation")
+        f = (raw.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        return np.ascontiguousarray(f.transpose(0, 4, 1, 2, 3).reshape(c, nz, ny, nx))
+
     def forward(self, in3, out):
         """in3: torch float32 CUDA tensor [3, nz, ny, nx]; out: [nz, ny, nx]."""
         _check(self.lib.turb_net_forward(self.h, _dev(in3), _dev(out), None), "turb_net_forward")
