@@ -276,7 +276,9 @@ int turb_net_forward(turb_net *net, const float *in3, float *out, void *stream);
 /* gradients for d loss / d out = gout (ncell FP32 device) of the last forward */
 int turb_net_backward(turb_net *net, const float *gout, void *stream);
 int turb_net_adam(turb_net *net, float lr, void *stream);
-/* snapshot store: the network inputs of pressure solves, in3 layout */
+/* snapshot store: per pressure solve the network inputs (3 channels, in3
+ * layout) and the target channel out* = (p - p_previous) diag(A) / s of the
+ * converged pressure p; a solve that does not converge leaves no snapshot */
 int turb_snaps_create(int nx, int ny, int nz, int capacity, turb_snaps **out);
 int turb_snaps_destroy(turb_snaps *snaps);
 int turb_snaps_count(const turb_snaps *snaps);
@@ -286,15 +288,24 @@ int turb_snaps_data(turb_snaps *snaps, int index, const float **dev_ptr);
 int turb_set_snapshot_store(turb_ctx *ctx, turb_snaps *snaps);
 /* use net for TURB_GUESS_LEARNED (grid of net = physical cells of ctx) */
 int turb_set_learned_net(turb_ctx *ctx, turb_net *net);
-/* steps of Adam on randomly drawn snapshots; loss = |r1 - A delta|^2/|r1|^2
- * with ctx's pressure operator; mean loss over the steps */
+/* training loss = w_residual L_R + w_energy L_E with ctx's pressure operator A:
+ * L_R = |r1 - A delta|^2 / |r1|^2 (the squared relative initial residual of
+ * the candidate, what the guard compares) and L_E = e^T A e / e0^T A e0 with
+ * e = dp* - delta, e0 = dp* (the A-norm error left, relative to the previous
+ * pressure's; dp* = the converged increment of that solve, recorded with the
+ * snapshot).  Default (1, 0). */
+int turb_net_set_loss(turb_net *net, double w_residual, double w_energy);
+/* steps of Adam on randomly drawn snapshots; mean training loss */
 int turb_net_train(turb_net *net, turb_ctx *ctx, turb_snaps *snaps, int steps, float lr,
                    unsigned long long seed, double *mean_loss);
+/* forward only: mean L_R and L_E over snapshots first .. first+count-1 */
 int turb_net_eval(turb_net *net, turb_ctx *ctx, turb_snaps *snaps, int first, int count,
-                  double *mean_loss);
+                  double *mean_residual, double *mean_energy);
 /* self-test of the tcgen05 operand descriptors: one 128 x 64 x 32 BF16 MMA
  * from K-major (mn_major = 0) or MN-major (1) shared-memory layouts; swap = 1
- * exchanges the LBO and SBO fields.  Returns the number of wrong results. */
+ * exchanges the LBO and SBO fields; swap = 2 issues no MMA so that the
+ * kernel's bounded completion wait runs out (>= 1000000 reported, the
+ * context stays usable).  Returns the number of wrong results. */
 int turb_selftest_umma(int mn_major, int swap, unsigned long long *mismatches);
 /* one convolution of the network's kernels on caller device buffers
  * (channel-blocked BF16 [C/8][Z][Y][X][8]; W FP32 [27][cout][cin]):

@@ -63,12 +63,15 @@ def test_learned_guess_trains_and_gains(mods):
 
     net = N.Net(nx, ny, nz, train=True)
     net.init_params(1)
+    net.set_loss(1.0, 1.0)
     before = net.eval_on(ctx, held, 0, len(held))
-    assert abs(before - 1.0) < 0.5          # near-zero output leaves the residual as it is
+    # a near-zero output leaves the previous pressure as it is
+    assert abs(before[0] - 1.0) < 0.5 and abs(before[1] - 1.0) < 0.5
     loss = net.train_on(ctx, train, 600, lr=1e-3, seed=7)
     after = net.eval_on(ctx, held, 0, len(held))
-    print("held-out |r|^2 ratio before %.4f after %.4f (train %.4f)" % (before, after, loss))
-    assert after < 0.5 * before
+    print("held-out |r|^2 ratio before %.4f after %.4f, energy-error ratio before %.4f after %.4f (train %.4f)"
+          % (before[0], after[0], before[1], after[1], loss))
+    assert after[0] < 0.5 * before[0] and after[1] < before[1]
 
     ref, it_prev, _, _, _ = _run(A, case, state, 12, dt, A.GUESS_PREVIOUS)
     got, it_learn, tried, taken, ratio = _run(A, case, state, 12, dt, A.GUESS_LEARNED, net)

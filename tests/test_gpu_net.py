@@ -32,6 +32,18 @@ def test_umma_descriptor_layouts(netmod, mn):
         pytest.fail("mn_major=%d: %d wrong results (%d with LBO/SBO exchanged)" % (mn, bad, other))
 
 
+def test_bounded_wait_times_out_and_context_survives(netmod):
+    """A completion wait that nothing satisfies gives up after its limit
+    (about 1 s) with an error count instead of hanging; the next launch on the
+    same context works."""
+    import time
+    t0 = time.time()
+    bad = netmod.selftest_umma(0, 2)
+    assert bad >= 1000000
+    assert time.time() - t0 < 30
+    assert netmod.selftest_umma(0, 0) == 0
+
+
 def _bf16_dev(a):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(torch.bfloat16).cuda()
 

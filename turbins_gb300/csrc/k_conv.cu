@@ -65,6 +65,76 @@ __device__ __forceinline__ void drain(uint32_t bars, int base, uint32_t n, int S
     }
 }
 
+// epilogue of one 128-voxel tile: this thread's accumulator row (all cout
+// columns from TMEM, loaded by the whole warp) -> bias, skip, ReLU, mask,
+// BF16 store, optional 1x1x1 head
+struct EpiP {
+    const float *bias;
+    int relu;
+    const bf16 *skip, *mask;
+    bf16 *out;
+    const float *headw, *headb;
+    float *hout;
+    int cout;
+    size_t plane;
+};
+
+__device__ __forceinline__ void epilogue(const EpiP &a, uint32_t taddr, size_t vox, bool valid)
+{
+    float hsum = 0.f;
+    for (int ch = 0; ch < (a.cout >> 4); ch++) {
+        uint32_t rr[16];
+        tc::tmem_ld16(taddr + (uint32_t)ch * 16u, rr);
+        tc::tmem_wait_ld();
+        if (!valid) continue;
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = __uint_as_float(rr[j]);
+        if (a.bias) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] += a.bias[ch * 16 + j];
+        }
+        size_t o0 = ((size_t)(2 * ch) * a.plane + vox) * 8, o1 = o0 + a.plane * 8;
+        if (a.skip) {
+            uint4 s0 = *reinterpret_cast<const uint4 *>(a.skip + o0);
+            uint4 s1 = *reinterpret_cast<const uint4 *>(a.skip + o1);
+            const bf16 *p0 = reinterpret_cast<const bf16 *>(&s0), *p1 = reinterpret_cast<const bf16 *>(&s1);
+#pragma unroll
+            for (int j = 0; j < 8; j++) { v[j] += __bfloat162float(p0[j]); v[8 + j] += __bfloat162float(p1[j]); }
+        }
+        if (a.relu) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.f);
+        }
+        if (a.mask) {
+            uint4 m0 = *reinterpret_cast<const uint4 *>(a.mask + o0);
+            uint4 m1 = *reinterpret_cast<const uint4 *>(a.mask + o1);
+            const bf16 *p0 = reinterpret_cast<const bf16 *>(&m0), *p1 = reinterpret_cast<const bf16 *>(&m1);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (!(__bfloat162float(p0[j]) > 0.f)) v[j] = 0.f;
+                if (!(__bfloat162float(p1[j]) > 0.f)) v[8 + j] = 0.f;
+            }
+        }
+        uint4 w0, w1;
+        bf16 *q0 = reinterpret_cast<bf16 *>(&w0), *q1 = reinterpret_cast<bf16 *>(&w1);
+#pragma unroll
+        for (int j = 0; j < 8; j++) { q0[j] = __float2bfloat16_rn(v[j]); q1[j] = __float2bfloat16_rn(v[8 + j]); }
+        if (a.out) {
+            *reinterpret_cast<uint4 *>(a.out + o0) = w0;
+            *reinterpret_cast<uint4 *>(a.out + o1) = w1;
+        }
+        if (a.headw) {
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                hsum = fmaf(a.headw[ch * 16 + j], __bfloat162float(q0[j]), hsum);
+                hsum = fmaf(a.headw[ch * 16 + 8 + j], __bfloat162float(q1[j]), hsum);
+            }
+        }
+    }
+    if (valid && a.hout) a.hout[vox] = hsum + *a.headb;
+}
+
 __global__ void __launch_bounds__(192) k_conv(const __grid_constant__ CUtensorMap mapA, ConvArgs a)
 {
     extern __shared__ uint8_t dsm[];
@@ -208,58 +278,8 @@ __global__ void __launch_bounds__(192) k_conv(const __grid_constant__ CUtensorMa
             bool valid = zz < a.bz && gx < a.X && gy < a.Y && gz < a.Z;
             size_t vox = ((size_t)gz * a.Y + gy) * a.X + gx;
             uint32_t taddr = tbase + ((uint32_t)(q * 32) << 16) + ab * (uint32_t)a.cout;
-            float hsum = 0.f;
-            for (int ch = 0; ch < (a.cout >> 4); ch++) {
-                uint32_t rr[16];
-                tc::tmem_ld16(taddr + (uint32_t)ch * 16u, rr);
-                tc::tmem_wait_ld();
-                if (!valid) continue;
-                float v[16];
-#pragma unroll
-                for (int j = 0; j < 16; j++) v[j] = __uint_as_float(rr[j]);
-                if (a.bias) {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) v[j] += a.bias[ch * 16 + j];
-                }
-                size_t o0 = ((size_t)(2 * ch) * plane + vox) * 8, o1 = o0 + plane * 8;
-                if (a.skip) {
-                    uint4 s0 = *reinterpret_cast<const uint4 *>(a.skip + o0);
-                    uint4 s1 = *reinterpret_cast<const uint4 *>(a.skip + o1);
-                    const bf16 *p0 = reinterpret_cast<const bf16 *>(&s0), *p1 = reinterpret_cast<const bf16 *>(&s1);
-#pragma unroll
-                    for (int j = 0; j < 8; j++) { v[j] += __bfloat162float(p0[j]); v[8 + j] += __bfloat162float(p1[j]); }
-                }
-                if (a.relu) {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.f);
-                }
-                if (a.mask) {
-                    uint4 m0 = *reinterpret_cast<const uint4 *>(a.mask + o0);
-                    uint4 m1 = *reinterpret_cast<const uint4 *>(a.mask + o1);
-                    const bf16 *p0 = reinterpret_cast<const bf16 *>(&m0), *p1 = reinterpret_cast<const bf16 *>(&m1);
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        if (!(__bfloat162float(p0[j]) > 0.f)) v[j] = 0.f;
-                        if (!(__bfloat162float(p1[j]) > 0.f)) v[8 + j] = 0.f;
-                    }
-                }
-                uint4 w0, w1;
-                bf16 *q0 = reinterpret_cast<bf16 *>(&w0), *q1 = reinterpret_cast<bf16 *>(&w1);
-#pragma unroll
-                for (int j = 0; j < 8; j++) { q0[j] = __float2bfloat16_rn(v[j]); q1[j] = __float2bfloat16_rn(v[8 + j]); }
-                if (a.out) {
-                    *reinterpret_cast<uint4 *>(a.out + o0) = w0;
-                    *reinterpret_cast<uint4 *>(a.out + o1) = w1;
-                }
-                if (a.headw) {
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        hsum = fmaf(a.headw[ch * 16 + j], __bfloat162float(q0[j]), hsum);
-                        hsum = fmaf(a.headw[ch * 16 + 8 + j], __bfloat162float(q1[j]), hsum);
-                    }
-                }
-            }
-            if (valid && a.hout) a.hout[vox] = hsum + *a.headb;
+            epilogue(EpiP{a.bias, a.relu, a.skip, a.mask, a.out, a.headw, a.headb, a.hout, a.cout, plane}, taddr, vox,
+                     valid);
             tc::fence_before();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(bars + 8 * (AE + ab));
@@ -269,6 +289,274 @@ __global__ void __launch_bounds__(192) k_conv(const __grid_constant__ CUtensorMa
     __syncthreads();
     tc::fence_after();
     if (warp == 1) tc::tmem_dealloc(tbase, ncols);
+}
+
+
+// ---- row-ring convolution (grids at least 128 voxels wide, cin <= 32) ------------
+// A CTA takes items of (x tile of 128 voxels, z, a run of consecutive y rows).
+// Input rows (3 z planes x 130 voxels x cin, contiguous per channel block in
+// global memory) stream through a ring of RING slots by bulk copies, producer
+// warp L % 4 loading row L.  Every input row r feeds the three output rows
+// r+1, r, r-1 (dy = 0, 1, 2): the weights of the three dy taps are stacked
+// along N, so one MMA (M = 128 voxels, N = 3 cout, K = 16) per (dz, dx) and
+// K step covers all of them -- 9 MMAs per output row instead of 27, which
+// matters because an MMA with a small N costs the same as one with N = 96.
+// The three targets are consecutive blocks of a TMEM ring of NBLK accumulator
+// blocks (block of virtual row v = NBLK-1 - v mod NBLK, so rows r+1, r, r-1
+// are ascending; a wrap splits the MMA).  Accumulation is always on: the
+// epilogue zeroes a block after draining it.  Weights are resident.
+constexpr int RING = 6, RW = 130;   // input row slots per z plane, voxels per slab row
+constexpr int NBLK = 8;             // TMEM accumulator blocks
+
+struct RowArgs {
+    int X, Y, Z, cin, cout;
+    int ntx, ych, nyc, nitems;
+    uint32_t lbo, slab_bytes, wbytes;
+    const bf16 *in, *wpk;
+    EpiP epi;
+    int *err;
+};
+
+// barrier slots of k_conv_rows
+constexpr int RF = 0, RE = RING, BRDY = 2 * RING, BFREE = 2 * RING + NBLK, RWB = 2 * RING + 2 * NBLK,
+              RFIN = RWB + 1, RNBAR = RWB + 2;
+
+__host__ __device__ inline uint32_t rows_ncols(int cout)
+{
+    uint32_t n = 32;
+    while (n < (uint32_t)(NBLK * cout)) n <<= 1;
+    return n;
+}
+__device__ __forceinline__ int blk_of(uint32_t v) { return NBLK - 1 - (int)(v % NBLK); }
+
+__device__ __forceinline__ void tmem_st16_zero(uint32_t taddr)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1};" ::"r"(taddr),
+        "r"(0u)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+__device__ __forceinline__ void row_item(const RowArgs &a, int it, int &x0, int &z, int &yb, int &ny)
+{
+    int tx = it % a.ntx, r = it / a.ntx;
+    z = r % a.Z;
+    int yc = r / a.Z;
+    x0 = tx * 128;
+    yb = yc * a.ych;
+    ny = min(a.ych, a.Y - yb);
+}
+
+__global__ void __launch_bounds__(288) k_conv_rows(RowArgs a)
+{
+    extern __shared__ uint8_t dsm[];
+    __shared__ __align__(8) uint64_t bar[RNBAR];
+    __shared__ uint32_t tslot;
+    __shared__ int abort_s;
+    volatile int *abort_ = &abort_s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t sS = (tc::smem_u32(dsm) + 1023u) & ~1023u;   // slab ring
+    const uint32_t sW = sS + ((a.slab_bytes + 1023u) & ~1023u);  // resident stacked weights
+    const uint32_t bars = tc::smem_u32(bar);
+    const uint32_t ncols = rows_ncols(a.cout);
+    const int nkg = a.cin >> 3;
+
+    if (threadIdx.x == 0) {
+        abort_s = 0;
+        for (int i = 0; i < RNBAR; i++) {
+            uint32_t cnt = 1;
+            if (i >= RF && i < RF + RING) cnt = 32;             // the producer warp of the row
+            if (i >= BFREE && i < BFREE + NBLK) cnt = 4;       // epilogue warps
+            tc::mbar_init(bars + 8 * i, cnt);
+        }
+        tc::mbar_fence_init();
+    }
+    if (warp == 8) {
+        tc::tmem_alloc(tc::smem_u32(&tslot), ncols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tbase = tslot;
+    if (warp < 4) {   // accumulators start at zero
+        for (int b = 0; b < NBLK; b++)
+            for (int ch = 0; ch < (a.cout >> 4); ch++)
+                tmem_st16_zero(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * a.cout + ch * 16));
+        tmem_wait_st();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+
+    if (warp >= 4 && warp < 8) {
+        // ---- producers
+        const int pw = warp - 4;
+        if (pw == 0 && lane == 0) {
+            tc::mbar_expect_tx(bars + 8 * RWB, a.wbytes);
+            tc::bulk_load(sW, a.wpk, a.wbytes, bars + 8 * RWB);
+        }
+        uint32_t L = 0;
+        bool ok = true;
+        for (int it = blockIdx.x; ok && it < a.nitems; it += gridDim.x) {
+            int x0, z, yb, ny;
+            row_item(a, it, x0, z, yb, ny);
+            for (int j = 0; j < ny + 2; j++, L++) {
+                if ((int)(L & 3u) != pw) continue;
+                uint32_t slot = L % RING;
+                if (L >= RING && !tc::mbar_wait(bars + 8 * (RE + slot), ((L / RING) & 1u) ^ 1u, abort_)) {
+                    ok = false;
+                    break;
+                }
+                // in-range voxels of each (channel block, z plane) segment by one
+                // bulk copy; voxels outside the grid zero-filled by cp.async
+                int yy = yb - 1 + j;
+                bool yok = yy >= 0 && yy < a.Y;
+                int xs = max(x0 - 1, 0), xe = min(x0 + RW - 1, a.X);
+                uint32_t fullb = bars + 8 * (RF + slot);
+                if (lane == 0) {
+                    uint32_t tx = 0;
+                    for (int zp = 0; zp < 3; zp++) {
+                        int zz = z + zp - 1;
+                        if (yok && zz >= 0 && zz < a.Z) tx += (uint32_t)(xe - xs) * 16u * (uint32_t)nkg;
+                    }
+                    if (tx) tc::mbar_add_tx(fullb, tx);
+                    for (int kg = 0; kg < nkg; kg++) {
+                        for (int zp = 0; zp < 3; zp++) {
+                            int zz = z + zp - 1;
+                            if (!(yok && zz >= 0 && zz < a.Z)) continue;
+                            const bf16 *src = a.in + ((((size_t)kg * a.Z + zz) * a.Y + yy) * a.X + xs) * 8;
+                            uint32_t dst =
+                                sS + (uint32_t)(((((kg * 3 + zp) * RING + (int)slot) * RW) + (xs - x0 + 1)) * 16);
+                            tc::bulk_load(dst, src, (uint32_t)(xe - xs) * 16u, fullb);
+                        }
+                    }
+                }
+                for (int kg = 0; kg < nkg; kg++) {
+                    for (int zp = 0; zp < 3; zp++) {
+                        int zz = z + zp - 1;
+                        bool rok = yok && zz >= 0 && zz < a.Z;
+                        uint32_t rdst = sS + (uint32_t)((((kg * 3 + zp) * RING + (int)slot) * RW) * 16);
+                        if (!rok) {
+                            for (int xx = lane; xx < RW; xx += 32) cp_async16(rdst + (uint32_t)xx * 16u, a.in, 0u);
+                        } else if (lane == 1 && xs > x0 - 1) {
+                            cp_async16(rdst, a.in, 0u);   // x = -1
+                        } else if (lane == 2 && xe < x0 + RW - 1) {
+                            for (int xx = xe - x0 + 1; xx < RW; xx++) cp_async16(rdst + (uint32_t)xx * 16u, a.in, 0u);
+                        }
+                    }
+                }
+                cp_async_commit();
+                cp_async_wait0();
+                tc::fence_proxy_async();
+                tc::mbar_arrive(fullb);
+            }
+        }
+        cp_async_wait0();
+        if (!ok) fail(abort_, a.err, 3);
+        if (pw == 0 && lane == 0) tc::mbar_wait(bars + 8 * RWB, 0, abort_);
+    } else if (warp == 8) {
+        if (lane == 0) {
+            const uint32_t N3 = 3u * (uint32_t)a.cout;
+            const uint32_t b_lbo = N3 * 16u;                       // stacked B: next 8 input channels
+            const uint32_t bdz = (uint32_t)nkg * b_lbo;            // next (dz, dx) block
+            uint32_t L = 0, V = 0;
+            bool ok = tc::mbar_wait(bars + 8 * RWB, 0, abort_);
+            for (int it = blockIdx.x; ok && it < a.nitems; it += gridDim.x) {
+                int x0, z, yb, ny;
+                row_item(a, it, x0, z, yb, ny);
+                const int nv = ny + 2;   // virtual output rows yb-1 .. yb+ny of this item
+                for (int j = 0; ok && j < nv; j++) {
+                    // blocks touched for the first time: rows j+1 (and j at the start)
+                    for (int v = (j == 0 ? 0 : j + 1); v <= j + 1 && v < nv; v++) {
+                        uint32_t g = V + (uint32_t)v;
+                        if (!tc::mbar_wait(bars + 8 * (BFREE + blk_of(g)), ((g / NBLK) & 1u) ^ 1u, abort_)) { ok = false; break; }
+                    }
+                    uint32_t Lr = L + (uint32_t)j, slot = Lr % RING;
+                    if (!ok || !tc::mbar_wait(bars + 8 * (RF + slot), (Lr / RING) & 1u, abort_)) { ok = false; break; }
+                    tc::fence_after();
+                    // runs of consecutive valid target blocks among rows j+1, j, j-1 (k = dy)
+                    int kb[3], kv[3];
+                    for (int k = 0; k < 3; k++) {
+                        int row = j + 1 - k;
+                        kv[k] = row >= 0 && row < nv;
+                        kb[k] = kv[k] ? blk_of(V + (uint32_t)row) : -1;
+                    }
+                    for (int dz = 0; dz < 3; dz++) {
+                        for (int dx = 0; dx < 3; dx++) {
+                            uint32_t abase = sS + (uint32_t)(((dz * RING + (int)slot) * RW + dx) * 16);
+                            uint32_t bbase = sW + (uint32_t)(dz * 3 + dx) * bdz;
+                            int k = 0;
+                            while (k < 3) {
+                                if (!kv[k]) { k++; continue; }
+                                int k1 = k + 1;
+                                while (k1 < 3 && kv[k1] && kb[k1] == kb[k1 - 1] + 1) k1++;
+                                uint32_t n = (uint32_t)(k1 - k) * (uint32_t)a.cout;
+                                uint32_t idesc = tc::idesc_bf16(128, (int)n, 0, 0);
+                                uint32_t dt = tbase + (uint32_t)(kb[k] * a.cout);
+                                for (int ks = 0; ks < (nkg >> 1); ks++) {
+                                    uint64_t ad = tc::sdesc(abase + (uint32_t)ks * 2u * a.lbo, a.lbo, 128);
+                                    uint64_t bd = tc::sdesc(bbase + (uint32_t)ks * 2u * b_lbo + (uint32_t)k * a.cout * 16u,
+                                                            b_lbo, 128);
+                                    tc::mma_bf16(dt, ad, bd, idesc, 1u);
+                                }
+                                k = k1;
+                            }
+                        }
+                    }
+                    tc::mma_commit(bars + 8 * (RE + slot));                           // input row done
+                    if (j >= 1) tc::mma_commit(bars + 8 * (BRDY + kb[2]));            // output row j-1 done
+                }
+                if (!ok) break;
+                tc::mma_commit(bars + 8 * (BRDY + blk_of(V + (uint32_t)(nv - 1))));   // partial last row
+                L += (uint32_t)nv;
+                V += (uint32_t)nv;
+            }
+            if (!ok) fail(abort_, a.err, 3);
+            tc::mma_commit(bars + 8 * RFIN);
+            tc::mbar_wait(bars + 8 * RFIN, 0, abort_);
+        }
+    } else if (warp < 4) {
+        // ---- epilogue: drain each virtual row's block, store the real rows, zero it
+        const int row = warp * 32 + lane;
+        uint32_t V = 0;
+        bool ok = true;
+        for (int it = blockIdx.x; ok && it < a.nitems; it += gridDim.x) {
+            int x0, z, yb, ny;
+            row_item(a, it, x0, z, yb, ny);
+            for (int j = 0; j < ny + 2; j++) {
+                uint32_t g = V + (uint32_t)j;
+                int b = blk_of(g);
+                if (!tc::mbar_wait(bars + 8 * (BRDY + b), (g / NBLK) & 1u, abort_)) { fail(abort_, a.err, 3); ok = false; break; }
+                tc::fence_after();
+                uint32_t taddr = tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * a.cout);
+                if (j >= 1 && j <= ny) {
+                    int gx = x0 + row;
+                    size_t vox = ((size_t)z * a.Y + (yb + j - 1)) * a.X + gx;
+                    epilogue(a.epi, taddr, vox, gx < a.X);
+                }
+                for (int ch = 0; ch < (a.cout >> 4); ch++) tmem_st16_zero(taddr + (uint32_t)ch * 16u);
+                tmem_wait_st();
+                tc::fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(bars + 8 * (BFREE + b));
+            }
+            V += (uint32_t)(ny + 2);
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 8) tc::tmem_dealloc(tbase, ncols);
 }
 
 // ---- weight gradient --------------------------------------------------------------
@@ -396,6 +684,9 @@ __global__ void __launch_bounds__(192) k_wgrad(const __grid_constant__ CUtensorM
 // into TMEM, the result compared with an exact FP32 product (all values are
 // small multiples of 1/4, so every sum is exact).  Shared memory is sized so
 // that every read stays inside it even if the LBO and SBO fields are swapped.
+// swap = 2 issues no MMA: the completion wait then runs out after its time
+// limit, which is how the bounded waits are tested (result: 1000000 + the
+// wrong values of the untouched accumulator).
 constexpr int ST_M = 128, ST_N = 64, ST_K = 32, ST_SMEM = 128 * 1024;
 
 __device__ __forceinline__ float st_a(int m, int k) { return (float)(((m * 3 + k * 7) % 9) - 4) * 0.25f; }
@@ -439,7 +730,7 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigne
     __syncthreads();
     tc::fence_after();
     const uint32_t tbase = tslot;
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && swap != 2) {
         // (K-group stride, M/N-group stride) of the layouts written above
         uint32_t a_k = mn ? 128u : ST_M * 16u, a_m = mn ? ST_K * 16u : 128u;
         uint32_t b_k = mn ? 128u : ST_N * 16u, b_n = mn ? ST_K * 16u : 128u;
@@ -475,10 +766,23 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigne
 }
 
 // ---- weight packing ------------------------------------------------------------------
-// fwd:  wf[((kci*27 + tap)*(kc/8) + kg)*cout + n][e] = W[tap][n][kci*kc + kg*8 + e]
-// bwd:  wd[((kci*27 + tap)*(kcb/8) + kg)*cin + n][e] = W[26 - tap][kci*kcb + kg*8 + e][n]
-__global__ void k_pack(const float *__restrict__ W, int cin, int cout, int kcf, int kcb, bf16 *__restrict__ wf,
-                       bf16 *__restrict__ wd)
+// Standard layout (TMA kernel), per (channel chunk, tap) the B operand
+// [kc/8][N][8]:
+//   fwd: wf[((kci*27 + tap)*(kc/8) + kg)*cout + n][e] = W[tap][n][kci*kc + kg*8 + e]
+//   bwd: wd[((kci*27 + tap)*(kcb/8) + kg)*cin + n][e] = W[26 - tap][kci*kcb + kg*8 + e][n]
+// Stacked layout (row kernel, one chunk): per (dz, dx) the three dy taps side
+// by side along N, [cin/8][3][N][8]:
+//   ws[(((dz*3 + dx)*(kc/8) + kg)*3 + dy)*N + n][e]
+__device__ __forceinline__ long long pack_index(int stacked, int kc, int nout, int tap, int n, int k)
+{
+    int kci = k / kc, r = k % kc, kg = r >> 3, e = r & 7;
+    if (!stacked) return ((((long long)kci * 27 + tap) * (kc >> 3) + kg) * nout + n) * 8 + e;
+    int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
+    return (((((long long)(dz * 3 + dx)) * (kc >> 3) + kg) * 3 + dy) * nout + n) * 8 + e;
+}
+
+__global__ void k_pack(const float *__restrict__ W, int cin, int cout, int kcf, int kcb, int stf, int stb,
+                       bf16 *__restrict__ wf, bf16 *__restrict__ wd)
 {
     long long n = 27LL * cin * cout;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
@@ -487,16 +791,8 @@ __global__ void k_pack(const float *__restrict__ W, int cin, int cout, int kcf, 
         long long t = idx / cin;
         int co = (int)(t % cout), tap = (int)(t / cout);
         bf16 w = __float2bfloat16_rn(W[idx]);
-        {
-            int kci = ci / kcf, r = ci % kcf, kg = r >> 3, e = r & 7;
-            long long o = ((((long long)kci * 27 + tap) * (kcf >> 3) + kg) * cout + co) * 8 + e;
-            wf[o] = w;
-        }
-        {
-            int kci = co / kcb, r = co % kcb, kg = r >> 3, e = r & 7;
-            long long o = ((((long long)kci * 27 + (26 - tap)) * (kcb >> 3) + kg) * cin + ci) * 8 + e;
-            wd[o] = w;
-        }
+        wf[pack_index(stf, kcf, cout, tap, co, ci)] = w;
+        wd[pack_index(stb, kcb, cin, 26 - tap, ci, co)] = w;
     }
 }
 
@@ -567,12 +863,17 @@ int launch_error(const char *what)
     return 1;
 }
 
-int blocks_per_sm(const void *fn, int threads, uint32_t smem)
+// resident CTAs per SM allowed by shared memory (228 KB per SM, 1 KB reserved
+// per CTA) and TMEM (512 columns), at most 4
+int ctas_per_sm(uint32_t smem, int ncols)
 {
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) n = 1;
+    int n = (int)((228u * 1024u) / (smem + 1024u + 512u));
+    int t = 512 / ncols;
+    if (n > t) n = t;
+    if (n > 4) n = 4;
     return n < 1 ? 1 : n;
 }
+
 
 }  // namespace
 
@@ -582,6 +883,7 @@ ConvPlan conv_plan(int X, int Y, int Z, int cin, int cout)
 {
     ConvPlan p{};
     p.slab = X >= 128;
+    p.rows = X >= 128 && cin <= 32 && 27u * cin * cout * 2u <= 65536u;
     p.kc = cin < (p.slab ? 32 : 64) ? cin : (p.slab ? 32 : 64);
     p.nkc = cin / p.kc;
     if (p.slab) { p.bx = 128; p.by = 1; p.bz = 1; }
@@ -609,11 +911,12 @@ ConvPlan conv_plan(int X, int Y, int Z, int cin, int cout)
     return p;
 }
 
-void conv_pack_weights(cudaStream_t s, const float *W, int cin, int cout, int kc_fwd, int kc_bwd, bf16 *wf, bf16 *wd)
+void conv_pack_weights(cudaStream_t s, const float *W, int cin, int cout, const ConvPlan &pf, const ConvPlan &pb,
+                       bf16 *wf, bf16 *wd)
 {
     long long n = 27LL * cin * cout;
     int nb = (int)((n + 255) / 256);
-    k_pack<<<nb < 2048 ? nb : 2048, 256, 0, s>>>(W, cin, cout, kc_fwd, kc_bwd, wf, wd);
+    k_pack<<<nb < 2048 ? nb : 2048, 256, 0, s>>>(W, cin, cout, pf.kc, pb.kc, pf.rows, pb.rows, wf, wd);
 }
 
 int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int cout, const bf16 *wpk,
@@ -633,11 +936,34 @@ int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int 
     a.a_lbo = p.a_lbo; a.wpk = wpk;
     a.bias = e.bias; a.relu = e.relu; a.skip = e.skip; a.mask = e.mask; a.out = e.out;
     a.headw = e.headw; a.headb = e.headb; a.hout = e.hout; a.err = err;
+    if (p.rows) {
+        RowArgs r{};
+        r.X = X; r.Y = Y; r.Z = Z; r.cin = cin; r.cout = cout;
+        r.ntx = (X + 127) / 128;
+        r.lbo = 3u * RING * RW * 16u;
+        r.slab_bytes = (uint32_t)(cin / 8) * r.lbo;
+        r.wbytes = p.wbytes;
+        r.in = in; r.wpk = wpk;
+        r.epi = EpiP{e.bias, e.relu, e.skip, e.mask, e.out, e.headw, e.headb, e.hout, cout, (size_t)X * Y * Z};
+        r.err = err;
+        uint32_t smem = ((r.slab_bytes + 1023u) & ~1023u) + ((r.wbytes + 1023u) & ~1023u) + 1024u;
+        static int rlim = dyn_smem_limit((const void *)k_conv_rows);
+        if ((int)smem > rlim) { snprintf(g_conv_err, sizeof(g_conv_err), "conv rows needs %u B of shared memory", smem); return 1; }
+        int bps = ctas_per_sm(smem, (int)rows_ncols(cout));
+        int grid = nsm * bps;
+        // rows per item: up to 32, fewer when that leaves CTAs without two items
+        long long rows = (long long)r.ntx * Z * Y;
+        r.ych = 32;
+        while (r.ych > 4 && rows / r.ych < 2LL * grid) r.ych >>= 1;
+        r.nyc = (Y + r.ych - 1) / r.ych;
+        r.nitems = r.ntx * Z * r.nyc;
+        if (grid > r.nitems) grid = r.nitems;
+        k_conv_rows<<<grid, 288, smem, s>>>(r);
+        return launch_error("k_conv_rows");
+    }
     static int lim = dyn_smem_limit((const void *)k_conv);
     if ((int)p.smem > lim) { snprintf(g_conv_err, sizeof(g_conv_err), "conv needs %u B of shared memory", p.smem); return 1; }
-    int bps = blocks_per_sm((const void *)k_conv, 192, p.smem);
-    int tm = 512 / p.ncols;
-    if (bps > tm) bps = tm;
+    int bps = ctas_per_sm(p.smem, p.ncols);
     int grid = nsm * bps;
     if (grid > p.ntiles) grid = p.ntiles;
     k_conv<<<grid, 192, p.smem, s>>>(map, a);

@@ -269,6 +269,32 @@ __global__ void k_prep(long long n, const double *__restrict__ r1, const double 
     }
 }
 
+// snapshot target: out* = (p - base) / (invd * s), s = |r1|_rms
+__global__ void k_target(long long n, const double *__restrict__ p, const double *__restrict__ base,
+                         const double *__restrict__ invd, const double *__restrict__ sc, float *__restrict__ t)
+{
+    double rs = sqrt(sc[0] / (double)n), ir = rs > 0.0 ? 1.0 / rs : 0.0;
+    GRID_STRIDE(v, n) t[v] = (float)((p[v] - base[v]) / invd[v] * ir);
+}
+
+// energy-norm loss: x = invd * (t - h); the S-products come from k_apply
+__global__ void k_energy_in(long long n, const float *__restrict__ h, const float *__restrict__ t,
+                            const double *__restrict__ invd, double *__restrict__ x)
+{
+    GRID_STRIDE(v, n) x[v] = invd[v] * ((double)t[v] - (double)h[v]);
+}
+// gout += -2 w / e0 * invd * q
+__global__ void k_grad_add(long long n, double w, const double *__restrict__ e0, const double *__restrict__ q,
+                           const double *__restrict__ invd, float *__restrict__ gout)
+{
+    double f = *e0 > 0.0 ? -2.0 * w / *e0 : 0.0;
+    GRID_STRIDE(v, n) gout[v] += (float)(f * invd[v] * q[v]);
+}
+__global__ void k_t64(long long n, const float *__restrict__ t, const double *__restrict__ invd, double *__restrict__ x)
+{
+    GRID_STRIDE(v, n) x[v] = invd[v] * (double)t[v];
+}
+
 // out = base + s * invd * h
 __global__ void k_post(long long n, const double *__restrict__ base, const double *__restrict__ invd,
                        const float *__restrict__ h, const double *__restrict__ sc, double *__restrict__ out)
@@ -286,6 +312,10 @@ __global__ void k_loss_in(long long n, const float *__restrict__ h, const double
         x[v] = (double)h[v] * invd[v];
         r[v] = (double)in3[v];
     }
+}
+__global__ void k_scale_f(long long n, float f, float *__restrict__ a)
+{
+    GRID_STRIDE(v, n) a[v] *= f;
 }
 __global__ void k_loss_grad(long long n, const double *__restrict__ q, const double *__restrict__ invd,
                             float *__restrict__ gout)
@@ -321,10 +351,10 @@ struct TurbNet {
     int X[4], Y[4], Z[4];
     long long V[4];
     long long nparam = 0, woff[NL], boff[NL], hw_off, hb_off;
-    int kcf[NL], kcb[NL];
     bf16 *wf[NL], *wd[NL];
     float *P = nullptr, *G = nullptr, *M = nullptr, *Vv = nullptr;
     long long adam_t = 0;
+    double wr = 1.0, we = 0.0;   // training loss weights: residual form, energy form
     bf16 *x0, *a0, *p0, *a1, *p1, *a2, *p2, *a3, *b3, *c2, *s2, *b2, *c1, *s1, *b1, *c0, *s0, *b0;
     bf16 *dz0b, *dzs0, *dc0, *dz1b, *dzs1, *dc1, *dz2b, *dzs2, *dc2, *dz3b, *dz3, *dp2, *dz2, *dp1, *dz1, *dp0, *dz0;
     float *in3 = nullptr, *hout = nullptr, *gout = nullptr;
@@ -349,11 +379,16 @@ struct TurbNet {
     }
 };
 
+// snapshot k: data[k][c][cell], channels 0-2 the network inputs, channel 3
+// the target out* = (p_converged - p_previous) diag(S) / s of that solve
+constexpr int SNAP_CH = 4;
 struct TurbSnaps {
     int nx, ny, nz, cap, n = 0;
+    int pending = -1;              // snapshot waiting for its solve's converged pressure
     long long V;
     float *data = nullptr;
-    double *sc = nullptr, *part = nullptr;
+    double *sc = nullptr, *part = nullptr, *base = nullptr, *x64 = nullptr, *q64 = nullptr;
+    double *e0 = nullptr;          // per snapshot: energy norm of its target, t^T invd S invd t
     long long nparts = 0;
 };
 
@@ -393,8 +428,13 @@ G3 g3(const TurbNet *n, int l) { return G3{n->X[l], n->Y[l], n->Z[l]}; }
 
 void pack_all(TurbNet *n, cudaStream_t s)
 {
-    for (int l = 0; l < NL; l++)
-        conv_pack_weights(s, n->P + n->woff[l], DEFS[l].cin, DEFS[l].cout, n->kcf[l], n->kcb[l], n->wf[l], n->wd[l]);
+    for (int l = 0; l < NL; l++) {
+        const LayerDef &d = DEFS[l];
+        int lv = d.lev;
+        ConvPlan pf = conv_plan(n->X[lv], n->Y[lv], n->Z[lv], d.cin, d.cout);
+        ConvPlan pb = conv_plan(n->X[lv], n->Y[lv], n->Z[lv], d.cout, d.cin);
+        conv_pack_weights(s, n->P + n->woff[l], d.cin, d.cout, pf, pb, n->wf[l], n->wd[l]);
+    }
 }
 
 #define NCHK(x)                          \
@@ -525,17 +565,27 @@ void input_norms(cudaStream_t s, long long n, const double *r1, const double *bw
     for (int k = 0; k < 3; k++) pcg_reduce(s, part + k * NSUM, 1, sc + k, NSUM);
 }
 
-// loss of the current forward output against snapshot inputs in3; gradient into n->gout when want_grad
-int loss(TurbNet *n, cudaStream_t s, const MgDevLevel &L0, const double *invd, const float *in3, int want_grad)
+// losses of the current forward output against snapshot `snap` (inputs and
+// target): sc[2] = |r1n - S invd h|^2 (residual form), sc[3] = e^T S e with
+// e = invd (t - h) (energy form, CG's own error norm); both are divided by
+// the cell count on the host.  gout = d(wr * L_R + we * L_E) / dh.
+int loss(TurbNet *n, cudaStream_t s, const MgDevLevel &L0, const double *invd, const float *snap, const double *e0,
+         int want_grad)
 {
     long long V = n->V[0];
-    k_loss_in<<<nblk(V), 256, 0, s>>>(V, n->hout, invd, in3, n->x64, n->r64);
+    int np = pcg_stencil_parts(L0);
+    k_loss_in<<<nblk(V), 256, 0, s>>>(V, n->hout, invd, snap, n->x64, n->r64);
     pcg_resid(s, L0, n->r64, n->x64, n->rr, n->part);
-    pcg_reduce(s, n->part, 1, n->sc + 2, pcg_stencil_parts(L0));
+    pcg_reduce(s, n->part, 1, n->sc + 2, np);
     if (want_grad) {
         pcg_apply(s, L0, n->rr, n->q64, n->part);
         k_loss_grad<<<nblk(V), 256, 0, s>>>(V, n->q64, invd, n->gout);
+        if (n->wr != 1.0) k_scale_f<<<nblk(V), 256, 0, s>>>(V, (float)n->wr, n->gout);
     }
+    k_energy_in<<<nblk(V), 256, 0, s>>>(V, n->hout, snap + 3 * V, invd, n->x64);
+    pcg_apply(s, L0, n->x64, n->q64, n->part);
+    pcg_reduce(s, n->part, 1, n->sc + 3, np);
+    if (want_grad && n->we != 0.0) k_grad_add<<<nblk(V), 256, 0, s>>>(V, n->we, e0, n->q64, invd, n->gout);
     return cudaGetLastError() == cudaSuccess ? TURB_OK : TURB_ERR_CUDA;
 }
 
@@ -572,15 +622,38 @@ int net_guess(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *i
 }
 
 int net_snapshot(TurbSnaps *sn, cudaStream_t st, const MgDevLevel &L0, const double *invd, const double *r1,
-                 const double *bw, const double *p1, const double *p2)
+                 const double *bw, const double *p1, const double *p2, const double *base)
 {
     if (!sn || L0.nx != sn->nx || L0.ny != sn->ny || L0.nz != sn->nz) return TURB_ERR_ARG;
     if (sn->n >= sn->cap) return TURB_OK;   // store full: later solves are not recorded
     if (ensure_parts(&sn->part, &sn->nparts, L0)) return TURB_ERR_ALLOC;
     long long V = sn->V;
     input_norms(st, V, r1, bw, p1, p2, sn->part, sn->sc);
-    k_prep<<<nblk(V), 256, 0, st>>>(V, r1, bw, p1, p2, sn->sc, sn->data + (long long)sn->n * 3 * V);
+    k_prep<<<nblk(V), 256, 0, st>>>(V, r1, bw, p1, p2, sn->sc, sn->data + (long long)sn->n * SNAP_CH * V);
+    cudaMemcpyAsync(sn->base, base, (size_t)V * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    sn->pending = sn->n;
     sn->n++;
+    return cudaGetLastError() == cudaSuccess ? TURB_OK : TURB_ERR_CUDA;
+}
+
+int net_snapshot_finish(TurbSnaps *sn, cudaStream_t st, const MgDevLevel &L0, const double *invd, const double *p,
+                        int converged)
+{
+    if (!sn || sn->pending < 0) return TURB_OK;
+    int k = sn->pending;
+    sn->pending = -1;
+    if (!converged) {   // keep only snapshots whose solve reached the tolerance
+        if (k == sn->n - 1) sn->n--;
+        return TURB_OK;
+    }
+    long long V = sn->V;
+    if (!sn->x64 && (cudaMalloc(&sn->x64, (size_t)V * 8) != cudaSuccess || cudaMalloc(&sn->q64, (size_t)V * 8) != cudaSuccess))
+        return TURB_ERR_ALLOC;
+    float *t = sn->data + (long long)k * SNAP_CH * V + 3 * V;
+    k_target<<<nblk(V), 256, 0, st>>>(V, p, sn->base, invd, sn->sc, t);
+    k_t64<<<nblk(V), 256, 0, st>>>(V, t, invd, sn->x64);
+    pcg_apply(st, L0, sn->x64, sn->q64, sn->part);
+    pcg_reduce(st, sn->part, 1, sn->e0 + k, pcg_stencil_parts(L0));
     return cudaGetLastError() == cudaSuccess ? TURB_OK : TURB_ERR_CUDA;
 }
 
@@ -590,25 +663,30 @@ int net_train(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *i
     if (!n || !sn || !n->train || !same_grid(n, L0) || sn->n < 1 || steps < 1) return TURB_ERR_ARG;
     if (ensure_parts(&n->part, &n->nparts, L0)) return TURB_ERR_ALLOC;
     Rng rng{seed};
-    std::vector<double> hl((size_t)steps);
     double *hbuf = nullptr;
-    if (cudaMallocHost(&hbuf, (size_t)steps * sizeof(double)) != cudaSuccess) return TURB_ERR_ALLOC;
+    if (cudaMallocHost(&hbuf, (size_t)steps * 3 * sizeof(double)) != cudaSuccess) return TURB_ERR_ALLOC;
     long long V = n->V[0];
     int rc = TURB_OK;
     for (int k = 0; k < steps && rc == TURB_OK; k++) {
         int idx = (int)(rng.next() % (unsigned long long)sn->n);
-        const float *in3 = sn->data + (long long)idx * 3 * V;
-        rc = forward(n, st, in3, n->hout);
-        if (rc == TURB_OK) rc = loss(n, st, L0, invd, in3, 1);
+        const float *snap = sn->data + (long long)idx * SNAP_CH * V;
+        rc = forward(n, st, snap, n->hout);
+        if (rc == TURB_OK) rc = loss(n, st, L0, invd, snap, sn->e0 + idx, 1);
         if (rc == TURB_OK) rc = backward(n, st, n->gout);
         if (rc == TURB_OK) adam(n, st, lr);
-        if (rc == TURB_OK && cudaMemcpyAsync(hbuf + k, n->sc + 2, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        if (rc == TURB_OK && (cudaMemcpyAsync(hbuf + 3 * k, n->sc + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                                  cudaSuccess ||
+                              cudaMemcpyAsync(hbuf + 3 * k + 2, sn->e0 + idx, sizeof(double), cudaMemcpyDeviceToHost,
+                                              st) != cudaSuccess))
             rc = TURB_ERR_CUDA;
     }
     if (rc == TURB_OK) rc = read_err(n, st);
     if (rc == TURB_OK && mean_loss) {
         double acc = 0.0;
-        for (int k = 0; k < steps; k++) acc += hbuf[k] / (double)V;
+        for (int k = 0; k < steps; k++) {
+            double lr_ = hbuf[3 * k] / (double)V, le = hbuf[3 * k + 2] > 0.0 ? hbuf[3 * k + 1] / hbuf[3 * k + 2] : 0.0;
+            acc += n->wr * lr_ + n->we * le;
+        }
         *mean_loss = acc / steps;
     }
     cudaFreeHost(hbuf);
@@ -616,26 +694,39 @@ int net_train(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *i
 }
 
 int net_eval(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *invd, TurbSnaps *sn, int first,
-             int count, double *mean_loss)
+             int count, double *mean_res, double *mean_energy)
 {
     if (!n || !sn || !same_grid(n, L0) || first < 0 || count < 1 || first + count > sn->n) return TURB_ERR_ARG;
     if (ensure_parts(&n->part, &n->nparts, L0)) return TURB_ERR_ALLOC;
+    if (!n->x64) {   // inference nets get the loss buffers on first use
+        n->x64 = n->alloc<double>(n->V[0]); n->r64 = n->alloc<double>(n->V[0]);
+        n->rr = n->alloc<double>(n->V[0]); n->q64 = n->alloc<double>(n->V[0]);
+        if (n->aerr != cudaSuccess) return TURB_ERR_ALLOC;
+    }
     double *hbuf = nullptr;
-    if (cudaMallocHost(&hbuf, (size_t)count * sizeof(double)) != cudaSuccess) return TURB_ERR_ALLOC;
+    if (cudaMallocHost(&hbuf, (size_t)count * 3 * sizeof(double)) != cudaSuccess) return TURB_ERR_ALLOC;
     long long V = n->V[0];
     int rc = TURB_OK;
     for (int k = 0; k < count && rc == TURB_OK; k++) {
-        const float *in3 = sn->data + (long long)(first + k) * 3 * V;
-        rc = forward(n, st, in3, n->hout);
-        if (rc == TURB_OK) rc = loss(n, st, L0, invd, in3, 0);
-        if (rc == TURB_OK && cudaMemcpyAsync(hbuf + k, n->sc + 2, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        int idx = first + k;
+        const float *snap = sn->data + (long long)idx * SNAP_CH * V;
+        rc = forward(n, st, snap, n->hout);
+        if (rc == TURB_OK) rc = loss(n, st, L0, invd, snap, sn->e0 + idx, 0);
+        if (rc == TURB_OK && (cudaMemcpyAsync(hbuf + 3 * k, n->sc + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                                  cudaSuccess ||
+                              cudaMemcpyAsync(hbuf + 3 * k + 2, sn->e0 + idx, sizeof(double), cudaMemcpyDeviceToHost,
+                                              st) != cudaSuccess))
             rc = TURB_ERR_CUDA;
     }
     if (rc == TURB_OK) rc = read_err(n, st);
-    if (rc == TURB_OK && mean_loss) {
-        double acc = 0.0;
-        for (int k = 0; k < count; k++) acc += hbuf[k] / (double)V;
-        *mean_loss = acc / count;
+    if (rc == TURB_OK) {
+        double ar = 0.0, ae = 0.0;
+        for (int k = 0; k < count; k++) {
+            ar += hbuf[3 * k] / (double)V;
+            ae += hbuf[3 * k + 2] > 0.0 ? hbuf[3 * k + 1] / hbuf[3 * k + 2] : 0.0;
+        }
+        if (mean_res) *mean_res = ar / count;
+        if (mean_energy) *mean_energy = ae / count;
     }
     cudaFreeHost(hbuf);
     return rc;
@@ -665,8 +756,6 @@ int turb_net_create(int nx, int ny, int nz, int train, turb_net **out)
         n->woff[l] = off; off += 27LL * d.cin * d.cout;
         n->boff[l] = off; off += d.cout;
         int lv = d.lev;
-        n->kcf[l] = conv_plan(n->X[lv], n->Y[lv], n->Z[lv], d.cin, d.cout).kc;
-        n->kcb[l] = conv_plan(n->X[lv], n->Y[lv], n->Z[lv], d.cout, d.cin).kc;
         n->wf[l] = n->alloc<bf16>(27LL * d.cin * d.cout);
         n->wd[l] = n->alloc<bf16>(27LL * d.cin * d.cout);
     }
@@ -780,6 +869,15 @@ int turb_net_backward(turb_net *h, const float *gout, void *stream)
     return read_err(n, s);
 }
 
+int turb_net_set_loss(turb_net *h, double w_residual, double w_energy)
+{
+    TurbNet *n = reinterpret_cast<TurbNet *>(h);
+    if (!n || !(w_residual >= 0.0) || !(w_energy >= 0.0) || w_residual + w_energy <= 0.0) return TURB_ERR_ARG;
+    n->wr = w_residual;
+    n->we = w_energy;
+    return TURB_OK;
+}
+
 int turb_net_adam(turb_net *h, float lr, void *stream)
 {
     TurbNet *n = reinterpret_cast<TurbNet *>(h);
@@ -811,8 +909,10 @@ int turb_snaps_create(int nx, int ny, int nz, int capacity, turb_snaps **out)
     TurbSnaps *s = new TurbSnaps();
     s->nx = nx; s->ny = ny; s->nz = nz; s->cap = capacity;
     s->V = (long long)nx * ny * nz;
-    if (cudaMalloc(&s->data, (size_t)capacity * 3 * s->V * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&s->sc, 8 * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&s->data, (size_t)capacity * SNAP_CH * s->V * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&s->sc, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&s->base, (size_t)s->V * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&s->e0, (size_t)capacity * sizeof(double)) != cudaSuccess) {
         if (s->data) cudaFree(s->data);
         delete s;
         return TURB_ERR_ALLOC;
@@ -828,6 +928,10 @@ int turb_snaps_destroy(turb_snaps *h)
     cudaDeviceSynchronize();
     cudaFree(s->data);
     cudaFree(s->sc);
+    cudaFree(s->base);
+    cudaFree(s->e0);
+    if (s->x64) cudaFree(s->x64);
+    if (s->q64) cudaFree(s->q64);
     if (s->part) cudaFree(s->part);
     delete s;
     return TURB_OK;
@@ -843,7 +947,7 @@ int turb_snaps_data(turb_snaps *h, int index, const float **dev_ptr)
 {
     TurbSnaps *s = reinterpret_cast<TurbSnaps *>(h);
     if (!s || !dev_ptr || index < 0 || index >= s->n) return TURB_ERR_ARG;
-    *dev_ptr = s->data + (long long)index * 3 * s->V;
+    *dev_ptr = s->data + (long long)index * SNAP_CH * s->V;
     return TURB_OK;
 }
 
@@ -856,7 +960,7 @@ int turb_conv3_test(int X, int Y, int Z, int cin, int cout, const void *in, cons
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    int kcf = conv_plan(X, Y, Z, cin, cout).kc, kcb = conv_plan(X, Y, Z, cout, cin).kc;
+    ConvPlan pf = conv_plan(X, Y, Z, cin, cout), pb = conv_plan(X, Y, Z, cout, cin);
     bf16 *wf = nullptr, *wd = nullptr;
     int *err = nullptr;
     size_t nw = 27ull * cin * cout;
@@ -866,7 +970,7 @@ int turb_conv3_test(int X, int Y, int Z, int cin, int cout, const void *in, cons
         return TURB_ERR_ALLOC;
     }
     cudaMemsetAsync(err, 0, sizeof(int), s);
-    conv_pack_weights(s, W, cin, cout, kcf, kcb, wf, wd);
+    conv_pack_weights(s, W, cin, cout, pf, pb, wf, wd);
     ConvEpi e;
     e.bias = dgrad_mode ? nullptr : bias;
     e.relu = relu;

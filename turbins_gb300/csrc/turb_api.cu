@@ -1001,11 +1001,12 @@ int turb_net_train(turb_net *net, turb_ctx *c, turb_snaps *snaps, int steps, flo
                      reinterpret_cast<TurbSnaps *>(snaps), steps, lr, seed, mean_loss);
 }
 
-int turb_net_eval(turb_net *net, turb_ctx *c, turb_snaps *snaps, int first, int count, double *mean_loss)
+int turb_net_eval(turb_net *net, turb_ctx *c, turb_snaps *snaps, int first, int count, double *mean_residual,
+                  double *mean_energy)
 {
     if (!c || !net || !snaps) return TURB_ERR_ARG;
     return net_eval(reinterpret_cast<TurbNet *>(net), c->s, c->H64.lev[0], c->H64.invd[0],
-                    reinterpret_cast<TurbSnaps *>(snaps), first, count, mean_loss);
+                    reinterpret_cast<TurbSnaps *>(snaps), first, count, mean_residual, mean_energy);
 }
 
 int turb_pressure_guess_ratio(turb_ctx *c, double *geo_mean)
@@ -1372,7 +1373,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     // lowers the initial residual below the previous-solution guess
     int st = c->stage & 1;
     if (c->snaps && c->nh[st] >= 2) {
-        int rc = net_snapshot(c->snaps, s, L0, c->H64.invd[0], c->pr, c->pbw, c->ph[st][0], c->ph[st][1]);
+        int rc = net_snapshot(c->snaps, s, L0, c->H64.invd[0], c->pr, c->pbw, c->ph[st][0], c->ph[st][1], c->px);
         if (rc) return rc;
         c->launches += 5;
     }
@@ -1478,6 +1479,10 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     }
     pcg_scatter(s, d, L0, c->px, c->fld[TURB_F_PHI]);
     c->launches += 1;
+    if (c->snaps) {
+        int rc = net_snapshot_finish(c->snaps, s, L0, c->H64.invd[0], c->px, status == TURB_OK);
+        if (rc) return rc;
+    }
     if (status == TURB_OK && (c->guess_mode != TURB_GUESS_PREVIOUS || c->snaps)) {
         if (!c->ph[st][0]) {
             c->ph[st][0] = c->mem.alloc<double>(n0);

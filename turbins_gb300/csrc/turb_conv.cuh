@@ -17,6 +17,7 @@ typedef __nv_bfloat16 bf16;
 // how one convolution on one grid is tiled
 struct ConvPlan {
     int slab;                 // 1: 128-voxel x rows, one halo slab per channel chunk
+    int rows;                 // 1: row-ring kernel (cp.async rows, resident weights)
     int kc, nkc;              // channels per K chunk, number of chunks
     int bx, by, bz, nb;       // output tile (nb = bx*by*bz <= 128 voxels)
     int ntx, nty, ntz, ntiles;
@@ -41,9 +42,10 @@ struct ConvEpi {
 };
 
 // Weight packs: W[27][cout][cin] FP32 -> the B operand of the forward
-// convolution ([chunk][tap][cin/8 in chunk][cout][8]) and of the data-gradient
-// convolution (taps mirrored, cin and cout exchanged).
-void conv_pack_weights(cudaStream_t s, const float *W, int cin, int cout, int kc_fwd, int kc_bwd, bf16 *wf, bf16 *wd);
+// convolution and of the data-gradient convolution (taps mirrored, cin and
+// cout exchanged), in the layout of the kernel each plan selects.
+void conv_pack_weights(cudaStream_t s, const float *W, int cin, int cout, const ConvPlan &pf, const ConvPlan &pb,
+                       bf16 *wf, bf16 *wd);
 
 int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int cout, const bf16 *wpk,
               const ConvEpi &e, int *err, int nsm);

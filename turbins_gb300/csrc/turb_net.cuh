@@ -21,10 +21,14 @@ int net_guess(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *i
               const double *bw, const double *p1, const double *p2, const double *base, double *out);
 // appends the network inputs of this solve to the snapshot store
 int net_snapshot(TurbSnaps *sn, cudaStream_t st, const MgDevLevel &L0, const double *invd, const double *r1,
-                 const double *bw, const double *p1, const double *p2);
+                 const double *bw, const double *p1, const double *p2, const double *base);
+// the solve of the pending snapshot ended with pressure p: store its target
+// (converged) or drop the snapshot (not converged)
+int net_snapshot_finish(TurbSnaps *sn, cudaStream_t st, const MgDevLevel &L0, const double *invd, const double *p,
+                        int converged);
 int net_dims(const TurbNet *n, int *nx, int *ny, int *nz);
 int snaps_dims(const TurbSnaps *s, int *nx, int *ny, int *nz);
 int net_train(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *invd, TurbSnaps *sn, int steps,
               float lr, unsigned long long seed, double *mean_loss);
 int net_eval(TurbNet *n, cudaStream_t st, const MgDevLevel &L0, const double *invd, TurbSnaps *sn, int first,
-             int count, double *mean_loss);
+             int count, double *mean_res, double *mean_energy);

@@ -44,12 +44,13 @@ def record(case_fn, seeds, steps, capacity=None):
     return store, ctx
 
 
-def train(store, ctx, iters=3000, lr=1e-3, seed=0, init_seed=1):
+def train(store, ctx, iters=3000, lr=1e-3, seed=0, init_seed=1, w_residual=1.0, w_energy=1.0):
     """Adam on randomly drawn snapshots (lr for 70% of the steps, lr/4 after);
     returns (net, mean loss of the last phase)."""
     nx, ny, nz = ctx.params.nx, ctx.params.ny, ctx.params.nz
     net = N.Net(nx, ny, nz, train=True)
     net.init_params(init_seed)
+    net.set_loss(w_residual, w_energy)
     n1 = int(0.7 * iters)
     net.train_on(ctx, store, n1, lr=lr, seed=seed)
     loss = net.train_on(ctx, store, iters - n1, lr=lr / 4, seed=seed + 1)
@@ -77,13 +78,15 @@ def turbidity_train_case(nx=128, ny=64, nz=64):
     return lambda seed: W.turbidity_bump_case(nx, ny, nz, seed=seed)
 
 
-def train_default(case_fn, seeds=8, steps=250, iters=3000, lr=1e-3):
+def train_default(case_fn, seeds=8, steps=250, iters=3000, lr=1e-3, w_residual=1.0, w_energy=1.0):
     t0 = time.perf_counter()
     store, ctx = record(case_fn, range(seeds), steps)
     t1 = time.perf_counter()
-    net, loss = train(store, ctx, iters=iters, lr=lr)
+    net, loss = train(store, ctx, iters=iters, lr=lr, w_residual=w_residual, w_energy=w_energy)
     t2 = time.perf_counter()
-    info = dict(snapshots=len(store), record_s=t1 - t0, train_s=t2 - t1, iters=iters, train_loss=loss)
+    res, en = net.eval_on(ctx, store, max(0, len(store) - 64), min(64, len(store)))
+    info = dict(snapshots=len(store), record_s=t1 - t0, train_s=t2 - t1, iters=iters, train_loss=loss,
+                loss_weights=[w_residual, w_energy], last64_residual=res, last64_energy=en)
     params = net.get_params()
     net.close()
     store.close()

@@ -102,10 +102,18 @@ class Net:
                                        C.byref(loss)), "turb_net_train")
         return loss.value
 
+    def set_loss(self, w_residual=1.0, w_energy=0.0):
+        """Training loss weights: relative squared initial residual and relative
+        energy-norm (A-norm) error of the corrected guess."""
+        _check(self.lib.turb_net_set_loss(self.h, C.c_double(w_residual), C.c_double(w_energy)), "turb_net_set_loss")
+
     def eval_on(self, ctx, snaps, first, count):
-        loss = C.c_double()
-        _check(self.lib.turb_net_eval(self.h, ctx.ctx, snaps.h, first, count, C.byref(loss)), "turb_net_eval")
-        return loss.value
+        """(mean relative squared residual, mean relative energy error) of the
+        candidates over snapshots first .. first+count-1."""
+        lr, le = C.c_double(), C.c_double()
+        _check(self.lib.turb_net_eval(self.h, ctx.ctx, snaps.h, first, count, C.byref(lr), C.byref(le)),
+               "turb_net_eval")
+        return lr.value, le.value
 
 
 class Snapshots:
