@@ -49,14 +49,17 @@ def parse():
     ap.add_argument("--ny", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
     ap.add_argument("--pmode", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--guess", default="previous", choices=["previous", "extrapolate", "learned"])
+    ap.add_argument("--guess", default="learned", choices=["previous", "extrapolate", "learned"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=3, help="timed steps of the plain FP64 MG-CG variant")
+    ap.add_argument("--prev-steps", type=int, default=3,
+                    help="timed steps of mixed MG-CG with the previous-pressure guess (learned runs)")
     ap.add_argument("--train-seeds", type=int, default=8, help="learned guess: training runs (one bump field each)")
     ap.add_argument("--train-steps", type=int, default=250, help="learned guess: steps per training run")
     ap.add_argument("--train-iters", type=int, default=3000, help="learned guess: Adam steps")
     ap.add_argument("--net-params", default=None, help="learned guess: .npy parameters instead of training")
+    ap.add_argument("--save-net-params", default=None, help="learned guess: write the trained parameters (.npy)")
     return ap.parse_args()
 
 
@@ -90,6 +93,14 @@ class Dist:
     def close(self):
         if self.pg:
             self.td.destroy_process_group()
+
+
+def bf16_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops)"
+    except Exception:
+        return 1900.0, "fallback"
 
 
 def hbm_peak():
@@ -253,6 +264,8 @@ def main():
             params, learned_info = LN.train_default(LN.multi_bump_train_case(*tn), seeds=a.train_seeds,
                                                     steps=a.train_steps, iters=a.train_iters)
             learned_info["train_grid"] = list(tn)
+            if a.save_net_params:
+                np.save(a.save_net_params, params)
     case = W.multi_bump_case(a.nx, a.ny, a.nz)
     g = case.grid
     nc = g.nx * g.ny * g.nz
@@ -292,6 +305,18 @@ def main():
     value = dist.world * nc * a.steps / (ms_max / 1e3) / 1e6
     divmax = max(max(s["div_max"]) for s in stats)
     assert divmax <= 1e-10, "divergence gate failed: %g" % divmax
+    # ---- mixed MG-CG with the previous-pressure guess (what the network adds) --
+    mixed_prev = None
+    if guess == api.GUESS_LEARNED and a.prev_steps > 0:
+        ctx.set_pressure_guess(api.GUESS_PREVIOUS)
+        ctx.step(dt)
+        api.event_record(ctx, 4)
+        mst = [ctx.step(dt) for _ in range(a.prev_steps)]
+        api.event_record(ctx, 5)
+        mms = dist.allmax(api.event_elapsed(ctx, 4, 5))
+        mixed_prev = {"value": dist.world * nc * a.prev_steps / (mms / 1e3) / 1e6, "ms_per_step": mms / a.prev_steps,
+                      "p_iters": [s["p_iters"] for s in mst], "steps": a.prev_steps}
+        ctx.set_pressure_guess(guess)
     # ---- plain FP64 MG-CG on the same state --------------------------------
     plain = None
     if a.plain_steps > 0:
@@ -340,6 +365,17 @@ def main():
             "frac": (ach / peak) if ach else None, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": None, "bytes_per_launch": bpl, "launches": gnl, "ms_per_launch": gms / gnl if gnl else None,
             "groups_ms": {k: v[0] for k, v in prof.items()}, "groups_launches": {k: v[1] for k, v in prof.items()}}
+    if learned_info is not None and prof["net"][1]:
+        # the network's tensor-core work: 2 * 27 * cin * cout FLOP per voxel and conv
+        # (25920 MAC per finest cell over the 11 convolutions), per guess
+        nguess = prof["net"][1] / 26.0
+        flops = 2.0 * 25920 * nc
+        net_ms = prof["net"][0] / nguess
+        learned_info.update({"guesses": nguess, "guess_ms": net_ms, "forward_tflop": flops / 1e12,
+                             "tensor_tflops": flops / (net_ms / 1e3) / 1e12,
+                             "frac_of_bf16_peak": flops / (net_ms / 1e3) / 1e12 / bf16_peak()[0],
+                             "bf16_peak_source": bf16_peak()[1],
+                             "guess_residual_ratio": ctx.pressure_guess_ratio()})
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline:
         from oracle import oracle as O
@@ -361,7 +397,7 @@ def main():
                            "l2": "inputs larger than L2: each FP64 field is %.0f MB" % (npts * 8 / 1e6),
                            "parallelism": "replicas" if dist.world > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "plain_fp64": plain, "learned": learned_info,
+                "clocks": clk, "plain_fp64": plain, "mixed_previous_guess": mixed_prev, "learned": learned_info,
                 "solver": {"p_iters": [s["p_iters"] for s in stats], "guess_tried_taken": ctx.pressure_guess_stats(),
                            "vel_iters": stats[-1]["vel_iters"],
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}

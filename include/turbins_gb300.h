@@ -145,6 +145,9 @@ int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
 /* geometric mean over the tried candidates of |r(candidate)| / |r(previous)|
  * (initial residuals; 1 when nothing was tried) */
 int turb_pressure_guess_ratio(turb_ctx *ctx, double *geo_mean);
+/* red-black Gauss-Seidel sweeps of the pressure V-cycle before / after the
+ * coarse-grid correction (default 2 / 2; 1..8) */
+int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 0 (default) uses IEEE division, 1 divides by a
@@ -303,7 +306,9 @@ int turb_net_eval(turb_net *net, turb_ctx *ctx, turb_snaps *snaps, int first, in
                   double *mean_residual, double *mean_energy);
 /* self-test of the tcgen05 operand descriptors: one 128 x 64 x 32 BF16 MMA
  * from K-major (mn_major = 0) or MN-major (1) shared-memory layouts; swap = 1
- * exchanges the LBO and SBO fields; swap = 2 issues no MMA so that the
+ * exchanges the LBO and SBO fields.  mn_major = 2: K-major 128-byte-swizzle
+ * operands (K = 64), A starting `swap` (0..7) rows into its tile (the
+ * swizzle follows absolute addresses: no descriptor base offset).  mn_major < 2, swap = 2 issues no MMA so that the
  * kernel's bounded completion wait runs out (>= 1000000 reported, the
  * context stays usable).  Returns the number of wrong results. */
 int turb_selftest_umma(int mn_major, int swap, unsigned long long *mismatches);

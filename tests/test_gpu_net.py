@@ -32,6 +32,11 @@ def test_umma_descriptor_layouts(netmod, mn):
         pytest.fail("mn_major=%d: %d wrong results (%d with LBO/SBO exchanged)" % (mn, bad, other))
 
 
+@pytest.mark.parametrize("shift", [0, 1, 2, 3, 5, 7])
+def test_umma_swizzle128_row_shift(netmod, shift):
+    assert netmod.selftest_umma(2, shift) == 0
+
+
 def test_bounded_wait_times_out_and_context_survives(netmod):
     """A completion wait that nothing satisfies gives up after its limit
     (about 1 s) with an error count instead of hanging; the next launch on the

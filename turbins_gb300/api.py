@@ -202,6 +202,9 @@ class Context:
         _check(self.lib.turb_pressure_guess_stats(self.ctx, C.byref(a), C.byref(b)), "pressure_guess_stats")
         return a.value, b.value
 
+    def set_mg_sweeps(self, npre, npost):
+        _check(self.lib.turb_set_mg_sweeps(self.ctx, npre, npost), "set_mg_sweeps")
+
     def pressure_guess_ratio(self):
         r = C.c_double()
         _check(self.lib.turb_pressure_guess_ratio(self.ctx, C.byref(r)), "pressure_guess_ratio")

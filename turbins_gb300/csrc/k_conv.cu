@@ -294,28 +294,41 @@ __global__ void __launch_bounds__(192) k_conv(const __grid_constant__ CUtensorMa
 
 // ---- row-ring convolution (grids at least 128 voxels wide, cin <= 32) ------------
 // A CTA takes items of (x tile of 128 voxels, z, a run of consecutive y rows).
-// Input rows (3 z planes x 130 voxels x cin, contiguous per channel block in
-// global memory) stream through a ring of RING slots by bulk copies, producer
-// warp L % 4 loading row L.  Every input row r feeds the three output rows
-// r+1, r, r-1 (dy = 0, 1, 2): the weights of the three dy taps are stacked
-// along N, so one MMA (M = 128 voxels, N = 3 cout, K = 16) per (dz, dx) and
-// K step covers all of them -- 9 MMAs per output row instead of 27, which
-// matters because an MMA with a small N costs the same as one with N = 96.
-// The three targets are consecutive blocks of a TMEM ring of NBLK accumulator
-// blocks (block of virtual row v = NBLK-1 - v mod NBLK, so rows r+1, r, r-1
-// are ascending; a wrap splits the MMA).  Accumulation is always on: the
-// epilogue zeroes a block after draining it.  Weights are resident.
-constexpr int RING = 6, RW = 130;   // input row slots per z plane, voxels per slab row
-constexpr int NBLK = 8;             // TMEM accumulator blocks
+// Operands use the 128-byte-swizzle K-major layout, the one the tensor core
+// fetches fastest: every shared-memory row is one voxel holding 64 K elements,
+// here the channels of its three z planes (K = dz * cin + ci, zero padded),
+// 16-byte chunk c of row p stored at chunk c ^ (p % 8).  One input y row of
+// the tile (136 voxel rows, x0 - 1 ...) is a ring slot, filled by 16-byte
+// cp.async (producer warp L % 4 loads row L).  The A operand of tap dx is the
+// slot shifted by dx rows; dz and the channels are the K steps.  Every input row r feeds the output rows r+1, r, r-1
+// (dy = 0, 1, 2): the weights of the three dy taps are stacked along N, so
+// one MMA (M = 128 voxels, N = 3 cout, K = 16) per dx and K step covers all
+// of them; the three targets are consecutive blocks of a TMEM ring of NBLK
+// accumulator blocks (block of virtual row v = NBLK-1 - v mod NBLK, so rows
+// r+1, r, r-1 are ascending; a wrap splits the MMA).  Accumulation is always
+// on: the epilogue zeroes a block after draining it.  Weights are resident.
+constexpr int RING = 4, RW = 130, RROWS = 136;   // ring slots, voxels used / stored per slot
+constexpr int NBLK = 8;                          // TMEM accumulator blocks
 
 struct RowArgs {
     int X, Y, Z, cin, cout;
     int ntx, ych, nyc, nitems;
-    uint32_t lbo, slab_bytes, wbytes;
+    int nkb;                      // 128-byte K blocks per voxel row: ceil(3 cin / 64)
+    uint32_t slot_bytes, slab_bytes, wbytes;
     const bf16 *in, *wpk;
     EpiP epi;
     int *err;
 };
+
+__host__ __device__ inline int rows_nkb(int cin) { return (3 * cin + 63) / 64; }
+// resident weights of the row kernel: per dx and K block, 3 cout rows of 128 bytes
+__host__ __device__ inline uint32_t rows_wbytes(int cin, int cout) { return 3u * (uint32_t)rows_nkb(cin) * 3u * cout * 128u; }
+// 128-byte-swizzle K-major operand at saddr (8-row groups 1024 bytes apart);
+// the swizzle follows the absolute address, so shifted starts need no offset
+__host__ __device__ inline uint64_t sw128_desc(uint32_t saddr)
+{
+    return tc::sdesc(saddr, 16, 1024) | (2ull << 61);
+}
 
 // barrier slots of k_conv_rows
 constexpr int RF = 0, RE = RING, BRDY = 2 * RING, BFREE = 2 * RING + NBLK, RWB = 2 * RING + 2 * NBLK,
@@ -368,7 +381,8 @@ __global__ void __launch_bounds__(288) k_conv_rows(RowArgs a)
     const uint32_t sW = sS + ((a.slab_bytes + 1023u) & ~1023u);  // resident stacked weights
     const uint32_t bars = tc::smem_u32(bar);
     const uint32_t ncols = rows_ncols(a.cout);
-    const int nkg = a.cin >> 3;
+    const int nkg = a.cin >> 3;           // channel blocks of 8
+    const int nreal = 3 * nkg;            // real 16-byte chunks per voxel row (3 z planes)
 
     if (threadIdx.x == 0) {
         abort_s = 0;
@@ -393,6 +407,17 @@ __global__ void __launch_bounds__(288) k_conv_rows(RowArgs a)
             for (int ch = 0; ch < (a.cout >> 4); ch++)
                 tmem_st16_zero(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * a.cout + ch * 16));
         tmem_wait_st();
+    } else if (warp < 8) {   // K padding chunks of the slab are never loaded: zero them once
+        uint8_t *g = dsm + (sS - tc::smem_u32(dsm));
+        int npad = 8 * a.nkb - nreal;
+        for (int i = threadIdx.x - 128; i < RING * RROWS * npad; i += 128) {
+            int c = nreal + i % npad, r = i / npad, p = r % RROWS, slot = r / RROWS;
+            int kb = c >> 3, cc = c & 7;
+            uint32_t off = (uint32_t)slot * a.slot_bytes + (uint32_t)kb * (RROWS * 128) + (uint32_t)p * 128u +
+                           (uint32_t)((cc ^ (p & 7)) << 4);
+            *reinterpret_cast<uint4 *>(g + off) = make_uint4(0, 0, 0, 0);
+        }
+        tc::fence_proxy_async();
     }
     tc::fence_before();
     __syncthreads();
@@ -417,42 +442,22 @@ __global__ void __launch_bounds__(288) k_conv_rows(RowArgs a)
                     ok = false;
                     break;
                 }
-                // in-range voxels of each (channel block, z plane) segment by one
-                // bulk copy; voxels outside the grid zero-filled by cp.async
+                // chunk c = dz * nkg + cb of voxel row p (x = x0 - 1 + p) comes from
+                // channel block cb of plane z + dz - 1; zero outside the grid
                 int yy = yb - 1 + j;
                 bool yok = yy >= 0 && yy < a.Y;
-                int xs = max(x0 - 1, 0), xe = min(x0 + RW - 1, a.X);
                 uint32_t fullb = bars + 8 * (RF + slot);
-                if (lane == 0) {
-                    uint32_t tx = 0;
-                    for (int zp = 0; zp < 3; zp++) {
-                        int zz = z + zp - 1;
-                        if (yok && zz >= 0 && zz < a.Z) tx += (uint32_t)(xe - xs) * 16u * (uint32_t)nkg;
-                    }
-                    if (tx) tc::mbar_add_tx(fullb, tx);
-                    for (int kg = 0; kg < nkg; kg++) {
-                        for (int zp = 0; zp < 3; zp++) {
-                            int zz = z + zp - 1;
-                            if (!(yok && zz >= 0 && zz < a.Z)) continue;
-                            const bf16 *src = a.in + ((((size_t)kg * a.Z + zz) * a.Y + yy) * a.X + xs) * 8;
-                            uint32_t dst =
-                                sS + (uint32_t)(((((kg * 3 + zp) * RING + (int)slot) * RW) + (xs - x0 + 1)) * 16);
-                            tc::bulk_load(dst, src, (uint32_t)(xe - xs) * 16u, fullb);
-                        }
-                    }
-                }
-                for (int kg = 0; kg < nkg; kg++) {
-                    for (int zp = 0; zp < 3; zp++) {
-                        int zz = z + zp - 1;
-                        bool rok = yok && zz >= 0 && zz < a.Z;
-                        uint32_t rdst = sS + (uint32_t)((((kg * 3 + zp) * RING + (int)slot) * RW) * 16);
-                        if (!rok) {
-                            for (int xx = lane; xx < RW; xx += 32) cp_async16(rdst + (uint32_t)xx * 16u, a.in, 0u);
-                        } else if (lane == 1 && xs > x0 - 1) {
-                            cp_async16(rdst, a.in, 0u);   // x = -1
-                        } else if (lane == 2 && xe < x0 + RW - 1) {
-                            for (int xx = xe - x0 + 1; xx < RW; xx++) cp_async16(rdst + (uint32_t)xx * 16u, a.in, 0u);
-                        }
+                uint32_t sbase = sS + slot * a.slot_bytes;
+                for (int c = 0; c < nreal; c++) {
+                    int dz = c / nkg, cb = c - dz * nkg, zz = z + dz - 1, kb = c >> 3, cc = c & 7;
+                    bool rok = yok && zz >= 0 && zz < a.Z;
+                    const bf16 *rsrc = a.in + ((((size_t)cb * a.Z + (rok ? zz : 0)) * a.Y + (rok ? yy : 0)) * a.X) * 8;
+                    uint32_t rdst = sbase + (uint32_t)kb * (RROWS * 128);
+                    for (int p = lane; p < RW; p += 32) {
+                        int xg = x0 - 1 + p;
+                        bool v = rok && xg >= 0 && xg < a.X;
+                        cp_async16(rdst + (uint32_t)p * 128u + (uint32_t)((cc ^ (p & 7)) << 4),
+                                   v ? rsrc + (size_t)xg * 8 : a.in, v ? 16u : 0u);
                     }
                 }
                 cp_async_commit();
@@ -467,8 +472,8 @@ __global__ void __launch_bounds__(288) k_conv_rows(RowArgs a)
     } else if (warp == 8) {
         if (lane == 0) {
             const uint32_t N3 = 3u * (uint32_t)a.cout;
-            const uint32_t b_lbo = N3 * 16u;                       // stacked B: next 8 input channels
-            const uint32_t bdz = (uint32_t)nkg * b_lbo;            // next (dz, dx) block
+            const uint32_t wreg = N3 * 128u;                        // weights of one (dx, K block)
+            const int nks = (3 * a.cin) / 16;                       // K steps of 16 per dx
             uint32_t L = 0, V = 0;
             bool ok = tc::mbar_wait(bars + 8 * RWB, 0, abort_);
             for (int it = blockIdx.x; ok && it < a.nitems; it += gridDim.x) {
@@ -491,26 +496,24 @@ __global__ void __launch_bounds__(288) k_conv_rows(RowArgs a)
                         kv[k] = row >= 0 && row < nv;
                         kb[k] = kv[k] ? blk_of(V + (uint32_t)row) : -1;
                     }
-                    for (int dz = 0; dz < 3; dz++) {
-                        for (int dx = 0; dx < 3; dx++) {
-                            uint32_t abase = sS + (uint32_t)(((dz * RING + (int)slot) * RW + dx) * 16);
-                            uint32_t bbase = sW + (uint32_t)(dz * 3 + dx) * bdz;
-                            int k = 0;
-                            while (k < 3) {
-                                if (!kv[k]) { k++; continue; }
-                                int k1 = k + 1;
-                                while (k1 < 3 && kv[k1] && kb[k1] == kb[k1 - 1] + 1) k1++;
-                                uint32_t n = (uint32_t)(k1 - k) * (uint32_t)a.cout;
-                                uint32_t idesc = tc::idesc_bf16(128, (int)n, 0, 0);
-                                uint32_t dt = tbase + (uint32_t)(kb[k] * a.cout);
-                                for (int ks = 0; ks < (nkg >> 1); ks++) {
-                                    uint64_t ad = tc::sdesc(abase + (uint32_t)ks * 2u * a.lbo, a.lbo, 128);
-                                    uint64_t bd = tc::sdesc(bbase + (uint32_t)ks * 2u * b_lbo + (uint32_t)k * a.cout * 16u,
-                                                            b_lbo, 128);
-                                    tc::mma_bf16(dt, ad, bd, idesc, 1u);
-                                }
-                                k = k1;
+                    const uint32_t sbase = sS + slot * a.slot_bytes;
+                    for (int dx = 0; dx < 3; dx++) {
+                        int k = 0;
+                        while (k < 3) {
+                            if (!kv[k]) { k++; continue; }
+                            int k1 = k + 1;
+                            while (k1 < 3 && kv[k1] && kb[k1] == kb[k1 - 1] + 1) k1++;
+                            uint32_t n = (uint32_t)(k1 - k) * (uint32_t)a.cout;
+                            uint32_t idesc = tc::idesc_bf16(128, (int)n, 0, 0);
+                            uint32_t dt = tbase + (uint32_t)(kb[k] * a.cout);
+                            for (int ks = 0; ks < nks; ks++) {
+                                uint32_t kbk = (uint32_t)(ks >> 2), kk = (uint32_t)(ks & 3);
+                                uint64_t ad = sw128_desc(sbase + kbk * (RROWS * 128) + (uint32_t)dx * 128u + kk * 32u);
+                                uint64_t bd = sw128_desc(sW + ((uint32_t)dx * (uint32_t)a.nkb + kbk) * wreg +
+                                                         (uint32_t)(k * a.cout) * 128u + kk * 32u);
+                                tc::mma_bf16(dt, ad, bd, idesc, 1u);
                             }
+                            k = k1;
                         }
                     }
                     tc::mma_commit(bars + 8 * (RE + slot));                           // input row done
@@ -692,6 +695,14 @@ constexpr int ST_M = 128, ST_N = 64, ST_K = 32, ST_SMEM = 128 * 1024;
 __device__ __forceinline__ float st_a(int m, int k) { return (float)(((m * 3 + k * 7) % 9) - 4) * 0.25f; }
 __device__ __forceinline__ float st_b(int n, int k) { return (float)(((n * 5 + k * 3) % 7) - 3) * 0.5f; }
 
+// mn = 2: both operands in the 128-byte-swizzle K-major layout (rows of 64
+// elements, 16-byte chunk c of row r stored at chunk c ^ (r % 8)), K = 64 in
+// four MMAs advancing 32 bytes; A starts `swap` (0..7) rows into a 136-row
+// tile.  The swizzle is applied to absolute shared-memory address bits, so a
+// start that is not 1024-byte aligned needs no base offset (field left 0).
+constexpr int SW_K = 64;
+__device__ __forceinline__ float sw_a(int p, int k) { return (float)(((p * 5 + k * 3) % 11) - 5) * 0.25f; }
+
 __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigned long long *bad)
 {
     extern __shared__ uint8_t dsm[];
@@ -713,13 +724,25 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigne
     }
     for (int i = threadIdx.x; i < (ST_SMEM - 1024) / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(g0)[i] = 0u;
     __syncthreads();
-    for (int i = threadIdx.x; i < ST_M * ST_K; i += blockDim.x) {
+    if (mn == 2) {
+        for (int i = threadIdx.x; i < 136 * SW_K; i += blockDim.x) {
+            int p = i / SW_K, k = i % SW_K;
+            uint32_t off = (uint32_t)(p * 128 + (((k >> 3) ^ (p & 7)) << 4) + (k & 7) * 2);
+            *reinterpret_cast<bf16 *>(g0 + off) = __float2bfloat16_rn(sw_a(p, k));
+        }
+        for (int i = threadIdx.x; i < ST_N * SW_K; i += blockDim.x) {
+            int n = i / SW_K, k = i % SW_K;
+            uint32_t off = (uint32_t)(n * 128 + (((k >> 3) ^ (n & 7)) << 4) + (k & 7) * 2);
+            *reinterpret_cast<bf16 *>(g0 + offB + off) = __float2bfloat16_rn(st_b(n, k));
+        }
+    }
+    for (int i = threadIdx.x; mn != 2 && i < ST_M * ST_K; i += blockDim.x) {
         int m = i / ST_K, k = i % ST_K;
         uint32_t off = mn ? (uint32_t)((m / 8) * (ST_K * 16) + (k / 8) * 128 + (k % 8) * 16 + (m % 8) * 2)
                           : (uint32_t)((k / 8) * (ST_M * 16) + (m / 8) * 128 + (m % 8) * 16 + (k % 8) * 2);
         *reinterpret_cast<bf16 *>(g0 + off) = __float2bfloat16_rn(st_a(m, k));
     }
-    for (int i = threadIdx.x; i < ST_N * ST_K; i += blockDim.x) {
+    for (int i = threadIdx.x; mn != 2 && i < ST_N * ST_K; i += blockDim.x) {
         int n = i / ST_K, k = i % ST_K;
         uint32_t off = mn ? (uint32_t)((n / 8) * (ST_K * 16) + (k / 8) * 128 + (k % 8) * 16 + (n % 8) * 2)
                           : (uint32_t)((k / 8) * (ST_N * 16) + (n / 8) * 128 + (n % 8) * 16 + (k % 8) * 2);
@@ -730,7 +753,17 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigne
     __syncthreads();
     tc::fence_after();
     const uint32_t tbase = tslot;
-    if (threadIdx.x == 0 && swap != 2) {
+    if (threadIdx.x == 0 && mn == 2) {
+        uint32_t idesc = tc::idesc_bf16(ST_M, ST_N, 0, 0);
+        uint32_t sh = (uint32_t)swap & 7u;
+        for (int ks = 0; ks < SW_K / 16; ks++) {
+            uint32_t aa = s0 + sh * 128u + (uint32_t)ks * 32u, bb = s0 + offB + (uint32_t)ks * 32u;
+            uint64_t ad = tc::sdesc(aa, 16, 1024) | (2ull << 61);
+            uint64_t bd = tc::sdesc(bb, 16, 1024) | (2ull << 61);
+            tc::mma_bf16(tbase, ad, bd, idesc, ks > 0);
+        }
+        tc::mma_commit(tc::smem_u32(bar));
+    } else if (threadIdx.x == 0 && swap != 2) {
         // (K-group stride, M/N-group stride) of the layouts written above
         uint32_t a_k = mn ? 128u : ST_M * 16u, a_m = mn ? ST_K * 16u : 128u;
         uint32_t b_k = mn ? 128u : ST_N * 16u, b_n = mn ? ST_K * 16u : 128u;
@@ -754,7 +787,11 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigne
         for (int j = 0; j < 16; j++) {
             int n = ch * 16 + j;
             float ref = 0.f;
-            for (int k = 0; k < ST_K; k++) ref += st_a(row, k) * st_b(n, k);
+            if (mn == 2) {
+                for (int k = 0; k < SW_K; k++) ref += sw_a(row + (swap & 7), k) * st_b(n, k);
+            } else {
+                for (int k = 0; k < ST_K; k++) ref += st_a(row, k) * st_b(n, k);
+            }
             if (__uint_as_float(rr[j]) != ref) nbad++;
         }
     }
@@ -770,15 +807,18 @@ __global__ void __launch_bounds__(128) k_umma_selftest(int mn, int swap, unsigne
 // [kc/8][N][8]:
 //   fwd: wf[((kci*27 + tap)*(kc/8) + kg)*cout + n][e] = W[tap][n][kci*kc + kg*8 + e]
 //   bwd: wd[((kci*27 + tap)*(kcb/8) + kg)*cin + n][e] = W[26 - tap][kci*kcb + kg*8 + e][n]
-// Stacked layout (row kernel, one chunk): per (dz, dx) the three dy taps side
-// by side along N, [cin/8][3][N][8]:
-//   ws[(((dz*3 + dx)*(kc/8) + kg)*3 + dy)*N + n][e]
+// Row-kernel layout (kc = cin): per (dx, 128-byte K block) the rows
+// n' = dy * N + n (three dy taps stacked along N) of 64 K elements
+// K = dz * cin + k, 128-byte swizzled: byte
+//   ((dx * nkb + K / 64) * 3N + n') * 128 + (((K % 64) / 8) ^ (n' % 8)) * 16 + (K % 8) * 2
 __device__ __forceinline__ long long pack_index(int stacked, int kc, int nout, int tap, int n, int k)
 {
     int kci = k / kc, r = k % kc, kg = r >> 3, e = r & 7;
     if (!stacked) return ((((long long)kci * 27 + tap) * (kc >> 3) + kg) * nout + n) * 8 + e;
     int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;
-    return (((((long long)(dz * 3 + dx)) * (kc >> 3) + kg) * 3 + dy) * nout + n) * 8 + e;
+    int K = dz * kc + k, kb = K >> 6, k64 = K & 63, np = dy * nout + n, nkb = rows_nkb(kc);
+    long long byte = ((long long)(dx * nkb + kb) * (3 * nout) + np) * 128 + (((k64 >> 3) ^ (np & 7)) << 4) + (k64 & 7) * 2;
+    return byte >> 1;
 }
 
 __global__ void k_pack(const float *__restrict__ W, int cin, int cout, int kcf, int kcb, int stf, int stb,
@@ -883,7 +923,7 @@ ConvPlan conv_plan(int X, int Y, int Z, int cin, int cout)
 {
     ConvPlan p{};
     p.slab = X >= 128;
-    p.rows = X >= 128 && cin <= 32 && 27u * cin * cout * 2u <= 65536u;
+    p.rows = X >= 128 && cin <= 32 && cout <= 32;
     p.kc = cin < (p.slab ? 32 : 64) ? cin : (p.slab ? 32 : 64);
     p.nkc = cin / p.kc;
     if (p.slab) { p.bx = 128; p.by = 1; p.bz = 1; }
@@ -940,9 +980,10 @@ int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int 
         RowArgs r{};
         r.X = X; r.Y = Y; r.Z = Z; r.cin = cin; r.cout = cout;
         r.ntx = (X + 127) / 128;
-        r.lbo = 3u * RING * RW * 16u;
-        r.slab_bytes = (uint32_t)(cin / 8) * r.lbo;
-        r.wbytes = p.wbytes;
+        r.nkb = rows_nkb(cin);
+        r.slot_bytes = (uint32_t)r.nkb * RROWS * 128u;
+        r.slab_bytes = RING * r.slot_bytes;
+        r.wbytes = rows_wbytes(cin, cout);
         r.in = in; r.wpk = wpk;
         r.epi = EpiP{e.bias, e.relu, e.skip, e.mask, e.out, e.headw, e.headb, e.hout, cout, (size_t)X * Y * Z};
         r.err = err;

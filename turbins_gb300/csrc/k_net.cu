@@ -756,8 +756,8 @@ int turb_net_create(int nx, int ny, int nz, int train, turb_net **out)
         n->woff[l] = off; off += 27LL * d.cin * d.cout;
         n->boff[l] = off; off += d.cout;
         int lv = d.lev;
-        n->wf[l] = n->alloc<bf16>(27LL * d.cin * d.cout);
-        n->wd[l] = n->alloc<bf16>(27LL * d.cin * d.cout);
+        n->wf[l] = n->alloc<bf16>(conv_pack_elems(d.cin, d.cout));
+        n->wd[l] = n->alloc<bf16>(conv_pack_elems(d.cout, d.cin));
     }
     n->hw_off = off; off += 16;
     n->hb_off = off; off += 1;
@@ -963,12 +963,14 @@ int turb_conv3_test(int X, int Y, int Z, int cin, int cout, const void *in, cons
     ConvPlan pf = conv_plan(X, Y, Z, cin, cout), pb = conv_plan(X, Y, Z, cout, cin);
     bf16 *wf = nullptr, *wd = nullptr;
     int *err = nullptr;
-    size_t nw = 27ull * cin * cout;
-    if (cudaMalloc(&wf, nw * 2) != cudaSuccess || cudaMalloc(&wd, nw * 2) != cudaSuccess ||
+    size_t nwf = (size_t)conv_pack_elems(cin, cout), nwd = (size_t)conv_pack_elems(cout, cin);
+    if (cudaMalloc(&wf, nwf * 2) != cudaSuccess || cudaMalloc(&wd, nwd * 2) != cudaSuccess ||
         cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
         cudaFree(wf); cudaFree(wd);
         return TURB_ERR_ALLOC;
     }
+    cudaMemsetAsync(wf, 0, nwf * 2, s);
+    cudaMemsetAsync(wd, 0, nwd * 2, s);
     cudaMemsetAsync(err, 0, sizeof(int), s);
     conv_pack_weights(s, W, cin, cout, pf, pb, wf, wd);
     ConvEpi e;

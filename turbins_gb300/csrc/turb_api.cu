@@ -115,6 +115,7 @@ struct turb_ctx {
     cudaGraphExec_t g_inner[3 + TURB_MAXCONC] = {nullptr};
     int g_inner_n[3 + TURB_MAXCONC] = {0};
     int use_graphs = 1;
+    int mg_pre = 2, mg_post = 2;   // red-black Gauss-Seidel sweeps before / after the coarse correction
     // pressure initial guess: history of the last two solutions per RK stage
     int guess_mode = TURB_GUESS_PREVIOUS;
     int stage = 0;
@@ -1031,6 +1032,18 @@ int turb_set_pressure_mode(turb_ctx *c, int mode)
     return TURB_OK;
 }
 
+int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost)
+{
+    if (!c || npre < 1 || npost < 1 || npre > 8 || npost > 8) return TURB_ERR_ARG;
+    if (npre != c->mg_pre || npost != c->mg_post) {   // the captured V-cycles change
+        for (int m = 0; m < 2; m++)
+            if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+    }
+    c->mg_pre = npre;
+    c->mg_post = npost;
+    return TURB_OK;
+}
+
 int turb_synchronize(turb_ctx *c)
 {
     if (!c) return TURB_ERR_ARG;
@@ -1413,7 +1426,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     }
     double tol = c->prm.p_rtol * nb;
     int it = 0, restart = 1, status = TURB_OK;
-    const int npre = 2, npost = 2;
+    const int npre = c->mg_pre, npost = c->mg_post;
     int vl = mg_vcycle_launches(c->H64.nl, npre, npost);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }

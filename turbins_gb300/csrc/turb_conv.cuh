@@ -47,6 +47,15 @@ struct ConvEpi {
 void conv_pack_weights(cudaStream_t s, const float *W, int cin, int cout, const ConvPlan &pf, const ConvPlan &pb,
                        bf16 *wf, bf16 *wd);
 
+// elements of a weight pack buffer for a conv of (cin, cout) on any grid
+// (the row kernel's layout pads K to 128-byte rows); buffers start zeroed
+inline long long conv_pack_elems(int cin, int cout)
+{
+    long long std = 27LL * cin * cout;
+    long long rows = 3LL * ((3 * cin + 63) / 64) * 3 * cout * 64;
+    return std > rows ? std : rows;
+}
+
 int conv3_fwd(cudaStream_t s, const bf16 *in, int X, int Y, int Z, int cin, int cout, const bf16 *wpk,
               const ConvEpi &e, int *err, int nsm);
 int conv3_wgrad(cudaStream_t s, const bf16 *x, const bf16 *dy, int X, int Y, int Z, int cin, int cout, float *dw,
