@@ -146,7 +146,8 @@ int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
  * (initial residuals; 1 when nothing was tried) */
 int turb_pressure_guess_ratio(turb_ctx *ctx, double *geo_mean);
 /* red-black Gauss-Seidel sweeps of the pressure V-cycle before / after the
- * coarse-grid correction (default 2 / 2; 1..8) */
+ * coarse-grid correction, for the current pressure mode (defaults: 4 / 4 with
+ * FP64 V-cycles, 6 / 6 with FP32 V-cycles; 1..8) */
 int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);

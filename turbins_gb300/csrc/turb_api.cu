@@ -115,7 +115,10 @@ struct turb_ctx {
     cudaGraphExec_t g_inner[3 + TURB_MAXCONC] = {nullptr};
     int g_inner_n[3 + TURB_MAXCONC] = {0};
     int use_graphs = 1;
-    int mg_pre = 2, mg_post = 2;   // red-black Gauss-Seidel sweeps before / after the coarse correction
+    // red-black Gauss-Seidel sweeps before / after the coarse correction, per
+    // pressure mode (FP64 V-cycles: 4 + 4; FP32 V-cycles are cheap enough that
+    // 6 + 6, 8 CG iterations at 512x256x256, beats fewer sweeps)
+    int mg_pre[2] = {4, 6}, mg_post[2] = {4, 6};
     // pressure initial guess: history of the last two solutions per RK stage
     int guess_mode = TURB_GUESS_PREVIOUS;
     int stage = 0;
@@ -1035,12 +1038,12 @@ int turb_set_pressure_mode(turb_ctx *c, int mode)
 int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost)
 {
     if (!c || npre < 1 || npost < 1 || npre > 8 || npost > 8) return TURB_ERR_ARG;
-    if (npre != c->mg_pre || npost != c->mg_post) {   // the captured V-cycles change
-        for (int m = 0; m < 2; m++)
-            if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+    int m = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
+    if (npre != c->mg_pre[m] || npost != c->mg_post[m]) {   // the captured V-cycle changes
+        if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
     }
-    c->mg_pre = npre;
-    c->mg_post = npost;
+    c->mg_pre[m] = npre;
+    c->mg_post[m] = npost;
     return TURB_OK;
 }
 
@@ -1426,7 +1429,8 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     }
     double tol = c->prm.p_rtol * nb;
     int it = 0, restart = 1, status = TURB_OK;
-    const int npre = c->mg_pre, npost = c->mg_post;
+    const int pmi = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
+    const int npre = c->mg_pre[pmi], npost = c->mg_post[pmi];
     int vl = mg_vcycle_launches(c->H64.nl, npre, npost);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
