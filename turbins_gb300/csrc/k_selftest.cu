@@ -34,7 +34,11 @@ __global__ void k_selftest(long long n, unsigned long long seed, unsigned long l
         double h = rnd(r2, -14, 3, false);               // spacings 6e-5 .. 16
         double y = __ddiv_rn(1.0, h);
         double a;
-        switch (r3 & 3) {
+        switch ((r3 >> 60) == 0 ? 4 + (int)((r3 >> 56) & 3) : (int)(r3 & 3)) {
+        case 4: a = ((r3 >> 1) & 1) ? -0.0 : 0.0; break;  // zero numerators keep their sign
+        case 5: a = rnd(r1, -1022, -880, true); break;    // tiny: IEEE branch and its edge
+        case 6: a = rnd(r1, 880, 1000, true); break;      // huge: IEEE branch and its edge
+        case 7: a = __longlong_as_double((long long)(r1 & 0x800FFFFFFFFFFFFFULL)); break;   // subnormal
         case 0: a = rnd(r1, -80, 80, true); break;        // generic
         case 1: a = __dmul_rn(rnd(r1, -40, 40, true), h); break;   // a/h near a double
         case 2: {                                         // a/h near a midpoint

@@ -261,7 +261,7 @@ EnoTab mk_eno(DevBuf &m, int r, const std::vector<double> &pos, int s0, int e0, 
     T.rh1 = m.upload(r1);
     T.rh2 = m.upload(r2);
     T.rh3 = m.upload(r3);
-    T.fastdiv = 0;
+    T.fastdiv = 1;   // reciprocal-based, correctly rounded (turb_div.cuh); 0 = IEEE division
     T.g2 = m.upload(g2);
     T.g3 = m.upload(g3);
     return T;

@@ -8,15 +8,20 @@
 // exact in one fused multiply-add and RN(q + r*y) is RN(a/h).  q0 = RN(a*y)
 // can be up to ~2 ulps away, so one correction brings it within an ulp and a
 // second one rounds correctly.  y comes from an IEEE division on the host.
-// Zeros (sign), and operands outside [2^-900, 2^900] (no underflow of the
-// remainder, no overflow) take the IEEE division instead.  The equality with
-// __ddiv_rn is checked on the GPU by turb_selftest_division.
+// A zero numerator returns itself (+-0 / h = +-0, h > 0); numerators with a
+// binary exponent outside [-900, 900] (no underflow of the remainder, no
+// overflow), infinities and NaNs take the IEEE division.  Both tests read the
+// exponent bits with integer instructions, so the FP64 pipe only sees the one
+// multiply and four fused multiply-adds.  The equality with __ddiv_rn is
+// checked on the GPU by turb_selftest_division.
 #pragma once
 
 __device__ __forceinline__ double div_by_spacing(double a, double h, double y)
 {
-    double aa = fabs(a);
-    if (!(aa >= 0x1p-900 && aa <= 0x1p+900)) return __ddiv_rn(a, h);
+    unsigned long long bits = (unsigned long long)__double_as_longlong(a);
+    unsigned e = (unsigned)(bits >> 52) & 0x7FFu;
+    if ((bits << 1) == 0ull) return a;
+    if (e < 123u || e > 1923u) return __ddiv_rn(a, h);
     double q = __dmul_rn(a, y);
     double r = __fma_rn(-q, h, a);
     q = __fma_rn(r, y, q);

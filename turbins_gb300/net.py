@@ -171,3 +171,37 @@ def conv3_wgrad(X, Y, Z, cin, cout, x, dy, dw):
     _check(load_library().turb_conv3_wgrad_test(X, Y, Z, cin, cout, _dev(x), _dev(dy), _dev(dw), None),
            "turb_conv3_wgrad_test")
     return dw
+
+
+def _main():
+    """Time the network forward on random inputs (3 warm-up passes, then the
+    timed ones, CUDA events):  python -m turbins_gb300.net NX NY NZ [REPS]"""
+    import json
+    import sys
+
+    import torch
+
+    nx, ny, nz = (int(v) for v in sys.argv[1:4])
+    reps = int(sys.argv[4]) if len(sys.argv) > 4 else 5
+    net = Net(nx, ny, nz, train=False)
+    net.init_params(1)
+    x = torch.randn(3, nz, ny, nx, device="cuda")
+    out = torch.zeros(nz, ny, nx, device="cuda")
+    for _ in range(3):
+        net.forward(x, out)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        net.forward(x, out)
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    flop = 2.0 * 25920 * nx * ny * nz
+    print(json.dumps({"dims": [nx, ny, nz], "forward_ms": ts, "tflops": flop / (min(ts) / 1e3) / 1e12}))
+    net.close()
+
+
+if __name__ == "__main__":
+    _main()
