@@ -220,6 +220,24 @@ class Oracle:
         self.lib.to_total_concentration(C.byref(self.cg), C.byref(self.cp), arr, _ptr(out))
         return out
 
+    def diagnostics(self, u, v, w, cs, front_limit=0.1):
+        """to_diagnostics: dict of the flow integrals and the h(x) profiles."""
+        class _Diag(C.Structure):
+            _fields_ = [("ke", C.c_double), ("rate", C.c_double), ("mass", C.c_double * MAXC),
+                        ("ep", C.c_double * MAXC), ("stokes", C.c_double * MAXC), ("rate_c", C.c_double * MAXC),
+                        ("front", C.c_double)]
+        d = _Diag()
+        arr = (_dp * MAXC)()
+        for i, c in enumerate(cs):
+            arr[i] = _ptr(c)
+        nc = self.p.nconc
+        h = np.zeros((nc, self.g.nx + 1))
+        self.lib.to_diagnostics(C.byref(self.cg), C.byref(self.cp), _ptr(u), _ptr(v), _ptr(w), arr,
+                                C.c_double(front_limit), C.byref(d), _ptr(h))
+        return dict(kinetic_energy=d.ke, conversion_rate=d.rate, suspended_mass=list(d.mass)[:nc],
+                    potential_energy=list(d.ep)[:nc], stokes_dissipation=list(d.stokes)[:nc],
+                    conversion_rate_c=list(d.rate_c)[:nc], front_location=d.front, ave_height=h)
+
     def step(self, state, dt):
         """One TVD-RK2 step in place on a dict of DA arrays."""
         n = self.p.nconc

@@ -19,6 +19,8 @@
 #include "Velocity.h"
 #include "Conc.h"
 #include "Pressure.h"
+#include "Extract.h"
+#include "Memory.h"
 #include <string.h>
 
 typedef struct {
@@ -29,6 +31,7 @@ typedef struct {
     Concentration *c[4];
     ENO_Scheme *eno;
     long n;
+    double *hbuf[8];   /* G_ / W_ave_height_x of each fraction (ref_diagnostics) */
 } ref_case;
 
 static void vset(Vec v, const double *a, long n) { memcpy(shim_vec_data(v), a, sizeof(double) * n); }
@@ -294,4 +297,53 @@ void ref_metrics(ref_case *r, double *mxc, double *myc, double *mzc, double *mxu
     MAC_grid *g = r->g;
     memcpy(mxc, g->metric_xc, 8 * g->NX); memcpy(myc, g->metric_yc, 8 * g->NY); memcpy(mzc, g->metric_zc, 8 * g->NZ);
     memcpy(mxu, g->metric_xu, 8 * g->NX); memcpy(myv, g->metric_yv, 8 * g->NY); memcpy(mzw, g->metric_zw, 8 * g->NZ);
+}
+
+/* flow diagnostics through the reference's own routines:
+ * out[0] = Extract_total_kinetic_energy, out[1] = Extract_kinetic_potential_conversion_rate,
+ * per fraction i (base 2 + 4 i): Conc_compute_total_suspended_mass, and
+ * Conc_compute_potential_energies' W_Ep, W_Stokes_dissipation_rate,
+ * W_kinetic_potential_conversion_rate (no deposit: the passive part is 0);
+ * out[2 + 4 nconc] = Conc_find_front_location(front_limit); h_ave (nconc x NX)
+ * = Conc_compute_ave_height_x. */
+void ref_diagnostics(ref_case *r, const double *u, const double *v, const double *w, const double *const *c,
+                     double front_limit, double *out, double *h_ave)
+{
+    long n = r->n;
+    int i, nc = r->p->NConc, NX = r->g->NX;
+    MAC_grid *g = r->g;
+    Parameters *p = r->p;
+    if (!g->interface_y_index) g->interface_y_index = Memory_allocate_2D_int(g->NX, g->NZ);
+    p->Ly = g->yv[g->NY - 1] - g->yv[0];
+    p->Lz = g->zw[g->NZ - 1] - g->zw[0];
+    vset(r->u->G_data, u, n); vset(r->v->G_data, v, n); vset(r->w->G_data, w, n);
+    Velocity_cell_center(r->u, r->v, r->w, g, p);
+    for (i = 0; i < nc; i++) vset(r->c[i]->G_data, c[i], n);
+    if (nc > 1) Conc_compute_total_concentration(r->c, p);
+    Extract_total_kinetic_energy(r->u, r->v, r->w, g);
+    Extract_kinetic_potential_conversion_rate(r->v, r->c, g, p);
+    out[0] = r->u->W_kinetic_energy;
+    out[1] = r->v->W_kinetic_potential_conversion_rate;
+    for (i = 0; i < nc; i++) {
+        Concentration *cc = r->c[i];
+        if (!cc->G_deposit_height) cc->G_deposit_height = Memory_allocate_2D_double(g->NX, g->NZ);
+        Conc_compute_total_suspended_mass(cc, g);
+        Conc_compute_potential_energies(cc, r->v, g, p);
+        out[2 + 4 * i] = cc->W_total_susp_mass;
+        out[3 + 4 * i] = cc->W_Ep;
+        out[4 + 4 * i] = cc->W_Stokes_dissipation_rate;
+        out[5 + 4 * i] = cc->W_kinetic_potential_conversion_rate;
+    }
+    for (i = 0; i < nc; i++) {   /* Conc_create leaves them unset without ave_height_output */
+        if (!r->hbuf[i]) {
+            r->hbuf[i] = Memory_allocate_1D_double(g->NX);
+            r->hbuf[4 + i] = Memory_allocate_1D_double(g->NX);
+        }
+        r->c[i]->G_ave_height_x = r->hbuf[i];
+        r->c[i]->W_ave_height_x = r->hbuf[4 + i];
+    }
+    Conc_compute_ave_height_x(r->c, g, p);
+    out[2 + 4 * nc] = Conc_find_front_location(r->c, g, p, front_limit);
+    if (h_ave)
+        for (i = 0; i < nc; i++) memcpy(h_ave + (long)i * NX, r->c[i]->W_ave_height_x, sizeof(double) * NX);
 }

@@ -109,6 +109,21 @@ class Reference:
         self.lib.ref_total_concentration(self.h, arr, _p(out))
         return out
 
+    def diagnostics(self, u, v, w, cs, front_limit=0.1):
+        nc = len(cs)
+        arr = (_dp * 4)()
+        for i, c in enumerate(cs):
+            arr[i] = _p(c)
+        out = np.zeros(3 + 4 * nc)
+        h = np.zeros((nc, self.g.nx + 1))
+        self.lib.ref_diagnostics(self.h, _p(u), _p(v), _p(w), arr, C.c_double(front_limit), _p(out), _p(h))
+        return dict(kinetic_energy=out[0], conversion_rate=out[1],
+                    suspended_mass=[out[2 + 4 * i] for i in range(nc)],
+                    potential_energy=[out[3 + 4 * i] for i in range(nc)],
+                    stokes_dissipation=[out[4 + 4 * i] for i in range(nc)],
+                    conversion_rate_c=[out[5 + 4 * i] for i in range(nc)],
+                    front_location=out[2 + 4 * nc], ave_height=h)
+
     def lhs_apply(self, q, ic, dt, x):
         y = self._z()
         self.lib.ref_lhs_apply(self.h, C.c_char(q.encode()), C.c_int(ic), C.c_double(dt),

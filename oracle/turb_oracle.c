@@ -1183,3 +1183,148 @@ int to_step(const to_grid *g, const to_params *p, to_state *s, double dt,
     for (ic = 0; ic < nc; ic++) free(cc[ic]);
     return 0;
 }
+
+/* ---- diagnostics ---------------------------------------------------------
+ * Cell widths dx_c, dy_c, dz_c of Grid_compute_metric_coefficients
+ * (Grid.c:633-637, 650-654, 667-671): x_{i+1} - x_i of the face coordinates,
+ * the last one repeating its neighbour. */
+static void cell_widths(const double *f, int n, double *d)
+{
+    int i;
+    for (i = 1; i < n - 1; i++) d[i] = f[i + 1] - f[i];
+    d[0] = f[1] - f[0];
+    d[n - 1] = f[n - 1] - f[n - 2];
+}
+
+void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
+                    const double *v, const double *w, const double *const *c,
+                    double front_limit, to_diag *out, double *h_ave)
+{
+    size_t n = NPTS(g);
+    int NX = g->NX, NY = g->NY, NZ = g->NZ, i, j, k, ic, nc = p->nconc;
+    double *ubc = (double *)calloc(n, sizeof(double)), *vbc = (double *)calloc(n, sizeof(double));
+    double *wbc = (double *)calloc(n, sizeof(double)), *ctot = NULL;
+    double *dxc = (double *)malloc(NX * sizeof(double)), *dyc = (double *)malloc(NY * sizeof(double));
+    double *dzc = (double *)malloc(NZ * sizeof(double)), *h = (double *)calloc((size_t)nc * NX, sizeof(double));
+    const double *ct;
+    const uint8_t *cs = g->st[3];
+    double ke = 0.0, rate = 0.0, y_ref = g->yv[0];
+    to_cell_center(g, u, v, w, ubc, vbc, wbc);
+    cell_widths(g->xu, NX, dxc);
+    cell_widths(g->yv, NY, dyc);
+    cell_widths(g->zw, NZ, dzc);
+    if (nc > 1) {
+        ctot = (double *)calloc(n, sizeof(double));
+        to_total_concentration(g, p, c, ctot);
+        ct = ctot;
+    } else {
+        ct = c[0];
+    }
+    /* Extract_total_kinetic_energy, Extract.c:803-882 */
+    for (k = 0; k < NZ; k++) {
+        double dz = dzc[k];
+        for (j = 0; j < NY; j++) {
+            double dy = dyc[j];
+            for (i = 0; i < NX; i++) {
+                size_t q = IDX(g, i, j, k);
+                if (cs[q] == TO_FLUID) {
+                    double dx = dxc[i], dV = dx * dy * dz;
+                    ke += (ubc[q] * ubc[q] + vbc[q] * vbc[q] + wbc[q] * wbc[q]) * dV;
+                }
+            }
+        }
+    }
+    out->kinetic_energy = ke * 0.5;
+    /* Extract_kinetic_potential_conversion_rate, Extract.c:727-801 */
+    for (k = 0; k < NZ; k++) {
+        double dz = dzc[k];
+        for (j = 0; j < NY; j++) {
+            double dy = dyc[j];
+            for (i = 0; i < NX; i++) {
+                size_t q = IDX(g, i, j, k);
+                if (cs[q] == TO_FLUID) {
+                    double dx = dxc[i];
+                    rate += -vbc[q] * ct[q] * (dx * dy * dz);
+                }
+            }
+        }
+    }
+    out->conversion_rate = rate;
+    for (ic = 0; ic < TO_MAXCONC; ic++) {
+        out->suspended_mass[ic] = out->potential_energy[ic] = 0.0;
+        out->stokes_dissipation[ic] = out->conversion_rate_c[ic] = 0.0;
+    }
+    for (ic = 0; ic < nc; ic++) {
+        const double *cc = c[ic];
+        double m = 0.0, ep = 0.0, st = 0.0, cr = 0.0;
+        /* Conc_compute_total_suspended_mass, Conc.c:1471-1522 */
+        for (k = 0; k < NZ; k++) {
+            double dz = dzc[k];
+            for (j = 0; j < NY; j++) {
+                double dy = dyc[j];
+                for (i = 0; i < NX; i++) {
+                    size_t q = IDX(g, i, j, k);
+                    if (cs[q] == TO_FLUID) {
+                        double dV = dz * dy * dxc[i];
+                        m += cc[q] * dV;
+                    }
+                }
+            }
+        }
+        out->suspended_mass[ic] = m;
+        /* Conc_compute_potential_energies, Conc.c:1934-2055 (suspended part) */
+        for (k = 0; k < NZ; k++) {
+            double dz = dzc[k];
+            for (j = 0; j < NY; j++) {
+                double dy = dyc[j];
+                for (i = 0; i < NX; i++) {
+                    size_t q = IDX(g, i, j, k);
+                    if (cs[q] == TO_FLUID) {
+                        double dx = dxc[i], dV = dx * dy * dz;
+                        ep += cc[q] * dV * (g->yc[j] - y_ref);
+                        st += cc[q] * dV;
+                        cr += vbc[q] * cc[q] * (dx * dy * dz);
+                    }
+                }
+            }
+        }
+        out->potential_energy[ic] = ep * p->alpha[ic];
+        out->stokes_dissipation[ic] = st * (fabs(p->vs0[ic]) * p->alpha[ic]);
+        out->conversion_rate_c[ic] = cr * p->alpha[ic];
+        /* Conc_compute_ave_height_x, Conc.c:1524-1608 */
+        {
+            double Ly = g->yv[NY - 1] - g->yv[0], Lz = g->zw[NZ - 1] - g->zw[0], coef = 1.0 / (Ly * Lz);
+            for (i = 0; i < NX; i++) {
+                double ht = 0.0;
+                for (k = 0; k < NZ; k++) {
+                    double dz = dzc[k];
+                    for (j = 0; j < NY; j++) {
+                        size_t q = IDX(g, i, j, k);
+                        if (cs[q] == TO_FLUID) {
+                            double dy = dyc[j];
+                            ht += cc[q] * dy * dz;
+                        }
+                    }
+                }
+                h[(size_t)ic * NX + i] = ht * coef;
+            }
+        }
+    }
+    /* Conc_find_front_location, Conc.c:1610-1672 */
+    out->front_location = -1.0;
+    for (i = NX - 2; i > 0; i--) {
+        double h0 = 0.0, h1 = 0.0;
+        for (ic = 0; ic < nc; ic++) {
+            h0 += h[(size_t)ic * NX + i - 1] * p->alpha[ic];
+            h1 += h[(size_t)ic * NX + i] * p->alpha[ic];
+        }
+        if (h1 <= front_limit && h0 >= front_limit) {
+            /* x at the limit: MyMath_interpolate_quantity with the heights as
+             * coordinates and the cell-centre x as values (Conc.c:1652-1662) */
+            out->front_location = interp2(g->xc[i - 1], g->xc[i], h0, h1, front_limit);
+            break;
+        }
+    }
+    if (h_ave) memcpy(h_ave, h, (size_t)nc * NX * sizeof(double));
+    free(ubc); free(vbc); free(wbc); free(ctot); free(dxc); free(dyc); free(dzc); free(h);
+}

@@ -120,6 +120,22 @@ typedef struct {
 } to_step_stats;
 
 void to_set_mg_options(int mode, int npre, int npost);
+/* Flow diagnostics of one state (cell-centred velocities computed here, as
+ * Velocity_cell_center does before the reference's output routines). */
+typedef struct {
+    double kinetic_energy;                 /* Extract_total_kinetic_energy           */
+    double conversion_rate;                /* Extract_kinetic_potential_conversion_rate */
+    double suspended_mass[TO_MAXCONC];     /* Conc_compute_total_suspended_mass      */
+    double potential_energy[TO_MAXCONC];   /* Conc_compute_potential_energies: W_Ep  */
+    double stokes_dissipation[TO_MAXCONC]; /*   ... W_Stokes_dissipation_rate        */
+    double conversion_rate_c[TO_MAXCONC];  /*   ... W_kinetic_potential_conversion_rate */
+    double front_location;                 /* Conc_find_front_location (-1: none)    */
+} to_diag;
+/* h_ave: nconc x NX spanwise-averaged heights (Conc_compute_ave_height_x) or NULL */
+void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
+                    const double *v, const double *w, const double *const *c,
+                    double front_limit, to_diag *out, double *h_ave);
+
 int to_step(const to_grid *g, const to_params *p, to_state *s, double dt,
             to_step_stats *stats);
 
