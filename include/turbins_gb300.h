@@ -324,6 +324,27 @@ int turb_conv3_test(int X, int Y, int Z, int cin, int cout, const void *in, cons
 int turb_conv3_wgrad_test(int X, int Y, int Z, int cin, int cout, const void *x, const void *dy,
                           float *dw, void *stream);
 
+/* ---- flow diagnostics of the current state --------------------------------
+ * Replaces the reference's output-time reductions: Extract_total_kinetic_energy
+ * (Extract.c:803-882), Extract_kinetic_potential_conversion_rate
+ * (Extract.c:727-801), Conc_compute_total_suspended_mass (Conc.c:1471-1522),
+ * Conc_compute_potential_energies (Conc.c:1934-2055; without deposited
+ * sediment), Conc_compute_ave_height_x (Conc.c:1524-1608) and
+ * Conc_find_front_location (Conc.c:1610-1672).  Refreshes the cell-centre
+ * velocities (and the total concentration) first, as the reference's output
+ * path does.  ave_height: host array of nconc x (nx+1) spanwise-averaged
+ * heights, or NULL. */
+typedef struct {
+    double kinetic_energy;                    /* W_kinetic_energy                       */
+    double conversion_rate;                   /* -int v c_total dV                      */
+    double suspended_mass[TURB_MAXCONC];      /* W_total_susp_mass                      */
+    double potential_energy[TURB_MAXCONC];    /* W_Ep                                   */
+    double stokes_dissipation[TURB_MAXCONC];  /* W_Stokes_dissipation_rate              */
+    double conversion_rate_c[TURB_MAXCONC];   /* W_kinetic_potential_conversion_rate    */
+    double front_location;                    /* -1 when no crossing                    */
+} turb_diag;
+int turb_diagnostics(turb_ctx *ctx, double front_limit, turb_diag *out, double *ave_height);
+
 /* operator hooks used by the parity tests: y = A x on device fields */
 int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);
 int turb_pressure_apply(turb_ctx *ctx, int field_x, int field_y);

@@ -77,6 +77,22 @@ def dump(name, case):
     mx, dv = ref.divergence(*arrs[:3])
     out["ref_divmax"] = np.array([mx])
     out["ref_div"] = dv
+    # flow diagnostics; the front limit is set between two heights of the
+    # alpha-weighted h(x) profile so that the fixture holds a front crossing
+    cs = [s["c%d" % i] for i in range(p.nconc)]
+    h = ref.diagnostics(s["u"], s["v"], s["w"], cs, 0.05)["ave_height"]
+    hw = sum(h[i] * p.alpha[i] for i in range(p.nconc))
+    limit = 0.05
+    for i in range(g.nx - 1, 0, -1):
+        if hw[i - 1] > hw[i]:
+            limit = 0.5 * (hw[i - 1] + hw[i])
+            break
+    d = ref.diagnostics(s["u"], s["v"], s["w"], cs, limit)
+    out["diag_front_limit"] = np.array([limit])
+    out["ref_diag"] = np.array([d["kinetic_energy"], d["conversion_rate"]] + d["suspended_mass"] +
+                               d["potential_energy"] + d["stokes_dissipation"] + d["conversion_rate_c"] +
+                               [d["front_location"]])
+    out["ref_ave_height"] = d["ave_height"]
     # ENO lines with ties and zero velocities
     rng = np.random.Generator(np.random.PCG64(5))
     for order in (1, 2, 3):

@@ -268,6 +268,40 @@ def test_step_matches_oracle(api, oracle_mod, name, mk):
     assert np.abs(g["c0"] - so["c0"]).max() <= 1e-9 * np.abs(so["c0"]).max()
 
 
+def _front_limit(h, alpha):
+    """a limit between two heights of the alpha-weighted h(x) profile, so the
+    front scan finds a crossing"""
+    hw = sum(h[i] * alpha[i] for i in range(len(h)))
+    for i in range(len(hw) - 2, 0, -1):
+        if hw[i - 1] > hw[i]:
+            return 0.5 * (hw[i - 1] + hw[i])
+    return 0.05
+
+
+@pytest.mark.parametrize("name,mk", CASES + [("bump_64", lambda: _cases.bump_small(64, 40, 24))])
+def test_diagnostics(api, oracle_mod, name, mk):
+    """Flow integrals, heights and front location on the GPU against the
+    oracle (itself pinned to the reference's Extract.c / Conc.c): the device
+    sums run in block order, so agreement is to 1e-12 relative, not bitwise."""
+    case = mk()
+    s = _cases.random_state(case, seed=9)
+    ctx, orc, _ = _pair(case, api, oracle_mod, s)
+    cs = [s["c%d" % i] for i in range(case.params.nconc)]
+    h0 = orc.diagnostics(s["u"], s["v"], s["w"], cs, 0.05)["ave_height"]
+    limit = _front_limit(h0, case.params.alpha)
+    ref = orc.diagnostics(s["u"], s["v"], s["w"], cs, limit)
+    got = ctx.diagnostics(limit)
+    for k in ("kinetic_energy", "conversion_rate"):
+        assert abs(got[k] - ref[k]) <= 1e-12 * abs(ref[k]) + 1e-300, k
+    for k in ("suspended_mass", "potential_energy", "stokes_dissipation", "conversion_rate_c"):
+        a, b = np.array(got[k]), np.array(ref[k])
+        assert np.all(np.abs(a - b) <= 1e-12 * np.abs(b)), k
+    hr = ref["ave_height"]
+    assert np.abs(got["ave_height"] - hr).max() <= 1e-12 * np.abs(hr).max()
+    assert ref["front_location"] > 0.0
+    assert abs(got["front_location"] - ref["front_location"]) <= 1e-9
+
+
 def test_failure_paths(api, oracle_mod):
     """Non-convergence and non-finite input come back as status codes; the
     context stays usable afterwards."""

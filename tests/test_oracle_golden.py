@@ -136,3 +136,17 @@ def test_pressure_rhs_projection_divergence(fixture):
     mx, dv = o.divergence(*arrs[:3])
     assert mx == z["ref_divmax"][0]
     assert np.array_equal(dv, z["ref_div"])
+
+
+def test_diagnostics(fixture):
+    """to_diagnostics reproduces Extract.c / Conc.c's flow integrals, the
+    spanwise-averaged heights and the front location bit for bit."""
+    z, g, p, dt, o = fixture
+    nc = p.nconc
+    cs = [z["in_c%d" % i] for i in range(nc)]
+    d = o.diagnostics(z["in_u"], z["in_v"], z["in_w"], cs, float(z["diag_front_limit"][0]))
+    got = np.array([d["kinetic_energy"], d["conversion_rate"]] + d["suspended_mass"] + d["potential_energy"] +
+                   d["stokes_dissipation"] + d["conversion_rate_c"] + [d["front_location"]])
+    assert np.array_equal(got, z["ref_diag"])
+    assert np.array_equal(d["ave_height"], z["ref_ave_height"])
+    assert d["front_location"] > 0.0

@@ -210,6 +210,22 @@ class Context:
         _check(self.lib.turb_pressure_guess_ratio(self.ctx, C.byref(r)), "pressure_guess_ratio")
         return r.value
 
+    def diagnostics(self, front_limit=0.1):
+        """Flow integrals of the current state (turb_diagnostics): kinetic
+        energy, conversion rates, suspended mass, potential energy and Stokes
+        dissipation per fraction, front location, spanwise-averaged heights."""
+        class _Diag(C.Structure):
+            _fields_ = [("ke", C.c_double), ("rate", C.c_double), ("mass", C.c_double * MAXC),
+                        ("ep", C.c_double * MAXC), ("stokes", C.c_double * MAXC), ("rate_c", C.c_double * MAXC),
+                        ("front", C.c_double)]
+        d = _Diag()
+        nc = self.params.nconc
+        h = np.zeros((nc, self.grid.nx + 1))
+        _check(self.lib.turb_diagnostics(self.ctx, C.c_double(front_limit), C.byref(d), _ptr(h)), "diagnostics")
+        return dict(kinetic_energy=d.ke, conversion_rate=d.rate, suspended_mass=list(d.mass)[:nc],
+                    potential_energy=list(d.ep)[:nc], stokes_dissipation=list(d.stokes)[:nc],
+                    conversion_rate_c=list(d.rate_c)[:nc], front_location=d.front, ave_height=h)
+
     def set_helmholtz_mode(self, mode, inner_sweeps=6):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")
 

@@ -29,6 +29,13 @@ int turb_set_cuda_error(cudaError_t e, const char *file, int line)
     return TURB_ERR_CUDA;
 }
 
+// flow diagnostics (k_diag.cu)
+long long diag_scratch_doubles(const Dims &d);
+void launch_diagnostics(cudaStream_t s, const Dims &d, const uint8_t *cst, const double *dxc, const double *dyc,
+                        const double *dzc, const double *yc, double y_ref, double coef, const double *ubc,
+                        const double *vbc, const double *wbc, const double *ct, const double *const *c, int nconc,
+                        double *scratch, double **sums, double **heights);
+
 // extra launchers defined at the end of this file
 void launch_pressure_apply(cudaStream_t s, const Dims &d, const uint8_t *st, const Geo &g, double dEta, double dXi,
                            double dPhi, const double *x, double *y);
@@ -129,6 +136,8 @@ struct turb_ctx {
     // learned guess (k_net.cu) and the snapshot store that training reads
     TurbNet *net = nullptr;
     TurbSnaps *snaps = nullptr;
+    // diagnostics: cell widths dx_c, dy_c, dz_c (Grid.c:633-671) and scratch
+    double *diag_dxc = nullptr, *diag_dyc = nullptr, *diag_dzc = nullptr, *diag_yc = nullptr, *diag_scr = nullptr;
 };
 
 namespace {
@@ -1090,6 +1099,83 @@ int turb_Velocity_transpose_velocities(turb_ctx *c, char which)
     launch_transpose(c->s, c->d, q, c->st[q], c->tw, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W],
                      c->fld[TURB_F_SCRATCH0], c->fld[TURB_F_SCRATCH1]);
     c->launches += 1;
+    return check_launch(c);
+}
+
+// Grid_compute_metric_coefficients' cell widths: f[i+1] - f[i], the last
+// repeating its neighbour (Grid.c:633-637)
+static std::vector<double> cell_widths(const std::vector<double> &f)
+{
+    size_t n = f.size();
+    std::vector<double> d(n, 0.0);
+    for (size_t i = 1; i + 1 < n; i++) d[i] = f[i + 1] - f[i];
+    d[0] = f[1] - f[0];
+    d[n - 1] = f[n - 1] - f[n - 2];
+    return d;
+}
+
+int turb_diagnostics(turb_ctx *c, double front_limit, turb_diag *out, double *ave_height)
+{
+    if (!c || !out) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    int nc = c->prm.nconc;
+    if (!c->diag_scr) {
+        c->diag_dxc = c->mem.upload(cell_widths(c->xu));
+        c->diag_dyc = c->mem.upload(cell_widths(c->yv));
+        c->diag_dzc = c->mem.upload(cell_widths(c->zw));
+        c->diag_yc = c->mem.upload(c->yc);
+        c->diag_scr = c->mem.alloc<double>(diag_scratch_doubles(d));
+        if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+    }
+    // the reference's output routines read the cell-centre velocities and the
+    // total concentration of the current state (Velocity_cell_center, Conc.c:1291)
+    int rc = turb_Velocity_cell_center(c);
+    if (rc) return rc;
+    const double *ct = c->fld[TURB_F_C0];
+    if (nc > 1) {
+        rc = turb_Conc_compute_total_concentration(c);
+        if (rc) return rc;
+        ct = c->fld[TURB_F_CTOT];
+    }
+    const double *cf[TURB_MAXCONC];
+    for (int i = 0; i < TURB_MAXCONC; i++) cf[i] = i < nc ? c->fld[TURB_F_C0 + i] : nullptr;
+    double Ly = c->yv[d.NY - 1] - c->yv[0], Lz = c->zw[d.NZ - 1] - c->zw[0];
+    double *sums = nullptr, *heights = nullptr;
+    launch_diagnostics(c->s, d, c->st[3], c->diag_dxc, c->diag_dyc, c->diag_dzc, c->diag_yc, c->yv[0],
+                       1.0 / (Ly * Lz), c->fld[TURB_F_UBC], c->fld[TURB_F_VBC], c->fld[TURB_F_WBC], ct, cf, nc,
+                       c->diag_scr, &sums, &heights);
+    c->launches += 4;
+    std::vector<double> sh(2 + 4 * TURB_MAXCONC), hh((size_t)nc * d.NX);
+    TURB_CHECK(cudaMemcpyAsync(sh.data(), sums, sh.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaMemcpyAsync(hh.data(), heights, hh.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    memset(out, 0, sizeof(*out));
+    out->kinetic_energy = sh[0] * 0.5;
+    out->conversion_rate = sh[1];
+    for (int i = 0; i < nc; i++) {
+        double a = c->prm.alpha[i];
+        out->suspended_mass[i] = sh[2 + 4 * i];
+        out->potential_energy[i] = sh[3 + 4 * i] * a;
+        out->stokes_dissipation[i] = sh[4 + 4 * i] * (std::fabs(c->prm.vs0[i]) * a);
+        out->conversion_rate_c[i] = sh[5 + 4 * i] * a;
+    }
+    // Conc_find_front_location, Conc.c:1610-1672: first x from the right where
+    // the alpha-weighted height crosses the limit, interpolated linearly in the
+    // height (MyMath_interpolate_quantity, two-point branch)
+    out->front_location = -1.0;
+    for (int i = d.NX - 2; i > 0; i--) {
+        double h0 = 0.0, h1 = 0.0;
+        for (int ic = 0; ic < nc; ic++) {
+            h0 += hh[(size_t)ic * d.NX + i - 1] * c->prm.alpha[ic];
+            h1 += hh[(size_t)ic * d.NX + i] * c->prm.alpha[ic];
+        }
+        if (h1 <= front_limit && h0 >= front_limit) {
+            double m = (c->xc[i] - c->xc[i - 1]) / (h1 - h0);
+            out->front_location = std::fabs(h1 - h0) < 1.0e-8 ? c->xc[i - 1] : m * (front_limit - h0) + c->xc[i - 1];
+            break;
+        }
+    }
+    if (ave_height) memcpy(ave_height, hh.data(), hh.size() * sizeof(double));
     return check_launch(c);
 }
 
