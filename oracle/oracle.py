@@ -65,6 +65,22 @@ def _ptr(a, t=_dp):
     return a.ctypes.data_as(t)
 
 
+class _Diag(C.Structure):
+    """to_diag / turb_diag"""
+    _fields_ = [("ke", C.c_double), ("rate", C.c_double), ("mass", C.c_double * MAXC),
+                ("ep", C.c_double * MAXC), ("stokes", C.c_double * MAXC), ("rate_c", C.c_double * MAXC),
+                ("front", C.c_double), ("visc", C.c_double), ("epp", C.c_double * MAXC),
+                ("epp_rate", C.c_double * MAXC), ("ep_rate", C.c_double * MAXC), ("sed", C.c_double * MAXC)]
+
+
+def diag_dict(d, nc, h, sb):
+    return dict(kinetic_energy=d.ke, conversion_rate=d.rate, suspended_mass=list(d.mass)[:nc],
+                potential_energy=list(d.ep)[:nc], stokes_dissipation=list(d.stokes)[:nc],
+                conversion_rate_c=list(d.rate_c)[:nc], front_location=d.front, viscous_dissipation=d.visc,
+                ep_passive=list(d.epp)[:nc], ep_passive_rate=list(d.epp_rate)[:nc], ep_rate=list(d.ep_rate)[:nc],
+                sed_rate=list(d.sed)[:nc], ave_height=h, sed_bottom=sb)
+
+
 class Oracle:
     """Holds one grid + parameter set in the oracle's C layout."""
 
@@ -220,23 +236,42 @@ class Oracle:
         self.lib.to_total_concentration(C.byref(self.cg), C.byref(self.cp), arr, _ptr(out))
         return out
 
-    def diagnostics(self, u, v, w, cs, front_limit=0.1):
-        """to_diagnostics: dict of the flow integrals and the h(x) profiles."""
-        class _Diag(C.Structure):
-            _fields_ = [("ke", C.c_double), ("rate", C.c_double), ("mass", C.c_double * MAXC),
-                        ("ep", C.c_double * MAXC), ("stokes", C.c_double * MAXC), ("rate_c", C.c_double * MAXC),
-                        ("front", C.c_double)]
+    def _bed_shape(self):
+        return (self.p.nconc, self.g.nz + 1, self.g.nx + 1)
+
+    def interface_y_index(self):
+        """to_interface_y_index: [NZ][NX] bed index (-1: none)"""
+        iy = np.zeros((self.g.nz + 1, self.g.nx + 1), dtype=np.int32)
+        self.lib.to_interface_y_index(C.byref(self.cg), iy.ctypes.data_as(C.c_void_p))
+        return iy
+
+    def deposit_integrate(self, cs, cs_old, dt, dep, iy=None):
+        """to_deposit_integrate on dep (nconc x NZ x NX) in place"""
+        iy = self.interface_y_index() if iy is None else iy
+        a, b = (_dp * MAXC)(), (_dp * MAXC)()
+        for i in range(len(cs)):
+            a[i], b[i] = _ptr(cs[i]), _ptr(cs_old[i])
+        assert dep.shape == self._bed_shape() and dep.flags.c_contiguous
+        self.lib.to_deposit_integrate(C.byref(self.cg), C.byref(self.cp), iy.ctypes.data_as(C.c_void_p), a, b,
+                                      C.c_double(dt), _ptr(dep))
+        return dep
+
+    def diagnostics(self, u, v, w, cs, front_limit=0.01, dep=None):
+        """to_diagnostics: dict of the flow integrals, the h(x) profiles and
+        the bed sedimentation rates"""
         d = _Diag()
         arr = (_dp * MAXC)()
         for i, c in enumerate(cs):
             arr[i] = _ptr(c)
         nc = self.p.nconc
         h = np.zeros((nc, self.g.nx + 1))
+        sb = np.zeros(self._bed_shape())
+        iy = self.interface_y_index()
+        dp = None if dep is None else _ptr(np.ascontiguousarray(dep))
         self.lib.to_diagnostics(C.byref(self.cg), C.byref(self.cp), _ptr(u), _ptr(v), _ptr(w), arr,
-                                C.c_double(front_limit), C.byref(d), _ptr(h))
-        return dict(kinetic_energy=d.ke, conversion_rate=d.rate, suspended_mass=list(d.mass)[:nc],
-                    potential_energy=list(d.ep)[:nc], stokes_dissipation=list(d.stokes)[:nc],
-                    conversion_rate_c=list(d.rate_c)[:nc], front_location=d.front, ave_height=h)
+                                C.c_double(front_limit), iy.ctypes.data_as(C.c_void_p), dp, C.byref(d), _ptr(h),
+                                _ptr(sb))
+        return diag_dict(d, nc, h, sb)
 
     def step(self, state, dt):
         """One TVD-RK2 step in place on a dict of DA arrays."""

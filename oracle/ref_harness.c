@@ -299,40 +299,109 @@ void ref_metrics(ref_case *r, double *mxc, double *myc, double *mzc, double *mxu
     memcpy(mxu, g->metric_xu, 8 * g->NX); memcpy(myv, g->metric_yv, 8 * g->NY); memcpy(mzw, g->metric_zw, 8 * g->NZ);
 }
 
+static void bed_index(MAC_grid *g)
+{
+    if (!g->interface_y_index) g->interface_y_index = Memory_allocate_2D_int(g->NX, g->NZ);
+    Grid_set_interface_y_index(g);
+}
+
+/* Grid_set_interface_y_index, copied out as iy[k * NX + i] */
+void ref_interface_y_index(ref_case *r, int *iy)
+{
+    MAC_grid *g = r->g;
+    int i, k;
+    bed_index(g);
+    for (k = 0; k < g->NZ; k++)
+        for (i = 0; i < g->NX; i++) iy[(long)k * g->NX + i] = g->interface_y_index[k][i];
+}
+
+/* G_deposit_height of fraction ic <- dep (nconc x NZ x NX), or zeros */
+static void set_deposit(ref_case *r, int ic, const double *dep)
+{
+    MAC_grid *g = r->g;
+    Concentration *cc = r->c[ic];
+    int i, k;
+    if (!cc->G_deposit_height) cc->G_deposit_height = Memory_allocate_2D_double(g->NX, g->NZ);
+    for (k = 0; k < g->NZ; k++)
+        for (i = 0; i < g->NX; i++)
+            cc->G_deposit_height[k][i] = dep ? dep[((long)ic * g->NZ + k) * g->NX + i] : 0.0;
+}
+
+/* Conc_integrate_deposited_height of every fraction (weight_factor =
+ * Conc_alpha, as Conc_dump_particles weighs the deposit) on dep in place */
+void ref_deposit_integrate(ref_case *r, const double *const *c, const double *const *c_old, double dt, double *dep)
+{
+    MAC_grid *g = r->g;
+    int i, k, ic;
+    bed_index(g);
+    for (ic = 0; ic < r->p->NConc; ic++) {
+        Concentration *cc = r->c[ic];
+        set_deposit(r, ic, dep);
+        vset(cc->G_data, c[ic], r->n);
+        vset(cc->G_data_old, c_old[ic], r->n);
+        Conc_integrate_deposited_height(cc, g, r->p->Conc_alpha[ic], dt);
+        for (k = 0; k < g->NZ; k++)
+            for (i = 0; i < g->NX; i++) dep[((long)ic * g->NZ + k) * g->NX + i] = cc->G_deposit_height[k][i];
+    }
+}
+
 /* flow diagnostics through the reference's own routines:
  * out[0] = Extract_total_kinetic_energy, out[1] = Extract_kinetic_potential_conversion_rate,
  * per fraction i (base 2 + 4 i): Conc_compute_total_suspended_mass, and
  * Conc_compute_potential_energies' W_Ep, W_Stokes_dissipation_rate,
- * W_kinetic_potential_conversion_rate (no deposit: the passive part is 0);
- * out[2 + 4 nconc] = Conc_find_front_location(front_limit); h_ave (nconc x NX)
- * = Conc_compute_ave_height_x. */
+ * W_kinetic_potential_conversion_rate;
+ * out[2 + 4 nconc] = Conc_find_front_location(front_limit);
+ * out[3 + 4 nconc] = Extract_viscous_dissipation_rate;
+ * per fraction i (base 4 + 4 nconc + 4 i): W_Ep_passive, W_Ep_passive_rate,
+ * W_Ep_rate, Conc_compute_sedimentation_rate's W_sed_rate.
+ * dep: deposited heights (nconc x NZ x NX) or NULL; h_ave (nconc x NX) =
+ * Conc_compute_ave_height_x; sed_bottom (nconc x NZ x NX) = Conc_bottom_sed_rate. */
 void ref_diagnostics(ref_case *r, const double *u, const double *v, const double *w, const double *const *c,
-                     double front_limit, double *out, double *h_ave)
+                     double front_limit, const double *dep, double *out, double *h_ave, double *sed_bottom)
 {
     long n = r->n;
-    int i, nc = r->p->NConc, NX = r->g->NX;
+    int i, k, x, nc = r->p->NConc, NX = r->g->NX, NZ = r->g->NZ;
     MAC_grid *g = r->g;
     Parameters *p = r->p;
-    if (!g->interface_y_index) g->interface_y_index = Memory_allocate_2D_int(g->NX, g->NZ);
+    double *ext = out + 3 + 4 * nc;
+    bed_index(g);
     p->Ly = g->yv[g->NY - 1] - g->yv[0];
     p->Lz = g->zw[g->NZ - 1] - g->zw[0];
     vset(r->u->G_data, u, n); vset(r->v->G_data, v, n); vset(r->w->G_data, w, n);
+    vset(r->u->L_data, u, n); vset(r->v->L_data, v, n); vset(r->w->L_data, w, n);
     Velocity_cell_center(r->u, r->v, r->w, g, p);
     for (i = 0; i < nc; i++) vset(r->c[i]->G_data, c[i], n);
     if (nc > 1) Conc_compute_total_concentration(r->c, p);
     Extract_total_kinetic_energy(r->u, r->v, r->w, g);
     Extract_kinetic_potential_conversion_rate(r->v, r->c, g, p);
+    Extract_viscous_dissipation_rate(r->u, r->v, r->w, g, p);
     out[0] = r->u->W_kinetic_energy;
     out[1] = r->v->W_kinetic_potential_conversion_rate;
+    ext[0] = r->u->W_dissipation_rate;
     for (i = 0; i < nc; i++) {
         Concentration *cc = r->c[i];
-        if (!cc->G_deposit_height) cc->G_deposit_height = Memory_allocate_2D_double(g->NX, g->NZ);
+        set_deposit(r, i, dep);
+        if (!cc->G_sed_rate_bottom) {
+            cc->G_sed_rate_bottom = Memory_allocate_2D_double(NX, NZ);
+            cc->W_sed_rate_bottom = Memory_allocate_2D_double(NX, NZ);
+        }
         Conc_compute_total_suspended_mass(cc, g);
         Conc_compute_potential_energies(cc, r->v, g, p);
+        Conc_compute_sedimentation_rate(cc, g, p);
+        Conc_bottom_sed_rate(cc, g, p);
         out[2 + 4 * i] = cc->W_total_susp_mass;
         out[3 + 4 * i] = cc->W_Ep;
         out[4 + 4 * i] = cc->W_Stokes_dissipation_rate;
         out[5 + 4 * i] = cc->W_kinetic_potential_conversion_rate;
+        ext[1 + 4 * i] = cc->W_Ep_passive;
+        ext[2 + 4 * i] = cc->W_Ep_passive_rate;
+        ext[3 + 4 * i] = cc->W_Ep_rate;
+        ext[4 + 4 * i] = cc->W_sed_rate;
+        if (sed_bottom)
+            for (k = 0; k < NZ; k++)
+                for (x = 0; x < NX; x++)
+                    sed_bottom[((long)i * NZ + k) * NX + x] =
+                        cc->Type == PARTICLE ? cc->W_sed_rate_bottom[k][x] : 0.0;
     }
     for (i = 0; i < nc; i++) {   /* Conc_create leaves them unset without ave_height_output */
         if (!r->hbuf[i]) {

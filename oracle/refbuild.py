@@ -30,7 +30,9 @@ def available():
 def build(force=False):
     if not available():
         raise FileNotFoundError("reference sources not found under %s" % SRC)
-    if not force and os.path.exists(LIB):
+    own = [os.path.join(HERE, "ref_harness.c")] + [os.path.join(HERE, "shim", f)
+                                                    for f in os.listdir(os.path.join(HERE, "shim"))]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in own):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     inc = ["-I" + os.path.join(HERE, "shim"), "-I" + os.path.join(SRC, "Include")]

@@ -109,20 +109,46 @@ class Reference:
         self.lib.ref_total_concentration(self.h, arr, _p(out))
         return out
 
-    def diagnostics(self, u, v, w, cs, front_limit=0.1):
+    def _bed_shape(self, nc):
+        return (nc, self.g.nz + 1, self.g.nx + 1)
+
+    def interface_y_index(self):
+        iy = np.zeros((self.g.nz + 1, self.g.nx + 1), dtype=np.int32)
+        self.lib.ref_interface_y_index(self.h, iy.ctypes.data_as(C.POINTER(C.c_int)))
+        return iy
+
+    def deposit_integrate(self, cs, cs_old, dt, dep):
+        """Conc_integrate_deposited_height of every fraction on dep (in place)"""
+        a, b = (_dp * 4)(), (_dp * 4)()
+        for i in range(len(cs)):
+            a[i], b[i] = _p(cs[i]), _p(cs_old[i])
+        assert dep.shape == self._bed_shape(len(cs)) and dep.flags.c_contiguous
+        self.lib.ref_deposit_integrate(self.h, a, b, C.c_double(dt), _p(dep))
+        return dep
+
+    def diagnostics(self, u, v, w, cs, front_limit=0.01, dep=None):
         nc = len(cs)
         arr = (_dp * 4)()
         for i, c in enumerate(cs):
             arr[i] = _p(c)
-        out = np.zeros(3 + 4 * nc)
+        out = np.zeros(4 + 8 * nc)
         h = np.zeros((nc, self.g.nx + 1))
-        self.lib.ref_diagnostics(self.h, _p(u), _p(v), _p(w), arr, C.c_double(front_limit), _p(out), _p(h))
+        sb = np.zeros(self._bed_shape(nc))
+        dp = None if dep is None else _p(np.ascontiguousarray(dep))
+        self.lib.ref_diagnostics(self.h, _p(u), _p(v), _p(w), arr, C.c_double(front_limit), dp, _p(out), _p(h),
+                                 _p(sb))
+        e = 4 + 4 * nc
         return dict(kinetic_energy=out[0], conversion_rate=out[1],
                     suspended_mass=[out[2 + 4 * i] for i in range(nc)],
                     potential_energy=[out[3 + 4 * i] for i in range(nc)],
                     stokes_dissipation=[out[4 + 4 * i] for i in range(nc)],
                     conversion_rate_c=[out[5 + 4 * i] for i in range(nc)],
-                    front_location=out[2 + 4 * nc], ave_height=h)
+                    front_location=out[2 + 4 * nc], viscous_dissipation=out[3 + 4 * nc],
+                    ep_passive=[out[e + 4 * i] for i in range(nc)],
+                    ep_passive_rate=[out[e + 1 + 4 * i] for i in range(nc)],
+                    ep_rate=[out[e + 2 + 4 * i] for i in range(nc)],
+                    sed_rate=[out[e + 3 + 4 * i] for i in range(nc)],
+                    ave_height=h, sed_bottom=sb)
 
     def lhs_apply(self, q, ic, dt, x):
         y = self._z()

@@ -1196,9 +1196,128 @@ static void cell_widths(const double *f, int n, double *d)
     d[n - 1] = f[n - 1] - f[n - 2];
 }
 
+void to_interface_y_index(const to_grid *g, int32_t *iy)
+{
+    int i, j, k;
+    for (k = 0; k < g->NZ; k++)
+        for (i = 0; i < g->NX; i++) {
+            int32_t r = -1;
+            for (j = 0; j < g->NY; j++) {
+                uint8_t s = g->st[3][IDX(g, i, j, k)];
+                if (s == TO_IMMERSED || (j == 0 && s == TO_FLUID)) {
+                    r = j;
+                    break;
+                }
+            }
+            iy[(size_t)k * g->NX + i] = r;
+        }
+}
+
+void to_deposit_integrate(const to_grid *g, const to_params *p, const int32_t *iy,
+                          const double *const *c, const double *const *c_old,
+                          double dt, double *dep)
+{
+    int i, k, ic;
+    for (ic = 0; ic < p->nconc; ic++) {
+        double *h = dep + (size_t)ic * g->NZ * g->NX;
+        for (k = 0; k < g->NZ; k++)
+            for (i = 0; i < g->NX; i++) {
+                int j = iy[(size_t)k * g->NX + i];
+                if (j >= 0 && j < g->NY) {
+                    size_t q = IDX(g, i, j, k);
+                    double dh = dt * fabs(p->vs0[ic]) * p->alpha[ic] * 0.5 * (c[ic][q] + c_old[ic][q]);
+                    h[(size_t)k * g->NX + i] += dh;
+                }
+            }
+    }
+}
+
+/* Extract_viscous_dissipation_rate, Extract.c:453-725: sum over FLUID c
+ * nodes of u lap(u) dV_u + v lap(v) dV_v + w lap(w) dV_w (each velocity at
+ * its own face node, the c node's index), over Re; box-wall ghosts are
+ * k * (own value) with k = -1 no-slip, +1 free-slip, the normal component
+ * 0; no inflow / outflow. */
+static double viscous_dissipation(const to_grid *g, const to_params *p, const double *u,
+                                  const double *v, const double *w, const double *dxc,
+                                  const double *dyc, const double *dzc)
+{
+    int NX = g->NX, NY = g->NY, NZ = g->NZ, NI = NX - 1, NJ = NY - 1, NK = NZ - 1, i, j, k;
+    double kw[6], G = 0.0;
+    double Cx = 1.0 / (g->dEta * g->dEta), Cy = 1.0 / (g->dXi * g->dXi), Cz = 1.0 / (g->dPhi * g->dPhi);
+    const double *mxc = g->mxc, *myc = g->myc, *mzc = g->mzc, *mxu = g->mxu, *myv = g->myv, *mzw = g->mzw;
+    for (i = 0; i < 6; i++) kw[i] = p->wall_noslip[i] ? -1.0 : 1.0;
+    for (k = 0; k < NZ; k++)
+        for (j = 0; j < NY; j++)
+            for (i = 0; i < NX; i++) {
+                size_t q = IDX(g, i, j, k);
+                double U_w, U_e, U_n, U_s, U_f, U_b, V_w, V_e, V_n, V_s, V_f, V_b, W_w, W_e, W_n, W_s, W_f, W_b;
+                if (g->st[3][q] != TO_FLUID) continue;
+                double U_ae = Cx * mxu[i] * mxc[i], U_aw = Cx * mxu[i];
+                double U_an = Cy * myc[j] * myv[j + 1], U_as = Cy * myc[j] * myv[j];
+                double U_af = Cz * mzc[k] * mzw[k + 1], U_ab = Cz * mzc[k] * mzw[k];
+                double V_ae = Cx * mxc[i] * mxu[i + 1], V_aw = Cx * mxc[i] * mxu[i];
+                double V_an = Cy * myv[j] * myc[j], V_as = Cy * myv[j];
+                double V_af = Cz * mzc[k] * mzw[k + 1], V_ab = Cz * mzc[k] * mzw[k];
+                double W_ae = Cx * mxc[i] * mxu[i + 1], W_aw = Cx * mxc[i] * mxu[i];
+                double W_an = Cy * myc[j] * myv[j + 1], W_as = Cy * myc[j] * myv[j];
+                double W_af = Cz * mzw[k] * mzc[k], W_ab = Cz * mzw[k];
+                double u_ = u[q], v_ = v[q], w_ = w[q];
+                if (i == 0) {
+                    U_aw *= mxc[i];
+                    U_w = 0.0; V_w = kw[0] * v_; W_w = kw[0] * w_;
+                } else {
+                    U_aw *= mxc[i - 1];
+                    U_w = u[q - 1]; V_w = v[q - 1]; W_w = w[q - 1];
+                }
+                if (j == 0) {
+                    V_as *= myc[j];
+                    U_s = kw[2] * u_; V_s = 0.0; W_s = kw[2] * w_;
+                } else {
+                    V_as *= myc[j - 1];
+                    U_s = u[IDX(g, i, j - 1, k)]; V_s = v[IDX(g, i, j - 1, k)]; W_s = w[IDX(g, i, j - 1, k)];
+                }
+                if (k == 0) {
+                    W_ab *= mzc[k];
+                    U_b = kw[4] * u_; V_b = kw[4] * v_; W_b = 0.0;
+                } else {
+                    W_ab *= mzc[k - 1];
+                    U_b = u[IDX(g, i, j, k - 1)]; V_b = v[IDX(g, i, j, k - 1)]; W_b = w[IDX(g, i, j, k - 1)];
+                }
+                if (i == NI - 1) {
+                    U_e = 0.0; V_e = kw[1] * v_; W_e = kw[1] * w_;
+                } else {
+                    U_e = u[q + 1]; V_e = v[q + 1]; W_e = w[q + 1];
+                }
+                if (j == NJ - 1) {
+                    U_n = kw[3] * u_; V_n = 0.0; W_n = kw[3] * w_;
+                } else {
+                    U_n = u[IDX(g, i, j + 1, k)]; V_n = v[IDX(g, i, j + 1, k)]; W_n = w[IDX(g, i, j + 1, k)];
+                }
+                if (k == NK - 1) {
+                    U_f = kw[5] * u_; V_f = kw[5] * v_; W_f = 0.0;
+                } else {
+                    U_f = u[IDX(g, i, j, k + 1)]; V_f = v[IDX(g, i, j, k + 1)]; W_f = w[IDX(g, i, j, k + 1)];
+                }
+                {
+                    double U_ap = -(U_ae + U_aw + U_ab + U_af + U_as + U_an);
+                    double V_ap = -(V_ae + V_aw + V_ab + V_af + V_as + V_an);
+                    double W_ap = -(W_ae + W_aw + W_ab + W_af + W_as + W_an);
+                    double lu = (U_ae * U_e + U_aw * U_w) + (U_an * U_n + U_as * U_s) + (U_af * U_f + U_ab * U_b) + U_ap * u_;
+                    double lv = (V_ae * V_e + V_aw * V_w) + (V_an * V_n + V_as * V_s) + (V_af * V_f + V_ab * V_b) + V_ap * v_;
+                    double lw = (W_ae * W_e + W_aw * W_w) + (W_an * W_n + W_as * W_s) + (W_af * W_f + W_ab * W_b) + W_ap * w_;
+                    double dVu = (g->xc[i + 1] - g->xc[i]) * dyc[j] * dzc[k];
+                    double dVv = (g->yc[j + 1] - g->yc[j]) * dxc[i] * dzc[k];
+                    double dVw = (g->zc[k + 1] - g->zc[k]) * dxc[i] * dyc[j];
+                    G += u_ * lu * dVu + v_ * lv * dVv + w_ * lw * dVw;
+                }
+            }
+    return G * (1.0 / p->re);
+}
+
 void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
                     const double *v, const double *w, const double *const *c,
-                    double front_limit, to_diag *out, double *h_ave)
+                    double front_limit, const int32_t *iy, const double *dep,
+                    to_diag *out, double *h_ave, double *sed_bottom)
 {
     size_t n = NPTS(g);
     int NX = g->NX, NY = g->NY, NZ = g->NZ, i, j, k, ic, nc = p->nconc;
@@ -1235,6 +1354,7 @@ void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
         }
     }
     out->kinetic_energy = ke * 0.5;
+    out->viscous_dissipation = viscous_dissipation(g, p, u, v, w, dxc, dyc, dzc);
     /* Extract_kinetic_potential_conversion_rate, Extract.c:727-801 */
     for (k = 0; k < NZ; k++) {
         double dz = dzc[k];
@@ -1253,6 +1373,7 @@ void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
     for (ic = 0; ic < TO_MAXCONC; ic++) {
         out->suspended_mass[ic] = out->potential_energy[ic] = 0.0;
         out->stokes_dissipation[ic] = out->conversion_rate_c[ic] = 0.0;
+        out->ep_passive[ic] = out->ep_passive_rate[ic] = out->ep_rate[ic] = out->sed_rate[ic] = 0.0;
     }
     for (ic = 0; ic < nc; ic++) {
         const double *cc = c[ic];
@@ -1291,6 +1412,31 @@ void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
         out->potential_energy[ic] = ep * p->alpha[ic];
         out->stokes_dissipation[ic] = st * (fabs(p->vs0[ic]) * p->alpha[ic]);
         out->conversion_rate_c[ic] = cr * p->alpha[ic];
+        /* the deposited part of Conc_compute_potential_energies (Conc.c:1955-1985),
+         * Conc_compute_sedimentation_rate (Conc.c:2098-2156) and
+         * Conc_bottom_sed_rate (Conc.c:2158-2230): bed nodes of particle fractions */
+        {
+            double epp = 0.0, sr = 0.0, us = fabs(p->vs0[ic]);
+            const double *dh = dep ? dep + (size_t)ic * NZ * NX : NULL;
+            double *sb = sed_bottom ? sed_bottom + (size_t)ic * NZ * NX : NULL;
+            for (k = 0; k < NZ; k++) {
+                double dz = dzc[k];
+                for (i = 0; i < NX; i++) {
+                    double dx = dxc[i], r = 0.0;
+                    int jb = iy[(size_t)k * NX + i];
+                    if (p->ctype[ic] == TO_PARTICLE && jb >= 0 && jb < NY) {
+                        if (dh) epp += dh[(size_t)k * NX + i] * dx * dz * (g->yc[jb] - y_ref);
+                        r = us * cc[IDX(g, i, jb, k)] * dx * dz;
+                        sr += r;
+                    }
+                    if (sb) sb[(size_t)k * NX + i] = r;
+                }
+            }
+            out->ep_passive[ic] = epp;
+            out->ep_passive_rate[ic] = epp * us;
+            out->ep_rate[ic] = out->conversion_rate_c[ic] + out->ep_passive_rate[ic] - out->stokes_dissipation[ic];
+            out->sed_rate[ic] = sr;
+        }
         /* Conc_compute_ave_height_x, Conc.c:1524-1608 */
         {
             double Ly = g->yv[NY - 1] - g->yv[0], Lz = g->zw[NZ - 1] - g->zw[0], coef = 1.0 / (Ly * Lz);

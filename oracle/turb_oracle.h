@@ -130,11 +130,30 @@ typedef struct {
     double stokes_dissipation[TO_MAXCONC]; /*   ... W_Stokes_dissipation_rate        */
     double conversion_rate_c[TO_MAXCONC];  /*   ... W_kinetic_potential_conversion_rate */
     double front_location;                 /* Conc_find_front_location (-1: none)    */
+    double viscous_dissipation;            /* Extract_viscous_dissipation_rate       */
+    double ep_passive[TO_MAXCONC];         /* Conc_compute_potential_energies: W_Ep_passive */
+    double ep_passive_rate[TO_MAXCONC];    /*   ... W_Ep_passive_rate                */
+    double ep_rate[TO_MAXCONC];            /*   ... W_Ep_rate                        */
+    double sed_rate[TO_MAXCONC];           /* Conc_compute_sedimentation_rate        */
 } to_diag;
-/* h_ave: nconc x NX spanwise-averaged heights (Conc_compute_ave_height_x) or NULL */
+/* Grid_set_interface_y_index (Grid.c:1972-2012): per (i, k), iy[k*NX + i] =
+ * the first j whose c node is IMMERSED, or 0 when the bottom c node is FLUID,
+ * else -1 (NOT_FOUND). */
+void to_interface_y_index(const to_grid *g, int32_t *iy);
+/* Conc_integrate_deposited_height (Conc.c:1675-1749) for every fraction with
+ * weight_factor = alpha_i: dep[ic][k][i] += dt |Vs0| alpha 0.5 (c + c_old)
+ * at the bed node (i, iy, k).  dep: nconc x NZ x NX. */
+void to_deposit_integrate(const to_grid *g, const to_params *p, const int32_t *iy,
+                          const double *const *c, const double *const *c_old,
+                          double dt, double *dep);
+/* iy: bed index (to_interface_y_index); dep: nconc x NZ x NX deposited
+ * heights, or NULL for none; h_ave: nconc x NX spanwise-averaged heights
+ * (Conc_compute_ave_height_x) or NULL; sed_bottom: nconc x NZ x NX bed
+ * sedimentation rates (Conc_bottom_sed_rate) or NULL. */
 void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
                     const double *v, const double *w, const double *const *c,
-                    double front_limit, to_diag *out, double *h_ave);
+                    double front_limit, const int32_t *iy, const double *dep,
+                    to_diag *out, double *h_ave, double *sed_bottom);
 
 int to_step(const to_grid *g, const to_params *p, to_state *s, double dt,
             to_step_stats *stats);

@@ -87,12 +87,24 @@ def dump(name, case):
         if hw[i - 1] > hw[i]:
             limit = 0.5 * (hw[i - 1] + hw[i])
             break
-    d = ref.diagnostics(s["u"], s["v"], s["w"], cs, limit)
+    # bed index, one deposit integration from a perturbed start-of-step state
+    out["ref_iy"] = ref.interface_y_index()
+    rng = np.random.Generator(np.random.PCG64(8))
+    cold = [c + 0.01 * rng.standard_normal(c.shape) for c in cs]
+    dep0 = rng.uniform(0.0, 0.01, (p.nconc, g.nz + 1, g.nx + 1))
+    for i in range(p.nconc):
+        out["in_cold%d" % i] = cold[i]
+    out["in_dep0"] = dep0
+    dep = ref.deposit_integrate(cs, cold, dt, dep0.copy())
+    out["ref_dep"] = dep
+    d = ref.diagnostics(s["u"], s["v"], s["w"], cs, limit, dep=dep)
     out["diag_front_limit"] = np.array([limit])
     out["ref_diag"] = np.array([d["kinetic_energy"], d["conversion_rate"]] + d["suspended_mass"] +
                                d["potential_energy"] + d["stokes_dissipation"] + d["conversion_rate_c"] +
-                               [d["front_location"]])
+                               [d["front_location"], d["viscous_dissipation"]] + d["ep_passive"] +
+                               d["ep_passive_rate"] + d["ep_rate"] + d["sed_rate"])
     out["ref_ave_height"] = d["ave_height"]
+    out["ref_sed_bottom"] = d["sed_bottom"]
     # ENO lines with ties and zero velocities
     rng = np.random.Generator(np.random.PCG64(5))
     for order in (1, 2, 3):

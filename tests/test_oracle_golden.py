@@ -140,13 +140,20 @@ def test_pressure_rhs_projection_divergence(fixture):
 
 def test_diagnostics(fixture):
     """to_diagnostics reproduces Extract.c / Conc.c's flow integrals, the
-    spanwise-averaged heights and the front location bit for bit."""
+    spanwise-averaged heights, the front location, the bed sedimentation
+    rates and, with to_deposit_integrate, the deposited heights bit for bit."""
     z, g, p, dt, o = fixture
     nc = p.nconc
     cs = [z["in_c%d" % i] for i in range(nc)]
-    d = o.diagnostics(z["in_u"], z["in_v"], z["in_w"], cs, float(z["diag_front_limit"][0]))
+    assert np.array_equal(o.interface_y_index(), z["ref_iy"])
+    cold = [z["in_cold%d" % i] for i in range(nc)]
+    dep = o.deposit_integrate(cs, cold, dt, z["in_dep0"].copy())
+    assert np.array_equal(dep, z["ref_dep"])
+    d = o.diagnostics(z["in_u"], z["in_v"], z["in_w"], cs, float(z["diag_front_limit"][0]), dep=dep)
     got = np.array([d["kinetic_energy"], d["conversion_rate"]] + d["suspended_mass"] + d["potential_energy"] +
-                   d["stokes_dissipation"] + d["conversion_rate_c"] + [d["front_location"]])
+                   d["stokes_dissipation"] + d["conversion_rate_c"] + [d["front_location"], d["viscous_dissipation"]] +
+                   d["ep_passive"] + d["ep_passive_rate"] + d["ep_rate"] + d["sed_rate"])
     assert np.array_equal(got, z["ref_diag"])
     assert np.array_equal(d["ave_height"], z["ref_ave_height"])
+    assert np.array_equal(d["sed_bottom"], z["ref_sed_bottom"])
     assert d["front_location"] > 0.0
