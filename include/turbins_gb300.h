@@ -325,15 +325,20 @@ int turb_conv3_wgrad_test(int X, int Y, int Z, int cin, int cout, const void *x,
                           float *dw, void *stream);
 
 /* ---- flow diagnostics of the current state --------------------------------
- * Replaces the reference's output-time reductions: Extract_total_kinetic_energy
- * (Extract.c:803-882), Extract_kinetic_potential_conversion_rate
- * (Extract.c:727-801), Conc_compute_total_suspended_mass (Conc.c:1471-1522),
- * Conc_compute_potential_energies (Conc.c:1934-2055; without deposited
- * sediment), Conc_compute_ave_height_x (Conc.c:1524-1608) and
- * Conc_find_front_location (Conc.c:1610-1672).  Refreshes the cell-centre
+ * Replaces the reference's output-time reductions (Output_flow_properties,
+ * Output.c:2062-2215): Extract_total_kinetic_energy (Extract.c:803-882),
+ * Extract_kinetic_potential_conversion_rate (Extract.c:727-801),
+ * Extract_viscous_dissipation_rate (Extract.c:453-725),
+ * Conc_compute_total_suspended_mass (Conc.c:1471-1522),
+ * Conc_compute_potential_energies (Conc.c:1934-2055),
+ * Conc_compute_ave_height_x (Conc.c:1524-1608), Conc_find_front_location
+ * (Conc.c:1610-1672), Conc_compute_sedimentation_rate and
+ * Conc_bottom_sed_rate (Conc.c:2098-2230).  Refreshes the cell-centre
  * velocities (and the total concentration) first, as the reference's output
  * path does.  ave_height: host array of nconc x (nx+1) spanwise-averaged
- * heights, or NULL. */
+ * heights, or NULL; sed_bottom: host array of nconc x (nz+1) x (nx+1) bed
+ * sedimentation rates, or NULL.  The passive potential energy uses the
+ * context's deposited heights (turb_deposit_*). */
 typedef struct {
     double kinetic_energy;                    /* W_kinetic_energy                       */
     double conversion_rate;                   /* -int v c_total dV                      */
@@ -342,8 +347,28 @@ typedef struct {
     double stokes_dissipation[TURB_MAXCONC];  /* W_Stokes_dissipation_rate              */
     double conversion_rate_c[TURB_MAXCONC];   /* W_kinetic_potential_conversion_rate    */
     double front_location;                    /* -1 when no crossing                    */
+    double viscous_dissipation;               /* W_dissipation_rate                     */
+    double ep_passive[TURB_MAXCONC];          /* W_Ep_passive (deposited sediment)      */
+    double ep_passive_rate[TURB_MAXCONC];     /* W_Ep_passive_rate                      */
+    double ep_rate[TURB_MAXCONC];             /* W_Ep_rate                              */
+    double sed_rate[TURB_MAXCONC];            /* W_sed_rate                             */
 } turb_diag;
-int turb_diagnostics(turb_ctx *ctx, double front_limit, turb_diag *out, double *ave_height);
+int turb_diagnostics(turb_ctx *ctx, double front_limit, turb_diag *out, double *ave_height, double *sed_bottom);
+
+/* ---- deposited sediment ---------------------------------------------------
+ * turb_bed_index: Grid_set_interface_y_index (Grid.c:1972-2012) copied out,
+ * iy[k*(nx+1) + i] = first IMMERSED c node of the column, 0 over a FLUID
+ * bottom, -1 none.  turb_deposit_integrate: Conc_integrate_deposited_height
+ * (Conc.c:1675-1749) of every fraction with weight_factor = alpha_i, from the
+ * current concentrations and those saved by turb_store_old_data.
+ * turb_deposit_enable(1) runs it at the end of every turb_step.
+ * turb_deposit_get / _set: the heights, nconc x (nz+1) x (nx+1) doubles
+ * (G_deposit_height of each fraction; restart state). */
+int turb_bed_index(turb_ctx *ctx, int32_t *iy);
+int turb_deposit_integrate(turb_ctx *ctx, double dt);
+int turb_deposit_enable(turb_ctx *ctx, int on);
+int turb_deposit_get(turb_ctx *ctx, double *host);
+int turb_deposit_set(turb_ctx *ctx, const double *host);
 
 /* operator hooks used by the parity tests: y = A x on device fields */
 int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);

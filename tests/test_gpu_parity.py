@@ -278,28 +278,79 @@ def _front_limit(h, alpha):
     return 0.05
 
 
-@pytest.mark.parametrize("name,mk", CASES + [("bump_64", lambda: _cases.bump_small(64, 40, 24))])
-def test_diagnostics(api, oracle_mod, name, mk):
-    """Flow integrals, heights and front location on the GPU against the
-    oracle (itself pinned to the reference's Extract.c / Conc.c): the device
-    sums run in block order, so agreement is to 1e-12 relative, not bitwise."""
+DIAG_CASES = CASES + [("bump_64", lambda: _cases.bump_small(64, 40, 24))]
+
+
+@pytest.mark.parametrize("name,mk", DIAG_CASES)
+def test_deposit_and_bed_index(api, oracle_mod, name, mk):
+    """Bed index and one deposited-height integration are per-node results:
+    bit-identical to the oracle."""
     case = mk()
     s = _cases.random_state(case, seed=9)
     ctx, orc, _ = _pair(case, api, oracle_mod, s)
-    cs = [s["c%d" % i] for i in range(case.params.nconc)]
+    nc = case.params.nconc
+    assert np.array_equal(ctx.bed_index(), orc.interface_y_index())
+    rng = np.random.default_rng(4)
+    cs = [s["c%d" % i] for i in range(nc)]
+    cold = [c + 0.01 * rng.standard_normal(c.shape) for c in cs]
+    dep0 = rng.uniform(0.0, 0.01, (nc, case.grid.nz + 1, case.grid.nx + 1))
+    for i in range(nc):
+        ctx.upload(api.F_C0 + i, cold[i])
+    ctx.store_old_data()
+    for i in range(nc):
+        ctx.upload(api.F_C0 + i, cs[i])
+    ctx.set_deposit(dep0)
+    ctx.deposit_integrate(case.dt)
+    assert same(ctx.deposit(), orc.deposit_integrate(cs, cold, case.dt, dep0.copy()))
+
+
+@pytest.mark.parametrize("name,mk", DIAG_CASES)
+def test_diagnostics(api, oracle_mod, name, mk):
+    """Flow integrals, heights, front location and bed rates on the GPU
+    against the oracle (itself pinned to the reference's Extract.c / Conc.c):
+    per-node terms are bit-identical, the device sums run in block order, so
+    agreement is to 1e-12 relative, not bitwise."""
+    case = mk()
+    s = _cases.random_state(case, seed=9)
+    ctx, orc, _ = _pair(case, api, oracle_mod, s)
+    nc = case.params.nconc
+    cs = [s["c%d" % i] for i in range(nc)]
+    dep = np.random.default_rng(5).uniform(0.0, 0.01, (nc, case.grid.nz + 1, case.grid.nx + 1))
+    ctx.set_deposit(dep)
     h0 = orc.diagnostics(s["u"], s["v"], s["w"], cs, 0.05)["ave_height"]
     limit = _front_limit(h0, case.params.alpha)
-    ref = orc.diagnostics(s["u"], s["v"], s["w"], cs, limit)
+    ref = orc.diagnostics(s["u"], s["v"], s["w"], cs, limit, dep=dep)
     got = ctx.diagnostics(limit)
-    for k in ("kinetic_energy", "conversion_rate"):
+    for k in ("kinetic_energy", "conversion_rate", "viscous_dissipation"):
         assert abs(got[k] - ref[k]) <= 1e-12 * abs(ref[k]) + 1e-300, k
-    for k in ("suspended_mass", "potential_energy", "stokes_dissipation", "conversion_rate_c"):
+    for k in ("suspended_mass", "potential_energy", "stokes_dissipation", "conversion_rate_c", "ep_passive",
+              "ep_passive_rate", "ep_rate", "sed_rate"):
         a, b = np.array(got[k]), np.array(ref[k])
         assert np.all(np.abs(a - b) <= 1e-12 * np.abs(b)), k
     hr = ref["ave_height"]
     assert np.abs(got["ave_height"] - hr).max() <= 1e-12 * np.abs(hr).max()
+    assert same(got["sed_bottom"], ref["sed_bottom"])
     assert ref["front_location"] > 0.0
     assert abs(got["front_location"] - ref["front_location"]) <= 1e-9
+
+
+def test_deposit_in_step(api, oracle_mod):
+    """turb_deposit_enable: two steps integrate the deposit from each step's
+    start and end concentrations, as the oracle does after its steps."""
+    case = _cases.multi_small()
+    ctx, orc, s = _pair(case, api, oracle_mod)
+    so = {k: v.copy() for k, v in s.items()}
+    nc = case.params.nconc
+    ctx.deposit_enable(True)
+    dep = np.zeros((nc, case.grid.nz + 1, case.grid.nx + 1))
+    for _ in range(2):
+        ctx.step(case.dt)
+        cold = [so["c%d" % i].copy() for i in range(nc)]
+        orc.step(so, case.dt)
+        orc.deposit_integrate([so["c%d" % i] for i in range(nc)], cold, case.dt, dep)
+    got = ctx.deposit()
+    assert dep.max() > 0.0
+    assert np.abs(got - dep).max() <= 1e-9 * dep.max()
 
 
 def test_failure_paths(api, oracle_mod):

@@ -118,6 +118,14 @@ def params_struct(p: W.Params):
     return cp
 
 
+class _Diag(C.Structure):
+    """turb_diag"""
+    _fields_ = [("ke", C.c_double), ("rate", C.c_double), ("mass", C.c_double * MAXC),
+                ("ep", C.c_double * MAXC), ("stokes", C.c_double * MAXC), ("rate_c", C.c_double * MAXC),
+                ("front", C.c_double), ("visc", C.c_double), ("epp", C.c_double * MAXC),
+                ("epp_rate", C.c_double * MAXC), ("ep_rate", C.c_double * MAXC), ("sed", C.c_double * MAXC)]
+
+
 class Context:
     """Device-resident state of one case (turb_ctx)."""
 
@@ -210,21 +218,51 @@ class Context:
         _check(self.lib.turb_pressure_guess_ratio(self.ctx, C.byref(r)), "pressure_guess_ratio")
         return r.value
 
-    def diagnostics(self, front_limit=0.1):
+    def diagnostics(self, front_limit=0.01):
         """Flow integrals of the current state (turb_diagnostics): kinetic
-        energy, conversion rates, suspended mass, potential energy and Stokes
-        dissipation per fraction, front location, spanwise-averaged heights."""
-        class _Diag(C.Structure):
-            _fields_ = [("ke", C.c_double), ("rate", C.c_double), ("mass", C.c_double * MAXC),
-                        ("ep", C.c_double * MAXC), ("stokes", C.c_double * MAXC), ("rate_c", C.c_double * MAXC),
-                        ("front", C.c_double)]
+        energy, conversion rates, viscous dissipation, and per fraction the
+        suspended mass, potential energies, Stokes dissipation and
+        sedimentation rate; front location (the reference's output path uses
+        front_limit 0.01, Output.c:2131); spanwise-averaged heights h(x) and
+        bed sedimentation rates."""
         d = _Diag()
         nc = self.params.nconc
         h = np.zeros((nc, self.grid.nx + 1))
-        _check(self.lib.turb_diagnostics(self.ctx, C.c_double(front_limit), C.byref(d), _ptr(h)), "diagnostics")
+        sb = np.zeros(self._bed_shape())
+        _check(self.lib.turb_diagnostics(self.ctx, C.c_double(front_limit), C.byref(d), _ptr(h), _ptr(sb)),
+               "diagnostics")
         return dict(kinetic_energy=d.ke, conversion_rate=d.rate, suspended_mass=list(d.mass)[:nc],
                     potential_energy=list(d.ep)[:nc], stokes_dissipation=list(d.stokes)[:nc],
-                    conversion_rate_c=list(d.rate_c)[:nc], front_location=d.front, ave_height=h)
+                    conversion_rate_c=list(d.rate_c)[:nc], front_location=d.front, viscous_dissipation=d.visc,
+                    ep_passive=list(d.epp)[:nc], ep_passive_rate=list(d.epp_rate)[:nc], ep_rate=list(d.ep_rate)[:nc],
+                    sed_rate=list(d.sed)[:nc], ave_height=h, sed_bottom=sb)
+
+    def _bed_shape(self):
+        return (self.params.nconc, self.grid.nz + 1, self.grid.nx + 1)
+
+    def bed_index(self):
+        """turb_bed_index: [nz+1][nx+1] index of the bed node of each column (-1: none)"""
+        iy = np.zeros((self.grid.nz + 1, self.grid.nx + 1), dtype=np.int32)
+        _check(self.lib.turb_bed_index(self.ctx, iy.ctypes.data_as(C.c_void_p)), "bed_index")
+        return iy
+
+    def deposit_integrate(self, dt):
+        _check(self.lib.turb_deposit_integrate(self.ctx, C.c_double(dt)), "deposit_integrate")
+
+    def deposit_enable(self, on=True):
+        """integrate the deposited heights at the end of every step"""
+        _check(self.lib.turb_deposit_enable(self.ctx, int(bool(on))), "deposit_enable")
+
+    def deposit(self):
+        out = np.zeros(self._bed_shape())
+        _check(self.lib.turb_deposit_get(self.ctx, _ptr(out)), "deposit_get")
+        return out
+
+    def set_deposit(self, dep):
+        dep = np.ascontiguousarray(dep, dtype=np.float64)
+        if dep.shape != self._bed_shape():
+            raise ValueError("deposit shape %s, expected %s" % (dep.shape, self._bed_shape()))
+        _check(self.lib.turb_deposit_set(self.ctx, _ptr(dep)), "deposit_set")
 
     def set_helmholtz_mode(self, mode, inner_sweeps=6):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")

@@ -11,6 +11,7 @@
 
 #include "../../include/turbins_gb300.h"
 #include "turb_internal.cuh"
+#include "turb_diag.cuh"
 #include "turb_kernels.cuh"
 #include "turb_mg.cuh"
 #include "turb_net.cuh"
@@ -29,12 +30,6 @@ int turb_set_cuda_error(cudaError_t e, const char *file, int line)
     return TURB_ERR_CUDA;
 }
 
-// flow diagnostics (k_diag.cu)
-long long diag_scratch_doubles(const Dims &d);
-void launch_diagnostics(cudaStream_t s, const Dims &d, const uint8_t *cst, const double *dxc, const double *dyc,
-                        const double *dzc, const double *yc, double y_ref, double coef, const double *ubc,
-                        const double *vbc, const double *wbc, const double *ct, const double *const *c, int nconc,
-                        double *scratch, double **sums, double **heights);
 
 // extra launchers defined at the end of this file
 void launch_pressure_apply(cudaStream_t s, const Dims &d, const uint8_t *st, const Geo &g, double dEta, double dXi,
@@ -137,7 +132,11 @@ struct turb_ctx {
     TurbNet *net = nullptr;
     TurbSnaps *snaps = nullptr;
     // diagnostics: cell widths dx_c, dy_c, dz_c (Grid.c:633-671) and scratch
-    double *diag_dxc = nullptr, *diag_dyc = nullptr, *diag_dzc = nullptr, *diag_yc = nullptr, *diag_scr = nullptr;
+    double *diag_dxc = nullptr, *diag_dyc = nullptr, *diag_dzc = nullptr, *diag_scr = nullptr;
+    // bed index [NZ][NX] and deposited heights [nconc][NZ][NX]
+    int32_t *bed_iy = nullptr;
+    double *dep = nullptr;
+    int deposit_on = 0;
 };
 
 namespace {
@@ -1114,22 +1113,37 @@ static std::vector<double> cell_widths(const std::vector<double> &f)
     return d;
 }
 
-int turb_diagnostics(turb_ctx *c, double front_limit, turb_diag *out, double *ave_height)
+// bed index and deposit buffer, made on first use
+static int bed_setup(turb_ctx *c)
+{
+    if (c->bed_iy) return TURB_OK;
+    const Dims &d = c->d;
+    c->bed_iy = c->mem.alloc<int32_t>((long long)d.NZ * d.NX);
+    c->dep = c->mem.alloc<double>((long long)TURB_MAXCONC * d.NZ * d.NX);
+    if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+    TURB_CHECK(cudaMemsetAsync(c->dep, 0, sizeof(double) * TURB_MAXCONC * d.NZ * d.NX, c->s));
+    launch_bed_index(c->s, d, c->st[3], c->bed_iy);
+    c->launches++;
+    return check_launch(c);
+}
+
+int turb_diagnostics(turb_ctx *c, double front_limit, turb_diag *out, double *ave_height, double *sed_bottom)
 {
     if (!c || !out) return TURB_ERR_ARG;
     const Dims &d = c->d;
     int nc = c->prm.nconc;
+    int rc = bed_setup(c);
+    if (rc) return rc;
     if (!c->diag_scr) {
         c->diag_dxc = c->mem.upload(cell_widths(c->xu));
         c->diag_dyc = c->mem.upload(cell_widths(c->yv));
         c->diag_dzc = c->mem.upload(cell_widths(c->zw));
-        c->diag_yc = c->mem.upload(c->yc);
         c->diag_scr = c->mem.alloc<double>(diag_scratch_doubles(d));
         if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
     }
     // the reference's output routines read the cell-centre velocities and the
     // total concentration of the current state (Velocity_cell_center, Conc.c:1291)
-    int rc = turb_Velocity_cell_center(c);
+    rc = turb_Velocity_cell_center(c);
     if (rc) return rc;
     const double *ct = c->fld[TURB_F_C0];
     if (nc > 1) {
@@ -1137,27 +1151,52 @@ int turb_diagnostics(turb_ctx *c, double front_limit, turb_diag *out, double *av
         if (rc) return rc;
         ct = c->fld[TURB_F_CTOT];
     }
-    const double *cf[TURB_MAXCONC];
-    for (int i = 0; i < TURB_MAXCONC; i++) cf[i] = i < nc ? c->fld[TURB_F_C0 + i] : nullptr;
+    DiagIn a;
+    memset(&a, 0, sizeof(a));
+    a.d = d;
+    a.geo = c->geo;
+    a.cst = c->st[3];
+    a.dxc = c->diag_dxc; a.dyc = c->diag_dyc; a.dzc = c->diag_dzc;
+    a.u = c->fld[TURB_F_U]; a.v = c->fld[TURB_F_V]; a.w = c->fld[TURB_F_W];
+    a.ubc = c->fld[TURB_F_UBC]; a.vbc = c->fld[TURB_F_VBC]; a.wbc = c->fld[TURB_F_WBC]; a.ct = ct;
+    a.nconc = nc;
+    for (int i = 0; i < nc; i++) {
+        a.c[i] = c->fld[TURB_F_C0 + i];
+        a.particle[i] = c->prm.ctype[i] == TURB_PARTICLE;
+        a.us[i] = std::fabs(c->prm.vs0[i]);
+    }
+    a.y_ref = c->yv[0];
     double Ly = c->yv[d.NY - 1] - c->yv[0], Lz = c->zw[d.NZ - 1] - c->zw[0];
-    double *sums = nullptr, *heights = nullptr;
-    launch_diagnostics(c->s, d, c->st[3], c->diag_dxc, c->diag_dyc, c->diag_dzc, c->diag_yc, c->yv[0],
-                       1.0 / (Ly * Lz), c->fld[TURB_F_UBC], c->fld[TURB_F_VBC], c->fld[TURB_F_WBC], ct, cf, nc,
-                       c->diag_scr, &sums, &heights);
-    c->launches += 4;
-    std::vector<double> sh(2 + 4 * TURB_MAXCONC), hh((size_t)nc * d.NX);
-    TURB_CHECK(cudaMemcpyAsync(sh.data(), sums, sh.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
-    TURB_CHECK(cudaMemcpyAsync(hh.data(), heights, hh.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    a.hcoef = 1.0 / (Ly * Lz);
+    a.Cx = 1.0 / (c->dEta * c->dEta); a.Cy = 1.0 / (c->dXi * c->dXi); a.Cz = 1.0 / (c->dPhi * c->dPhi);
+    for (int q = 0; q < 6; q++) a.kw[q] = c->prm.wall_noslip[q] ? -1.0 : 1.0;
+    a.iy = c->bed_iy;
+    a.dep = c->dep;
+    DiagOut o;
+    launch_diagnostics(c->s, a, c->diag_scr, &o);
+    c->launches += 6;
+    std::vector<double> sh(DIAG_NQ), bs(2 * TURB_MAXCONC), hh((size_t)nc * d.NX);
+    TURB_CHECK(cudaMemcpyAsync(sh.data(), o.sums, sh.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaMemcpyAsync(bs.data(), o.bed_sums, bs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaMemcpyAsync(hh.data(), o.heights, hh.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    if (sed_bottom)
+        TURB_CHECK(cudaMemcpyAsync(sed_bottom, o.sed_bottom, sizeof(double) * nc * d.NZ * d.NX,
+                                   cudaMemcpyDeviceToHost, c->s));
     TURB_CHECK(cudaStreamSynchronize(c->s));
     memset(out, 0, sizeof(*out));
     out->kinetic_energy = sh[0] * 0.5;
     out->conversion_rate = sh[1];
+    out->viscous_dissipation = sh[2] * (1.0 / c->prm.re);
     for (int i = 0; i < nc; i++) {
-        double a = c->prm.alpha[i];
-        out->suspended_mass[i] = sh[2 + 4 * i];
-        out->potential_energy[i] = sh[3 + 4 * i] * a;
-        out->stokes_dissipation[i] = sh[4 + 4 * i] * (std::fabs(c->prm.vs0[i]) * a);
-        out->conversion_rate_c[i] = sh[5 + 4 * i] * a;
+        double al = c->prm.alpha[i], us = std::fabs(c->prm.vs0[i]);
+        out->suspended_mass[i] = sh[3 + 4 * i];
+        out->potential_energy[i] = sh[4 + 4 * i] * al;
+        out->stokes_dissipation[i] = sh[5 + 4 * i] * (us * al);
+        out->conversion_rate_c[i] = sh[6 + 4 * i] * al;
+        out->ep_passive[i] = bs[2 * i];
+        out->ep_passive_rate[i] = bs[2 * i] * us;
+        out->ep_rate[i] = out->conversion_rate_c[i] + out->ep_passive_rate[i] - out->stokes_dissipation[i];
+        out->sed_rate[i] = bs[2 * i + 1];
     }
     // Conc_find_front_location, Conc.c:1610-1672: first x from the right where
     // the alpha-weighted height crosses the limit, interpolated linearly in the
@@ -1177,6 +1216,67 @@ int turb_diagnostics(turb_ctx *c, double front_limit, turb_diag *out, double *av
     }
     if (ave_height) memcpy(ave_height, hh.data(), hh.size() * sizeof(double));
     return check_launch(c);
+}
+
+int turb_bed_index(turb_ctx *c, int32_t *iy)
+{
+    if (!c || !iy) return TURB_ERR_ARG;
+    int rc = bed_setup(c);
+    if (rc) return rc;
+    TURB_CHECK(cudaMemcpyAsync(iy, c->bed_iy, sizeof(int32_t) * c->d.NZ * c->d.NX, cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_deposit_integrate(turb_ctx *c, double dt)
+{
+    if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
+    int rc = bed_setup(c);
+    if (rc) return rc;
+    DepIn a;
+    memset(&a, 0, sizeof(a));
+    a.nconc = c->prm.nconc;
+    a.dt = dt;
+    for (int i = 0; i < a.nconc; i++) {
+        a.us[i] = std::fabs(c->prm.vs0[i]);
+        a.alpha[i] = c->prm.alpha[i];
+        a.c[i] = c->fld[TURB_F_C0 + i];
+        a.c_old[i] = c->old[3 + i];
+    }
+    launch_deposit(c->s, c->d, c->bed_iy, a, c->dep);
+    c->launches++;
+    return check_launch(c);
+}
+
+int turb_deposit_enable(turb_ctx *c, int on)
+{
+    if (!c) return TURB_ERR_ARG;
+    int rc = bed_setup(c);
+    if (rc) return rc;
+    c->deposit_on = on ? 1 : 0;
+    return TURB_OK;
+}
+
+int turb_deposit_get(turb_ctx *c, double *host)
+{
+    if (!c || !host) return TURB_ERR_ARG;
+    int rc = bed_setup(c);
+    if (rc) return rc;
+    size_t b = sizeof(double) * c->prm.nconc * c->d.NZ * c->d.NX;
+    TURB_CHECK(cudaMemcpyAsync(host, c->dep, b, cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_deposit_set(turb_ctx *c, const double *host)
+{
+    if (!c || !host) return TURB_ERR_ARG;
+    int rc = bed_setup(c);
+    if (rc) return rc;
+    size_t b = sizeof(double) * c->prm.nconc * c->d.NZ * c->d.NX;
+    TURB_CHECK(cudaMemcpyAsync(c->dep, host, b, cudaMemcpyHostToDevice, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
 }
 
 int turb_Conc_compute_total_concentration(turb_ctx *c)
@@ -1755,6 +1855,7 @@ int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
         STEP_TRY(turb_Pressure_compute_velocity_divergence(c, &st->div_max[stage]));
     }
     STEP_TRY(turb_rk_average(c, 0.5, 0.5));
+    if (c->deposit_on) STEP_TRY(turb_deposit_integrate(c, dt));
     st->kernel_launches = (int)(c->launches - l0);
     return TURB_OK;
 }
