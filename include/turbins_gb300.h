@@ -34,7 +34,9 @@ typedef enum {
     TURB_ERR_NOT_CONVERGED = 3,  /* solver reached max_iter (cf. Solver.c:326-348) */
     TURB_ERR_NAN = 4,            /* non-finite residual                     */
     TURB_ERR_ALLOC = 5,          /* device allocation failed                */
-    TURB_ERR_SCRATCH_LIMIT = 6   /* grid larger than the fixed scratch of turb_velocity_divergence_noalloc */
+    TURB_ERR_SCRATCH_LIMIT = 6,  /* grid larger than the fixed scratch of turb_velocity_divergence_noalloc */
+    TURB_ERR_IO = 7,             /* a restart file could not be opened, written or read in full */
+    TURB_ERR_FORMAT = 8          /* a restart file does not hold what the context expects */
 } turb_status;
 
 /* node status codes, Include/definitions.h:93-99 */
@@ -369,6 +371,43 @@ int turb_deposit_integrate(turb_ctx *ctx, double dt);
 int turb_deposit_enable(turb_ctx *ctx, int on);
 int turb_deposit_get(turb_ctx *ctx, double *host);
 int turb_deposit_set(turb_ctx *ctx, const double *host);
+
+/* ---- checkpoint / resume ---------------------------------------------------
+ * The reference's restart set (Resume_set_data, Resume.c:208-244) in its
+ * formats, written to / read from directory dir:
+ *   Resume_u.bin, Resume_v.bin, Resume_w.bin, Resume_dpdx.bin, Resume_dpdy.bin,
+ *   Resume_dpdz.bin, [Resume_gridc.bin], Resume_conc<i>.bin: PETSc binary
+ *   vectors (VecView / VecLoadIntoVector: int32 {1211214, N}, N doubles, all
+ *   big-endian) in the DA order [k][j][i];
+ *   Resume_primary.dat: Resume_write_primary_data's text (time, dt, dt_old,
+ *   iteration, output_iter);
+ * and, with flags:
+ *   TURB_RESUME_GRID: Resume_gridc.bin, the c node status as FP64 codes (on
+ *     read it must equal the context's geometry, else TURB_ERR_FORMAT);
+ *   TURB_RESUME_DEPOSIT: Resume_deposit_height<i>.bin per particle fraction,
+ *     Resume_write_2D_data's raw [NZ][NX] doubles (the reference ships no
+ *     caller of it; the name is this library's);
+ *   TURB_RESUME_PHI: Resume_phi.bin, the last pressure (not in the
+ *     reference's set; with it a resumed run repeats the uninterrupted one
+ *     bit for bit).  Without it, reading sets the pressure to 0 as a fresh
+ *     reference process has it.
+ * Reading resets the pressure-guess history.  The host helpers work without a
+ * GPU. */
+#define TURB_RESUME_GRID 1
+#define TURB_RESUME_DEPOSIT 2
+#define TURB_RESUME_PHI 4
+typedef struct {
+    double time, dt, dt_old;
+    int iter, output_iter;
+} turb_primary;
+int turb_resume_write(turb_ctx *ctx, const char *dir, const turb_primary *prim, int flags);
+int turb_resume_read(turb_ctx *ctx, const char *dir, turb_primary *prim, int flags);
+int turb_petsc_vec_write(const char *path, const double *data, long long n);
+int turb_petsc_vec_read(const char *path, double *data, long long n);
+int turb_resume_primary_write(const char *dir, const turb_primary *prim);
+int turb_resume_primary_read(const char *dir, turb_primary *prim);
+int turb_resume_2d_write(const char *path, const double *data, int nx, int nz);
+int turb_resume_2d_read(const char *path, double *data, int nx, int nz);
 
 /* operator hooks used by the parity tests: y = A x on device fields */
 int turb_helmholtz_apply(turb_ctx *ctx, char which, int ic, double dt, int field_x, int field_y);

@@ -21,7 +21,9 @@
 #include "Pressure.h"
 #include "Extract.h"
 #include "Memory.h"
+#include "Resume.h"
 #include <string.h>
+#include <unistd.h>
 
 typedef struct {
     MAC_grid *g;
@@ -415,4 +417,88 @@ void ref_diagnostics(ref_case *r, const double *u, const double *v, const double
     out[2 + 4 * nc] = Conc_find_front_location(r->c, g, p, front_limit);
     if (h_ave)
         for (i = 0; i < nc; i++) memcpy(h_ave + (long)i * NX, r->c[i]->W_ave_height_x, sizeof(double) * NX);
+}
+
+/* ---- restart files through Resume.c --------------------------------------
+ * Resume_set_data / Resume_write_data / Resume_write_primary_data in the
+ * directory dir (the reference writes to the working directory), and
+ * Resume_write_2D_data of each fraction's deposited height to
+ * "Resume_deposit_height<i>.bin" (the reference ships no caller of it; the
+ * name is this harness's).  fields: u, v, w, dp_dx, dp_dy, dp_dz, c_0.. */
+static Resume *resume_of(ref_case *r, int grid_flag, GVG_bag *bag)
+{
+    Resume *rs = Resume_create(6 + r->p->NConc + (grid_flag ? 1 : 0));
+    Resume_reset_read_flag(rs);
+    Resume_reset_write_flag(rs);
+    if (grid_flag) Resume_set_IO_grid_flag(rs); else Resume_reset_IO_grid_flag(rs);
+    memset(bag, 0, sizeof(*bag));
+    bag->u = r->u; bag->v = r->v; bag->w = r->w; bag->p = r->pr; bag->c = r->c;
+    bag->grid = r->g; bag->params = r->p;
+    Resume_set_data(rs, bag);
+    return rs;
+}
+
+static void dep_name(char *s, int ic) { sprintf(s, "Resume_deposit_height%d.bin", ic); }
+
+int ref_resume_write(ref_case *r, const char *dir, const double *const *fields, int grid_flag, double time,
+                     double dt, double dt_old, int iter, int output_iter, const double *dep)
+{
+    char cwd[4096], name[64];
+    GVG_bag bag;
+    Resume *rs;
+    int i, k, ic, nc = r->p->NConc;
+    MAC_grid *g = r->g;
+    Vec *v[6];
+    if (!getcwd(cwd, sizeof(cwd)) || chdir(dir)) return 1;
+    v[0] = &r->u->G_data; v[1] = &r->v->G_data; v[2] = &r->w->G_data;
+    v[3] = &r->pr->G_dp_dx; v[4] = &r->pr->G_dp_dy; v[5] = &r->pr->G_dp_dz;
+    for (i = 0; i < 6; i++) vset(*v[i], fields[i], r->n);
+    for (i = 0; i < nc; i++) vset(r->c[i]->G_data, fields[6 + i], r->n);
+    rs = resume_of(r, grid_flag, &bag);
+    bag.time = time; bag.dt = dt; bag.dt_old = dt_old; bag.iter = iter; bag.output_iter = output_iter;
+    Resume_write_data(rs);
+    Resume_write_primary_data(rs, &bag);
+    if (dep)   /* G_deposit_height exists for particle fractions only (Conc.c:188-199) */
+        for (ic = 0; ic < nc; ic++) {
+            Concentration *cc = r->c[ic];
+            if (cc->Type != PARTICLE) continue;
+            set_deposit(r, ic, dep);
+            dep_name(name, ic);
+            Resume_write_2D_data(rs, cc->G_deposit_height, name, g->NX, g->NZ);
+        }
+    (void)k;
+    Resume_destroy(rs);
+    return chdir(cwd) ? 1 : 0;
+}
+
+/* the reverse: Resume_read_data, Resume_read_primary_data and
+ * Resume_read_2D_data; prim = {time, dt, dt_old, iter, output_iter} */
+int ref_resume_read(ref_case *r, const char *dir, double *const *fields, int grid_flag, double *prim, double *dep)
+{
+    char cwd[4096], name[64];
+    GVG_bag bag;
+    Resume *rs;
+    int i, k, x, ic, nc = r->p->NConc;
+    MAC_grid *g = r->g;
+    if (!getcwd(cwd, sizeof(cwd)) || chdir(dir)) return 1;
+    rs = resume_of(r, grid_flag, &bag);
+    Resume_read_data(rs);
+    Resume_read_primary_data(rs, &bag);
+    vget(r->u->G_data, fields[0], r->n); vget(r->v->G_data, fields[1], r->n); vget(r->w->G_data, fields[2], r->n);
+    vget(r->pr->G_dp_dx, fields[3], r->n); vget(r->pr->G_dp_dy, fields[4], r->n);
+    vget(r->pr->G_dp_dz, fields[5], r->n);
+    for (i = 0; i < nc; i++) vget(r->c[i]->G_data, fields[6 + i], r->n);
+    prim[0] = bag.time; prim[1] = bag.dt; prim[2] = bag.dt_old; prim[3] = bag.iter; prim[4] = bag.output_iter;
+    if (dep)
+        for (ic = 0; ic < nc; ic++) {
+            Concentration *cc = r->c[ic];
+            set_deposit(r, ic, NULL);
+            if (cc->Type != PARTICLE) continue;
+            dep_name(name, ic);
+            Resume_read_2D_data(rs, cc->G_deposit_height, name, g->NX, g->NZ);
+            for (k = 0; k < g->NZ; k++)
+                for (x = 0; x < g->NX; x++) dep[((long)ic * g->NZ + k) * g->NX + x] = cc->G_deposit_height[k][x];
+        }
+    Resume_destroy(rs);
+    return chdir(cwd) ? 1 : 0;
 }

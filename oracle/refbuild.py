@@ -19,7 +19,8 @@ REF = os.environ.get("TURB_REFERENCE_ROOT", "/root/reference")
 SRC = os.path.join(REF, "src")
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libturbins_ref.so")
-FILES = ["ENO", "Velocity", "Conc", "Pressure", "Grid", "Immersed", "MyMath", "Memory", "Communication", "Extract"]
+FILES = ["ENO", "Velocity", "Conc", "Pressure", "Grid", "Immersed", "MyMath", "Memory", "Communication", "Extract",
+         "Resume"]
 CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w"]
 
 

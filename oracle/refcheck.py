@@ -126,6 +126,32 @@ class Reference:
         self.lib.ref_deposit_integrate(self.h, a, b, C.c_double(dt), _p(dep))
         return dep
 
+    def resume_write(self, dirname, state, prim, grid=False, dep=None):
+        """Resume_write_data / Resume_write_primary_data / Resume_write_2D_data
+        of state (u, v, w, dpx, dpy, dpz, c0..) into dirname"""
+        nc = self.p.nconc
+        keys = ["u", "v", "w", "dpx", "dpy", "dpz"] + ["c%d" % i for i in range(nc)]
+        arrs = [np.ascontiguousarray(state[k], dtype=np.float64) for k in keys]
+        ptrs = (_dp * len(arrs))(*[_p(a) for a in arrs])
+        dp = None if dep is None else _p(np.ascontiguousarray(dep))
+        rc = self.lib.ref_resume_write(self.h, dirname.encode(), ptrs, C.c_int(int(grid)), C.c_double(prim["time"]),
+                                       C.c_double(prim["dt"]), C.c_double(prim["dt_old"]), C.c_int(prim["iter"]),
+                                       C.c_int(prim["output_iter"]), dp)
+        assert rc == 0
+
+    def resume_read(self, dirname, grid=False, dep=True):
+        nc = self.p.nconc
+        keys = ["u", "v", "w", "dpx", "dpy", "dpz"] + ["c%d" % i for i in range(nc)]
+        arrs = [self._z() for _ in keys]
+        ptrs = (_dp * len(arrs))(*[_p(a) for a in arrs])
+        prim = np.zeros(5)
+        d = np.zeros((nc, self.g.nz + 1, self.g.nx + 1)) if dep else None
+        rc = self.lib.ref_resume_read(self.h, dirname.encode(), ptrs, C.c_int(int(grid)), _p(prim),
+                                      None if d is None else _p(d))
+        assert rc == 0
+        out = dict(zip(keys, arrs))
+        return out, dict(time=prim[0], dt=prim[1], dt_old=prim[2], iter=int(prim[3]), output_iter=int(prim[4])), d
+
     def diagnostics(self, u, v, w, cs, front_limit=0.01, dep=None):
         nc = len(cs)
         arr = (_dp * 4)()

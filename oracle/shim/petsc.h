@@ -162,6 +162,7 @@ int PCFactorSetFill(PC pc, PetscReal f);
 int PCFactorSetUseDropTolerance(PC pc, PetscReal a, PetscReal b, int c);
 int PetscViewerBinaryOpen(MPI_Comm c, const char *name, PetscFileMode m, PetscViewer *v);
 int PetscViewerDestroy(PetscViewer v);
+int VecLoadIntoVector(PetscViewer v, Vec x);
 
 /* shim-only access used by the harness */
 double *shim_vec_data(Vec v);

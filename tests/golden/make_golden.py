@@ -120,7 +120,32 @@ def dump(name, case):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=np.array(json.dumps(meta)), **out)
 
 
+# restart set written by the reference's Resume.c (through the harness) for
+# the 16x8x8 bump case: the files themselves are the fixture
+RESUME_CASE = dict(nx=16, ny=8, nz=8, seed=31)
+RESUME_PRIM = dict(time=0.1234567891, dt=2.5e-4, dt_old=2.4e-4, iter=17, output_iter=3)
+
+
+def resume_case():
+    c = RESUME_CASE
+    return _cases.bump_small(c["nx"], c["ny"], c["nz"])
+
+
+def dump_resume():
+    case = resume_case()
+    g, p = case.grid, case.params
+    s = _cases.random_state(case, seed=RESUME_CASE["seed"])
+    dep = np.random.Generator(np.random.PCG64(2)).uniform(0.0, 0.01, (p.nconc, g.nz + 1, g.nx + 1))
+    d = os.path.join(HERE, "resume_bump")
+    os.makedirs(d, exist_ok=True)
+    Reference(g, p).resume_write(d, s, RESUME_PRIM, grid=True, dep=dep)
+    with open(os.path.join(d, "case.json"), "w") as f:
+        json.dump(dict(case=RESUME_CASE, prim=RESUME_PRIM), f)
+
+
 if __name__ == "__main__":
     for nm, mk in CASES.items():
         dump(nm, mk())
         print("wrote", nm)
+    dump_resume()
+    print("wrote resume_bump")

@@ -28,7 +28,8 @@ HMODE_FP64, HMODE_MIXED = 0, 1
 GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
-          5: "device allocation failed", 6: "scratch limit"}
+          5: "device allocation failed", 6: "scratch limit", 7: "restart file I/O", 8: "restart file mismatch"}
+RESUME_GRID, RESUME_DEPOSIT, RESUME_PHI = 1, 2, 4
 
 
 class TurbError(RuntimeError):
@@ -116,6 +117,54 @@ def params_struct(p: W.Params):
     cp.vel_rtol, cp.vel_maxit = p.vel_rtol, p.vel_maxit
     cp.p_rtol, cp.p_maxit = p.p_rtol, p.p_maxit
     return cp
+
+
+class Primary(C.Structure):
+    """turb_primary: the scalars of Resume_primary.dat"""
+    _fields_ = [("time", C.c_double), ("dt", C.c_double), ("dt_old", C.c_double), ("iter", C.c_int),
+                ("output_iter", C.c_int)]
+
+    @classmethod
+    def of(cls, d):
+        return cls(d["time"], d["dt"], d["dt_old"], int(d["iter"]), int(d["output_iter"]))
+
+    def as_dict(self):
+        return dict(time=self.time, dt=self.dt, dt_old=self.dt_old, iter=self.iter, output_iter=self.output_iter)
+
+
+def petsc_vec_write(path, a):
+    """a PETSc binary vector file (the reference's Resume_*.bin), no GPU needed"""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    _check(load_library().turb_petsc_vec_write(os.fsencode(path), _ptr(a), C.c_longlong(a.size)), "petsc_vec_write")
+
+
+def petsc_vec_read(path, shape):
+    a = np.zeros(shape)
+    _check(load_library().turb_petsc_vec_read(os.fsencode(path), _ptr(a), C.c_longlong(a.size)), "petsc_vec_read")
+    return a
+
+
+def resume_primary_write(dirname, prim):
+    _check(load_library().turb_resume_primary_write(os.fsencode(dirname), C.byref(Primary.of(prim))),
+           "resume_primary_write")
+
+
+def resume_primary_read(dirname):
+    q = Primary()
+    _check(load_library().turb_resume_primary_read(os.fsencode(dirname), C.byref(q)), "resume_primary_read")
+    return q.as_dict()
+
+
+def resume_2d_write(path, a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    nz, nx = a.shape
+    _check(load_library().turb_resume_2d_write(os.fsencode(path), _ptr(a), nx, nz), "resume_2d_write")
+
+
+def resume_2d_read(path, nz, nx):
+    a = np.zeros((nz, nx))
+    _check(load_library().turb_resume_2d_read(os.fsencode(path), _ptr(a), nx, nz), "resume_2d_read")
+    return a
 
 
 class _Diag(C.Structure):
@@ -263,6 +312,19 @@ class Context:
         if dep.shape != self._bed_shape():
             raise ValueError("deposit shape %s, expected %s" % (dep.shape, self._bed_shape()))
         _check(self.lib.turb_deposit_set(self.ctx, _ptr(dep)), "deposit_set")
+
+    def resume_write(self, dirname, prim, grid=False, deposit=False, phi=False):
+        """turb_resume_write: the reference's restart set (+ options) into dirname"""
+        flags = (RESUME_GRID if grid else 0) | (RESUME_DEPOSIT if deposit else 0) | (RESUME_PHI if phi else 0)
+        _check(self.lib.turb_resume_write(self.ctx, os.fsencode(dirname), C.byref(Primary.of(prim)), flags),
+               "resume_write")
+
+    def resume_read(self, dirname, grid=False, deposit=False, phi=False):
+        """turb_resume_read: state from a restart set; returns the primary scalars"""
+        flags = (RESUME_GRID if grid else 0) | (RESUME_DEPOSIT if deposit else 0) | (RESUME_PHI if phi else 0)
+        q = Primary()
+        _check(self.lib.turb_resume_read(self.ctx, os.fsencode(dirname), C.byref(q), flags), "resume_read")
+        return q.as_dict()
 
     def set_helmholtz_mode(self, mode, inner_sweeps=6):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")

@@ -7,11 +7,21 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/turbins_gb300.h"
 #include "turb_internal.cuh"
 #include "turb_diag.cuh"
+
+// restart files (k_resume.cu, turb_resume.cu)
+void launch_pack_be(cudaStream_t s, const Dims &d, const double *src, unsigned long long *dst);
+void launch_pack_status_be(cudaStream_t s, const Dims &d, const uint8_t *st, unsigned long long *dst);
+void launch_unpack_be(cudaStream_t s, const Dims &d, const unsigned long long *src, double *dst);
+int petsc_vec_write_be(const char *path, const void *be_words, long long n);
+int petsc_vec_read_be(const char *path, void *be_words, long long n);
+std::string resume_path(const char *dir, const char *name);
 #include "turb_kernels.cuh"
 #include "turb_mg.cuh"
 #include "turb_net.cuh"
@@ -137,6 +147,9 @@ struct turb_ctx {
     int32_t *bed_iy = nullptr;
     double *dep = nullptr;
     int deposit_on = 0;
+    // restart staging: one field as big-endian words, on the device and pinned
+    unsigned long long *rs_dev = nullptr;
+    void *rs_host = nullptr;
 };
 
 namespace {
@@ -794,6 +807,8 @@ const char *turb_status_string(int status)
     case TURB_ERR_NAN: return "non-finite residual";
     case TURB_ERR_ALLOC: return "device allocation failed";
     case TURB_ERR_SCRATCH_LIMIT: return "grid larger than the static scratch of the no-allocation entry point";
+    case TURB_ERR_IO: return "restart file could not be opened, written or read";
+    case TURB_ERR_FORMAT: return "restart file does not match the context";
     default: return "unknown status";
     }
 }
@@ -932,6 +947,7 @@ int turb_destroy(turb_ctx *c)
         if (e) cudaEventDestroy(e);
     c->mem.release();
     if (c->hscal) cudaFreeHost(c->hscal);
+    if (c->rs_host) cudaFreeHost(c->rs_host);
     cudaStreamDestroy(c->s);
     delete c;
     return TURB_OK;
@@ -1277,6 +1293,110 @@ int turb_deposit_set(turb_ctx *c, const double *host)
     TURB_CHECK(cudaMemcpyAsync(c->dep, host, b, cudaMemcpyHostToDevice, c->s));
     TURB_CHECK(cudaStreamSynchronize(c->s));
     return TURB_OK;
+}
+
+// the restart set of Resume_set_data (Resume.c:208-244): file name, field
+static std::vector<std::pair<std::string, int>> resume_set(const turb_ctx *c)
+{
+    std::vector<std::pair<std::string, int>> v = {
+        {"Resume_u.bin", TURB_F_U},       {"Resume_v.bin", TURB_F_V},       {"Resume_w.bin", TURB_F_W},
+        {"Resume_dpdx.bin", TURB_F_DPX}, {"Resume_dpdy.bin", TURB_F_DPY}, {"Resume_dpdz.bin", TURB_F_DPZ}};
+    for (int ic = 0; ic < c->prm.nconc; ic++) v.push_back({"Resume_conc" + std::to_string(ic) + ".bin", TURB_F_C0 + ic});
+    return v;
+}
+
+static int resume_staging(turb_ctx *c)
+{
+    const Dims &d = c->d;
+    long long n = (long long)d.NX * d.NY * d.NZ;
+    if (!c->rs_dev) {
+        c->rs_dev = c->mem.alloc<unsigned long long>(n);
+        if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+    }
+    if (!c->rs_host) TURB_CHECK(cudaMallocHost(&c->rs_host, (size_t)n * 8));
+    return TURB_OK;
+}
+
+static std::string dep_name(int ic) { return "Resume_deposit_height" + std::to_string(ic) + ".bin"; }
+
+int turb_resume_write(turb_ctx *c, const char *dir, const turb_primary *prim, int flags)
+{
+    if (!c || !prim) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    long long n = (long long)d.NX * d.NY * d.NZ;
+    int rc = resume_staging(c);
+    if (rc) return rc;
+    auto put = [&](const std::string &name, const double *f, const uint8_t *st) -> int {
+        if (f) launch_pack_be(c->s, d, f, c->rs_dev);
+        else launch_pack_status_be(c->s, d, st, c->rs_dev);
+        c->launches++;
+        TURB_CHECK(cudaMemcpyAsync(c->rs_host, c->rs_dev, (size_t)n * 8, cudaMemcpyDeviceToHost, c->s));
+        TURB_CHECK(cudaStreamSynchronize(c->s));
+        return petsc_vec_write_be(resume_path(dir, name.c_str()).c_str(), c->rs_host, n);
+    };
+    for (auto &e : resume_set(c))
+        if ((rc = put(e.first, c->fld[e.second], nullptr))) return rc;
+    if ((flags & TURB_RESUME_GRID) && (rc = put("Resume_gridc.bin", nullptr, c->st[3]))) return rc;
+    if ((flags & TURB_RESUME_PHI) && (rc = put("Resume_phi.bin", c->fld[TURB_F_PHI], nullptr))) return rc;
+    if ((rc = turb_resume_primary_write(dir, prim))) return rc;
+    if (flags & TURB_RESUME_DEPOSIT) {
+        std::vector<double> h((size_t)c->prm.nconc * d.NZ * d.NX);
+        if ((rc = turb_deposit_get(c, h.data()))) return rc;
+        for (int ic = 0; ic < c->prm.nconc; ic++)
+            if (c->prm.ctype[ic] == TURB_PARTICLE &&
+                (rc = turb_resume_2d_write(resume_path(dir, dep_name(ic).c_str()).c_str(),
+                                           h.data() + (size_t)ic * d.NZ * d.NX, d.NX, d.NZ)))
+                return rc;
+    }
+    return check_launch(c);
+}
+
+int turb_resume_read(turb_ctx *c, const char *dir, turb_primary *prim, int flags)
+{
+    if (!c || !prim) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    long long n = (long long)d.NX * d.NY * d.NZ;
+    int rc = resume_staging(c);
+    if (rc) return rc;
+    auto get = [&](const std::string &name, double *f) -> int {
+        int r = petsc_vec_read_be(resume_path(dir, name.c_str()).c_str(), c->rs_host, n);
+        if (r) return r;
+        TURB_CHECK(cudaMemcpyAsync(c->rs_dev, c->rs_host, (size_t)n * 8, cudaMemcpyHostToDevice, c->s));
+        launch_unpack_be(c->s, d, c->rs_dev, f);
+        c->launches++;
+        TURB_CHECK(cudaStreamSynchronize(c->s));   // the staging buffers are reused by the next file
+        return TURB_OK;
+    };
+    turb_primary q;
+    if ((rc = turb_resume_primary_read(dir, &q))) return rc;
+    if (flags & TURB_RESUME_GRID) {
+        std::vector<unsigned long long> file((size_t)n);
+        if ((rc = petsc_vec_read_be(resume_path(dir, "Resume_gridc.bin").c_str(), file.data(), n))) return rc;
+        launch_pack_status_be(c->s, d, c->st[3], c->rs_dev);
+        c->launches++;
+        TURB_CHECK(cudaMemcpyAsync(c->rs_host, c->rs_dev, (size_t)n * 8, cudaMemcpyDeviceToHost, c->s));
+        TURB_CHECK(cudaStreamSynchronize(c->s));
+        if (memcmp(file.data(), c->rs_host, (size_t)n * 8) != 0) return TURB_ERR_FORMAT;
+    }
+    for (auto &e : resume_set(c))
+        if ((rc = get(e.first, c->fld[e.second]))) return rc;
+    if (flags & TURB_RESUME_PHI) {
+        if ((rc = get("Resume_phi.bin", c->fld[TURB_F_PHI]))) return rc;
+    } else {
+        TURB_CHECK(cudaMemsetAsync(c->fld[TURB_F_PHI], 0, sizeof(double) * d.n, c->s));
+    }
+    if (flags & TURB_RESUME_DEPOSIT) {
+        std::vector<double> h((size_t)c->prm.nconc * d.NZ * d.NX, 0.0);
+        for (int ic = 0; ic < c->prm.nconc; ic++)
+            if (c->prm.ctype[ic] == TURB_PARTICLE &&
+                (rc = turb_resume_2d_read(resume_path(dir, dep_name(ic).c_str()).c_str(),
+                                          h.data() + (size_t)ic * d.NZ * d.NX, d.NX, d.NZ)))
+                return rc;
+        if ((rc = turb_deposit_set(c, h.data()))) return rc;
+    }
+    c->nh[0] = c->nh[1] = 0;
+    *prim = q;
+    return check_launch(c);
 }
 
 int turb_Conc_compute_total_concentration(turb_ctx *c)
