@@ -151,6 +151,10 @@ int turb_pressure_guess_ratio(turb_ctx *ctx, double *geo_mean);
  * coarse-grid correction, for the current pressure mode (defaults: 4 / 4 with
  * FP64 V-cycles, 6 / 6 with FP32 V-cycles; 1..8) */
 int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
+/* storage order of the FP32 multigrid levels: 1 (default) colour-split (red
+ * and black cells in separate halves, dense half sweeps), 0 natural.  The
+ * arithmetic is the same, so results are bit-identical either way. */
+int turb_set_mg_split(turb_ctx *ctx, int on);
 /* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 1 (default) divides by a grid spacing through its

@@ -212,6 +212,26 @@ def test_pressure_solve(api, oracle_mod, name, mk, mode):
     assert ctx.Pressure_compute_velocity_divergence() <= 1e-10
 
 
+@pytest.mark.parametrize("name,mk", CASES + [("bump_64", lambda: _cases.bump_small(64, 40, 24))])
+def test_mg_split_storage_is_bit_identical(api, oracle_mod, name, mk):
+    """The FP32 multigrid levels' colour-split storage changes only where
+    values live: the mixed-precision solve gives the same iterates bit for
+    bit as with natural storage."""
+    case = mk()
+    s = _cases.random_state(case, seed=11)
+    out = []
+    for split in (False, True):
+        ctx, orc, _ = _pair(case, api, oracle_mod, s)
+        ctx.set_pressure_mode(api.PMODE_MIXED)
+        ctx.set_mg_split(split)
+        ctx.Pressure_set_RHS(case.dt)
+        it, rr = ctx.Pressure_solve()
+        out.append((it, rr, ctx.download(api.F_PHI)))
+        ctx.close()
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert same(out[0][2], out[1][2])
+
+
 @pytest.mark.parametrize("name,mk", CASES[:3])
 @pytest.mark.parametrize("hmode", [0, 1])
 def test_helmholtz_solve(api, oracle_mod, name, mk, hmode):

@@ -262,6 +262,10 @@ class Context:
     def set_mg_sweeps(self, npre, npost):
         _check(self.lib.turb_set_mg_sweeps(self.ctx, npre, npost), "set_mg_sweeps")
 
+    def set_mg_split(self, on):
+        """colour-split (True) or natural (False) storage of the FP32 multigrid levels"""
+        _check(self.lib.turb_set_mg_split(self.ctx, int(bool(on))), "set_mg_split")
+
     def pressure_guess_ratio(self):
         r = C.c_double()
         _check(self.lib.turb_pressure_guess_ratio(self.ctx, C.byref(r)), "pressure_guess_ratio")

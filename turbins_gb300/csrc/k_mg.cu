@@ -23,7 +23,19 @@ struct LevelT {
     int nx, ny, nz;
     const T *dx, *dy, *dz, *rfx, *rfy, *rfz;
     T pin;
+    int split;
+    long long half;
+    // storage index of cell c = (i, j, k)
+    __device__ __forceinline__ long long at(long long c, int i, int j, int k) const
+    {
+        return split ? ((long long)((i + j + k) & 1) * half + (c >> 1)) : c;
+    }
 };
+
+__device__ __forceinline__ long long lev_at(const MgDevLevel &L, long long c, int i, int j, int k)
+{
+    return L.split ? ((long long)((i + j + k) & 1) * (((long long)L.nx * L.ny * L.nz) >> 1) + (c >> 1)) : c;
+}
 
 template <typename T>
 __device__ __forceinline__ LevelT<T> lev_of(const MgDevLevel &L);
@@ -31,15 +43,26 @@ __device__ __forceinline__ LevelT<T> lev_of(const MgDevLevel &L);
 template <>
 __device__ __forceinline__ LevelT<double> lev_of<double>(const MgDevLevel &L)
 {
-    LevelT<double> o{L.nx, L.ny, L.nz, L.dxd, L.dyd, L.dzd, L.rfxd, L.rfyd, L.rfzd, L.pin};
+    LevelT<double> o{L.nx, L.ny, L.nz, L.dxd, L.dyd, L.dzd, L.rfxd, L.rfyd, L.rfzd, L.pin, L.split,
+                     ((long long)L.nx * L.ny * L.nz) >> 1};
     return o;
 }
 template <>
 __device__ __forceinline__ LevelT<float> lev_of<float>(const MgDevLevel &L)
 {
-    LevelT<float> o{L.nx, L.ny, L.nz, L.dxf, L.dyf, L.dzf, L.rfxf, L.rfyf, L.rfzf, (float)L.pin};
+    LevelT<float> o{L.nx, L.ny, L.nz, L.dxf, L.dyf, L.dzf, L.rfxf, L.rfyf, L.rfzf, (float)L.pin, L.split,
+                    ((long long)L.nx * L.ny * L.nz) >> 1};
     return o;
 }
+
+// explicitly rounded arithmetic, so that every smoother variant (natural,
+// colour-split, vectorised) evaluates a row with the same operations
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 // S x - evaluated as  diag*x_p - sum f*x_nb ; returns (offsum, diag)
 template <typename T>
@@ -48,15 +71,15 @@ __device__ __forceinline__ void s_row(const LevelT<T> &L, const T *__restrict__ 
 {
     long long nx = L.nx, nxy = (long long)L.nx * L.ny;
     long long c = ((long long)k * L.ny + j) * nx + i;
-    T dyz = L.dy[j] * L.dz[k], dxz = L.dx[i] * L.dz[k], dxy = L.dx[i] * L.dy[j];
+    T dyz = rmul(L.dy[j], L.dz[k]), dxz = rmul(L.dx[i], L.dz[k]), dxy = rmul(L.dx[i], L.dy[j]);
     T o = 0, d = 0, f;
-    if (i > 0) { f = dyz * L.rfx[i]; d += f; o += f * x[c - 1]; }
-    if (i < L.nx - 1) { f = dyz * L.rfx[i + 1]; d += f; o += f * x[c + 1]; }
-    if (j > 0) { f = dxz * L.rfy[j]; d += f; o += f * x[c - nx]; }
-    if (j < L.ny - 1) { f = dxz * L.rfy[j + 1]; d += f; o += f * x[c + nx]; }
-    if (k > 0) { f = dxy * L.rfz[k]; d += f; o += f * x[c - nxy]; }
-    if (k < L.nz - 1) { f = dxy * L.rfz[k + 1]; d += f; o += f * x[c + nxy]; }
-    if (i == L.nx - 1 && j == L.ny - 1 && k == L.nz - 1) d += L.pin;
+    if (i > 0) { f = rmul(dyz, L.rfx[i]); d = radd(d, f); o = rfma(f, x[L.at(c - 1, i - 1, j, k)], o); }
+    if (i < L.nx - 1) { f = rmul(dyz, L.rfx[i + 1]); d = radd(d, f); o = rfma(f, x[L.at(c + 1, i + 1, j, k)], o); }
+    if (j > 0) { f = rmul(dxz, L.rfy[j]); d = radd(d, f); o = rfma(f, x[L.at(c - nx, i, j - 1, k)], o); }
+    if (j < L.ny - 1) { f = rmul(dxz, L.rfy[j + 1]); d = radd(d, f); o = rfma(f, x[L.at(c + nx, i, j + 1, k)], o); }
+    if (k > 0) { f = rmul(dxy, L.rfz[k]); d = radd(d, f); o = rfma(f, x[L.at(c - nxy, i, j, k - 1)], o); }
+    if (k < L.nz - 1) { f = rmul(dxy, L.rfz[k + 1]); d = radd(d, f); o = rfma(f, x[L.at(c + nxy, i, j, k + 1)], o); }
+    if (i == L.nx - 1 && j == L.ny - 1 && k == L.nz - 1) d = radd(d, L.pin);
     off = o;
     dg = d;
 }
@@ -76,7 +99,7 @@ __global__ void k_invdiag(MgDevLevel Ld, T *__restrict__ invd)
         if (k > 0) d += dxy * L.rfz[k];
         if (k < L.nz - 1) d += dxy * L.rfz[k + 1];
         if (i == L.nx - 1 && j == L.ny - 1 && k == L.nz - 1) d += L.pin;
-        invd[c] = T(1) / d;
+        invd[L.at(c, i, j, k)] = T(1) / d;
     }
 }
 
@@ -92,10 +115,70 @@ __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restr
     int i = 2 * i2 + ((j + k + color) & 1);
     if (i >= L.nx) return;
     long long c = ((long long)k * L.ny + j) * L.nx + i;
-    if (zero_init) { x[c] = b[c] * invd[c]; return; }
+    long long o = L.at(c, i, j, k);
+    if (zero_init) { x[o] = rmul(b[o], invd[o]); return; }
     T off, dg;
     s_row<T>(L, x, i, j, k, off, dg);
-    x[c] = (b[c] + off) * invd[c];
+    x[o] = rmul(radd(b[o], off), invd[o]);
+}
+
+// The same half sweep on colour-split FP32 storage, four cells of one row per
+// thread (nx a multiple of 8): the cells' own b and invd, their x-neighbours
+// (other colour, indices m-1+p .. m+p for row parity p) and the j+-1 / k+-1
+// neighbours are float4 loads, indices are 32-bit, and the row constants are
+// loaded once.  The arithmetic per cell is s_row's, operation for operation.
+__global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__restrict__ b,
+                        const float *__restrict__ invd, float *__restrict__ x)
+{
+    const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
+    int q4 = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (j >= ny || 4 * q4 >= hx) return;
+    const int half = (int)(((long long)nx * ny * nz) >> 1), hxy = hx * ny;
+    const int p = (color + j + k) & 1;
+    const int rowm = (k * ny + j) * hx, m0 = rowm + 4 * q4;
+    const float4 bb = *reinterpret_cast<const float4 *>(b + (size_t)color * half + m0);
+    const float4 dd = *reinterpret_cast<const float4 *>(invd + (size_t)color * half + m0);
+    float4 res;
+    if (zero_init) {
+        res = make_float4(rmul(bb.x, dd.x), rmul(bb.y, dd.y), rmul(bb.z, dd.z), rmul(bb.w, dd.w));
+        *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) = res;
+        return;
+    }
+    const float *oth = x + (size_t)(1 - color) * half;
+    const float4 c4 = *reinterpret_cast<const float4 *>(oth + m0);
+    float ex = 0.0f;   // the fifth x-neighbour: left of the group (p = 0) or right of it (p = 1)
+    if (p == 0) { if (q4 > 0) ex = oth[m0 - 1]; }
+    else { if (4 * q4 + 4 < hx) ex = oth[m0 + 4]; }
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 jm = j > 0 ? *reinterpret_cast<const float4 *>(oth + m0 - hx) : zero4;
+    const float4 jp = j < ny - 1 ? *reinterpret_cast<const float4 *>(oth + m0 + hx) : zero4;
+    const float4 km = k > 0 ? *reinterpret_cast<const float4 *>(oth + m0 - hxy) : zero4;
+    const float4 kp = k < nz - 1 ? *reinterpret_cast<const float4 *>(oth + m0 + hxy) : zero4;
+    const float dyj = Ld.dyf[j], dzk = Ld.dzf[k];
+    const float dyz = rmul(dyj, dzk);
+    const float ryj = Ld.rfyf[j], ryj1 = Ld.rfyf[j + 1], rzk = Ld.rfzf[k], rzk1 = Ld.rfzf[k + 1];
+    const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+    const float bv[4] = {bb.x, bb.y, bb.z, bb.w}, dv[4] = {dd.x, dd.y, dd.z, dd.w};
+    const float jmv[4] = {jm.x, jm.y, jm.z, jm.w}, jpv[4] = {jp.x, jp.y, jp.z, jp.w};
+    const float kmv[4] = {km.x, km.y, km.z, km.w}, kpv[4] = {kp.x, kp.y, kp.z, kp.w};
+    float out[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const int i = 2 * (4 * q4 + e) + p;
+        const float xl = p == 0 ? (e == 0 ? ex : cv[e - 1]) : cv[e];
+        const float xr = p == 0 ? cv[e] : (e == 3 ? ex : cv[e + 1]);
+        const float dxi = Ld.dxf[i];
+        const float dxz = rmul(dxi, dzk), dxy = rmul(dxi, dyj);
+        float o = 0.0f, f;
+        if (i > 0) { f = rmul(dyz, Ld.rfxf[i]); o = rfma(f, xl, o); }
+        if (i < nx - 1) { f = rmul(dyz, Ld.rfxf[i + 1]); o = rfma(f, xr, o); }
+        if (j > 0) { f = rmul(dxz, ryj); o = rfma(f, jmv[e], o); }
+        if (j < ny - 1) { f = rmul(dxz, ryj1); o = rfma(f, jpv[e], o); }
+        if (k > 0) { f = rmul(dxy, rzk); o = rfma(f, kmv[e], o); }
+        if (k < nz - 1) { f = rmul(dxy, rzk1); o = rfma(f, kpv[e], o); }
+        out[e] = rmul(radd(bv[e], o), dv[e]);
+    }
+    *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
 template <typename T>
@@ -107,7 +190,8 @@ __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restr
     long long c = ((long long)k * L.ny + j) * L.nx + i;
     T off, dg;
     s_row<T>(L, x, i, j, k, off, dg);
-    r[c] = b[c] - (dg * x[c] - off);
+    long long o = L.at(c, i, j, k);
+    r[c] = b[o] - (dg * x[o] - off);
 }
 
 template <typename T>
@@ -150,7 +234,7 @@ __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ r
             for (int a = 0; a < nxx; a++) s += wyz * rwx[4 * I + a] * row[Lf.tx.rf[4 * I + a]];
         }
     }
-    bc[c] = s;
+    bc[lev_at(Lc, c, I, J, K)] = s;
 }
 
 // linear prolongation (stretching-aware weights), added to the fine iterate
@@ -171,14 +255,14 @@ __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc
 #pragma unroll
         for (int b = 0; b < 2; b++) {
             if (wy[b] == T(0)) continue;
-            const T *row = xc + ((long long)Iz[d] * Lc.ny + Iy[b]) * Lc.nx;
+            long long row = ((long long)Iz[d] * Lc.ny + Iy[b]) * Lc.nx;
             T wyz = wz[d] * wy[b];
 #pragma unroll
             for (int a = 0; a < 2; a++)
-                if (wx[a] != T(0)) acc += wyz * wx[a] * row[Ix[a]];
+                if (wx[a] != T(0)) acc += wyz * wx[a] * xc[lev_at(Lc, row + Ix[a], Ix[a], Iy[b], Iz[d])];
         }
     }
-    xf[c] += acc;
+    xf[lev_at(Lf, c, i, j, k)] += acc;
 }
 
 template <typename T>
@@ -189,6 +273,22 @@ __global__ void k_coarse(int n, const double *__restrict__ ainv, const T *__rest
     double s = 0.0;
     for (int c = 0; c < n; c++) s += ainv[r * n + c] * (double)b[c];
     x[r] = (T)s;
+}
+
+// FP64 <-> FP32 between the natural order and a level's storage order
+__global__ void k_to_float_lev(MgDevLevel L, const double *__restrict__ a, float *__restrict__ b)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= L.nx || j >= L.ny) return;
+    long long c = ((long long)k * L.ny + j) * L.nx + i;
+    b[lev_at(L, c, i, j, k)] = (float)a[c];
+}
+__global__ void k_to_double_lev(MgDevLevel L, const float *__restrict__ a, double *__restrict__ b)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= L.nx || j >= L.ny) return;
+    long long c = ((long long)k * L.ny + j) * L.nx + i;
+    b[c] = (double)a[lev_at(L, c, i, j, k)];
 }
 
 inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -204,6 +304,21 @@ void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd)
 }
 
 // One V-cycle from level l: input b[l], output x[l] (x starts at zero).
+// one red-black half sweep of level L: the vectorised kernel where the
+// level is colour-split FP32 with nx a multiple of 8
+template <typename T>
+void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, const T *b, const T *invd, T *x)
+{
+    if constexpr (sizeof(T) == 4) {
+        if (L.split && L.nx % 8 == 0) {
+            dim3 g4((unsigned)((L.nx / 8 + 31) / 32), (unsigned)((L.ny + 7) / 8), (unsigned)L.nz);
+            k_rbgs4<<<g4, B38, 0, s>>>(L, color, zero_init, b, invd, x);
+            return;
+        }
+    }
+    k_rbgs<T><<<g3((L.nx + 1) >> 1, L.ny, L.nz), B38, 0, s>>>(L, color, zero_init, b, invd, x);
+}
+
 template <typename T>
 void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
 {
@@ -213,12 +328,11 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
         k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
         return;
     }
-    dim3 g = g3((L.nx + 1) >> 1, L.ny, L.nz);
     for (int it = 0; it < npre; it++) {
         // the first colour-0 half sweep takes x = 0 (it reads no neighbours);
         // every colour-1 point is then rewritten from colour-0 values only
-        k_rbgs<T><<<g, B38, 0, s>>>(L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
-        k_rbgs<T><<<g, B38, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+        rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
+        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l]);
     }
     k_resid<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, H.b[l], H.x[l], H.r[l]);
     const MgDevLevel &C = H.lev[l + 1];
@@ -226,9 +340,18 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
     mg_vcycle<T>(s, H, l + 1, npre, npost);
     k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
     for (int it = 0; it < npost; it++) {
-        k_rbgs<T><<<g, B38, 0, s>>>(L, 1, 0, H.b[l], H.invd[l], H.x[l]);
-        k_rbgs<T><<<g, B38, 0, s>>>(L, 0, 0, H.b[l], H.invd[l], H.x[l]);
+        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+        rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l]);
     }
+}
+
+void mg_to_float(cudaStream_t s, const MgDevLevel &L, const double *a, float *b)
+{
+    k_to_float_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
+}
+void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b)
+{
+    k_to_double_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
 
 int mg_vcycle_launches(int nl, int npre, int npost)

@@ -131,6 +131,7 @@ struct turb_ctx {
     // pressure mode (FP64 V-cycles: 4 + 4; FP32 V-cycles are cheap enough that
     // 6 + 6, 8 CG iterations at 512x256x256, beats fewer sweeps)
     int mg_pre[2] = {4, 6}, mg_post[2] = {4, 6};
+    int mg_split = 1;   // colour-split storage of the FP32 levels
     // pressure initial guess: history of the last two solutions per RK stage
     int guess_mode = TURB_GUESS_PREVIOUS;
     int stage = 0;
@@ -622,6 +623,9 @@ int build_mg(turb_ctx *c)
         m.dxf = c->mem.upload(Df[0]); m.dyf = c->mem.upload(Df[1]); m.dzf = c->mem.upload(Df[2]);
         m.rfxf = c->mem.upload(rff[0]); m.rfyf = c->mem.upload(rff[1]); m.rfzf = c->mem.upload(rff[2]);
         c->H64.lev[l] = m;
+        // FP32 levels store x, b, invd colour-split where nx is even (not on
+        // the coarsest level, which the dense inverse reads in natural order)
+        m.split = c->mg_split && (h.nx % 2 == 0) && l + 1 < nl;
         c->H32.lev[l] = m;
         long long n = (long long)h.nx * h.ny * h.nz;
         if (l > 0) {
@@ -635,8 +639,8 @@ int build_mg(turb_ctx *c)
         c->H32.r[l] = c->mem.alloc<float>(n);
         c->H32.invd[l] = c->mem.alloc<float>(n);
         if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
-        mg_setup_invdiag<double>(c->s, m, c->H64.invd[l]);
-        mg_setup_invdiag<float>(c->s, m, c->H32.invd[l]);
+        mg_setup_invdiag<double>(c->s, c->H64.lev[l], c->H64.invd[l]);
+        mg_setup_invdiag<float>(c->s, c->H32.lev[l], c->H32.invd[l]);
     }
     // dense inverse of the coarsest operator (Gauss-Jordan, partial pivoting)
     HostLev &h = L[nl - 1];
@@ -1069,6 +1073,19 @@ int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost)
     c->mg_pre[m] = npre;
     c->mg_post[m] = npost;
     return TURB_OK;
+}
+
+int turb_set_mg_split(turb_ctx *c, int on)
+{
+    if (!c) return TURB_ERR_ARG;
+    c->mg_split = on ? 1 : 0;
+    for (int l = 0; l < c->H32.nl; l++) {
+        MgDevLevel &m = c->H32.lev[l];
+        m.split = c->mg_split && (m.nx % 2 == 0) && l + 1 < c->H32.nl;
+        mg_setup_invdiag<float>(c->s, m, c->H32.invd[l]);
+    }
+    if (c->g_mg[1]) { cudaGraphExecDestroy(c->g_mg[1]); c->g_mg[1] = nullptr; }
+    return check_launch(c);
 }
 
 int turb_synchronize(turb_ctx *c)
@@ -1756,9 +1773,9 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             if (pm == 0) {
                 mg_vcycle<double>(s, c->H64, 0, npre, npost);
             } else {
-                pcg_to_float(s, n0, c->pr, c->H32.b[0]);
+                mg_to_float(s, c->H32.lev[0], c->pr, c->H32.b[0]);
                 mg_vcycle<float>(s, c->H32, 0, npre, npost);
-                pcg_to_double(s, n0, c->H32.x[0], c->pz);
+                mg_to_double(s, c->H32.lev[0], c->H32.x[0], c->pz);
             }
         };
         auto cgstep = [&](int rs) {

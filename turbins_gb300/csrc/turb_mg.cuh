@@ -23,6 +23,10 @@ struct MgDevLevel {
     const double *dxd, *dyd, *dzd, *rfxd, *rfyd, *rfzd;
     const float *dxf, *dyf, *dzf, *rfxf, *rfyf, *rfzf;
     double pin;
+    // colour-split storage (x, b, invd; not r): with nx even, cell c of colour
+    // (i+j+k)&1 lives at colour*(n/2) + c/2, so a red-black half sweep reads
+    // and writes dense half arrays
+    int split = 0;
 };
 
 template <typename T>
@@ -58,6 +62,9 @@ void pcg_xrupdate(cudaStream_t s, long long n, double *x, double *r, double *rol
 void pcg_scalars(cudaStream_t s, PcgScal *sc, int what);
 void pcg_to_float(cudaStream_t s, long long n, const double *a, float *b);
 void pcg_to_double(cudaStream_t s, long long n, const float *a, double *b);
+// the same into / out of a level's storage order (colour-split or not)
+void mg_to_float(cudaStream_t s, const MgDevLevel &L, const double *a, float *b);
+void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b);
 void pcg_copy(cudaStream_t s, long long n, const double *a, double *b);
 int pcg_nparts();
 void pcg_lincomb(cudaStream_t s, long long n, double a, const double *x, double b, const double *y, double *out);

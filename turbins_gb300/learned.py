@@ -67,10 +67,17 @@ def attach(ctx, params):
     return net
 
 
-def multi_bump_train_case(nx=128, ny=64, nz=64):
-    """Training runs for the 512x256x256 multi-bump step: the same physics and
-    x spacing on a quarter-length domain, one bump field per seed."""
-    return lambda seed: W.multi_bump_case(nx, ny, nz, seed=100 + seed, lx=32.0 * nx / 512.0)
+def multi_bump_train_case(nx=128, ny=64, nz=64, full=(512, 256, 256)):
+    """Training runs for the multi-bump step on a `full` grid: the same
+    physics with the x extent cut to nx / full[0] of the full domain, one bump
+    field per seed.  With ny = full[1] the training grid keeps the full case's
+    spacing in every direction: the z extent is cut to nz / full[2] too, and
+    the number of bumps follows the domain's area (16 on the full one)."""
+    if ny != full[1]:
+        return lambda seed: W.multi_bump_case(nx, ny, nz, seed=100 + seed, lx=32.0 * nx / full[0])
+    fx, fz = nx / full[0], nz / full[2]
+    nb = max(1, int(round(16 * fx * fz)))
+    return lambda seed: W.multi_bump_case(nx, ny, nz, seed=100 + seed, lx=32.0 * fx, lz=2.0 * fz, nbump=nb)
 
 
 def turbidity_train_case(nx=128, ny=64, nz=64):

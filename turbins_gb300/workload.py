@@ -409,18 +409,20 @@ def turbidity_bump_case(nx=256, ny=128, nz=128, seed=0):
     return Case("turbidity_bump_%dx%dx%d" % (nx, ny, nz), g, p, 5e-4, 200, s)
 
 
-def multi_bump_case(nx=512, ny=256, nz=256, seed=4, lx=32.0):
+def multi_bump_case(nx=512, ny=256, nz=256, seed=4, lx=32.0, lz=2.0, nbump=16):
     """Full coupled step: [0,32]x[0,2]x[0,2] y-stretched, 16 seeded Gaussian
     bumps (heights U[0.05,0.3], widths U[0.2,1.0], centres x U[4,28],
-    z U[0,2]), two fractions settling at 0.005 and 0.02, Re=5000, dt=2.5e-4."""
-    g = make_grid(nx, ny, nz, (lx, 2.0, 2.0), ystretch=1.5)
+    z U[0,2]), two fractions settling at 0.005 and 0.02, Re=5000, dt=2.5e-4.
+    lx, lz shrink the domain (bump centres scale with it) and nbump sets the
+    number of bumps, for training runs at the full case's grid spacing."""
+    g = make_grid(nx, ny, nz, (lx, 2.0, lz), ystretch=1.5)
     rng = np.random.Generator(np.random.PCG64(seed))
-    hs = rng.uniform(0.05, 0.3, 16)
-    ws = rng.uniform(0.2, 1.0, 16)
-    xs = rng.uniform(4.0 * lx / 32.0, 28.0 * lx / 32.0, 16)
-    zs = rng.uniform(0.0, 2.0, 16)
+    hs = rng.uniform(0.05, 0.3, nbump)
+    ws = rng.uniform(0.2, 1.0, nbump)
+    xs = rng.uniform(4.0 * lx / 32.0, 28.0 * lx / 32.0, nbump)
+    zs = rng.uniform(0.0, lz, nbump)
     dy0 = g.yv[1] - g.yv[0]
-    bed = Bed([(hs[i], ws[i], xs[i], zs[i]) for i in range(16)], 2.001 * dy0)
+    bed = Bed([(hs[i], ws[i], xs[i], zs[i]) for i in range(nbump)], 2.001 * dy0)
     tag_status(g, bed)
     build_immersed(g, bed)
     p = Params(nx, ny, nz, eno_order=3, re=5000.0, nconc=2, pe=[5000.0, 5000.0],
