@@ -191,7 +191,62 @@ __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restr
     T off, dg;
     s_row<T>(L, x, i, j, k, off, dg);
     long long o = L.at(c, i, j, k);
-    r[c] = b[o] - (dg * x[o] - off);
+    r[c] = radd(b[o], -rfma(dg, x[o], -off));
+}
+
+// residual r = b - S x of a colour-split FP32 level (nx a multiple of 8),
+// eight cells of one row per thread: cells 2(m0+e) and 2(m0+e)+1 of the row
+// live at index m0+e of colour halves c0 = (j+k)&1 and c0^1, so every x and
+// b access is a float4 (two scalars for the row ends); r is written in the
+// natural order the restriction reads.  Per cell the arithmetic is s_row's.
+__global__ void k_resid8(MgDevLevel Ld, const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ r)
+{
+    const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
+    int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (j >= ny || 4 * q >= hx) return;
+    const int half = (int)(((long long)nx * ny * nz) >> 1), hxy = hx * ny;
+    const int c0 = (j + k) & 1;
+    const int m0 = (k * ny + j) * hx + 4 * q;
+    const float *h0 = x + (size_t)c0 * half, *h1 = x + (size_t)(c0 ^ 1) * half;
+    auto ld4 = [](const float *p) { return *reinterpret_cast<const float4 *>(p); };
+    auto inter = [](float4 a, float4 b, float (&v)[8]) {   // cells 2e from a, 2e+1 from b
+        v[0] = a.x; v[1] = b.x; v[2] = a.y; v[3] = b.y; v[4] = a.z; v[5] = b.z; v[6] = a.w; v[7] = b.w;
+    };
+    float xc[8], bc[8], xjm[8], xjp[8], xkm[8], xkp[8];
+    inter(ld4(h0 + m0), ld4(h1 + m0), xc);
+    inter(ld4(b + (size_t)c0 * half + m0), ld4(b + (size_t)(c0 ^ 1) * half + m0), bc);
+    // rows j+-1 and planes k+-1 have the opposite colour at the same i
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    inter(j > 0 ? ld4(h1 + m0 - hx) : z4, j > 0 ? ld4(h0 + m0 - hx) : z4, xjm);
+    inter(j < ny - 1 ? ld4(h1 + m0 + hx) : z4, j < ny - 1 ? ld4(h0 + m0 + hx) : z4, xjp);
+    inter(k > 0 ? ld4(h1 + m0 - hxy) : z4, k > 0 ? ld4(h0 + m0 - hxy) : z4, xkm);
+    inter(k < nz - 1 ? ld4(h1 + m0 + hxy) : z4, k < nz - 1 ? ld4(h0 + m0 + hxy) : z4, xkp);
+    const int i0 = 8 * q;
+    const float xl = i0 > 0 ? h1[m0 - 1] : 0.0f;             // cell i0-1: colour c0^1, pair m0-1
+    const float xr = i0 + 8 < nx ? h0[m0 + 4] : 0.0f;        // cell i0+8: colour c0, pair m0+4
+    const float dyj = Ld.dyf[j], dzk = Ld.dzf[k];
+    const float dyz = rmul(dyj, dzk);
+    const float ryj = Ld.rfyf[j], ryj1 = Ld.rfyf[j + 1], rzk = Ld.rfzf[k], rzk1 = Ld.rfzf[k + 1];
+    float out[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+        const int i = i0 + e;
+        const float dxi = Ld.dxf[i];
+        const float dxz = rmul(dxi, dzk), dxy = rmul(dxi, dyj);
+        const float xw = e == 0 ? xl : xc[e - 1], xe = e == 7 ? xr : xc[e + 1];
+        float o = 0.0f, d = 0.0f, f;
+        if (i > 0) { f = rmul(dyz, Ld.rfxf[i]); d = radd(d, f); o = rfma(f, xw, o); }
+        if (i < nx - 1) { f = rmul(dyz, Ld.rfxf[i + 1]); d = radd(d, f); o = rfma(f, xe, o); }
+        if (j > 0) { f = rmul(dxz, ryj); d = radd(d, f); o = rfma(f, xjm[e], o); }
+        if (j < ny - 1) { f = rmul(dxz, ryj1); d = radd(d, f); o = rfma(f, xjp[e], o); }
+        if (k > 0) { f = rmul(dxy, rzk); d = radd(d, f); o = rfma(f, xkm[e], o); }
+        if (k < nz - 1) { f = rmul(dxy, rzk1); d = radd(d, f); o = rfma(f, xkp[e], o); }
+        if (i == nx - 1 && j == ny - 1 && k == nz - 1) d = radd(d, (float)Ld.pin);
+        out[e] = radd(bc[e], -rfma(d, xc[e], -o));
+    }
+    float *rr = r + ((size_t)(k * ny + j) * nx + i0);
+    *reinterpret_cast<float4 *>(rr) = make_float4(out[0], out[1], out[2], out[3]);
+    *reinterpret_cast<float4 *>(rr + 4) = make_float4(out[4], out[5], out[6], out[7]);
 }
 
 template <typename T>
@@ -320,6 +375,19 @@ void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, cons
 }
 
 template <typename T>
+void resid_lev(cudaStream_t s, const MgDevLevel &L, const T *b, const T *x, T *r)
+{
+    if constexpr (sizeof(T) == 4) {
+        if (L.split && L.nx % 8 == 0) {
+            dim3 g8((unsigned)((L.nx / 8 + 31) / 32), (unsigned)((L.ny + 7) / 8), (unsigned)L.nz);
+            k_resid8<<<g8, B38, 0, s>>>(L, b, x, r);
+            return;
+        }
+    }
+    k_resid<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, b, x, r);
+}
+
+template <typename T>
 void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
 {
     const MgDevLevel &L = H.lev[l];
@@ -334,7 +402,7 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
         rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
         rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l]);
     }
-    k_resid<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, H.b[l], H.x[l], H.r[l]);
+    resid_lev<T>(s, L, H.b[l], H.x[l], H.r[l]);
     const MgDevLevel &C = H.lev[l + 1];
     k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
     mg_vcycle<T>(s, H, l + 1, npre, npost);
