@@ -208,7 +208,78 @@ __global__ void k_ib_resid64(IbDev ib, const double *__restrict__ b, const doubl
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
 }
 
-// inner FP32 Jacobi sweep on A e = r (first sweep from e = 0)
+// inner FP32 Jacobi sweep on A e = r (first sweep from e = 0), four points
+// of a row per thread: e, r, status and the j+-1 / k+-1 neighbours are
+// 16-byte (4-byte for status) loads, the x tables are padded to the pitch.
+// Immersed points get a placeholder that k_ib_jac32 overwrites; pad columns
+// (i >= NX) are not written.
+__global__ void k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
+                              const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
+                              int first)
+{
+    const int i0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x), j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i0 >= d.NX || j >= d.NY) return;
+    const float4 apx = *reinterpret_cast<const float4 *>(h.apx + i0);
+    const float4 aw = *reinterpret_cast<const float4 *>(h.aw + i0);
+    const float4 ae = *reinterpret_cast<const float4 *>(h.ae + i0);
+    const float apxv[4] = {apx.x, apx.y, apx.z, apx.w}, awv[4] = {aw.x, aw.y, aw.z, aw.w};
+    const float aev[4] = {ae.x, ae.y, ae.z, ae.w};
+    const float apyj = h.apy[j], asj = h.as[j], anj = h.an[j];
+    const int nvalid = min(4, d.NX - i0);
+    for (int kk = 0; kk < KC; kk++) {
+        const int k = blockIdx.z * KC + kk;
+        if (k >= d.NZ) break;
+        const long long p = d.at(i0, j, k);
+        const uchar4 s4 = *reinterpret_cast<const uchar4 *>(st + p);
+        const int sv[4] = {s4.x, s4.y, s4.z, s4.w};
+        const float4 r4 = *reinterpret_cast<const float4 *>(r + p);
+        const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
+        const float apzk = h.apz[k], abk = h.ab[k], afk = h.af[k];
+        float out[4];
+        if (first) {
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const bool stn = is_stencil(h.q, sv[t]);
+                const float dg = stn ? __fadd_rn(__fadd_rn(__fadd_rn(apxv[t], apyj), apzk), a_dt)
+                                     : __fadd_rn(h.ap_solid, a_dt);
+                out[t] = __fmul_rn(rv[t], __frcp_rn(dg));
+            }
+        } else {
+            const float4 e4 = *reinterpret_cast<const float4 *>(e + p);
+            const float ev[4] = {e4.x, e4.y, e4.z, e4.w};
+            const float xw = i0 > 0 ? e[p - 1] : ev[0];
+            const float xe = i0 + 4 < d.NX ? e[p + 4] : ev[3];
+            const float4 s_ = j > 0 ? *reinterpret_cast<const float4 *>(e + p - d.PX) : e4;
+            const float4 n_ = j < d.NY - 1 ? *reinterpret_cast<const float4 *>(e + p + d.PX) : e4;
+            const float4 b_ = k > 0 ? *reinterpret_cast<const float4 *>(e + p - d.plane) : e4;
+            const float4 f_ = k < d.NZ - 1 ? *reinterpret_cast<const float4 *>(e + p + d.plane) : e4;
+            const float sv_[4] = {s_.x, s_.y, s_.z, s_.w}, nv_[4] = {n_.x, n_.y, n_.z, n_.w};
+            const float bv_[4] = {b_.x, b_.y, b_.z, b_.w}, fv_[4] = {f_.x, f_.y, f_.z, f_.w};
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const bool stn = is_stencil(h.q, sv[t]);
+                const float dg = stn ? __fadd_rn(__fadd_rn(__fadd_rn(apxv[t], apyj), apzk), a_dt)
+                                     : __fadd_rn(h.ap_solid, a_dt);
+                float acc = __fmul_rn(dg, ev[t]);
+                if (stn) {
+                    acc = __fmaf_rn(awv[t], t == 0 ? xw : ev[t - 1], acc);
+                    acc = __fmaf_rn(aev[t], t == 3 ? xe : ev[t + 1], acc);
+                    acc = __fmaf_rn(asj, sv_[t], acc);
+                    acc = __fmaf_rn(anj, nv_[t], acc);
+                    acc = __fmaf_rn(abk, bv_[t], acc);
+                    acc = __fmaf_rn(afk, fv_[t], acc);
+                }
+                out[t] = __fmaf_rn(__fadd_rn(rv[t], -acc), __frcp_rn(dg), ev[t]);
+            }
+        }
+        if (nvalid == 4) {
+            *reinterpret_cast<float4 *>(en + p) = make_float4(out[0], out[1], out[2], out[3]);
+        } else {
+            for (int t = 0; t < nvalid; t++) en[p + t] = out[t];
+        }
+    }
+}
+
 __global__ void k_helm_jac32(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
                              const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
                              int first)
@@ -324,6 +395,8 @@ void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const 
 void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
                        const float *r, const float *e, float *en, const IbDevF &ib, int first)
 {
-    k_helm_jac32<<<hgrid(d), dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
+    dim3 g((unsigned)((d.NX + 4 * HBX - 1) / (4 * HBX)), (unsigned)((d.NY + HBY - 1) / HBY),
+           (unsigned)((d.NZ + KC - 1) / KC));
+    k_helm_jac32v<<<g, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
     if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
 }

@@ -459,17 +459,20 @@ IbDev mk_ib(turb_ctx *c, int q, const turb_ib_desc &ib, double aps)
 
 HelmTabF mk_helmf(turb_ctx *c, const HelmTab &h)
 {
-    auto cp = [&](const double *dp, int n) {
+    // x tables padded with zeros to the row pitch, for the four-point loads
+    // of the vectorised sweep
+    auto cp = [&](const double *dp, int n, int npad) {
         std::vector<double> tmp(n);
         cudaMemcpy(tmp.data(), dp, sizeof(double) * n, cudaMemcpyDeviceToHost);
         std::vector<float> f(tmp.begin(), tmp.end());
+        f.resize(std::max(n, npad), 0.0f);
         return (const float *)c->mem.upload(f);
     };
     HelmTabF o;
-    int NX = c->d.NX, NY = c->d.NY, NZ = c->d.NZ;
-    o.apx = cp(h.apx, NX); o.aw = cp(h.aw, NX); o.ae = cp(h.ae, NX);
-    o.apy = cp(h.apy, NY); o.as = cp(h.as, NY); o.an = cp(h.an, NY);
-    o.apz = cp(h.apz, NZ); o.ab = cp(h.ab, NZ); o.af = cp(h.af, NZ);
+    int NX = c->d.NX, NY = c->d.NY, NZ = c->d.NZ, PX = c->d.PX;
+    o.apx = cp(h.apx, NX, PX); o.aw = cp(h.aw, NX, PX); o.ae = cp(h.ae, NX, PX);
+    o.apy = cp(h.apy, NY, 0); o.as = cp(h.as, NY, 0); o.an = cp(h.an, NY, 0);
+    o.apz = cp(h.apz, NZ, 0); o.ab = cp(h.ab, NZ, 0); o.af = cp(h.af, NZ, 0);
     o.ap_solid = (float)h.ap_solid;
     o.q = h.q;
     return o;
