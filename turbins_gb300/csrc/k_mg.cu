@@ -320,6 +320,93 @@ __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc
     xf[lev_at(Lf, c, i, j, k)] += acc;
 }
 
+// eight consecutive values (cells i0..i0+7 of row (j, k)) of a level's FP32
+// storage; nx a multiple of 8, i0 a multiple of 8
+__device__ __forceinline__ void ld8(const MgDevLevel &L, const float *a, int i0, int j, int k, float (&v)[8])
+{
+    const int hx = L.nx >> 1;
+    if (L.split) {
+        const int half = (int)(((long long)L.nx * L.ny * L.nz) >> 1), c0 = (j + k) & 1;
+        const int m0 = (k * L.ny + j) * hx + (i0 >> 1);
+        const float4 a0 = *reinterpret_cast<const float4 *>(a + (size_t)c0 * half + m0);
+        const float4 a1 = *reinterpret_cast<const float4 *>(a + (size_t)(c0 ^ 1) * half + m0);
+        v[0] = a0.x; v[1] = a1.x; v[2] = a0.y; v[3] = a1.y; v[4] = a0.z; v[5] = a1.z; v[6] = a0.w; v[7] = a1.w;
+    } else {
+        const float *p = a + ((size_t)(k * L.ny + j) * L.nx + i0);
+        const float4 a0 = *reinterpret_cast<const float4 *>(p), a1 = *reinterpret_cast<const float4 *>(p + 4);
+        v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w; v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
+    }
+}
+__device__ __forceinline__ void st8(const MgDevLevel &L, float *a, int i0, int j, int k, const float (&v)[8])
+{
+    const int hx = L.nx >> 1;
+    if (L.split) {
+        const int half = (int)(((long long)L.nx * L.ny * L.nz) >> 1), c0 = (j + k) & 1;
+        const int m0 = (k * L.ny + j) * hx + (i0 >> 1);
+        *reinterpret_cast<float4 *>(a + (size_t)c0 * half + m0) = make_float4(v[0], v[2], v[4], v[6]);
+        *reinterpret_cast<float4 *>(a + (size_t)(c0 ^ 1) * half + m0) = make_float4(v[1], v[3], v[5], v[7]);
+    } else {
+        float *p = a + ((size_t)(k * L.ny + j) * L.nx + i0);
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4 *>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+    }
+}
+
+// restriction where x is not coarsened (cx = 0: identity in x), eight cells
+// of a coarse row per thread; r is natural, b of the coarse level in its
+// storage order
+__global__ void k_restrict_yz8(MgDevLevel Lf, MgDevLevel Lc, const float *__restrict__ rf, float *__restrict__ bc)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
+    if (8 * q >= Lc.nx || J >= Lc.ny) return;
+    const int i0 = 8 * q;
+    const int nyy = Lf.ty.rcnt[J], nzz = Lf.tz.rcnt[K];
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int c3 = 0; c3 < nzz; c3++) {
+        const int k = Lf.tz.rf[4 * K + c3];
+        const float wz = Lf.tz.rwf[4 * K + c3];
+        for (int b = 0; b < nyy; b++) {
+            const int j = Lf.ty.rf[4 * J + b];
+            const float wyz = __fmul_rn(wz, Lf.ty.rwf[4 * J + b]);
+            const float *row = rf + ((size_t)(k * Lf.ny + j) * Lf.nx + i0);
+            const float4 a0 = *reinterpret_cast<const float4 *>(row), a1 = *reinterpret_cast<const float4 *>(row + 4);
+            const float v[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+            for (int e = 0; e < 8; e++) s[e] = __fmaf_rn(wyz, v[e], s[e]);
+        }
+    }
+    st8(Lc, bc, i0, J, K, s);
+}
+
+// prolongation where x is not coarsened, eight cells of a fine row per thread
+__global__ void k_prolong_yz8(MgDevLevel Lf, MgDevLevel Lc, const float *__restrict__ xc, float *__restrict__ xf)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (8 * q >= Lf.nx || j >= Lf.ny) return;
+    const int i0 = 8 * q;
+    const int Iy[2] = {Lf.ty.I0[j], Lf.ty.I1[j]}, Iz[2] = {Lf.tz.I0[k], Lf.tz.I1[k]};
+    const float wy[2] = {Lf.ty.w0f[j], Lf.ty.w1f[j]}, wz[2] = {Lf.tz.w0f[k], Lf.tz.w1f[k]};
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+        if (wz[d] == 0.0f) continue;
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            if (wy[b] == 0.0f) continue;
+            const float wyz = __fmul_rn(wz[d], wy[b]);
+            float v[8];
+            ld8(Lc, xc, i0, Iy[b], Iz[d], v);
+#pragma unroll
+            for (int e = 0; e < 8; e++) acc[e] = __fmaf_rn(wyz, v[e], acc[e]);
+        }
+    }
+    float x8[8];
+    ld8(Lf, xf, i0, j, k, x8);
+#pragma unroll
+    for (int e = 0; e < 8; e++) x8[e] = __fadd_rn(x8[e], acc[e]);
+    st8(Lf, xf, i0, j, k, x8);
+}
+
 template <typename T>
 __global__ void k_coarse(int n, const double *__restrict__ ainv, const T *__restrict__ b, T *__restrict__ x)
 {
@@ -404,9 +491,19 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
     }
     resid_lev<T>(s, L, H.b[l], H.x[l], H.r[l]);
     const MgDevLevel &C = H.lev[l + 1];
-    k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
-    mg_vcycle<T>(s, H, l + 1, npre, npost);
-    k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+    bool yz8 = false;
+    if constexpr (sizeof(T) == 4) yz8 = L.cx == 0 && L.nx % 8 == 0 && C.nx == L.nx;
+    if (yz8) {
+        if constexpr (sizeof(T) == 4) {
+            k_restrict_yz8<<<g3((C.nx / 8 + 31) / 32 * 32, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
+            mg_vcycle<T>(s, H, l + 1, npre, npost);
+            k_prolong_yz8<<<g3((L.nx / 8 + 31) / 32 * 32, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+        }
+    } else {
+        k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
+        mg_vcycle<T>(s, H, l + 1, npre, npost);
+        k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+    }
     for (int it = 0; it < npost; it++) {
         rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l]);
         rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l]);
