@@ -284,6 +284,17 @@ EnoTab mk_eno(DevBuf &m, int r, const std::vector<double> &pos, int s0, int e0, 
     T.rh2 = m.upload(r2);
     T.rh3 = m.upload(r3);
     T.fastdiv = 1;   // reciprocal-based, correctly rounded (turb_div.cuh); 0 = IEEE division
+    // power-of-two spacings (uniform grids with 2^k cells per unit length):
+    // the reciprocal is exact and a/h = a*(1/h) is the same real number, so
+    // one multiplication rounds exactly as the division does
+    auto pow2 = [](double h) {
+        int e;
+        return h > 0.0 && std::isfinite(h) && std::frexp(h, &e) == 0.5;
+    };
+    std::vector<uint8_t> p2(nb, 0);
+    for (int b = 0; b < nb; b++)
+        p2[b] = (uint8_t)((pow2(h1[b]) ? 1 : 0) | (pow2(h2[b]) ? 2 : 0) | (pow2(h3[b]) ? 4 : 0));
+    T.p2 = m.upload(p2);
     T.g2 = m.upload(g2);
     T.g3 = m.upload(g3);
     return T;

@@ -60,6 +60,8 @@ struct EnoTab {
     const double *g3;    // [nb*3]: kstar=b-2,b-1,b -> three-product sum
     const double *rh1, *rh2, *rh3;   // RN(1/h*) for the reciprocal-based division
     int fastdiv;         // 1: div_by_spacing (turb_div.cuh), 0: IEEE division
+    const uint8_t *p2;   // per b: bit 0/1/2 set when h1/h2/h3 is a power of two, so that
+                         // a/h = a*RN(1/h) exactly (fastdiv only)
     int gsrc[6];         // ghost b<r: [0..r), ghost b>=nb-r: [3..3+r) by ex
     double gm[6];        // 0: zero, 1: m*q[s0], 2: m*q[e0]
 };
