@@ -22,6 +22,7 @@
 #include "Extract.h"
 #include "Memory.h"
 #include "Resume.h"
+#include "Solver.h"
 #include <string.h>
 #include <unistd.h>
 
@@ -48,6 +49,10 @@ ref_case *ref_create(int nx, int ny, int nz, const double *xc, const double *yc,
     ref_case *r = (ref_case *)calloc(1, sizeof(ref_case));
     Parameters *p = (Parameters *)calloc(1, sizeof(Parameters));
     MAC_grid *g = (MAC_grid *)calloc(1, sizeof(MAC_grid));
+    /* the reference pauses on getchar() after some warnings (e.g.
+     * Immersed_is_valid, Immersed.c:1422-1425); with stdin at end of file
+     * those pauses return at once instead of waiting on the caller's stdin */
+    if (!freopen("/dev/null", "r", stdin)) clearerr(stdin);
     int NX = nx + 1, NY = ny + 1, NZ = nz + 1, i;
     long n = (long)NX * NY * NZ, t;
     const unsigned char *st[4] = {st_u, st_v, st_w, st_c};
@@ -254,6 +259,56 @@ void ref_lhs_apply(ref_case *r, char q, int ic, double dt, const double *x, doub
         A = V->A;
     }
     shim_mat_mult(A, x, y);
+}
+
+/* the reference's linear solves (the shim's KSPSolve is BiCGStab without a
+ * preconditioner, Solver.c's KSPIBCGS; for the pressure it stands in for
+ * GMRES(20) + BoomerAMG): LHS formed and diagonal modified as ref_lhs_apply,
+ * the KSP from Solver_get_*_solver (rtol = resmax), initial guess x.
+ * Returns the iteration count. */
+int ref_solve(ref_case *r, char q, int ic, double dt, const double *b, double *x)
+{
+    long n = r->n;
+    int its;
+    if (q == 'p') {
+        Pressure *P = r->pr;
+        MatDestroy(P->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &P->A);
+        Pressure_form_LHS_matrix(P, r->g);
+        P->solver = Solver_get_pressure_solver(P->A, r->p);
+        vset(P->G_b, b, n); vset(P->G_data, x, n);
+        its = Pressure_solve(P);
+        vget(P->G_data, x, n);
+        KSPDestroy(P->solver);
+        return its;
+    }
+    if (q == 'c') {
+        Concentration *c = r->c[ic];
+        MatDestroy(c->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &c->A);
+        Conc_form_LHS_matrix(c, r->g, r->p);
+        Conc_modify_diagonal(c, r->g, dt, 0.0);
+        c->solver = Solver_get_concentration_solver(c->A, r->p);
+        vset(c->G_b, b, n); vset(c->G_data, x, n);
+        its = Conc_solve(c);
+        vget(c->G_data, x, n);
+        KSPDestroy(c->solver);
+        return its;
+    } else {
+        Velocity *V = vel_of(r, q);
+        MatDestroy(V->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &V->A);
+        if (q == 'u') Velocity_u_form_LHS_matrix(V, r->g, r->p);
+        else if (q == 'v') Velocity_v_form_LHS_matrix(V, r->g, r->p);
+        else Velocity_w_form_LHS_matrix(V, r->g, r->p);
+        Velocity_modify_diagonal(V, r->g, r->p, dt, 0.0);
+        V->solver = Solver_get_velocity_solver(V->A, r->p);
+        vset(V->G_b, b, n); vset(V->G_data, x, n);
+        its = Velocity_solve(V);
+        vget(V->G_data, x, n);
+        KSPDestroy(V->solver);
+        return its;
+    }
 }
 
 void ref_pressure_apply(ref_case *r, const double *x, double *y)

@@ -200,6 +200,74 @@ class Reference:
         m = self.lib.ref_divergence(self.h, _p(u), _p(v), _p(w), _p(d))
         return m, d
 
+    def c_term(self, ct):
+        """the buoyancy term at v nodes that Velocity_v_set_RHS computes
+        (2-point y interpolation of the total concentration, Velocity.c:1861-
+        1878) and then multiplies by 0.0 (Velocity.c:1883); the restated
+        driver subtracts it at FLUID / BUFFER_SOLID v nodes"""
+        g = self.g
+        yc, yv = g.yc, g.yv
+        c0, c1 = ct[:, :-1, :], ct[:, 1:, :]
+        slope = (c1 - c0) / (yc[1:] - yc[:-1])[None, :, None]
+        out = np.zeros_like(ct)
+        out[:, 1:, :] = slope * (yv[1:] - yc[:-1])[None, :, None] + c0
+        st = g.status["v"]
+        return np.where((st == 3) | (st == 11), out, 0.0)
+
+    def solve(self, q, ic, dt, b, x):
+        """the reference's Velocity_solve / Conc_solve / Pressure_solve
+        (q = 'u', 'v', 'w', 'c' or 'p') from initial guess x; returns
+        (solution, iterations)"""
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        its = self.lib.ref_solve(self.h, C.c_char(q.encode()), C.c_int(ic), C.c_double(dt),
+                                 _p(np.ascontiguousarray(b)), _p(x))
+        return x, its
+
+    def step(self, s, dt):
+        """One TVD-RK2 step through the reference's routines, in the stage
+        order of the restated driver (the oracle's to_step): store old; two
+        stages of {cell centre, total concentration, convection of u, v, w
+        and c_i, momentum RHS, u/v/w solves, concentration RHS and solves,
+        pressure RHS, pressure solve, projection, divergence}; rk average
+        (0.5, 0.5).  s: dict of DA arrays, updated in place; returns the
+        per-stage divergence maxima."""
+        p = self.p
+        nc = p.nconc
+        old = {k: s[k].copy() for k in ["u", "v", "w"] + ["c%d" % i for i in range(nc)]}
+        divs = []
+        for stage in range(2):
+            ub, vb, wb = self.cell_center(s["u"], s["v"], s["w"])
+            cs = [s["c%d" % i] for i in range(nc)]
+            ct = self.total_concentration(cs) if nc > 1 else s["c0"].copy()
+            conv = {}
+            A, B = self.transpose("u", s["u"], s["v"], s["w"])
+            conv["u"] = self.convection("u", 0, s["u"], s["u"], A, B)
+            A, B = self.transpose("v", s["u"], s["v"], s["w"])
+            conv["v"] = self.convection("v", 0, s["v"], A, s["v"], B)
+            A, B = self.transpose("w", s["u"], s["v"], s["w"])
+            conv["w"] = self.convection("w", 0, s["w"], A, B, s["w"])
+            for ic in range(nc):
+                va = vb + p.vs0[ic] if p.ctype[ic] == 2 else vb
+                conv["c%d" % ic] = self.convection("c", ic, s["c%d" % ic], ub, va, wb)
+            bs = {q: self.set_rhs_vel(q, dt, s[q], conv[q], s[dk], ct)
+                  for q, dk in (("u", "dpx"), ("v", "dpy"), ("w", "dpz"))}
+            if p.buoyancy:
+                bs["v"] = bs["v"] - self.c_term(ct)
+            for q in "uvw":
+                s[q], _ = self.solve(q, 0, dt, bs[q], s[q])
+            for ic in range(nc):
+                k = "c%d" % ic
+                b = self.set_rhs_conc(ic, dt, s[k], conv[k])
+                s[k], _ = self.solve("c", ic, dt, b, s[k])
+            pb = self.pressure_rhs(dt, s["u"], s["v"], s["w"])
+            s["phi"], _ = self.solve("p", 0, dt, pb, s["phi"])
+            s["pb"] = pb
+            self.project(dt, s["phi"], pb, s["u"], s["v"], s["w"], s["dpx"], s["dpy"], s["dpz"])
+            divs.append(self.divergence(s["u"], s["v"], s["w"])[0])
+        for k, a in old.items():
+            s[k] = 0.5 * a + 0.5 * s[k]
+        return divs
+
     # -- restated line driver around the reference's ghost and ENO routines --
     def convection(self, q, ic, fld, vx, vy, vz):
         """conv = Vx dq/dx + Vy dq/dy + Vz dq/dz over full box lines of

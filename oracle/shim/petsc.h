@@ -149,6 +149,7 @@ int KSPSetInitialGuessNonzero(KSP k, PetscTruth t);
 int KSPSetFromOptions(KSP k);
 int KSPDestroy(KSP k);
 int KSPView(KSP k, PetscViewer v);
+#define PETSC_VIEWER_STDOUT_WORLD ((PetscViewer)0)
 int KSPGMRESSetRestart(KSP k, int r);
 int KSPSetNullSpace(KSP k, MatNullSpace sp);
 int PCSetType(PC pc, PCType t);

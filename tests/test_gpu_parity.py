@@ -373,6 +373,38 @@ def test_deposit_in_step(api, oracle_mod):
     assert np.abs(got - dep).max() <= 1e-9 * dep.max()
 
 
+def _golden_cases():
+    import glob
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    return sorted(glob.glob(os.path.join(here, "*_eno*.npz")))
+
+
+@pytest.mark.parametrize("path", _golden_cases(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_step_matches_reference_trace(api, path):
+    """Two GPU steps from the fixture's state against two steps composed of
+    the reference's own routines (tests/golden/make_golden.py), solvers at
+    relative residual 1e-12: fields agree to the solvers' tolerance."""
+    from tests.test_oracle_golden import load
+    z, g, p, dt = load(path)
+    p.p_rtol = 1e-12
+    p.vel_rtol = 1e-12
+    keys = ["u", "v", "w", "phi", "dpx", "dpy", "dpz"] + ["c%d" % i for i in range(p.nconc)]
+    ctx = api.Context(g, p)
+    ctx.load_state({k: z["in_" + k] for k in keys})
+    for _ in range(2):
+        st = ctx.step(dt)
+        assert max(st["div_max"]) <= 1e-10
+    s = ctx.state()
+    vscale = max(np.abs(z["ref_step2_" + k]).max() for k in "uvw")
+    for k in ("u", "v", "w"):
+        assert np.abs(s[k] - z["ref_step2_" + k]).max() <= 1e-7 * vscale, k
+    for i in range(p.nconc):
+        ref = z["ref_step2_c%d" % i]
+        assert np.abs(s["c%d" % i] - ref).max() <= 1e-9 * max(np.abs(ref).max(), 1.0)
+    ctx.close()
+
+
 def test_failure_paths(api, oracle_mod):
     """Non-convergence and non-finite input come back as status codes; the
     context stays usable afterwards."""
