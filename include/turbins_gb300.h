@@ -376,6 +376,41 @@ int turb_deposit_enable(turb_ctx *ctx, int on);
 int turb_deposit_get(turb_ctx *ctx, double *host);
 int turb_deposit_set(turb_ctx *ctx, const double *host);
 
+/* ---- open boundaries -------------------------------------------------------
+ * params->inflow / outflow of the reference: an inflow face at x = xmin and a
+ * convective outflow face at x = xmax.  turb_set_open_boundaries turns them
+ * on (U: convective velocity params->U; transient_inflow, time_c: the
+ * 1 - exp(-(t + 0.01)/time_c) ramp of Inflow.c) and makes every routine of
+ * the step take the faces into account: cell centres (Velocity.c:1544-1558),
+ * transposes (Velocity.c:3491-3605), RHS of u, v, w, c (Velocity.c:1691-1721,
+ * 1885-1896, 2011-2022; Conc.c:938-962), Helmholtz rows (Velocity.c:989,
+ * 1336; Conc.c:583-606), ENO ghosts of x lines (Velocity.c:2194-2235,
+ * 2442-2449, 2669-2676; Conc.c:1099-1124), pressure RHS and divergence
+ * (Pressure.c:242-248, 541-547), viscous dissipation (Extract.c:582-639).
+ * Planes are [nz+1][ny+1] doubles (j fastest): which 0 = inflow (u: q 0; c:
+ * q 3, ic), 1 = outflow, 2 = outflow_old (q 0..2 = u, v, w, 3 = c_ic).
+ * The routines replace Inflow_u_velocity_profile / Inflow_conc_profile
+ * (Inflow.c:13-260), Outflow_{vel,conc}_impose_convective_boundary with the
+ * mass correction of u (Outflow.c:30-303), *_store_old_outflow /
+ * *_rk_average_outflow (Velocity.c:2059-2118, Conc.c:1224-1290) and
+ * Outflow_*_copy_data_into_{last_plane,2D_array} (Outflow.c:306-503).
+ * turb_set_influx sets u's W_influx that the mass correction uses (normally
+ * left by turb_Inflow_u_velocity_profile). */
+int turb_set_open_boundaries(turb_ctx *ctx, int inflow, int outflow, double U, int transient_inflow,
+                             double time_c);
+int turb_open_plane_get(turb_ctx *ctx, int which, int q, int ic, double *host);
+int turb_open_plane_set(turb_ctx *ctx, int which, int q, int ic, const double *host);
+int turb_Inflow_u_velocity_profile(turb_ctx *ctx, double time, double *influx);
+int turb_Inflow_conc_profile(turb_ctx *ctx, int ic, double time);
+int turb_set_influx(turb_ctx *ctx, double influx);
+int turb_Outflow_vel_impose_convective_boundary(turb_ctx *ctx, char which, double dt);
+int turb_Outflow_conc_impose_convective_boundary(turb_ctx *ctx, int ic, double dt);
+int turb_Outflow_impose_convective_boundary(turb_ctx *ctx, double dt);
+int turb_store_old_outflow(turb_ctx *ctx);
+int turb_rk_average_outflow(turb_ctx *ctx, double old_frac, double new_frac);
+int turb_Outflow_copy_data_into_last_plane(turb_ctx *ctx, char which, int ic, int should_set);
+int turb_Outflow_copy_data_into_2D_array(turb_ctx *ctx, char which, int ic);
+
 /* ---- checkpoint / resume ---------------------------------------------------
  * The reference's restart set (Resume_set_data, Resume.c:208-244) in its
  * formats, written to / read from directory dir:

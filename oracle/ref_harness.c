@@ -557,3 +557,136 @@ int ref_resume_read(ref_case *r, const char *dir, double *const *fields, int gri
     Resume_destroy(rs);
     return chdir(cwd) ? 1 : 0;
 }
+
+/* ---- open boundaries (Inflow.c, Outflow.c and the inflow / outflow
+ * branches of the step routines) ----------------------------------------
+ * ref_set_open turns params->inflow / outflow on and allocates the 2-D
+ * [NZ][NY] arrays Velocity_create / Conc_create would have made
+ * (Velocity.c:128-158, Conc.c:67-98).  Arrays are exchanged flat, j fastest. */
+#include "Inflow.h"
+#include "Outflow.h"
+
+void ref_set_open(ref_case *r, int inflow, int outflow, double U, int transient, double time_c, double Ly,
+                  double Lz)
+{
+    MAC_grid *g = r->g;
+    Parameters *p = r->p;
+    int i;
+    Velocity *V[3] = {r->u, r->v, r->w};
+    p->inflow = (short)inflow;
+    p->outflow = (short)outflow;
+    p->U = U;
+    p->transient_inflow = (short)transient;
+    p->time_c = time_c;
+    p->Ly = Ly;
+    p->Lz = Lz;
+    for (i = 0; i < 3; i++) {
+        if (outflow && !V[i]->G_outflow) {
+            V[i]->G_outflow = Memory_allocate_2D_double(g->NY, g->NZ);
+            V[i]->G_outflow_old = Memory_allocate_2D_double(g->NY, g->NZ);
+        }
+    }
+    if (inflow && !r->u->G_inflow) r->u->G_inflow = Memory_allocate_2D_double(g->NY, g->NZ);
+    for (i = 0; i < p->NConc; i++) {
+        Concentration *c = r->c[i];
+        if (outflow && !c->G_outflow) {
+            c->G_outflow = Memory_allocate_2D_double(g->NY, g->NZ);
+            c->G_outflow_old = Memory_allocate_2D_double(g->NY, g->NZ);
+        }
+        if (inflow && !c->G_inflow) c->G_inflow = Memory_allocate_2D_double(g->NY, g->NZ);
+    }
+}
+
+/* which: 0 inflow, 1 outflow, 2 outflow_old; q: 'u', 'v', 'w', 'c' (ic) */
+static double **open_arr(ref_case *r, int which, char q, int ic)
+{
+    if (q == 'c') {
+        Concentration *c = r->c[ic];
+        return which == 0 ? c->G_inflow : which == 1 ? c->G_outflow : c->G_outflow_old;
+    } else {
+        Velocity *V = vel_of(r, q);
+        return which == 0 ? V->G_inflow : which == 1 ? V->G_outflow : V->G_outflow_old;
+    }
+}
+
+void ref_open_set(ref_case *r, int which, char q, int ic, const double *a)
+{
+    double **d = open_arr(r, which, q, ic);
+    int j, k;
+    for (k = 0; k < r->g->NZ; k++)
+        for (j = 0; j < r->g->NY; j++) d[k][j] = a[(long)k * r->g->NY + j];
+}
+
+void ref_open_get(ref_case *r, int which, char q, int ic, double *a)
+{
+    double **d = open_arr(r, which, q, ic);
+    int j, k;
+    for (k = 0; k < r->g->NZ; k++)
+        for (j = 0; j < r->g->NY; j++) a[(long)k * r->g->NY + j] = d[k][j];
+}
+
+/* Inflow_u_velocity_profile (returns W_influx) and Inflow_conc_profile */
+double ref_inflow_u(ref_case *r, double time)
+{
+    Inflow_u_velocity_profile(r->u, r->g, r->p, time);
+    return r->u->W_influx;
+}
+
+void ref_inflow_c(ref_case *r, int ic, double time) { Inflow_conc_profile(r->c[ic], r->g, r->p, time); }
+
+/* Outflow_vel_impose_convective_boundary (with the mass correction for u,
+ * from the influx `influx`) / Outflow_conc_impose_convective_boundary on the
+ * field x */
+void ref_outflow_impose(ref_case *r, char q, int ic, double dt, const double *x, double influx)
+{
+    if (q == 'c') {
+        vset(r->c[ic]->G_data, x, r->n);
+        Outflow_conc_impose_convective_boundary(r->c[ic], r->g, r->p, dt);
+    } else {
+        Velocity *V = vel_of(r, q);
+        vset(V->G_data, x, r->n);
+        r->u->W_influx = influx;
+        Outflow_vel_impose_convective_boundary(V, r->g, r->p, dt);
+    }
+}
+
+/* *_store_old_outflow and *_rk_average_outflow of one quantity */
+void ref_outflow_store_old(ref_case *r, char q, int ic)
+{
+    if (q == 'c') Conc_store_old_outflow(r->c[ic]);
+    else Velocity_store_old_outflow(vel_of(r, q));
+}
+
+void ref_outflow_rk_average(ref_case *r, char q, int ic, double old_frac, double new_frac)
+{
+    if (q == 'c') Conc_rk_average_outflow(r->c[ic], old_frac, new_frac);
+    else Velocity_rk_average_outflow(vel_of(r, q), old_frac, new_frac);
+}
+
+/* Outflow_*_copy_data_into_last_plane (field x in / out) and
+ * Outflow_*_copy_data_into_2D_array */
+void ref_outflow_to_plane(ref_case *r, char q, int ic, int should_set, double *x)
+{
+    if (q == 'c') {
+        vset(r->c[ic]->G_data, x, r->n);
+        Outflow_concentration_copy_data_into_last_plane(r->c[ic], r->g, should_set);
+        vget(r->c[ic]->G_data, x, r->n);
+    } else {
+        Velocity *V = vel_of(r, q);
+        vset(V->G_data, x, r->n);
+        Outflow_vel_copy_data_into_last_plane(V, r->g, should_set);
+        vget(V->G_data, x, r->n);
+    }
+}
+
+void ref_outflow_from_plane(ref_case *r, char q, int ic, const double *x)
+{
+    if (q == 'c') {
+        vset(r->c[ic]->G_data, x, r->n);
+        Outflow_concentration_copy_data_into_2D_array(r->c[ic], r->g);
+    } else {
+        Velocity *V = vel_of(r, q);
+        vset(V->G_data, x, r->n);
+        Outflow_vel_copy_data_into_2D_array(V, r->g);
+    }
+}

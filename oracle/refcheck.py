@@ -200,6 +200,52 @@ class Reference:
         m = self.lib.ref_divergence(self.h, _p(u), _p(v), _p(w), _p(d))
         return m, d
 
+    # -- open boundaries ----------------------------------------------------
+    OPEN = {"in": 0, "out": 1, "out_old": 2}
+
+    def set_open(self, inflow, outflow, U=1.0, transient=0, time_c=1.0):
+        g = self.g
+        self.lib.ref_set_open(self.h, int(inflow), int(outflow), C.c_double(U), int(transient), C.c_double(time_c),
+                              C.c_double(g.yv[-1] - g.yv[0]), C.c_double(g.zw[-1] - g.zw[0]))
+
+    def _plane(self):
+        return np.zeros((self.g.nz + 1, self.g.ny + 1))
+
+    def open_set(self, which, q, ic, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self.lib.ref_open_set(self.h, self.OPEN[which], C.c_char(q.encode()), int(ic), _p(a))
+
+    def open_get(self, which, q, ic=0):
+        a = self._plane()
+        self.lib.ref_open_get(self.h, self.OPEN[which], C.c_char(q.encode()), int(ic), _p(a))
+        return a
+
+    def inflow_u(self, time):
+        self.lib.ref_inflow_u.restype = C.c_double
+        return self.lib.ref_inflow_u(self.h, C.c_double(time))
+
+    def inflow_c(self, ic, time):
+        self.lib.ref_inflow_c(self.h, int(ic), C.c_double(time))
+
+    def outflow_impose(self, q, ic, dt, x, influx=0.0):
+        self.lib.ref_outflow_impose(self.h, C.c_char(q.encode()), int(ic), C.c_double(dt),
+                                    _p(np.ascontiguousarray(x)), C.c_double(influx))
+
+    def outflow_store_old(self, q, ic=0):
+        self.lib.ref_outflow_store_old(self.h, C.c_char(q.encode()), int(ic))
+
+    def outflow_rk_average(self, q, ic, old_frac, new_frac):
+        self.lib.ref_outflow_rk_average(self.h, C.c_char(q.encode()), int(ic), C.c_double(old_frac),
+                                        C.c_double(new_frac))
+
+    def outflow_to_plane(self, q, ic, should_set, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        self.lib.ref_outflow_to_plane(self.h, C.c_char(q.encode()), int(ic), int(should_set), _p(x))
+        return x
+
+    def outflow_from_plane(self, q, ic, x):
+        self.lib.ref_outflow_from_plane(self.h, C.c_char(q.encode()), int(ic), _p(np.ascontiguousarray(x)))
+
     def c_term(self, ct):
         """the buoyancy term at v nodes that Velocity_v_set_RHS computes
         (2-point y interpolation of the total concentration, Velocity.c:1861-

@@ -317,6 +317,59 @@ class Context:
             raise ValueError("deposit shape %s, expected %s" % (dep.shape, self._bed_shape()))
         _check(self.lib.turb_deposit_set(self.ctx, _ptr(dep)), "deposit_set")
 
+    # -- open boundaries ----------------------------------------------------
+    OPEN = {"in": 0, "out": 1, "out_old": 2}
+    QIDX = {"u": 0, "v": 1, "w": 2, "c": 3}
+
+    def set_open_boundaries(self, inflow, outflow, U=1.0, transient=False, time_c=1.0):
+        _check(self.lib.turb_set_open_boundaries(self.ctx, int(bool(inflow)), int(bool(outflow)), C.c_double(U),
+                                                 int(bool(transient)), C.c_double(time_c)), "set_open_boundaries")
+
+    def open_plane(self, which, q, ic=0):
+        a = np.zeros((self.grid.nz + 1, self.grid.ny + 1))
+        _check(self.lib.turb_open_plane_get(self.ctx, self.OPEN[which], self.QIDX[q], int(ic), _ptr(a)),
+               "open_plane_get")
+        return a
+
+    def set_open_plane(self, which, q, ic, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _check(self.lib.turb_open_plane_set(self.ctx, self.OPEN[which], self.QIDX[q], int(ic), _ptr(a)),
+               "open_plane_set")
+
+    def Inflow_u_velocity_profile(self, time):
+        f = C.c_double()
+        _check(self.lib.turb_Inflow_u_velocity_profile(self.ctx, C.c_double(time), C.byref(f)), "inflow_u")
+        return f.value
+
+    def Inflow_conc_profile(self, ic, time):
+        _check(self.lib.turb_Inflow_conc_profile(self.ctx, int(ic), C.c_double(time)), "inflow_c")
+
+    def set_influx(self, influx):
+        _check(self.lib.turb_set_influx(self.ctx, C.c_double(influx)), "set_influx")
+
+    def Outflow_vel_impose_convective_boundary(self, which, dt):
+        _check(self.lib.turb_Outflow_vel_impose_convective_boundary(self.ctx, C.c_char(which.encode()),
+                                                                    C.c_double(dt)), "outflow_vel")
+
+    def Outflow_conc_impose_convective_boundary(self, ic, dt):
+        _check(self.lib.turb_Outflow_conc_impose_convective_boundary(self.ctx, int(ic), C.c_double(dt)),
+               "outflow_conc")
+
+    def store_old_outflow(self):
+        _check(self.lib.turb_store_old_outflow(self.ctx), "store_old_outflow")
+
+    def rk_average_outflow(self, old_frac=0.5, new_frac=0.5):
+        _check(self.lib.turb_rk_average_outflow(self.ctx, C.c_double(old_frac), C.c_double(new_frac)),
+               "rk_average_outflow")
+
+    def Outflow_copy_data_into_last_plane(self, which, ic, should_set):
+        _check(self.lib.turb_Outflow_copy_data_into_last_plane(self.ctx, C.c_char(which.encode()), int(ic),
+                                                               int(bool(should_set))), "copy_into_last_plane")
+
+    def Outflow_copy_data_into_2D_array(self, which, ic):
+        _check(self.lib.turb_Outflow_copy_data_into_2D_array(self.ctx, C.c_char(which.encode()), int(ic)),
+               "copy_into_2d")
+
     def resume_write(self, dirname, prim, grid=False, deposit=False, phi=False):
         """turb_resume_write: the reference's restart set (+ options) into dirname"""
         flags = (RESUME_GRID if grid else 0) | (RESUME_DEPOSIT if deposit else 0) | (RESUME_PHI if phi else 0)

@@ -48,7 +48,8 @@ __device__ double visc_term(const DiagIn &a, int i, int j, int k, long long p)
     double U_w, U_e, U_n, U_s, U_f, U_b, V_w, V_e, V_n, V_s, V_f, V_b, W_w, W_e, W_n, W_s, W_f, W_b;
     if (i == 0) {
         U_aw = MUL(U_aw, g.mxc[i]);
-        U_w = 0.0; V_w = MUL(a.kw[0], v_); W_w = MUL(a.kw[0], w_);
+        U_w = a.ob.in ? a.ob.pl(a.ob.u_in, j, k) : 0.0;   // Extract.c:582-592
+        V_w = MUL(a.kw[0], v_); W_w = MUL(a.kw[0], w_);
     } else {
         U_aw = MUL(U_aw, g.mxc[i - 1]);
         U_w = u[p - 1]; V_w = v[p - 1]; W_w = w[p - 1];
@@ -68,7 +69,11 @@ __device__ double visc_term(const DiagIn &a, int i, int j, int k, long long p)
         U_b = u[p - d.plane]; V_b = v[p - d.plane]; W_b = w[p - d.plane];
     }
     if (i == NI - 1) {
-        U_e = 0.0; V_e = MUL(a.kw[1], v_); W_e = MUL(a.kw[1], w_);
+        if (a.ob.out) {   // Extract.c:634-639
+            U_e = a.ob.pl(a.ob.out_f[0], j, k); V_e = a.ob.pl(a.ob.out_f[1], j, k); W_e = a.ob.pl(a.ob.out_f[2], j, k);
+        } else {
+            U_e = 0.0; V_e = MUL(a.kw[1], v_); W_e = MUL(a.kw[1], w_);
+        }
     } else {
         U_e = u[p + 1]; V_e = v[p + 1]; W_e = w[p + 1];
     }

@@ -52,22 +52,41 @@ __device__ __forceinline__ double adv_vel(const AdvSrc &a, const Dims &d, long l
     case 1: return ad(f[p], a.shift);
     case 2: return interp4(f[p - X], f[p], f[p - X + Y], f[p + Y], a.wx.w0[i], a.wx.w1[i], a.wy.w0[j], a.wy.w1[j]);
     case 3: return interp4(f[p - X], f[p], f[p - X + Z], f[p + Z], a.wx.w0[i], a.wx.w1[i], a.wy.w0[k], a.wy.w1[k]);
-    case 4: return interp4(f[p - Y], f[p - Y + X], f[p], f[p + X], a.wx.w0[i], a.wx.w1[i], a.wy.w0[j], a.wy.w1[j]);
+    case 4: {
+        double q0 = f[p - Y], q1 = f[p - Y + X], q2 = f[p], q3 = f[p + X];
+        if (a.pin && i == 0 && j > 0) { q0 = a.pin[(long long)k * a.pNY + j - 1]; q2 = a.pin[(long long)k * a.pNY + j]; }
+        if (a.pout && i == a.nx - 1 && j > 0) {
+            q1 = a.pout[(long long)k * a.pNY + j - 1];
+            q3 = a.pout[(long long)k * a.pNY + j];
+        }
+        return interp4(q0, q1, q2, q3, a.wx.w0[i], a.wx.w1[i], a.wy.w0[j], a.wy.w1[j]);
+    }
     case 5: return interp4(f[p - Y], f[p - Y + Z], f[p], f[p + Z], a.wx.w0[k], a.wx.w1[k], a.wy.w0[j], a.wy.w1[j]);
-    case 6: return interp4(f[p - Z], f[p - Z + X], f[p], f[p + X], a.wx.w0[i], a.wx.w1[i], a.wy.w0[k], a.wy.w1[k]);
+    case 6: {
+        double q0 = f[p - Z], q1 = f[p - Z + X], q2 = f[p], q3 = f[p + X];
+        if (a.pin && i == 0 && k > 0) { q0 = a.pin[(long long)(k - 1) * a.pNY + j]; q2 = a.pin[(long long)k * a.pNY + j]; }
+        if (a.pout && i == a.nx - 1 && k > 0) {
+            q1 = a.pout[(long long)(k - 1) * a.pNY + j];
+            q3 = a.pout[(long long)k * a.pNY + j];
+        }
+        return interp4(q0, q1, q2, q3, a.wx.w0[i], a.wx.w1[i], a.wy.w0[k], a.wy.w1[k]);
+    }
     default: return interp4(f[p - Z], f[p], f[p - Z + Y], f[p + Y], a.wx.w0[k], a.wx.w1[k], a.wy.w0[j], a.wy.w1[j]);
     }
 }
 
-// D0 of buffer index b (ghost rules precomputed in the table)
+// D0 of buffer index b (ghost rules precomputed in the table; line = k*NY + j
+// of an x line, for the open-face planes)
 __device__ __forceinline__ double d0_at(const EnoTab &T, const double *__restrict__ q, long long base,
-                                        long long stride, int b, double qf, double ql)
+                                        long long stride, int b, double qf, double ql, long long line = 0)
 {
     int r = T.r;
     if (b >= r && b < T.nb - r) return q[base + (long long)(b - r + T.s0) * stride];
     int gi = (b < r) ? b : 3 + (T.nb - 1 - b);
     int src = T.gsrc[gi];
     if (src == 0) return 0.0;
+    if (src == 3) return T.glo[line];
+    if (src == 4) return T.ghi[line];
     return ml(T.gm[gi], src == 1 ? qf : ql);
 }
 
@@ -106,7 +125,8 @@ __global__ void k_eno_x(Dims d, EnoTab T, const double *__restrict__ q, AdvSrc a
     int j = t1a + blockIdx.x, k = t2a + blockIdx.y;
     long long base = d.at(0, j, k);
     double qf = q[base + T.s0], ql = q[base + T.e0];
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) s0[b] = d0_at(T, q, base, 1, b, qf, ql);
+    const long long line = (long long)k * T.gNY + j;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s0[b] = d0_at(T, q, base, 1, b, qf, ql, line);
     __syncthreads();
     for (int b = threadIdx.x; b < nb - 1; b += blockDim.x) s1[b] = dd(T, sb(s0[b + 1], s0[b]), T.h1, T.rh1, b, 1);
     __syncthreads();

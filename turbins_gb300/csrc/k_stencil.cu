@@ -47,21 +47,25 @@ __device__ __forceinline__ Ijk ijk_of(const Dims &d)
     return r;
 }
 
-// Velocity_cell_center, Velocity.c:1476-1602
-__global__ void k_cell_center(Dims d, Interp2 ix, Interp2 iy, Interp2 iz, const double *__restrict__ u,
+// Velocity_cell_center, Velocity.c:1476-1602 (u on the inflow / outflow
+// faces from the open-boundary planes, Velocity.c:1544-1558)
+__global__ void k_cell_center(Dims d, Interp2 ix, Interp2 iy, Interp2 iz, OpenBC ob, const double *__restrict__ u,
                               const double *__restrict__ v, const double *__restrict__ w,
                               double *__restrict__ ubc, double *__restrict__ vbc, double *__restrict__ wbc)
 {
     Ijk t = ijk_of(d);
     if (!t.ok || t.i >= d.nx || t.j >= d.ny || t.k >= d.nz) return;
     long long p = d.at(t.i, t.j, t.k);
-    ubc[p] = interp2(u[p], u[p + 1], ix.dx[t.i], ix.dq[t.i], ix.flat[t.i]);
+    double u0 = (ob.in && t.i == 0) ? ob.pl(ob.u_in, t.j, t.k) : u[p];
+    double u1 = (ob.out && t.i == d.nx - 1) ? ob.pl(ob.out_f[0], t.j, t.k) : u[p + 1];
+    ubc[p] = interp2(u0, u1, ix.dx[t.i], ix.dq[t.i], ix.flat[t.i]);
     vbc[p] = interp2(v[p], v[p + d.PX], iy.dx[t.j], iy.dq[t.j], iy.flat[t.j]);
     wbc[p] = interp2(w[p], w[p + d.plane], iz.dx[t.k], iz.dq[t.k], iz.flat[t.k]);
 }
 
-// Velocity_transpose_velocities, Velocity.c:3341-3663
-__global__ void k_transpose(Dims d, int which, const uint8_t *__restrict__ st, TransW tw,
+// Velocity_transpose_velocities, Velocity.c:3341-3663 (u from the inflow /
+// outflow planes next to the open faces, Velocity.c:3491-3507, 3589-3605)
+__global__ void k_transpose(Dims d, int which, const uint8_t *__restrict__ st, TransW tw, OpenBC ob,
                             const double *__restrict__ u, const double *__restrict__ v,
                             const double *__restrict__ w, double *__restrict__ A, double *__restrict__ B)
 {
@@ -75,10 +79,16 @@ __global__ void k_transpose(Dims d, int which, const uint8_t *__restrict__ st, T
         A[p] = interp4(v[p - X], v[p], v[p - X + Y], v[p + Y], tw.xu.w0[i], tw.xu.w1[i], tw.yc.w0[j], tw.yc.w1[j]);
         B[p] = interp4(w[p - X], w[p], w[p - X + Z], w[p + Z], tw.xu.w0[i], tw.xu.w1[i], tw.zc.w0[k], tw.zc.w1[k]);
     } else if (which == 1) {
-        A[p] = interp4(u[p - Y], u[p - Y + X], u[p], u[p + X], tw.xc.w0[i], tw.xc.w1[i], tw.yv.w0[j], tw.yv.w1[j]);
+        double q0 = u[p - Y], q1 = u[p - Y + X], q2 = u[p], q3 = u[p + X];
+        if (ob.in && i == 0 && j > 0) { q0 = ob.pl(ob.u_in, j - 1, k); q2 = ob.pl(ob.u_in, j, k); }
+        if (ob.out && i == d.nx - 1 && j > 0) { q1 = ob.pl(ob.out_f[0], j - 1, k); q3 = ob.pl(ob.out_f[0], j, k); }
+        A[p] = interp4(q0, q1, q2, q3, tw.xc.w0[i], tw.xc.w1[i], tw.yv.w0[j], tw.yv.w1[j]);
         B[p] = interp4(w[p - Y], w[p - Y + Z], w[p], w[p + Z], tw.zc.w0[k], tw.zc.w1[k], tw.yv.w0[j], tw.yv.w1[j]);
     } else {
-        A[p] = interp4(u[p - Z], u[p - Z + X], u[p], u[p + X], tw.xc.w0[i], tw.xc.w1[i], tw.zw.w0[k], tw.zw.w1[k]);
+        double q0 = u[p - Z], q1 = u[p - Z + X], q2 = u[p], q3 = u[p + X];
+        if (ob.in && i == 0 && k > 0) { q0 = ob.pl(ob.u_in, j, k - 1); q2 = ob.pl(ob.u_in, j, k); }
+        if (ob.out && i == d.nx - 1 && k > 0) { q1 = ob.pl(ob.out_f[0], j, k - 1); q3 = ob.pl(ob.out_f[0], j, k); }
+        A[p] = interp4(q0, q1, q2, q3, tw.xc.w0[i], tw.xc.w1[i], tw.zw.w0[k], tw.zw.w1[k]);
         B[p] = interp4(v[p - Z], v[p], v[p - Z + Y], v[p + Y], tw.zw.w0[k], tw.zw.w1[k], tw.yc.w0[j], tw.yc.w1[j]);
     }
 }
@@ -101,11 +111,14 @@ __global__ void k_shift(long long n, const double *__restrict__ x, double s, dou
     y[p] = ad(x[p], s);
 }
 
-// Velocity_{u,v,w}_set_RHS, Velocity.c:1607-2043
+// Velocity_{u,v,w}_set_RHS, Velocity.c:1607-2043; open boundaries add the
+// known face values of the boundary-adjacent rows (u: inflow at i = 1,
+// outflow at i = nx-1, Velocity.c:1691-1721; v, w: outflow at i = nx-1,
+// Velocity.c:1885-1896, 2011-2022)
 __global__ void k_rhs_vel(Dims d, int q, const uint8_t *__restrict__ st, double a_dt,
                           const double *__restrict__ x, const double *__restrict__ conv,
                           const double *__restrict__ dp, const double *__restrict__ ct, int buoy,
-                          Interp2 iyv, double *__restrict__ b)
+                          Interp2 iyv, OpenBC ob, double *__restrict__ b)
 {
     Ijk t = ijk_of(d);
     if (!t.ok) return;
@@ -114,6 +127,12 @@ __global__ void k_rhs_vel(Dims d, int q, const uint8_t *__restrict__ st, double 
     double r = 0.0;
     if (s == T_FLUID || s == T_BUFFER_SOLID) {
         r = sb(sb(ml(x[p], a_dt), conv[p]), dp[p]);
+        if (q == 0) {
+            if (ob.in && t.i == 1) r = ad(r, ml(ob.u_aw, ob.pl(ob.u_in, t.j, t.k)));
+            if (ob.out && t.i == d.nx - 1) r = ad(r, ml(ob.u_ae, ob.pl(ob.out_f[0], t.j, t.k)));
+        } else if (ob.out && t.i == d.nx - 1) {
+            r = ad(r, ml(ob.vw_ae[q - 1], ob.pl(ob.out_f[q], t.j, t.k)));
+        }
         if (q == 1 && buoy) {
             double c = interp2(ct[p - d.PX], ct[p], iyv.dx[t.j], iyv.dq[t.j], iyv.flat[t.j]);
             r = sb(r, c);
@@ -122,19 +141,27 @@ __global__ void k_rhs_vel(Dims d, int q, const uint8_t *__restrict__ st, double 
     b[p] = r;
 }
 
-// Conc_set_RHS, Conc.c:864-992
-__global__ void k_rhs_conc(long long n, const uint8_t *__restrict__ st, double a_dt,
-                           const double *__restrict__ c, const double *__restrict__ conv,
+// Conc_set_RHS, Conc.c:864-992 (inflow at i = 0, outflow at i = nx-1:
+// Conc.c:938-962)
+__global__ void k_rhs_conc(Dims d, int ic, const uint8_t *__restrict__ st, double a_dt,
+                           const double *__restrict__ c, const double *__restrict__ conv, OpenBC ob,
                            double *__restrict__ b)
 {
-    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    b[p] = (st[p] == T_FLUID) ? sb(ml(c[p], a_dt), conv[p]) : 0.0;
+    Ijk t = ijk_of(d);
+    if (!t.ok) return;
+    long long p = d.at(t.i, t.j, t.k);
+    double r = 0.0;
+    if (st[p] == T_FLUID) {
+        r = sb(ml(c[p], a_dt), conv[p]);
+        if (ob.in && t.i == 0) r = ad(r, ml(ob.c_aw[ic], ob.pl(ob.c_in[ic], t.j, t.k)));
+        if (ob.out && t.i == d.nx - 1) r = ad(r, ml(ob.c_ae[ic], ob.pl(ob.out_f[3 + ic], t.j, t.k)));
+    }
+    b[p] = r;
 }
 
 // Pressure_set_RHS, Pressure.c:171-276
 __global__ void k_pressure_rhs(Dims d, const uint8_t *__restrict__ st, const double *__restrict__ cx,
-                               const double *__restrict__ cy, const double *__restrict__ cz, double a_dt,
+                               const double *__restrict__ cy, const double *__restrict__ cz, double a_dt, OpenBC ob,
                                const double *__restrict__ u, const double *__restrict__ v,
                                const double *__restrict__ w, double *__restrict__ b)
 {
@@ -143,7 +170,10 @@ __global__ void k_pressure_rhs(Dims d, const uint8_t *__restrict__ st, const dou
     long long p = d.at(t.i, t.j, t.k);
     double r = 0.0;
     if (st[p] != T_BOUNDARY) {
-        double dudx = ml(sb(u[p + 1], u[p]), cx[t.i]);
+        double ue = u[p + 1], uw = u[p];   // open faces: Pressure.c:242-248
+        if (ob.in && t.i == 0) uw = ob.pl(ob.u_in, t.j, t.k);
+        if (ob.out && t.i == d.nx - 1) ue = ob.pl(ob.out_f[0], t.j, t.k);
+        double dudx = ml(sb(ue, uw), cx[t.i]);
         double dvdy = ml(sb(v[p + d.PX], v[p]), cy[t.j]);
         double dwdz = ml(sb(w[p + d.plane], w[p]), cz[t.k]);
         r = ml(-ad(ad(dudx, dvdy), dwdz), a_dt);
@@ -185,7 +215,7 @@ __global__ void k_project(Dims d, ProjArgs a, const double *__restrict__ phi, co
 // Pressure_compute_velocity_divergence, Pressure.c:462-586 (block max)
 __global__ void k_divergence(Dims d, const uint8_t *__restrict__ st, const double *__restrict__ mxc,
                              const double *__restrict__ myc, const double *__restrict__ mzc, double a_dEta,
-                             double a_dXi, double a_dPhi, const double *__restrict__ u,
+                             double a_dXi, double a_dPhi, OpenBC ob, const double *__restrict__ u,
                              const double *__restrict__ v, const double *__restrict__ w,
                              double *__restrict__ div, double *__restrict__ part)
 {
@@ -194,7 +224,10 @@ __global__ void k_divergence(Dims d, const uint8_t *__restrict__ st, const doubl
     if (t.ok) {
         long long p = d.at(t.i, t.j, t.k);
         if (st[p] != T_BOUNDARY) {
-            double dudx = ml(ml(sb(u[p + 1], u[p]), a_dEta), mxc[t.i]);
+            double ue = u[p + 1], uw = u[p];   // open faces: Pressure.c:541-547
+            if (ob.in && t.i == 0) uw = ob.pl(ob.u_in, t.j, t.k);
+            if (ob.out && t.i == d.nx - 1) ue = ob.pl(ob.out_f[0], t.j, t.k);
+            double dudx = ml(ml(sb(ue, uw), a_dEta), mxc[t.i]);
             double dvdy = ml(ml(sb(v[p + d.PX], v[p]), a_dXi), myc[t.j]);
             double dwdz = ml(ml(sb(w[p + d.plane], w[p]), a_dPhi), mzc[t.k]);
             dc = fabs(ad(ad(dudx, dvdy), dwdz));
@@ -249,16 +282,16 @@ static inline dim3 grid_of(const Dims &d, int)
     return dim3((unsigned)((d.NX + 31) / 32), (unsigned)((d.NY + 7) / 8), (unsigned)d.NZ);
 }
 
-void launch_cell_center(cudaStream_t s, const Dims &d, Interp2 ix, Interp2 iy, Interp2 iz, const double *u,
-                        const double *v, const double *w, double *ubc, double *vbc, double *wbc)
+void launch_cell_center(cudaStream_t s, const Dims &d, Interp2 ix, Interp2 iy, Interp2 iz, const OpenBC &ob,
+                        const double *u, const double *v, const double *w, double *ubc, double *vbc, double *wbc)
 {
-    k_cell_center<<<grid_of(d, 256), B3, 0, s>>>(d, ix, iy, iz, u, v, w, ubc, vbc, wbc);
+    k_cell_center<<<grid_of(d, 256), B3, 0, s>>>(d, ix, iy, iz, ob, u, v, w, ubc, vbc, wbc);
 }
 
-void launch_transpose(cudaStream_t s, const Dims &d, int which, const uint8_t *st, TransW tw, const double *u,
-                      const double *v, const double *w, double *A, double *B)
+void launch_transpose(cudaStream_t s, const Dims &d, int which, const uint8_t *st, TransW tw, const OpenBC &ob,
+                      const double *u, const double *v, const double *w, double *A, double *B)
 {
-    k_transpose<<<grid_of(d, 256), B3, 0, s>>>(d, which, st, tw, u, v, w, A, B);
+    k_transpose<<<grid_of(d, 256), B3, 0, s>>>(d, which, st, tw, ob, u, v, w, A, B);
 }
 
 void launch_total_conc(cudaStream_t s, long long n, int nc, ConcPtrs c, ConcW a, double *ct)
@@ -272,22 +305,23 @@ void launch_shift(cudaStream_t s, long long n, const double *x, double sh, doubl
 }
 
 void launch_rhs_vel(cudaStream_t s, const Dims &d, int q, const uint8_t *st, double a_dt, const double *x,
-                    const double *conv, const double *dp, const double *ct, int buoy, Interp2 iyv, double *b)
+                    const double *conv, const double *dp, const double *ct, int buoy, Interp2 iyv,
+                    const OpenBC &ob, double *b)
 {
-    k_rhs_vel<<<grid_of(d, 256), B3, 0, s>>>(d, q, st, a_dt, x, conv, dp, ct, buoy, iyv, b);
+    k_rhs_vel<<<grid_of(d, 256), B3, 0, s>>>(d, q, st, a_dt, x, conv, dp, ct, buoy, iyv, ob, b);
 }
 
-void launch_rhs_conc(cudaStream_t s, long long n, const uint8_t *st, double a_dt, const double *c,
-                     const double *conv, double *b)
+void launch_rhs_conc(cudaStream_t s, const Dims &d, int ic, const uint8_t *st, double a_dt, const double *c,
+                     const double *conv, const OpenBC &ob, double *b)
 {
-    k_rhs_conc<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, st, a_dt, c, conv, b);
+    k_rhs_conc<<<grid_of(d, 256), B3, 0, s>>>(d, ic, st, a_dt, c, conv, ob, b);
 }
 
 void launch_pressure_rhs(cudaStream_t s, const Dims &d, const uint8_t *st, const double *cx, const double *cy,
-                         const double *cz, double a_dt, const double *u, const double *v, const double *w,
-                         double *b)
+                         const double *cz, double a_dt, const OpenBC &ob, const double *u, const double *v,
+                         const double *w, double *b)
 {
-    k_pressure_rhs<<<grid_of(d, 256), B3, 0, s>>>(d, st, cx, cy, cz, a_dt, u, v, w, b);
+    k_pressure_rhs<<<grid_of(d, 256), B3, 0, s>>>(d, st, cx, cy, cz, a_dt, ob, u, v, w, b);
 }
 
 void launch_project(cudaStream_t s, const Dims &d, ProjArgs a, const double *phi, const double *pb, double *u,
@@ -303,11 +337,11 @@ long long divergence_parts(const Dims &d)
 }
 
 void launch_divergence(cudaStream_t s, const Dims &d, const uint8_t *st, const double *mxc, const double *myc,
-                       const double *mzc, double a_dEta, double a_dXi, double a_dPhi, const double *u,
-                       const double *v, const double *w, double *div, double *part, double *out)
+                       const double *mzc, double a_dEta, double a_dXi, double a_dPhi, const OpenBC &ob,
+                       const double *u, const double *v, const double *w, double *div, double *part, double *out)
 {
     dim3 g = grid_of(d, 256);
-    k_divergence<<<g, B3, 0, s>>>(d, st, mxc, myc, mzc, a_dEta, a_dXi, a_dPhi, u, v, w, div, part);
+    k_divergence<<<g, B3, 0, s>>>(d, st, mxc, myc, mzc, a_dEta, a_dXi, a_dPhi, ob, u, v, w, div, part);
     k_max_final<<<1, 1024, 0, s>>>((long long)g.x * g.y * g.z, part, out);
 }
 

@@ -15,6 +15,18 @@
 #include "turb_internal.cuh"
 #include "turb_diag.cuh"
 
+// open boundaries (k_open.cu)
+int open_parts(const Dims &d);
+void launch_inflow_u(cudaStream_t s, const Dims &d, const uint8_t *st_u, const double *yv, const double *zw,
+                     double tf, double *in, double *part, double *influx);
+void launch_inflow_c(cudaStream_t s, const Dims &d, const uint8_t *st_c, double tf, double *in);
+void launch_outflow_conv(cudaStream_t s, const Dims &d, const uint8_t *st, double coef, const double *q, double *out);
+void launch_outflow_mass(cudaStream_t s, const Dims &d, const uint8_t *st_u, const double *yv, const double *zw,
+                         const double *influx, double *out, double *part, double *res);
+void launch_plane_axpby(cudaStream_t s, int n, double a, const double *old, double b, double *out);
+void launch_plane_to_field(cudaStream_t s, const Dims &d, const double *pl, int set, double *q);
+void launch_field_to_plane(cudaStream_t s, const Dims &d, const double *q, double *pl);
+
 // restart files (k_resume.cu, turb_resume.cu)
 void launch_pack_be(cudaStream_t s, const Dims &d, const double *src, unsigned long long *dst);
 void launch_pack_status_be(cudaStream_t s, const Dims &d, const uint8_t *st, unsigned long long *dst);
@@ -148,6 +160,15 @@ struct turb_ctx {
     int32_t *bed_iy = nullptr;
     double *dep = nullptr;
     int deposit_on = 0;
+    // open boundaries: the planes of Inflow.c / Outflow.c ([NZ][NY]) and the
+    // device view the kernels take; conc x-pass ENO tables per fraction
+    OpenBC ob;
+    double *pl_in_u = nullptr, *pl_in_c[TURB_MAXCONC] = {}, *pl_out[3 + TURB_MAXCONC] = {},
+           *pl_out_old[3 + TURB_MAXCONC] = {};
+    double open_U = 0.0, open_time_c = 1.0;
+    int open_transient = 0;
+    double *open_scr = nullptr;   // partials; influx at [open_parts], mass results after it
+    EnoTab eno_cx[TURB_MAXCONC];
     // restart staging: one field as big-endian words, on the device and pinned
     unsigned long long *rs_dev = nullptr;
     void *rs_host = nullptr;
@@ -367,8 +388,14 @@ HelmTab mk_helm(turb_ctx *c, int q, int ic)
         } else {
             aw[i] = i > 0 ? a_w : 0.0;
             ae[i] = i < nx - 1 ? a_e : 0.0;
-            if (i == 0) apx[i] += q == 3 ? a_w : wallfold(a_w, ns[0]);
-            if (i == nx - 1) apx[i] += q == 3 ? a_e : wallfold(a_e, ns[1]);
+            // open faces: concentration drops the Neumann fold (Conc.c:583-606,
+            // the face value goes to the RHS); v and w keep the east column
+            // at i = nx (Velocity.c:989, 1336)
+            if (i == 0 && !(q == 3 && c->ob.in)) apx[i] += q == 3 ? a_w : wallfold(a_w, ns[0]);
+            if (i == nx - 1) {
+                if (c->ob.out && q != 3) ae[i] = a_e;
+                else if (!(c->ob.out && q == 3)) apx[i] += q == 3 ? a_e : wallfold(a_e, ns[1]);
+            }
         }
     }
     // y
@@ -1089,6 +1116,231 @@ int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost)
     return TURB_OK;
 }
 
+// ---- open boundaries ------------------------------------------------------
+int turb_set_open_boundaries(turb_ctx *c, int inflow, int outflow, double U, int transient_inflow, double time_c)
+{
+    if (!c || !(time_c > 0.0)) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    int np = d.NY * d.NZ, nc = c->prm.nconc;
+    if (!c->open_scr) {
+        c->pl_in_u = c->mem.alloc<double>(np);
+        for (int q = 0; q < 3 + TURB_MAXCONC; q++) {
+            c->pl_out[q] = c->mem.alloc<double>(np);
+            c->pl_out_old[q] = c->mem.alloc<double>(np);
+        }
+        for (int ic = 0; ic < TURB_MAXCONC; ic++) c->pl_in_c[ic] = c->mem.alloc<double>(np);
+        c->open_scr = c->mem.alloc<double>(open_parts(d) + 8);
+        if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+    }
+    c->open_U = U;
+    c->open_transient = transient_inflow ? 1 : 0;
+    c->open_time_c = time_c;
+    OpenBC &o = c->ob;
+    o = OpenBC();
+    o.in = inflow ? 1 : 0;
+    o.out = outflow ? 1 : 0;
+    o.NY = d.NY;
+    o.u_in = c->pl_in_u;
+    for (int ic = 0; ic < TURB_MAXCONC; ic++) o.c_in[ic] = c->pl_in_c[ic];
+    for (int q = 0; q < 3 + TURB_MAXCONC; q++) o.out_f[q] = c->pl_out[q];
+    // RHS coefficients of the rows next to the open faces, in the reference's
+    // expression order: u Velocity.c:1691-1717, v / w Velocity.c:1885-1893 and
+    // 2011-2019, c Conc.c:938-960
+    int nx = d.nx;
+    double Cx = -1.0 / (c->prm.re * c->dEta * c->dEta);
+    o.u_aw = -Cx * c->mxu[1] * c->mxc[0];
+    o.u_ae = -Cx * c->mxu[nx - 1] * c->mxc[nx - 1];
+    o.vw_ae[0] = o.vw_ae[1] = -Cx * c->mxc[nx - 1] * c->mxu[nx];
+    for (int ic = 0; ic < nc; ic++) {
+        double Cc = -1.0 / (c->prm.pe[ic] * c->dEta * c->dEta);
+        o.c_aw[ic] = -Cc * c->mxc[0] * c->mxu[0];
+        o.c_ae[ic] = -Cc * c->mxc[nx - 1] * c->mxu[nx - 1];
+    }
+    // operators and ENO x tables follow the faces
+    for (int q = 0; q < 3; q++) c->helm[q] = mk_helm(c, q, 0);
+    for (int ic = 0; ic < nc; ic++) c->helm_c[ic] = mk_helm(c, 3, ic);
+    for (int q = 0; q < 3; q++) c->helmf[q] = mk_helmf(c, c->helm[q]);
+    for (int ic = 0; ic < nc; ic++) c->helmf_c[ic] = mk_helmf(c, c->helm_c[ic]);
+    build_eno(c);
+    int r = c->prm.eno_order;
+    auto open_lo = [&](EnoTab &T, const double *pl) {
+        for (int ex = 0; ex < r; ex++) T.gsrc[ex] = 3;
+        T.glo = pl;
+        T.gNY = d.NY;
+    };
+    auto open_hi = [&](EnoTab &T, const double *pl) {
+        for (int ex = 0; ex < r; ex++) T.gsrc[3 + ex] = 4;
+        T.ghi = pl;
+        T.gNY = d.NY;
+    };
+    // ghosts of x lines at the open faces (Velocity.c:2194-2235, 2442-2449,
+    // 2669-2676; Conc.c:1099-1124)
+    if (o.in) open_lo(c->eno[0][0], c->pl_in_u);
+    if (o.out) {
+        open_hi(c->eno[0][0], c->pl_out[0]);
+        open_hi(c->eno[1][0], c->pl_out[1]);
+        open_hi(c->eno[2][0], c->pl_out[2]);
+    }
+    for (int ic = 0; ic < nc; ic++) {
+        c->eno_cx[ic] = c->eno[3][0];
+        if (o.in) open_lo(c->eno_cx[ic], c->pl_in_c[ic]);
+        if (o.out) open_hi(c->eno_cx[ic], c->pl_out[3 + ic]);
+    }
+    free_graphs(c);
+    return check_launch(c);
+}
+
+static double *open_plane(turb_ctx *c, int which, int q, int ic)
+{
+    if (q < 0 || q > 3 || (q == 3 && (ic < 0 || ic >= c->prm.nconc))) return nullptr;
+    int f = q < 3 ? q : 3 + ic;
+    if (which == 0) return q == 0 ? c->pl_in_u : q == 3 ? c->pl_in_c[ic] : nullptr;
+    if (which == 1) return c->pl_out[f];
+    if (which == 2) return c->pl_out_old[f];
+    return nullptr;
+}
+
+int turb_open_plane_get(turb_ctx *c, int which, int q, int ic, double *host)
+{
+    if (!c || !host || !c->open_scr) return TURB_ERR_ARG;
+    double *p = open_plane(c, which, q, ic);
+    if (!p) return TURB_ERR_ARG;
+    TURB_CHECK(cudaMemcpyAsync(host, p, sizeof(double) * c->d.NY * c->d.NZ, cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_open_plane_set(turb_ctx *c, int which, int q, int ic, const double *host)
+{
+    if (!c || !host || !c->open_scr) return TURB_ERR_ARG;
+    double *p = open_plane(c, which, q, ic);
+    if (!p) return TURB_ERR_ARG;
+    TURB_CHECK(cudaMemcpyAsync(p, host, sizeof(double) * c->d.NY * c->d.NZ, cudaMemcpyHostToDevice, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+static double open_time_factor(const turb_ctx *c, double time)
+{
+    return c->open_transient ? (1.0 - std::exp(-(time + 0.01) / c->open_time_c)) : 1.0;
+}
+
+int turb_Inflow_u_velocity_profile(turb_ctx *c, double time, double *influx)
+{
+    if (!c || !c->ob.in) return TURB_ERR_ARG;
+    double *inf = c->open_scr + open_parts(c->d);
+    launch_inflow_u(c->s, c->d, c->st[0], c->geo.yv, c->geo.zw, open_time_factor(c, time), c->pl_in_u,
+                    c->open_scr, inf);
+    c->launches += 2;
+    if (influx) {
+        TURB_CHECK(cudaMemcpyAsync(influx, inf, sizeof(double), cudaMemcpyDeviceToHost, c->s));
+        TURB_CHECK(cudaStreamSynchronize(c->s));
+    }
+    return check_launch(c);
+}
+
+int turb_set_influx(turb_ctx *c, double influx)
+{
+    if (!c || !c->open_scr) return TURB_ERR_ARG;
+    TURB_CHECK(cudaMemcpyAsync(c->open_scr + open_parts(c->d), &influx, sizeof(double), cudaMemcpyHostToDevice, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+int turb_Inflow_conc_profile(turb_ctx *c, int ic, double time)
+{
+    if (!c || !c->ob.in || ic < 0 || ic >= c->prm.nconc) return TURB_ERR_ARG;
+    launch_inflow_c(c->s, c->d, c->st[3], open_time_factor(c, time), c->pl_in_c[ic]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+static double open_coef(const turb_ctx *c, double dt)
+{
+    int NI = c->d.nx;
+    double dx = c->xu[NI] - c->xu[NI - 1];
+    return dt * c->open_U / dx;
+}
+
+int turb_Outflow_vel_impose_convective_boundary(turb_ctx *c, char which, double dt)
+{
+    int q = qidx(which);
+    if (!c || !c->ob.out || q < 0 || q > 2 || !(dt > 0.0)) return TURB_ERR_ARG;
+    launch_outflow_conv(c->s, c->d, c->st[q], open_coef(c, dt), c->fld[TURB_F_U + q], c->pl_out[q]);
+    c->launches += 1;
+    if (q == 0) {
+        double *inf = c->open_scr + open_parts(c->d);
+        launch_outflow_mass(c->s, c->d, c->st[0], c->geo.yv, c->geo.zw, inf, c->pl_out[0], c->open_scr, inf + 1);
+        c->launches += 3;
+    }
+    return check_launch(c);
+}
+
+int turb_Outflow_conc_impose_convective_boundary(turb_ctx *c, int ic, double dt)
+{
+    if (!c || !c->ob.out || ic < 0 || ic >= c->prm.nconc || !(dt > 0.0)) return TURB_ERR_ARG;
+    launch_outflow_conv(c->s, c->d, c->st[3], open_coef(c, dt), c->fld[TURB_F_C0 + ic], c->pl_out[3 + ic]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Outflow_impose_convective_boundary(turb_ctx *c, double dt)
+{
+    int rc;
+    for (char q : {'u', 'v', 'w'})
+        if ((rc = turb_Outflow_vel_impose_convective_boundary(c, q, dt))) return rc;
+    for (int ic = 0; ic < c->prm.nconc; ic++)
+        if ((rc = turb_Outflow_conc_impose_convective_boundary(c, ic, dt))) return rc;
+    return TURB_OK;
+}
+
+int turb_store_old_outflow(turb_ctx *c)
+{
+    if (!c || !c->ob.out) return TURB_ERR_ARG;
+    size_t b = sizeof(double) * c->d.NY * c->d.NZ;
+    for (int q = 0; q < 3 + c->prm.nconc; q++)
+        TURB_CHECK(cudaMemcpyAsync(c->pl_out_old[q], c->pl_out[q], b, cudaMemcpyDeviceToDevice, c->s));
+    return TURB_OK;
+}
+
+int turb_rk_average_outflow(turb_ctx *c, double old_frac, double new_frac)
+{
+    if (!c || !c->ob.out) return TURB_ERR_ARG;
+    for (int q = 0; q < 3 + c->prm.nconc; q++)
+        launch_plane_axpby(c->s, c->d.NY * c->d.NZ, old_frac, c->pl_out_old[q], new_frac, c->pl_out[q]);
+    c->launches += 3 + c->prm.nconc;
+    return check_launch(c);
+}
+
+static int open_field(turb_ctx *c, char which, int ic)
+{
+    int q = which == 'c' ? 3 : qidx(which);
+    if (q < 0 || q > 3 || (q == 3 && (ic < 0 || ic >= c->prm.nconc))) return -1;
+    return q < 3 ? q : 3 + ic;
+}
+
+int turb_Outflow_copy_data_into_last_plane(turb_ctx *c, char which, int ic, int should_set)
+{
+    if (!c || !c->open_scr) return TURB_ERR_ARG;
+    int f = open_field(c, which, ic);
+    if (f < 0) return TURB_ERR_ARG;
+    double *q = f < 3 ? c->fld[TURB_F_U + f] : c->fld[TURB_F_C0 + f - 3];
+    launch_plane_to_field(c->s, c->d, c->pl_out[f], should_set, q);
+    c->launches += 1;
+    return check_launch(c);
+}
+
+int turb_Outflow_copy_data_into_2D_array(turb_ctx *c, char which, int ic)
+{
+    if (!c || !c->open_scr) return TURB_ERR_ARG;
+    int f = open_field(c, which, ic);
+    if (f < 0) return TURB_ERR_ARG;
+    const double *q = f < 3 ? c->fld[TURB_F_U + f] : c->fld[TURB_F_C0 + f - 3];
+    launch_field_to_plane(c->s, c->d, q, c->pl_out[f]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
 int turb_set_mg_split(turb_ctx *c, int on)
 {
     if (!c) return TURB_ERR_ARG;
@@ -1132,8 +1384,8 @@ int turb_ENO_compute_convective_terms(int order, int n, const double *D0, const 
 int turb_Velocity_cell_center(turb_ctx *c)
 {
     if (!c) return TURB_ERR_ARG;
-    launch_cell_center(c->s, c->d, c->icx, c->icy, c->icz, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W],
-                       c->fld[TURB_F_UBC], c->fld[TURB_F_VBC], c->fld[TURB_F_WBC]);
+    launch_cell_center(c->s, c->d, c->icx, c->icy, c->icz, c->ob, c->fld[TURB_F_U], c->fld[TURB_F_V],
+                       c->fld[TURB_F_W], c->fld[TURB_F_UBC], c->fld[TURB_F_VBC], c->fld[TURB_F_WBC]);
     c->launches += 1;
     return check_launch(c);
 }
@@ -1142,7 +1394,7 @@ int turb_Velocity_transpose_velocities(turb_ctx *c, char which)
 {
     int q = qidx(which);
     if (!c || q < 0 || q > 2) return TURB_ERR_ARG;
-    launch_transpose(c->s, c->d, q, c->st[q], c->tw, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W],
+    launch_transpose(c->s, c->d, q, c->st[q], c->tw, c->ob, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W],
                      c->fld[TURB_F_SCRATCH0], c->fld[TURB_F_SCRATCH1]);
     c->launches += 1;
     return check_launch(c);
@@ -1217,6 +1469,7 @@ int turb_diagnostics(turb_ctx *c, double front_limit, turb_diag *out, double *av
     a.hcoef = 1.0 / (Ly * Lz);
     a.Cx = 1.0 / (c->dEta * c->dEta); a.Cy = 1.0 / (c->dXi * c->dXi); a.Cz = 1.0 / (c->dPhi * c->dPhi);
     for (int q = 0; q < 6; q++) a.kw[q] = c->prm.wall_noslip[q] ? -1.0 : 1.0;
+    a.ob = c->ob;
     a.iy = c->bed_iy;
     a.dep = c->dep;
     DiagOut o;
@@ -1464,6 +1717,15 @@ static AdvSrc adv_of(int kind, const double *a, W2 wx, W2 wy, double shift = 0.0
     return s;
 }
 
+// u next to the open faces for the transposes inside the ENO x pass
+static void open_adv(const turb_ctx *c, AdvSrc &a)
+{
+    a.pin = c->ob.in ? c->pl_in_u : nullptr;
+    a.pout = c->ob.out ? c->pl_out[0] : nullptr;
+    a.pNY = c->d.NY;
+    a.nx = c->d.nx;
+}
+
 int turb_Velocity_convective_terms(turb_ctx *c, char which)
 {
     int q = qidx(which);
@@ -1482,10 +1744,12 @@ int turb_Velocity_convective_terms(turb_ctx *c, char which)
         az = adv_of(3, w, c->tw.xu, c->tw.zc);
     } else if (q == 1) {
         ax = adv_of(4, u, c->tw.xc, c->tw.yv);
+        open_adv(c, ax);
         ay = adv_of(0, v, z, z);
         az = adv_of(5, w, c->tw.zc, c->tw.yv);
     } else {
         ax = adv_of(6, u, c->tw.xc, c->tw.zw);
+        open_adv(c, ax);
         ay = adv_of(7, v, c->tw.zw, c->tw.yc);
         az = adv_of(0, w, z, z);
     }
@@ -1514,7 +1778,8 @@ int turb_Conc_convective_terms(turb_ctx *c, int ic)
     AdvSrc az = adv_of(0, c->fld[TURB_F_WBC], z, z);
     cudaMemsetAsync(conv, 0, d.n * 8, c->s);
     int h = prof_begin(c, TURB_PROF_ENO_X);
-    launch_eno_pass(c->s, d, 0, c->eno[3][0], cf, ax, 0, d.ny - 1, 0, d.nz - 1, 1, conv);
+    launch_eno_pass(c->s, d, 0, c->ob.in || c->ob.out ? c->eno_cx[ic] : c->eno[3][0], cf, ax, 0, d.ny - 1, 0,
+                    d.nz - 1, 1, conv);
     prof_end(c, h, 1);
     h = prof_begin(c, TURB_PROF_ENO_YZ);
     launch_eno_pass(c->s, d, 1, c->eno_cy[ic], cf, ay, 0, d.nx - 1, 0, d.nz - 1, 0, conv);
@@ -1530,7 +1795,7 @@ int turb_Velocity_set_RHS(turb_ctx *c, char which, double dt)
     if (!c || q < 0 || q > 2 || !(dt > 0.0)) return TURB_ERR_ARG;
     const double *ct = c->prm.nconc > 1 ? c->fld[TURB_F_CTOT] : c->fld[TURB_F_C0];
     launch_rhs_vel(c->s, c->d, q, c->st[q], 1.0 / dt, c->fld[TURB_F_U + q], c->fld[TURB_F_CONV_U + q],
-                   c->fld[TURB_F_DPX + q], ct, c->prm.buoyancy, c->iyv, c->fld[TURB_F_B_U + q]);
+                   c->fld[TURB_F_DPX + q], ct, c->prm.buoyancy, c->iyv, c->ob, c->fld[TURB_F_B_U + q]);
     c->launches += 1;
     return check_launch(c);
 }
@@ -1538,7 +1803,7 @@ int turb_Velocity_set_RHS(turb_ctx *c, char which, double dt)
 int turb_Conc_set_RHS(turb_ctx *c, int ic, double dt)
 {
     if (!c || ic < 0 || ic >= c->prm.nconc || !(dt > 0.0)) return TURB_ERR_ARG;
-    launch_rhs_conc(c->s, c->d.n, c->st[3], 1.0 / dt, c->fld[TURB_F_C0 + ic], c->fld[TURB_F_CCONV0 + ic],
+    launch_rhs_conc(c->s, c->d, ic, c->st[3], 1.0 / dt, c->fld[TURB_F_C0 + ic], c->fld[TURB_F_CCONV0 + ic], c->ob,
                     c->fld[TURB_F_CB0 + ic]);
     c->launches += 1;
     return check_launch(c);
@@ -1697,7 +1962,7 @@ int turb_helmholtz_apply(turb_ctx *c, char which, int ic, double dt, int fx, int
 int turb_Pressure_set_RHS(turb_ctx *c, double dt)
 {
     if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
-    launch_pressure_rhs(c->s, c->d, c->st[3], c->pcx, c->pcy, c->pcz, 1.0 / dt, c->fld[TURB_F_U],
+    launch_pressure_rhs(c->s, c->d, c->st[3], c->pcx, c->pcy, c->pcz, 1.0 / dt, c->ob, c->fld[TURB_F_U],
                         c->fld[TURB_F_V], c->fld[TURB_F_W], c->fld[TURB_F_PB]);
     c->launches += 1;
     return check_launch(c);
@@ -1878,7 +2143,7 @@ int turb_Pressure_compute_velocity_divergence(turb_ctx *c, double *div_max)
 {
     if (!c) return TURB_ERR_ARG;
     launch_divergence(c->s, c->d, c->st[3], c->geo.mxc, c->geo.myc, c->geo.mzc, 1.0 / c->dEta, 1.0 / c->dXi,
-                      1.0 / c->dPhi, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W], c->fld[TURB_F_DIV],
+                      1.0 / c->dPhi, c->ob, c->fld[TURB_F_U], c->fld[TURB_F_V], c->fld[TURB_F_W], c->fld[TURB_F_DIV],
                       c->part, c->dscal);
     c->launches += 2;
     int rc = check_launch(c);

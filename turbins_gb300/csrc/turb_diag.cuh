@@ -21,6 +21,7 @@ struct DiagIn {
     double hcoef;                             // 1 / (Ly Lz)
     double Cx, Cy, Cz;                        // 1/dEta^2, 1/dXi^2, 1/dPhi^2
     double kw[6];                             // wall ghost factors: -1 no-slip, +1 free-slip
+    OpenBC ob;                                // open faces (viscous dissipation)
     const int32_t *iy;                        // bed index [NZ][NX]
     const double *dep;                        // deposited heights [nconc][NZ][NX] or null
 };

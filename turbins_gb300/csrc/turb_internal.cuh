@@ -27,6 +27,21 @@ struct Dims {
     }
 };
 
+// Open boundaries (params->inflow / outflow): the inflow and outflow planes
+// of Inflow.c / Outflow.c as [NZ][NY] arrays (j fastest) and the RHS
+// coefficients of the boundary-adjacent rows.  in = out = 0 is the closed box.
+struct OpenBC {
+    int in = 0, out = 0;
+    int NY = 0;
+    const double *u_in = nullptr;            // Velocity.G_inflow of u
+    const double *c_in[4] = {};              // Concentration.G_inflow
+    const double *out_f[7] = {};             // G_outflow of u, v, w, c_0..c_3
+    // RHS terms: u at i = 1 (aw u_in), u at i = nx-2+1... see k_stencil.cu
+    double u_aw = 0.0, u_ae = 0.0, vw_ae[2] = {0.0, 0.0};
+    double c_aw[4] = {}, c_ae[4] = {};
+    __host__ __device__ double pl(const double *a, int j, int k) const { return a[(long long)k * NY + j]; }
+};
+
 // 1-D grid arrays on the device (coordinates and metrics of Grid.c:595-708)
 struct Geo {
     const double *xc, *yc, *zc, *xu, *yv, *zw;
@@ -63,7 +78,9 @@ struct EnoTab {
     const uint8_t *p2;   // per b: bit 0/1/2 set when h1/h2/h3 is a power of two, so that
                          // a/h = a*RN(1/h) exactly (fastdiv only)
     int gsrc[6];         // ghost b<r: [0..r), ghost b>=nb-r: [3..3+r) by ex
-    double gm[6];        // 0: zero, 1: m*q[s0], 2: m*q[e0]
+    double gm[6];        // 0: zero, 1: m*q[s0], 2: m*q[e0], 3: glo[line], 4: ghi[line]
+    const double *glo = nullptr, *ghi = nullptr;   // x lines at open faces: [NZ][NY] planes
+    int gNY = 0;
 };
 
 struct IbDev {

@@ -18,25 +18,26 @@ struct ProjArgs {
 };
 
 // element-wise / stencil kernels (k_stencil.cu)
-void launch_cell_center(cudaStream_t s, const Dims &d, Interp2 ix, Interp2 iy, Interp2 iz, const double *u,
-                        const double *v, const double *w, double *ubc, double *vbc, double *wbc);
-void launch_transpose(cudaStream_t s, const Dims &d, int which, const uint8_t *st, TransW tw, const double *u,
-                      const double *v, const double *w, double *A, double *B);
+void launch_cell_center(cudaStream_t s, const Dims &d, Interp2 ix, Interp2 iy, Interp2 iz, const OpenBC &ob,
+                        const double *u, const double *v, const double *w, double *ubc, double *vbc, double *wbc);
+void launch_transpose(cudaStream_t s, const Dims &d, int which, const uint8_t *st, TransW tw, const OpenBC &ob,
+                      const double *u, const double *v, const double *w, double *A, double *B);
 void launch_total_conc(cudaStream_t s, long long n, int nc, ConcPtrs c, ConcW a, double *ct);
 void launch_shift(cudaStream_t s, long long n, const double *x, double sh, double *y);
 void launch_rhs_vel(cudaStream_t s, const Dims &d, int q, const uint8_t *st, double a_dt, const double *x,
-                    const double *conv, const double *dp, const double *ct, int buoy, Interp2 iyv, double *b);
-void launch_rhs_conc(cudaStream_t s, long long n, const uint8_t *st, double a_dt, const double *c,
-                     const double *conv, double *b);
+                    const double *conv, const double *dp, const double *ct, int buoy, Interp2 iyv,
+                    const OpenBC &ob, double *b);
+void launch_rhs_conc(cudaStream_t s, const Dims &d, int ic, const uint8_t *st, double a_dt, const double *c,
+                     const double *conv, const OpenBC &ob, double *b);
 void launch_pressure_rhs(cudaStream_t s, const Dims &d, const uint8_t *st, const double *cx, const double *cy,
-                         const double *cz, double a_dt, const double *u, const double *v, const double *w,
-                         double *b);
+                         const double *cz, double a_dt, const OpenBC &ob, const double *u, const double *v,
+                         const double *w, double *b);
 void launch_project(cudaStream_t s, const Dims &d, ProjArgs a, const double *phi, const double *pb, double *u,
                     double *v, double *w, double *dpx, double *dpy, double *dpz);
 long long divergence_parts(const Dims &d);
 void launch_divergence(cudaStream_t s, const Dims &d, const uint8_t *st, const double *mxc, const double *myc,
-                       const double *mzc, double a_dEta, double a_dXi, double a_dPhi, const double *u,
-                       const double *v, const double *w, double *div, double *part, double *out);
+                       const double *mzc, double a_dEta, double a_dXi, double a_dPhi, const OpenBC &ob,
+                       const double *u, const double *v, const double *w, double *div, double *part, double *out);
 void launch_axpby(cudaStream_t s, long long n, double a, const double *x, double b, double *y);
 
 // ENO convection (k_eno.cu)
@@ -46,6 +47,10 @@ struct AdvSrc {
     const double *a;        // primary array
     double shift;
     W2 wx, wy;              // weights of the bilinear transposes
+    // u at v (kind 4) / w (kind 6) nodes next to open faces: the inflow and
+    // outflow planes replace u at i = 0 / i = nx ([NZ][NY], null when closed)
+    const double *pin = nullptr, *pout = nullptr;
+    int pNY = 0, nx = 0;
 };
 void launch_eno_pass(cudaStream_t s, const Dims &d, int dir, const EnoTab &tab, const double *q, AdvSrc adv,
                      int t1a, int t1b, int t2a, int t2b, int first, double *conv);
