@@ -151,9 +151,101 @@ def dump_resume():
         json.dump(dict(case=RESUME_CASE, prim=RESUME_PRIM), f)
 
 
+# open boundaries: the 24x12x8 bump case with inflow and convective outflow,
+# every open-face routine through the reference's own code
+OPEN_ARGS = dict(U=0.8, transient=1, time_c=0.5)
+
+
+def dump_open():
+    case = _cases.bump_small(24, 12, 8)
+    g, p = case.grid, case.params
+    s = _cases.random_state(case, seed=23)
+    ref = Reference(g, p)
+    ref.set_open(1, 1, **OPEN_ARGS)
+    rng = np.random.Generator(np.random.PCG64(9))
+    shp = (g.nz + 1, g.ny + 1)
+    out = {}
+    for k in ("xc", "yc", "zc", "xu", "yv", "zw"):
+        out["grid_" + k] = getattr(g, k)
+    for q in "uvwc":
+        out["status_" + q] = g.status[q]
+        for k in ("im", "nf", "fidx", "fcoef", "bcoef"):
+            out["ib_%s_%s" % (q, k)] = np.asarray(g.ib[q][k])
+    for k, v in s.items():
+        out["in_" + k] = v
+    planes = {"in_u": rng.uniform(0.0, 1.0, shp), "in_c": rng.uniform(0.0, 1.0, shp)}
+    for q in "uvwc":
+        planes["out_" + q] = rng.uniform(-0.5, 0.5, shp)
+        planes["old_" + q] = rng.uniform(-0.5, 0.5, shp)
+    for k, v in planes.items():
+        out["pl_" + k] = v
+
+    def load_planes():
+        ref.open_set("in", "u", 0, planes["in_u"])
+        ref.open_set("in", "c", 0, planes["in_c"])
+        for q in "uvwc":
+            ref.open_set("out", q, 0, planes["out_" + q])
+            ref.open_set("out_old", q, 0, planes["old_" + q])
+
+    dt = case.dt
+    # inflow profiles
+    load_planes()
+    out["ref_influx"] = np.array([ref.inflow_u(0.3)])
+    ref.inflow_c(0, 0.3)
+    out["ref_inflow_u"] = ref.open_get("in", "u")
+    out["ref_inflow_c"] = ref.open_get("in", "c")
+    # convective outflow (u with the mass correction from influx 0.75)
+    load_planes()
+    for q in "uvw":
+        ref.outflow_impose(q, 0, dt, s[q], influx=0.75)
+        out["ref_outflow_" + q] = ref.open_get("out", q)
+    ref.outflow_impose("c", 0, dt, s["c0"])
+    out["ref_outflow_c"] = ref.open_get("out", "c")
+    # rk average of the outflow planes, plane copies
+    load_planes()
+    for q in "uvwc":
+        ref.outflow_rk_average(q, 0, 0.5, 0.5)
+        out["ref_rkavg_" + q] = ref.open_get("out", q)
+    load_planes()
+    out["ref_toplane_u"] = ref.outflow_to_plane("u", 0, 1, s["u"])
+    out["ref_toplane_c"] = ref.outflow_to_plane("c", 0, 0, s["c0"])
+    ref.outflow_from_plane("w", 0, s["w"])
+    out["ref_fromplane_w"] = ref.open_get("out", "w")
+    # the step routines with both faces open
+    load_planes()
+    ub, vb, wb = ref.cell_center(s["u"], s["v"], s["w"])
+    out["ref_ubc"], out["ref_vbc"], out["ref_wbc"] = ub, vb, wb
+    vel = {}
+    for q in "uvw":
+        A, B = ref.transpose(q, s["u"], s["v"], s["w"])
+        out["ref_T%sA" % q], out["ref_T%sB" % q] = A, B
+        vel[q] = (s["u"], A, B) if q == "u" else (A, s["v"], B) if q == "v" else (A, B, s["w"])
+        out["ref_conv_" + q] = ref.convection(q, 0, s[q], *vel[q])
+    va = vb + p.vs0[0] if p.ctype[0] == 2 else vb
+    out["ref_conv_c0"] = ref.convection("c", 0, s["c0"], ub, va, wb)
+    for q, dk in (("u", "dpx"), ("v", "dpy"), ("w", "dpz")):
+        out["ref_rhs_" + q] = ref.set_rhs_vel(q, dt, s[q], out["ref_conv_" + q], s[dk], s["c0"])
+    out["ref_rhs_c0"] = ref.set_rhs_conc(0, dt, s["c0"], out["ref_conv_c0"])
+    x = s["phi"]
+    for q in "uvw":
+        out["ref_lhs_" + q] = ref.lhs_apply(q, 0, dt, x)
+    out["ref_lhs_c0"] = ref.lhs_apply("c", 0, dt, x)
+    out["ref_pb"] = ref.pressure_rhs(dt, s["u"], s["v"], s["w"])
+    mx, dv = ref.divergence(s["u"], s["v"], s["w"])
+    out["ref_divmax"] = np.array([mx])
+    out["ref_div"] = dv
+    d = ref.diagnostics(s["u"], s["v"], s["w"], [s["c0"]], 0.01)
+    out["ref_visc"] = np.array([d["viscous_dissipation"]])
+    meta = dict(name="open_bump", nx=g.nx, ny=g.ny, nz=g.nz, dt=dt, params=p.__dict__, open=OPEN_ARGS)
+    np.savez_compressed(os.path.join(HERE, "open", "open_bump.npz"), meta=np.array(json.dumps(meta)), **out)
+
+
 if __name__ == "__main__":
     for nm, mk in CASES.items():
         dump(nm, mk())
         print("wrote", nm)
     dump_resume()
     print("wrote resume_bump")
+    os.makedirs(os.path.join(HERE, "open"), exist_ok=True)
+    dump_open()
+    print("wrote open_bump")
