@@ -388,14 +388,12 @@ HelmTab mk_helm(turb_ctx *c, int q, int ic)
         } else {
             aw[i] = i > 0 ? a_w : 0.0;
             ae[i] = i < nx - 1 ? a_e : 0.0;
-            // open faces: concentration drops the Neumann fold (Conc.c:583-606,
-            // the face value goes to the RHS); v and w keep the east column
-            // at i = nx (Velocity.c:989, 1336)
+            // open faces drop the wall fold, the face value goes to the RHS:
+            // concentration at both faces (Conc.c:583-606), v and w at the
+            // outflow face, where the east column is not inserted either
+            // (Velocity.c:989-1011, 1336-1358)
             if (i == 0 && !(q == 3 && c->ob.in)) apx[i] += q == 3 ? a_w : wallfold(a_w, ns[0]);
-            if (i == nx - 1) {
-                if (c->ob.out && q != 3) ae[i] = a_e;
-                else if (!(c->ob.out && q == 3)) apx[i] += q == 3 ? a_e : wallfold(a_e, ns[1]);
-            }
+            if (i == nx - 1 && !c->ob.out) apx[i] += q == 3 ? a_e : wallfold(a_e, ns[1]);
         }
     }
     // y
