@@ -403,6 +403,13 @@ int turb_open_plane_set(turb_ctx *ctx, int which, int q, int ic, const double *h
 int turb_Inflow_u_velocity_profile(turb_ctx *ctx, double time, double *influx);
 int turb_Inflow_conc_profile(turb_ctx *ctx, int ic, double time);
 int turb_set_influx(turb_ctx *ctx, double influx);
+/* simulated time (GVG_bag.time): advanced by dt in every turb_step; the
+ * inflow ramp is evaluated at the step's starting time.  With open faces a
+ * step first sets the inflow planes (u, then each c) and stores the outflow
+ * planes, imposes the convective outflow (with u's mass correction) at the
+ * start of each RK stage, and RK-averages the outflow planes at the end. */
+int turb_set_time(turb_ctx *ctx, double time);
+int turb_get_time(turb_ctx *ctx, double *time);
 int turb_Outflow_vel_impose_convective_boundary(turb_ctx *ctx, char which, double dt);
 int turb_Outflow_conc_impose_convective_boundary(turb_ctx *ctx, int ic, double dt);
 int turb_Outflow_impose_convective_boundary(turb_ctx *ctx, double dt);

@@ -205,6 +205,7 @@ class Reference:
 
     def set_open(self, inflow, outflow, U=1.0, transient=0, time_c=1.0):
         g = self.g
+        self._open = (int(inflow), int(outflow))
         self.lib.ref_set_open(self.h, int(inflow), int(outflow), C.c_double(U), int(transient), C.c_double(time_c),
                               C.c_double(g.yv[-1] - g.yv[0]), C.c_double(g.zw[-1] - g.zw[0]))
 
@@ -269,7 +270,7 @@ class Reference:
                                  _p(np.ascontiguousarray(b)), _p(x))
         return x, its
 
-    def step(self, s, dt):
+    def step(self, s, dt, time=None):
         """One TVD-RK2 step through the reference's routines, in the stage
         order of the restated driver (the oracle's to_step): store old; two
         stages of {cell centre, total concentration, convection of u, v, w
@@ -279,9 +280,25 @@ class Reference:
         per-stage divergence maxima."""
         p = self.p
         nc = p.nconc
+        op = getattr(self, "_open", None)
+        influx = 0.0
+        if op and op[0]:
+            influx = self.inflow_u(time)
+            for ic in range(nc):
+                self.inflow_c(ic, time)
+        if op and op[1]:
+            for q in "uvw":
+                self.outflow_store_old(q)
+            for ic in range(nc):
+                self.outflow_store_old("c", ic)
         old = {k: s[k].copy() for k in ["u", "v", "w"] + ["c%d" % i for i in range(nc)]}
         divs = []
         for stage in range(2):
+            if op and op[1]:
+                for q in "uvw":
+                    self.outflow_impose(q, 0, dt, s[q], influx)
+                for ic in range(nc):
+                    self.outflow_impose("c", ic, dt, s["c%d" % ic])
             ub, vb, wb = self.cell_center(s["u"], s["v"], s["w"])
             cs = [s["c%d" % i] for i in range(nc)]
             ct = self.total_concentration(cs) if nc > 1 else s["c0"].copy()
@@ -312,6 +329,11 @@ class Reference:
             divs.append(self.divergence(s["u"], s["v"], s["w"])[0])
         for k, a in old.items():
             s[k] = 0.5 * a + 0.5 * s[k]
+        if op and op[1]:
+            for q in "uvw":
+                self.outflow_rk_average(q, 0, 0.5, 0.5)
+            for ic in range(nc):
+                self.outflow_rk_average("c", ic, 0.5, 0.5)
         return divs
 
     # -- restated line driver around the reference's ghost and ENO routines --

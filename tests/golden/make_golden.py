@@ -236,6 +236,16 @@ def dump_open():
     out["ref_div"] = dv
     d = ref.diagnostics(s["u"], s["v"], s["w"], [s["c0"]], 0.01)
     out["ref_visc"] = np.array([d["viscous_dissipation"]])
+    # two steps with both faces open, from time 0.3 (the restated driver's
+    # order: inflow planes, outflow stored, imposed per stage, RK-averaged)
+    load_planes()
+    st = {k: s[k].copy() for k in ["u", "v", "w", "phi", "dpx", "dpy", "dpz", "c0"]}
+    for n in range(2):
+        ref.step(st, dt, time=0.3 + n * dt)
+    for k in ["u", "v", "w", "phi", "dpx", "dpy", "dpz", "c0"]:
+        out["ref_step2_" + k] = st[k]
+    for q in "uvwc":
+        out["ref_step2_out_" + q] = ref.open_get("out", q)
     meta = dict(name="open_bump", nx=g.nx, ny=g.ny, nz=g.nz, dt=dt, params=p.__dict__, open=OPEN_ARGS)
     np.savez_compressed(os.path.join(HERE, "open", "open_bump.npz"), meta=np.array(json.dumps(meta)), **out)
 

@@ -132,3 +132,31 @@ def test_step_routines_with_open_faces(api, fx):
     d = ctx.diagnostics()
     assert abs(d["viscous_dissipation"] - z["ref_visc"][0]) <= 1e-12 * abs(z["ref_visc"][0])
     ctx.close()
+
+
+def test_steps_with_open_faces_match_reference_trace(api, fx):
+    """Two GPU steps with both faces open against two steps composed of the
+    reference's routines in the same order (tests/golden/make_golden.py),
+    solvers at relative residual 1e-12."""
+    z, g, p, dt, op = fx
+    p.buoyancy = 1
+    p.p_rtol = 1e-12
+    p.vel_rtol = 1e-12
+    try:
+        ctx = ctx_of(api, fx)
+        ctx.set_time(0.3)
+        for _ in range(2):
+            st = ctx.step(dt)
+            assert max(st["div_max"]) <= 1e-10
+        s = ctx.state()
+    finally:
+        p.buoyancy = 0
+    vscale = max(np.abs(z["ref_step2_" + k]).max() for k in "uvw")
+    for k in ("u", "v", "w"):
+        assert np.abs(s[k] - z["ref_step2_" + k]).max() <= 1e-7 * vscale, k
+    assert np.abs(s["c0"] - z["ref_step2_c0"]).max() <= 1e-6
+    for q in "uvw":
+        assert np.abs(ctx.open_plane("out", q) - z["ref_step2_out_" + q]).max() <= 1e-7 * vscale, q
+    assert np.abs(ctx.open_plane("out", "c") - z["ref_step2_out_c"]).max() <= 1e-6
+    assert abs(ctx.time() - (0.3 + 2 * dt)) <= 1e-15
+    ctx.close()

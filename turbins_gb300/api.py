@@ -344,6 +344,14 @@ class Context:
     def Inflow_conc_profile(self, ic, time):
         _check(self.lib.turb_Inflow_conc_profile(self.ctx, int(ic), C.c_double(time)), "inflow_c")
 
+    def set_time(self, t):
+        _check(self.lib.turb_set_time(self.ctx, C.c_double(t)), "set_time")
+
+    def time(self):
+        t = C.c_double()
+        _check(self.lib.turb_get_time(self.ctx, C.byref(t)), "get_time")
+        return t.value
+
     def set_influx(self, influx):
         _check(self.lib.turb_set_influx(self.ctx, C.c_double(influx)), "set_influx")
 

@@ -166,6 +166,7 @@ struct turb_ctx {
     double *pl_in_u = nullptr, *pl_in_c[TURB_MAXCONC] = {}, *pl_out[3 + TURB_MAXCONC] = {},
            *pl_out_old[3 + TURB_MAXCONC] = {};
     double open_U = 0.0, open_time_c = 1.0;
+    double time = 0.0;            // simulated time, advanced by turb_step (GVG_bag.time)
     int open_transient = 0;
     double *open_scr = nullptr;   // partials; influx at [open_parts], mass results after it
     EnoTab eno_cx[TURB_MAXCONC];
@@ -1237,6 +1238,20 @@ int turb_Inflow_u_velocity_profile(turb_ctx *c, double time, double *influx)
     return check_launch(c);
 }
 
+int turb_set_time(turb_ctx *c, double time)
+{
+    if (!c) return TURB_ERR_ARG;
+    c->time = time;
+    return TURB_OK;
+}
+
+int turb_get_time(turb_ctx *c, double *time)
+{
+    if (!c || !time) return TURB_ERR_ARG;
+    *time = c->time;
+    return TURB_OK;
+}
+
 int turb_set_influx(turb_ctx *c, double influx)
 {
     if (!c || !c->open_scr) return TURB_ERR_ARG;
@@ -2244,9 +2259,18 @@ int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
     if (!st) st = &local;
     memset(st, 0, sizeof(*st));
     long long l0 = c->launches;
+    // open faces (restated driver order): inflow planes at the step's time,
+    // outflow planes stored, advanced by the convective condition at the
+    // start of every stage and RK-averaged with the fields
+    if (c->ob.in) {
+        STEP_TRY(turb_Inflow_u_velocity_profile(c, c->time, nullptr));
+        for (int ic = 0; ic < c->prm.nconc; ic++) STEP_TRY(turb_Inflow_conc_profile(c, ic, c->time));
+    }
+    if (c->ob.out) STEP_TRY(turb_store_old_outflow(c));
     STEP_TRY(turb_store_old_data(c));
     for (int stage = 0; stage < 2; stage++) {
         c->stage = stage;
+        if (c->ob.out) STEP_TRY(turb_Outflow_impose_convective_boundary(c, dt));
         STEP_TRY(turb_Velocity_cell_center(c));
         if (c->prm.nconc > 1) STEP_TRY(turb_Conc_compute_total_concentration(c));
         STEP_TRY(turb_Velocity_convective_terms(c, 'u'));
@@ -2269,7 +2293,9 @@ int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
         STEP_TRY(turb_Pressure_compute_velocity_divergence(c, &st->div_max[stage]));
     }
     STEP_TRY(turb_rk_average(c, 0.5, 0.5));
+    if (c->ob.out) STEP_TRY(turb_rk_average_outflow(c, 0.5, 0.5));
     if (c->deposit_on) STEP_TRY(turb_deposit_integrate(c, dt));
+    c->time += dt;
     st->kernel_launches = (int)(c->launches - l0);
     return TURB_OK;
 }
