@@ -237,8 +237,13 @@ def dump_open():
     d = ref.diagnostics(s["u"], s["v"], s["w"], [s["c0"]], 0.01)
     out["ref_visc"] = np.array([d["viscous_dissipation"]])
     # two steps with both faces open, from time 0.3 (the restated driver's
-    # order: inflow planes, outflow stored, imposed per stage, RK-averaged)
-    load_planes()
+    # order: inflow planes, outflow stored, imposed per stage, RK-averaged),
+    # the planes starting at zero as the reference allocates them
+    for q in "uvwc":
+        ref.open_set("out", q, 0, np.zeros(shp))
+        ref.open_set("out_old", q, 0, np.zeros(shp))
+    ref.open_set("in", "u", 0, np.zeros(shp))
+    ref.open_set("in", "c", 0, np.zeros(shp))
     st = {k: s[k].copy() for k in ["u", "v", "w", "phi", "dpx", "dpy", "dpz", "c0"]}
     for n in range(2):
         ref.step(st, dt, time=0.3 + n * dt)

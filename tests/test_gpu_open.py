@@ -144,6 +144,12 @@ def test_steps_with_open_faces_match_reference_trace(api, fx):
     p.vel_rtol = 1e-12
     try:
         ctx = ctx_of(api, fx)
+        zero = np.zeros((g.nz + 1, g.ny + 1))
+        ctx.set_open_plane("in", "u", 0, zero)
+        ctx.set_open_plane("in", "c", 0, zero)
+        for q in "uvwc":
+            ctx.set_open_plane("out", q, 0, zero)
+            ctx.set_open_plane("out_old", q, 0, zero)
         ctx.set_time(0.3)
         for _ in range(2):
             st = ctx.step(dt)
