@@ -56,7 +56,9 @@ def parse():
     ap.add_argument("--prev-steps", type=int, default=3,
                     help="timed steps of mixed MG-CG with the previous-pressure guess (learned runs)")
     ap.add_argument("--train-seeds", type=int, default=8, help="learned guess: training runs (one bump field each)")
-    ap.add_argument("--train-steps", type=int, default=250, help="learned guess: steps per training run")
+    ap.add_argument("--train-steps", type=int, default=125, help="learned guess: steps per training run")
+    ap.add_argument("--guess-stages", type=int, default=2,
+                    help="learned guess: RK stages that try it (bit 0 first, bit 1 second)")
     ap.add_argument("--train-iters", type=int, default=3000, help="learned guess: Adam steps")
     ap.add_argument("--net-params", default=None, help="learned guess: .npy parameters instead of training")
     ap.add_argument("--save-net-params", default=None, help="learned guess: write the trained parameters (.npy)")
@@ -260,10 +262,14 @@ def main():
             params = np.load(a.net_params)
             learned_info = {"params": os.path.basename(a.net_params)}
         else:
-            tn = (max(16, a.nx // 4), max(16, a.ny // 4), max(16, a.nz // 4))
-            params, learned_info = LN.train_default(LN.multi_bump_train_case(*tn), seeds=a.train_seeds,
-                                                    steps=a.train_steps, iters=a.train_iters)
+            # training domains at the full case's grid spacing: a quarter of
+            # its x and z extents, the whole height (8 x 125 steps = 2000
+            # solves of snapshots)
+            tn = (max(16, a.nx // 4), a.ny, max(16, a.nz // 4))
+            params, learned_info = LN.train_default(LN.multi_bump_train_case(*tn, full=(a.nx, a.ny, a.nz)),
+                                                    seeds=a.train_seeds, steps=a.train_steps, iters=a.train_iters)
             learned_info["train_grid"] = list(tn)
+        learned_info["guess_stages"] = a.guess_stages
             if a.save_net_params:
                 np.save(a.save_net_params, params)
     case = W.multi_bump_case(a.nx, a.ny, a.nz)
@@ -277,6 +283,7 @@ def main():
     net = None
     if guess == api.GUESS_LEARNED:
         net = LN.attach(ctx, params)
+        ctx.set_guess_stages(a.guess_stages)
     elif guess != api.GUESS_PREVIOUS:
         ctx.set_pressure_guess(guess)
     dt = case.dt

@@ -143,6 +143,9 @@ int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 #define TURB_GUESS_EXTRAPOLATE 1
 #define TURB_GUESS_LEARNED 2
 int turb_set_pressure_guess(turb_ctx *ctx, int mode);
+/* RK stages whose pressure solve tries the extrapolated / learned candidate:
+ * bit 0 the first stage, bit 1 the second (default 3, both) */
+int turb_set_guess_stages(turb_ctx *ctx, int mask);
 int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
 /* geometric mean over the tried candidates of |r(candidate)| / |r(previous)|
  * (initial residuals; 1 when nothing was tried) */

@@ -254,6 +254,9 @@ class Context:
     def set_pressure_guess(self, mode):
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
+    def set_guess_stages(self, mask):
+        _check(self.lib.turb_set_guess_stages(self.ctx, int(mask)), "set_guess_stages")
+
     def pressure_guess_stats(self):
         a, b = C.c_int(), C.c_int()
         _check(self.lib.turb_pressure_guess_stats(self.ctx, C.byref(a), C.byref(b)), "pressure_guess_stats")

@@ -146,6 +146,7 @@ struct turb_ctx {
     int mg_split = 1;   // colour-split storage of the FP32 levels
     // pressure initial guess: history of the last two solutions per RK stage
     int guess_mode = TURB_GUESS_PREVIOUS;
+    int guess_stages = 3;   // RK stages (bit 0: first, bit 1: second) that try the candidate guess
     int stage = 0;
     double *ph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int nh[2] = {0, 0};
@@ -1032,6 +1033,13 @@ int turb_set_pressure_guess(turb_ctx *c, int mode)
     if (!c || mode < TURB_GUESS_PREVIOUS || mode > TURB_GUESS_LEARNED) return TURB_ERR_ARG;
     if (mode == TURB_GUESS_LEARNED && !c->net) return TURB_ERR_ARG;
     c->guess_mode = mode;
+    return TURB_OK;
+}
+
+int turb_set_guess_stages(turb_ctx *c, int mask)
+{
+    if (!c || mask < 0 || mask > 3) return TURB_ERR_ARG;
+    c->guess_stages = mask;
     return TURB_OK;
 }
 
@@ -2008,7 +2016,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         if (rc) return rc;
         c->launches += 5;
     }
-    if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2) {
+    if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2 && ((c->guess_stages >> st) & 1)) {
         int ok = 0, ph = -1;
         if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
             pcg_lincomb(s, n0, 2.0, c->ph[st][0], -1.0, c->ph[st][1], c->pz);
