@@ -269,9 +269,9 @@ def main():
             params, learned_info = LN.train_default(LN.multi_bump_train_case(*tn, full=(a.nx, a.ny, a.nz)),
                                                     seeds=a.train_seeds, steps=a.train_steps, iters=a.train_iters)
             learned_info["train_grid"] = list(tn)
-        learned_info["guess_stages"] = a.guess_stages
             if a.save_net_params:
                 np.save(a.save_net_params, params)
+        learned_info["guess_stages"] = a.guess_stages
     case = W.multi_bump_case(a.nx, a.ny, a.nz)
     g = case.grid
     nc = g.nx * g.ny * g.nz
