@@ -690,3 +690,46 @@ void ref_outflow_from_plane(ref_case *r, char q, int ic, const double *x)
         Outflow_vel_copy_data_into_2D_array(V, r->g);
     }
 }
+
+/* ---- immersed-boundary geometry (row f4) -----------------------------------
+ * The reference's set-up of a bottom topography y = h(x, z): the sdf guess
+ * yc - interface_position (Surface_initialize, Surface.c:96-195), level-set
+ * reinitialisation (Surface_find_exact_sdf -> Levelset_reinitialize,
+ * Levelset.c:85-160), sdf at the u, v, w nodes (Surface_find_q_sdf,
+ * Surface.c:216-336) and the node status (Grid_identify_geometry,
+ * Grid.c:1825-1871: box boundaries, surface tagging, BUFFER_SOLID layers,
+ * interface index).  ipos: [NZ][NX] interface heights at the cell centres.
+ * Outputs: sdf of c, u, v, w (DA arrays) and the four status arrays as codes. */
+#include "Surface.h"
+#include "Levelset.h"
+
+void ref_geometry(ref_case *r, const double *ipos, double *c_sdf, double *u_sdf, double *v_sdf, double *w_sdf,
+                  unsigned char *st_out)
+{
+    MAC_grid *g = r->g;
+    Parameters *p = r->p;
+    int i, k, q;
+    long t;
+    Vec *gs[4];
+    if (!g->interface_position) g->interface_position = Memory_allocate_2D_double(g->NX, g->NZ);
+    for (k = 0; k < g->NZ; k++)
+        for (i = 0; i < g->NX; i++) g->interface_position[k][i] = ipos[(long)k * g->NX + i];
+    p->Lx = g->xu[g->NX - 1] - g->xu[0];
+    p->Ly = g->yv[g->NY - 1] - g->yv[0];
+    p->Lz = g->zw[g->NZ - 1] - g->zw[0];
+    if (!g->interface_y_index) g->interface_y_index = Memory_allocate_2D_int(g->NX, g->NZ);
+    g->surf = Surface_create(g);
+    Surface_initialize(g->surf, g, p);
+    Surface_find_exact_sdf(g->surf, g);
+    Surface_find_q_sdf(g->surf, g);
+    Grid_identify_geometry(g);
+    vget(g->surf->G_c_sdf, c_sdf, r->n);
+    vget(g->surf->G_u_sdf, u_sdf, r->n);
+    vget(g->surf->G_v_sdf, v_sdf, r->n);
+    vget(g->surf->G_w_sdf, w_sdf, r->n);
+    gs[0] = &g->G_u_status; gs[1] = &g->G_v_status; gs[2] = &g->G_w_status; gs[3] = &g->G_c_status;
+    for (q = 0; q < 4; q++) {
+        const double *a = shim_vec_data(*gs[q]);
+        for (t = 0; t < r->n; t++) st_out[(long)q * r->n + t] = (unsigned char)a[t];
+    }
+}

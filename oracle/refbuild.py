@@ -20,7 +20,7 @@ SRC = os.path.join(REF, "src")
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libturbins_ref.so")
 FILES = ["ENO", "Velocity", "Conc", "Pressure", "Grid", "Immersed", "MyMath", "Memory", "Communication", "Extract",
-         "Resume", "Solver", "Inflow", "Outflow"]
+         "Resume", "Solver", "Inflow", "Outflow", "Surface", "Levelset"]
 CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w"]
 
 

@@ -247,6 +247,17 @@ class Reference:
     def outflow_from_plane(self, q, ic, x):
         self.lib.ref_outflow_from_plane(self.h, C.c_char(q.encode()), int(ic), _p(np.ascontiguousarray(x)))
 
+    def geometry(self, ipos):
+        """the reference's geometry set-up from interface heights ipos
+        [NZ][NX]: returns sdf of c, u, v, w and the status of u, v, w, c"""
+        g = self.g
+        ipos = np.ascontiguousarray(ipos, dtype=np.float64)
+        sd = [self._z() for _ in range(4)]
+        st = np.zeros((4,) + g.shape, dtype=np.uint8)
+        self.lib.ref_geometry(self.h, _p(ipos), _p(sd[0]), _p(sd[1]), _p(sd[2]), _p(sd[3]),
+                              st.ctypes.data_as(C.c_void_p))
+        return dict(c=sd[0], u=sd[1], v=sd[2], w=sd[3]), dict(u=st[0], v=st[1], w=st[2], c=st[3])
+
     def c_term(self, ct):
         """the buoyancy term at v nodes that Velocity_v_set_RHS computes
         (2-point y interpolation of the total concentration, Velocity.c:1861-
