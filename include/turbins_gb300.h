@@ -379,6 +379,21 @@ int turb_deposit_enable(turb_ctx *ctx, int on);
 int turb_deposit_get(turb_ctx *ctx, double *host);
 int turb_deposit_set(turb_ctx *ctx, const double *host);
 
+/* ---- immersed-boundary geometry ------------------------------------------
+ * turb_geometry: the set-up of a bottom surface on the device, replacing
+ * Surface_create + Surface_initialize + Surface_find_exact_sdf +
+ * Surface_find_q_sdf (Surface.c:16-336) and Grid_identify_geometry
+ * (Grid.c:1825-1870, with the BUFFER_SOLID pass of SOLVE_INSIDE_SOLID).
+ * ipos: interface heights [nz+1][nx+1] (MAC_grid.interface_position).  The
+ * cell-centre guess yc - ipos is reinitialised to a signed distance by the
+ * Godunov level-set iteration of Levelset.c:85-578 (up to 503 steps, stop at
+ * an L2 change below 1e-5), copied to the last planes, interpolated to the
+ * u/v/w nodes and tagged.  Outputs, host, DA layout [nz+1][ny+1][nx+1], each
+ * array or pointer may be null: sdf c, u, v, w (doubles); status u, v, w, c
+ * (TURB_* codes); iterations = Godunov steps taken.  The context's own
+ * statuses and stencils are left as they are. */
+int turb_geometry(turb_ctx *ctx, const double *ipos, double *const *sdf, uint8_t *const *status, int *iterations);
+
 /* ---- open boundaries -------------------------------------------------------
  * params->inflow / outflow of the reference: an inflow face at x = xmin and a
  * convective outflow face at x = xmax.  turb_set_open_boundaries turns them

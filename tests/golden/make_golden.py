@@ -255,6 +255,34 @@ def dump_open():
     np.savez_compressed(os.path.join(HERE, "open", "open_bump.npz"), meta=np.array(json.dumps(meta)), **out)
 
 
+# immersed-boundary geometry: the reference's surface set-up (level-set
+# reinitialisation of yc - h, q-sdf, node tagging) from the bed heights
+GEOM_CASES = {
+    "bump": lambda: _cases.bump_small(24, 12, 8),
+    "multi": lambda: _cases.multi_small(40, 20, 12),
+}
+
+
+def bed_heights(case):
+    """interface_position [NZ][NX]: the bed height at the cell-centre columns"""
+    g = case.grid
+    return case.bed.h(g.xc[None, :], g.zc[:, None])[0]
+
+
+def dump_geom(name, case):
+    g = case.grid
+    ipos = np.ascontiguousarray(bed_heights(case))
+    sdf, st = Reference(g, case.params).geometry(ipos)
+    out = {"ipos": ipos}
+    for k in ("xc", "yc", "zc", "xu", "yv", "zw"):
+        out["grid_" + k] = getattr(g, k)
+    for q in "cuvw":
+        out["ref_sdf_" + q] = sdf[q]
+        out["ref_status_" + q] = st[q]
+    meta = dict(name=name, nx=g.nx, ny=g.ny, nz=g.nz)
+    np.savez_compressed(os.path.join(HERE, "geom", "geom_%s.npz" % name), meta=np.array(json.dumps(meta)), **out)
+
+
 if __name__ == "__main__":
     for nm, mk in CASES.items():
         dump(nm, mk())
@@ -264,3 +292,7 @@ if __name__ == "__main__":
     os.makedirs(os.path.join(HERE, "open"), exist_ok=True)
     dump_open()
     print("wrote open_bump")
+    os.makedirs(os.path.join(HERE, "geom"), exist_ok=True)
+    for nm, mk in GEOM_CASES.items():
+        dump_geom(nm, mk())
+        print("wrote geom", nm)

@@ -302,6 +302,23 @@ class Context:
         _check(self.lib.turb_bed_index(self.ctx, iy.ctypes.data_as(C.c_void_p)), "bed_index")
         return iy
 
+    def geometry(self, ipos):
+        """turb_geometry: the device set-up of a bottom surface at heights
+        ipos [nz+1][nx+1].  Returns (sdf, status, iterations): sdf of c, u, v,
+        w and status of u, v, w, c as dicts of [nz+1][ny+1][nx+1] arrays"""
+        g = self.grid
+        shape = (g.nz + 1, g.ny + 1, g.nx + 1)
+        ipos = np.ascontiguousarray(ipos, dtype=np.float64)
+        if ipos.shape != (g.nz + 1, g.nx + 1):
+            raise ValueError("ipos must be [nz+1][nx+1]")
+        sd = [np.zeros(shape) for _ in range(4)]
+        st = [np.zeros(shape, dtype=np.uint8) for _ in range(4)]
+        sp = (C.c_void_p * 4)(*[a.ctypes.data for a in sd])
+        tp = (C.c_void_p * 4)(*[a.ctypes.data for a in st])
+        it = C.c_int(0)
+        _check(self.lib.turb_geometry(self.ctx, ipos.ctypes.data_as(C.c_void_p), sp, tp, C.byref(it)), "geometry")
+        return (dict(c=sd[0], u=sd[1], v=sd[2], w=sd[3]), dict(u=st[0], v=st[1], w=st[2], c=st[3]), it.value)
+
     def deposit_integrate(self, dt):
         _check(self.lib.turb_deposit_integrate(self.ctx, C.c_double(dt)), "deposit_integrate")
 

@@ -14,6 +14,7 @@
 #include "../../include/turbins_gb300.h"
 #include "turb_internal.cuh"
 #include "turb_diag.cuh"
+#include "turb_geom.cuh"
 
 // open boundaries (k_open.cu)
 int open_parts(const Dims &d);
@@ -1597,6 +1598,67 @@ int turb_deposit_set(turb_ctx *c, const double *host)
     size_t b = sizeof(double) * c->prm.nconc * c->d.NZ * c->d.NX;
     TURB_CHECK(cudaMemcpyAsync(c->dep, host, b, cudaMemcpyHostToDevice, c->s));
     TURB_CHECK(cudaStreamSynchronize(c->s));
+    return TURB_OK;
+}
+
+// immersed-boundary geometry set-up for a bottom surface (k_geom.cu)
+int turb_geometry(turb_ctx *c, const double *ipos, double *const *sdf, uint8_t *const *status, int *iterations)
+{
+    if (!c || !ipos) return TURB_ERR_ARG;
+    const Dims &d = c->d;
+    std::vector<double> wx = cell_widths(c->xu), wy = cell_widths(c->yv), wz = cell_widths(c->zw);
+    if (!c->diag_dxc) {
+        c->diag_dxc = c->mem.upload(wx);
+        c->diag_dyc = c->mem.upload(wy);
+        c->diag_dzc = c->mem.upload(wz);
+        if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+    }
+    // Levelset_compute_fictitious_time (Levelset.c:590-640): half the
+    // smallest cell width of the physical cells
+    double mxw = 1000.0, myw = 1000.0, mzw = 1000.0;
+    for (int i = 0; i < d.nx; i++) if (wx[i] < mxw) mxw = wx[i];
+    for (int j = 0; j < d.ny; j++) if (wy[j] < myw) myw = wy[j];
+    for (int k = 0; k < d.nz; k++) if (wz[k] < mzw) mzw = wz[k];
+    double dmin = myw < mxw ? myw : mxw;
+    dmin = mzw < dmin ? mzw : dmin;
+    GeomArgs a;
+    a.d = d;
+    a.xc = c->geo.xc; a.yc = c->geo.yc; a.zc = c->geo.zc;
+    a.xu = c->geo.xu; a.yv = c->geo.yv; a.zw = c->geo.zw;
+    a.mxu = c->geo.mxu; a.myv = c->geo.myv; a.mzw = c->geo.mzw;
+    a.dxc = c->diag_dxc; a.dyc = c->diag_dyc; a.dzc = c->diag_dzc;
+    a.a_dEta = 1.0 / c->dEta; a.a_dXi = 1.0 / c->dXi; a.a_dPhi = 1.0 / c->dPhi;
+    a.dt = 0.5 * dmin;
+    a.max_iterations = 500;
+    // results and scratch live only for the call
+    size_t fb = sizeof(double) * d.n;
+    size_t need = 4 * fb + 4 * (size_t)d.n + (size_t)d.n + sizeof(double) * geom_scratch_doubles(d) +
+                  sizeof(double) * d.NX * d.NZ;
+    char *buf = nullptr;
+    TURB_CHECK(cudaMalloc(&buf, need));
+    GeomOut o;
+    char *q = buf;
+    for (int f = 0; f < 4; f++, q += fb) o.sdf[f] = (double *)q;
+    double *scr = (double *)q;
+    q += sizeof(double) * geom_scratch_doubles(d);
+    double *dip = (double *)q;
+    q += sizeof(double) * d.NX * d.NZ;
+    for (int f = 0; f < 4; f++, q += d.n) o.st[f] = (uint8_t *)q;
+    uint8_t *tmp = (uint8_t *)q;
+    cudaError_t e = cudaMemcpyAsync(dip, ipos, sizeof(double) * d.NX * d.NZ, cudaMemcpyHostToDevice, c->s);
+    if (e == cudaSuccess) e = geom_setup(c->s, a, dip, scr, tmp, &o);
+    for (int f = 0; f < 4 && e == cudaSuccess; f++) {
+        if (sdf && sdf[f])
+            e = cudaMemcpy2DAsync(sdf[f], (size_t)d.NX * 8, o.sdf[f], (size_t)d.PX * 8, (size_t)d.NX * 8,
+                                  (size_t)d.NY * d.NZ, cudaMemcpyDeviceToHost, c->s);
+        if (e == cudaSuccess && status && status[f])
+            e = cudaMemcpy2DAsync(status[f], (size_t)d.NX, o.st[f], (size_t)d.PX, (size_t)d.NX,
+                                  (size_t)d.NY * d.NZ, cudaMemcpyDeviceToHost, c->s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    cudaFree(buf);
+    if (e != cudaSuccess) return TURB_ERR_CUDA;
+    if (iterations) *iterations = o.iterations;
     return TURB_OK;
 }
 

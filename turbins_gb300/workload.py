@@ -355,6 +355,7 @@ class Case:
     dt: float
     steps: int
     state: dict
+    bed: object = None     # Bed of an immersed-boundary case
 
 
 def _lock_ic(g, params, seed, smooth=0.02, x_lock=1.0):
@@ -406,7 +407,7 @@ def turbidity_bump_case(nx=256, ny=128, nz=128, seed=0):
                alpha=[1.0], ctype=[PARTICLE], p_rtol=1e-10)
     s = _zero_state(g, 1)
     s["c0"] = _lock_ic(g, p, seed)
-    return Case("turbidity_bump_%dx%dx%d" % (nx, ny, nz), g, p, 5e-4, 200, s)
+    return Case("turbidity_bump_%dx%dx%d" % (nx, ny, nz), g, p, 5e-4, 200, s, bed)
 
 
 def multi_bump_case(nx=512, ny=256, nz=256, seed=4, lx=32.0, lz=2.0, nbump=16):
@@ -432,4 +433,4 @@ def multi_bump_case(nx=512, ny=256, nz=256, seed=4, lx=32.0, lz=2.0, nbump=16):
     c = _lock_ic(g, p, seed)
     s["c0"] = c.copy()
     s["c1"] = c.copy()
-    return Case("multi_bump_%dx%dx%d" % (nx, ny, nz), g, p, 2.5e-4, 500, s)
+    return Case("multi_bump_%dx%dx%d" % (nx, ny, nz), g, p, 2.5e-4, 500, s, bed)
