@@ -9,7 +9,7 @@ Re=5000, dt=2.5e-4, every step checked to max|div u| <= 1e-10.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-N > 1 runs independent replicas (the path is single-GPU),
+N > 1 runs independent replicas (the step has no exchange between GPUs),
 one rank per GPU, and reports the aggregate over ranks.  ``value`` is the
 device-timed throughput with all fields resident in HBM; ``e2e`` is the same
 step driven through the C ABI with the state copied host->device before and

@@ -394,6 +394,18 @@ int turb_deposit_set(turb_ctx *ctx, const double *host);
  * statuses and stencils are left as they are. */
 int turb_geometry(turb_ctx *ctx, const double *ipos, double *const *sdf, uint8_t *const *status, int *iterations);
 
+/* The ghost-cell stencils that the last turb_geometry built from its statuses
+ * and sdf, quantity q = 0..3 (u, v, w, c), as Immersed_setup_q_immersed_nodes
+ * (Immersed.c:546-616) builds them: IMMERSED nodes in DA order, normal from
+ * the sdf gradient, control point on the surface, image point twice as far
+ * into the fluid, the 8-node box around it (or the nearest fluid node), and
+ * Dirichlet (u, v, w) / Neumann (c) coefficients.  *n = node count; each
+ * array may be null, else holds n (im, nf, bcoef), 8n (fidx, fcoef) or 12n
+ * (pts: normal, control point, image point, node point) entries; im / fidx
+ * are DA linear indices (the turb_ib_desc layout). */
+int turb_geometry_stencils(turb_ctx *ctx, int q, int *n, int32_t *im, int32_t *nf, int32_t *fidx, double *fcoef,
+                           double *bcoef, double *pts);
+
 /* ---- open boundaries -------------------------------------------------------
  * params->inflow / outflow of the reference: an inflow face at x = xmin and a
  * convective outflow face at x = xmax.  turb_set_open_boundaries turns them

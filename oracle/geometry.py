@@ -201,3 +201,242 @@ def geometry(g, ipos):
     sdf = dict(c=c, u=u, v=v, w=w)
     st = {q: tag(g, q, sdf[q]) for q in "uvwc"}
     return sdf, st, n
+
+
+# ---- ghost-cell stencils (Immersed.c) ---------------------------------------
+DIRX = (0, 1, 0, 1, 0, 1, 0, 1)
+DIRY = (0, 0, 1, 1, 0, 0, 1, 1)
+DIRZ = (0, 0, 0, 0, 1, 1, 1, 1)
+NOT_FOUND, GVG_INF = -1, 10000000
+
+
+def node_coords(g, q):
+    """xq, yq, zq of Grid.c:1350-1370: u at (xu, yc, zc), v at (xc, yv, zc),
+    w at (xc, yc, zw), c at the centres"""
+    return (g.xu if q == "u" else g.xc, g.yv if q == "v" else g.yc, g.zw if q == "w" else g.zc)
+
+
+def _bsearch(data, v, lo, hi):
+    """MyMath_binary_search, MyMath.c:384-398"""
+    while lo <= hi:
+        mid = (lo + hi) // 2
+        if v >= data[mid]:
+            if v < data[mid + 1]:
+                return mid
+            lo = mid + 1
+        elif v < data[mid]:
+            hi = mid - 1
+    return -1
+
+
+def _index(a, v, n):
+    """Grid_get_x_index / _y_ / _z_ (Grid.c:1877-1966) with n = NI / NJ / NK"""
+    if v < a[0]:
+        return NOT_FOUND
+    if v > a[n - 1]:
+        return GVG_INF
+    return _bsearch(a, v, 0, n - 1)
+
+
+def _dist(a, b):
+    """MyMath_get_point_point_distance, MyMath.c:105-111"""
+    dx, dy, dz = a[0] - b[0], a[1] - b[1], a[2] - b[2]
+    return np.sqrt(dx * dx + dy * dy + dz * dz)
+
+
+def _gauss_jordan(A):
+    """MyMath_GaussJordan_matrix_inv (MyMath.c:117-195), full pivoting with
+    the reference's tie rule (the last maximum) and operation order"""
+    n = 8
+    B = [list(map(float, r)) for r in A]
+    piv = [-1] * n
+    irow = [0] * n
+    icol = [0] * n
+    in_row = in_col = -1
+    for i in range(n):
+        mx = 0.0
+        for j in range(n):
+            if piv[j] != 0:
+                for k in range(n):
+                    if piv[k] == -1 and abs(B[j][k]) >= mx:
+                        mx = abs(B[j][k])
+                        in_row, in_col = j, k
+        piv[in_col] += 1
+        if in_row != in_col:
+            B[in_row], B[in_col] = B[in_col], B[in_row]
+        irow[i], icol[i] = in_row, in_col
+        a = np.float64(1.0) / np.float64(B[in_col][in_col])
+        B[in_col][in_col] = 1.0
+        B[in_col] = [float(np.float64(x) * a) for x in B[in_col]]
+        for hh in range(n):
+            if hh != in_col:
+                t = B[hh][in_col]
+                B[hh][in_col] = 0.0
+                B[hh] = [float(np.float64(B[hh][h]) - np.float64(B[in_col][h]) * np.float64(t)) for h in range(n)]
+    for h in range(n - 1, -1, -1):
+        if irow[h] != icol[h]:
+            for k in range(n):
+                B[k][irow[h]], B[k][icol[h]] = B[k][icol[h]], B[k][irow[h]]
+    return B
+
+
+def immersed(g, q, sdf, st):
+    """Immersed_setup_q_immersed_nodes (Immersed.c:546-616) for quantity q
+    from its sdf and status arrays ([NZ][NY][NX]): returns im, nf, fidx [N,8]
+    and im/fidx as DA linear indices, fcoef [N,8], bcoef, pts [N,12]
+    (normal, control point, image point, node point)."""
+    f = np.float64
+    NI, NJ, NK = g.nx, g.ny, g.nz
+    NX, NY = NI + 1, NJ + 1
+    xq, yq, zq = node_coords(g, q)
+    dxc, dyc, dzc = cell_widths(g.xu), cell_widths(g.yv), cell_widths(g.zw)
+    ni = NI + (q == "u"); nj = NJ + (q == "v"); nk = NK + (q == "w")
+
+    def status(i, j, k):
+        if i < 0 or i > NI or j < 0 or j > NJ or k < 0 or k > NK:
+            return -1
+        return int(st[k, j, i])
+
+    def grad(i, j, k):
+        iw, ie = max(i - 1, 0), min(i + 1, ni - 1)
+        js, jn = max(j - 1, 0), min(j + 1, nj - 1)
+        kb, kf = max(k - 1, 0), min(k + 1, nk - 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return ((sdf[k, j, ie] - sdf[k, j, iw]) / (xq[ie] - xq[iw]),
+                    (sdf[k, jn, i] - sdf[k, js, i]) / (yq[jn] - yq[js]),
+                    (sdf[kf, j, i] - sdf[kb, j, i]) / (zq[kf] - zq[kb]))
+
+    kk, jj, ii = np.nonzero(st == IMMERSED)   # DA order
+    N = len(ii)
+    im = ((kk * NY + jj) * NX + ii).astype(np.int32)
+    nf = np.zeros(N, np.int32)
+    fidx = np.zeros((N, 8), np.int32)
+    fcoef = np.zeros((N, 8))
+    bcoef = np.zeros(N)
+    pts = np.zeros((N, 12))
+    for t in range(N):
+        i, j, k = int(ii[t]), int(jj[t]), int(kk[t])
+        P = (f(xq[i]), f(yq[j]), f(zq[k]))
+        # Surface_compute_normal, Surface.c:547-615
+        gx, gy, gz = grad(i, j, k)
+        an = f(1.0) / np.sqrt(gx * gx + gy * gy + gz * gz)
+        n = (gx * an, gy * an, gz * an)
+        # Surface_find_Dn_to_surface, Surface.c:475-541
+        dn = n[0] * gx + n[1] * gy + n[2] * gz
+        if abs(dn) < 1.0e-2 or np.isnan(dn):
+            dn = f(1.0e-2)
+        D = sdf[k, j, i] / dn
+        C = (P[0] - n[0] * D, P[1] - n[1] * D, P[2] - n[2] * D)
+        # Immersed_find_image_point, Immersed.c:1063-1150
+        ds = _dist(P, C)
+        D2 = f(2.0) * ds
+        I = (P[0] + n[0] * D2, P[1] + n[1] * D2, P[2] + n[2] * D2)
+        # Immersed_find_box, Immersed.c:1210-1402
+        tx = max(f(0.005) * dxc[i], 1e-12)
+        ty = max(f(0.005) * dyc[j], 1e-12)
+        tz = max(f(0.005) * dzc[k], 1e-12)
+        px = (tx, -tx, tx, -tx, tx, -tx, tx, -tx)
+        py = (ty, ty, -ty, -ty, ty, ty, -ty, -ty)
+        pz = (tz, tz, tz, tz, -tz, -tz, -tz, -tz)
+        found = False
+        m = 0
+        while not found and m < 8:
+            ig = _index(xq, I[0] + px[m], NI)
+            jg = _index(yq, I[1] + py[m], NJ)
+            kg = _index(zq, I[2] + pz[m], NK)
+            good = True
+            for gg in range(8):
+                s = status(ig + DIRX[gg], jg + DIRY[gg], kg + DIRZ[gg])
+                if s != FLUID and s != IMMERSED:
+                    good = False
+                    break
+            found = good
+            if found and not (xq[ig] <= I[0] <= xq[ig + 1] and yq[jg] <= I[1] <= yq[jg + 1]
+                              and zq[kg] <= I[2] <= zq[kg + 1]):
+                found = False
+            m += 1
+        box = []
+        if found:
+            box = [(ig + DIRX[gg], jg + DIRY[gg], kg + DIRZ[gg]) for gg in range(8)]
+        else:
+            ig = min(max(_index(xq, I[0], NI), 0), NI - 1)
+            jg = min(max(_index(yq, I[1], NJ), 0), NJ - 1)
+            kg = min(max(_index(zq, I[2], NK), 0), NK - 1)
+            dmin, gf = 1e12, -1
+            for gg in range(8):
+                a, b, c = ig + DIRX[gg], jg + DIRY[gg], kg + DIRZ[gg]
+                if status(a, b, c) == FLUID:
+                    dd = _dist(I, (xq[a], yq[b], zq[c]))
+                    if dd < dmin:
+                        dmin, gf = dd, gg
+            if gf >= 0:
+                box = [(ig + DIRX[gf], jg + DIRY[gf], kg + DIRZ[gf])]
+        nfl = len(box)
+        # Immersed_compute_interpolation_coef, Immersed.c:122-376
+        df = _dist(I, C)
+        if abs(ds) <= 1e-10 and abs(df) <= 1e-10:
+            coef = f(1.0)
+        else:
+            coef = ds / df
+        fp = [(f(xq[a]), f(yq[b]), f(zq[c])) for a, b, c in box]
+        w = [f(0.0)] * 8
+        if nfl == 8:
+            x7, y7, z7 = fp[7]
+            x0, y0, z0 = fp[0]
+            al = (x7 - I[0]) / (x7 - x0)
+            be = (y7 - I[1]) / (y7 - y0)
+            ga = (z7 - I[2]) / (z7 - z0)
+            w = [al * be * ga, (1.0 - al) * be * ga, al * (1.0 - be) * ga, (1.0 - al) * (1.0 - be) * ga,
+                 al * be * (1.0 - ga), (1.0 - al) * be * (1.0 - ga), al * (1.0 - be) * (1.0 - ga),
+                 (1.0 - al) * (1.0 - be) * (1.0 - ga)]
+        elif nfl == 1:
+            w[0] = f(1.0)
+        fc = [f(0.0)] * 8
+        if q != "c":
+            bc = f(1.0) + coef
+            for gg in range(nfl):
+                fc[gg] = w[gg] * coef
+        elif nfl == 1:
+            bc = -(ds + df)
+            fc[0] = w[0] * f(-1.0)
+        else:
+            A = [[0.0] * 8 for _ in range(8)]
+            selfin = False
+            r = 0
+            for gg in range(nfl):
+                if box[gg] == (i, j, k):
+                    selfin = True
+                else:
+                    x = fp[gg][0] - I[0]
+                    y = fp[gg][1] - I[1]
+                    z = fp[gg][2] - I[2]
+                    A[r] = [x * y * z, x * y, x * z, y * z, x, y, z, 1.0]
+                    r += 1
+            if selfin:
+                xc_, yc_, zc_ = C[0] - I[0], C[1] - I[1], C[2] - I[2]
+                nx_, ny_, nz_ = n
+                A[r] = [nx_ * yc_ * zc_ + ny_ * xc_ * zc_ + nz_ * xc_ * yc_, yc_ * nx_ + xc_ * ny_,
+                        zc_ * nx_ + xc_ * nz_, zc_ * ny_ + yc_ * nz_, nx_, ny_, nz_, 0.0]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                B = _gauss_jordan(A)
+            rhs = f(B[7][7]) if selfin else f(0.0)
+            bc = -(ds + df) + rhs
+            r = 0
+            for gg in range(nfl):
+                if box[gg] == (i, j, k):
+                    fc[gg] = f(0.0)
+                else:
+                    fc[gg] = -f(B[7][r])
+                    r += 1
+        for gg in range(nfl):
+            if np.isnan(fc[gg]) or np.isinf(fc[gg]):
+                fc[gg] = f(0.0)
+                bc = f(0.0)
+        nf[t] = nfl
+        for gg in range(nfl):
+            a, b, c = box[gg]
+            fidx[t, gg] = (c * NY + b) * NX + a
+            fcoef[t, gg] = fc[gg]
+        bcoef[t] = bc
+        pts[t] = (n[0], n[1], n[2], C[0], C[1], C[2], I[0], I[1], I[2], P[0], P[1], P[2])
+    return dict(n=N, im=im, nf=nf, fidx=fidx, fcoef=fcoef, bcoef=bcoef, pts=pts)

@@ -691,7 +691,7 @@ void ref_outflow_from_plane(ref_case *r, char q, int ic, const double *x)
     }
 }
 
-/* ---- immersed-boundary geometry (row f4) -----------------------------------
+/* ---- immersed-boundary geometry ------------------------------------------
  * The reference's set-up of a bottom topography y = h(x, z): the sdf guess
  * yc - interface_position (Surface_initialize, Surface.c:96-195), level-set
  * reinitialisation (Surface_find_exact_sdf -> Levelset_reinitialize,
@@ -732,4 +732,45 @@ void ref_geometry(ref_case *r, const double *ipos, double *c_sdf, double *u_sdf,
         const double *a = shim_vec_data(*gs[q]);
         for (t = 0; t < r->n; t++) st_out[(long)q * r->n + t] = (unsigned char)a[t];
     }
+}
+
+/* The reference's ghost-cell stencils of quantity q built from the current
+ * geometry (call ref_geometry first): Immersed_setup_q_immersed_nodes
+ * (Immersed.c:546-616: indices in DA order, coordinates, normals, control and
+ * image points, boundary condition, 8-node box or nearest fluid node,
+ * Dirichlet / Neumann coefficients).  Returns N; with cap >= N the arrays get
+ * im (DA linear index), nf, fidx[8] (DA linear), fcoef[8], bcoef and pts[12]
+ * (normal, control, image point, im_point). */
+int ref_immersed(ref_case *r, char q, int cap, int *im, int *nf, int *fidx, double *fcoef, double *bcoef,
+                 double *pts)
+{
+    MAC_grid *g = r->g;
+    Immersed *I;
+    int t, m;
+    long NX = g->NX, NY = g->NY;
+    Immersed_setup_q_immersed_nodes(g, q);
+    I = q == 'u' ? g->u_immersed : q == 'v' ? g->v_immersed : q == 'w' ? g->w_immersed : g->c_immersed;
+    if (I->N > cap) return I->N;
+    for (t = 0; t < I->N; t++) {
+        ImmersedNode *nd = &I->ib_nodes[t];
+        im[t] = (int)((nd->im_index.z_index * NY + nd->im_index.y_index) * NX + nd->im_index.x_index);
+        nf[t] = nd->n_fluid;
+        for (m = 0; m < 8; m++) {
+            if (m < nd->n_fluid) {
+                fidx[t * 8 + m] = (int)((nd->fluid_index[m].z_index * NY + nd->fluid_index[m].y_index) * NX +
+                                        nd->fluid_index[m].x_index);
+                fcoef[t * 8 + m] = nd->fluid_coef[m];
+            } else {
+                fidx[t * 8 + m] = 0;
+                fcoef[t * 8 + m] = 0.0;
+            }
+        }
+        bcoef[t] = nd->boundary_coef;
+        pts[t * 12 + 0] = nd->n.vx; pts[t * 12 + 1] = nd->n.vy; pts[t * 12 + 2] = nd->n.vz;
+        pts[t * 12 + 3] = nd->control_point.x; pts[t * 12 + 4] = nd->control_point.y;
+        pts[t * 12 + 5] = nd->control_point.z;
+        pts[t * 12 + 6] = nd->image_point.x; pts[t * 12 + 7] = nd->image_point.y; pts[t * 12 + 8] = nd->image_point.z;
+        pts[t * 12 + 9] = nd->im_point.x; pts[t * 12 + 10] = nd->im_point.y; pts[t * 12 + 11] = nd->im_point.z;
+    }
+    return I->N;
 }

@@ -258,6 +258,25 @@ class Reference:
                               st.ctypes.data_as(C.c_void_p))
         return dict(c=sd[0], u=sd[1], v=sd[2], w=sd[3]), dict(u=st[0], v=st[1], w=st[2], c=st[3])
 
+    def immersed(self, q, cap=None):
+        """the reference's stencils of quantity q from the current geometry
+        (after geometry()): dict of im, nf, fidx [N,8], fcoef [N,8], bcoef,
+        pts [N,12] (normal, control point, image point, node point)"""
+        if cap is None:
+            cap = self.g.npts
+        im = np.zeros(cap, np.int32)
+        nf = np.zeros(cap, np.int32)
+        fidx = np.zeros((cap, 8), np.int32)
+        fcoef = np.zeros((cap, 8))
+        bcoef = np.zeros(cap)
+        pts = np.zeros((cap, 12))
+        n = self.lib.ref_immersed(self.h, C.c_char(q.encode()), cap, im.ctypes.data_as(C.c_void_p),
+                                  nf.ctypes.data_as(C.c_void_p), fidx.ctypes.data_as(C.c_void_p), _p(fcoef),
+                                  _p(bcoef), _p(pts))
+        if n > cap:
+            return self.immersed(q, n)
+        return dict(n=n, im=im[:n], nf=nf[:n], fidx=fidx[:n], fcoef=fcoef[:n], bcoef=bcoef[:n], pts=pts[:n])
+
     def c_term(self, ct):
         """the buoyancy term at v nodes that Velocity_v_set_RHS computes
         (2-point y interpolation of the total concentration, Velocity.c:1861-

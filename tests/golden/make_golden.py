@@ -256,7 +256,8 @@ def dump_open():
 
 
 # immersed-boundary geometry: the reference's surface set-up (level-set
-# reinitialisation of yc - h, q-sdf, node tagging) from the bed heights
+# reinitialisation of yc - h, q-sdf, node tagging) from the bed heights, and
+# the ghost-cell stencils it builds on them
 GEOM_CASES = {
     "bump": lambda: _cases.bump_small(24, 12, 8),
     "multi": lambda: _cases.multi_small(40, 20, 12),
@@ -272,8 +273,13 @@ def bed_heights(case):
 def dump_geom(name, case):
     g = case.grid
     ipos = np.ascontiguousarray(bed_heights(case))
-    sdf, st = Reference(g, case.params).geometry(ipos)
+    ref = Reference(g, case.params)
+    sdf, st = ref.geometry(ipos)
     out = {"ipos": ipos}
+    for q in "uvwc":
+        ib = ref.immersed(q)
+        for k in ("im", "nf", "fidx", "fcoef", "bcoef", "pts"):
+            out["ref_ib_%s_%s" % (q, k)] = ib[k]
     for k in ("xc", "yc", "zc", "xu", "yv", "zw"):
         out["grid_" + k] = getattr(g, k)
     for q in "cuvw":

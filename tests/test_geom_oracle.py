@@ -41,3 +41,15 @@ def test_flat_bed_keeps_the_interface():
     assert np.all(np.sign(c) == np.sign(yc - h)[None, :, None])
     want = np.where(yc >= h, G.FLUID, np.where(np.r_[yc[1:], np.inf] >= h, G.IMMERSED, G.SOLID))
     assert np.all(st["c"][:-1, :-1, :-1] == want[None, :, None].astype(np.uint8))
+
+
+@pytest.mark.parametrize("name", sorted(GEOM))
+def test_stencil_oracle_matches_reference(name):
+    """Immersed_setup_q_immersed_nodes restated: node order, boxes, nearest-
+    node fallbacks, Dirichlet and Neumann (Gauss-Jordan) coefficients"""
+    z = np.load(os.path.join(HERE, "golden", "geom", "geom_%s.npz" % name))
+    g = GEOM[name]().grid
+    for q in "uvwc":
+        ib = G.immersed(g, q, z["ref_sdf_" + q], z["ref_status_" + q])
+        for k in ("im", "nf", "fidx", "fcoef", "bcoef", "pts"):
+            assert np.array_equal(ib[k], z["ref_ib_%s_%s" % (q, k)]), (q, k)

@@ -319,6 +319,27 @@ class Context:
         _check(self.lib.turb_geometry(self.ctx, ipos.ctypes.data_as(C.c_void_p), sp, tp, C.byref(it)), "geometry")
         return (dict(c=sd[0], u=sd[1], v=sd[2], w=sd[3]), dict(u=st[0], v=st[1], w=st[2], c=st[3]), it.value)
 
+    def geometry_stencils(self, q):
+        """turb_geometry_stencils: the ghost-cell stencils of quantity q
+        ('u', 'v', 'w', 'c') made by the last geometry() call"""
+        qi = "uvwc".index(q)
+        n = C.c_int(0)
+        _check(self.lib.turb_geometry_stencils(self.ctx, qi, C.byref(n), None, None, None, None, None, None),
+               "geometry_stencils")
+        n = n.value
+        im = np.zeros(n, np.int32)
+        nf = np.zeros(n, np.int32)
+        fidx = np.zeros((n, 8), np.int32)
+        fcoef = np.zeros((n, 8))
+        bcoef = np.zeros(n)
+        pts = np.zeros((n, 12))
+        m = C.c_int(0)
+        v = C.c_void_p
+        _check(self.lib.turb_geometry_stencils(self.ctx, qi, C.byref(m), v(im.ctypes.data), v(nf.ctypes.data),
+                                               v(fidx.ctypes.data), v(fcoef.ctypes.data), v(bcoef.ctypes.data),
+                                               v(pts.ctypes.data)), "geometry_stencils")
+        return dict(n=n, im=im, nf=nf, fidx=fidx, fcoef=fcoef, bcoef=bcoef, pts=pts)
+
     def deposit_integrate(self, dt):
         _check(self.lib.turb_deposit_integrate(self.ctx, C.c_double(dt)), "deposit_integrate")
 

@@ -255,6 +255,325 @@ __global__ void k_buffer(Dims d, int q, int width, const uint8_t *__restrict__ b
 inline dim3 g3(const Dims &d) { return dim3((unsigned)((d.NX + 31) / 32), (unsigned)((d.NY + 7) / 8), (unsigned)d.NZ); }
 const dim3 B38(32, 8, 1);
 
+
+// ---- ghost-cell stencils (Immersed.c) --------------------------------------
+
+// IMMERSED nodes per (j, k) row, one thread per row
+__global__ void k_ib_count(Dims d, const uint8_t *__restrict__ st, int *__restrict__ cnt)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (long long)d.NY * d.NZ) return;
+    int j = (int)(r % d.NY), k = (int)(r / d.NY);
+    const uint8_t *row = st + d.at(0, j, k);
+    int c = 0;
+    for (int i = 0; i < d.NX; i++) c += row[i] == T_IMMERSED;
+    cnt[r] = c;
+}
+
+// exclusive scan of the row counts in place, total at cnt[nr]; one block
+__global__ void k_ib_scan(long long nr, int *__restrict__ cnt)
+{
+    __shared__ int sm[1024];
+    long long per = (nr + blockDim.x - 1) / blockDim.x;
+    long long a = threadIdx.x * per, b = a + per < nr ? a + per : nr;
+    int s = 0;
+    for (long long r = a; r < b; r++) s += cnt[r];
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < (int)blockDim.x; t++) {
+            int v = sm[t];
+            sm[t] = run;
+            run += v;
+        }
+        cnt[nr] = run;
+    }
+    __syncthreads();
+    int run = sm[threadIdx.x];
+    for (long long r = a; r < b; r++) {
+        int v = cnt[r];
+        cnt[r] = run;
+        run += v;
+    }
+}
+
+// node list in DA order (Immersed_set_q_immersed_indices, Immersed.c:379-447)
+__global__ void k_ib_emit(Dims d, const uint8_t *__restrict__ st, const int *__restrict__ off,
+                          int *__restrict__ node)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (long long)d.NY * d.NZ) return;
+    int j = (int)(r % d.NY), k = (int)(r / d.NY);
+    const uint8_t *row = st + d.at(0, j, k);
+    int o = off[r];
+    for (int i = 0; i < d.NX; i++)
+        if (row[i] == T_IMMERSED) node[o++] = (int)(((long long)k * d.NY + j) * d.NX + i);
+}
+
+struct IbArgs {
+    Dims d;
+    int neumann;                          // c: NEUMANN, u/v/w: DIRICHLET
+    int ni, nj, nk;                       // NI / NJ / NK, +1 along the node's own face axis
+    const double *xq, *yq, *zq;           // node coordinates of the quantity
+    const double *dxc, *dyc, *dzc;
+    const double *sdf;                    // pitched DA
+    const uint8_t *st;                    // pitched DA
+};
+
+__device__ __forceinline__ int ib_status(const IbArgs &a, int i, int j, int k)
+{
+    const Dims &d = a.d;
+    if (i < 0 || i > d.nx || j < 0 || j > d.ny || k < 0 || k > d.nz) return -1;   // OUTSIDE
+    return a.st[d.at(i, j, k)];
+}
+
+// MyMath_binary_search (MyMath.c:384-398) behind Grid_get_x_index
+// (Grid.c:1877-1903): NOT_FOUND below q[0], GVG_INF above q[n-1]
+__device__ int ib_index(const double *q, double v, int n)
+{
+    if (v < q[0]) return -1;
+    if (v > q[n - 1]) return 10000000;
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) / 2;
+        if (v >= q[mid]) {
+            if (v < q[mid + 1]) return mid;
+            lo = mid + 1;
+        } else if (v < q[mid]) {
+            hi = mid - 1;
+        } else {
+            return -1;   // unordered (NaN) search value: the reference loops; treat as not found
+        }
+    }
+    return -1;
+}
+
+__device__ __forceinline__ double dist3(double ax, double ay, double az, double bx, double by, double bz)
+{
+    double x = sb(ax, bx), y = sb(ay, by), z = sb(az, bz);
+    return __dsqrt_rn(ad(ad(ml(x, x), ml(y, y)), ml(z, z)));
+}
+
+// MyMath_GaussJordan_matrix_inv (MyMath.c:117-195) of an 8x8 matrix in place
+__device__ void ib_gauss_jordan(double (*A)[8])
+{
+    int piv[8], irow[8], icol[8];
+    for (int j = 0; j < 8; j++) piv[j] = -1;
+    int in_row = -1, in_col = -1;
+    for (int i = 0; i < 8; i++) {
+        double mxv = 0.0;
+        for (int j = 0; j < 8; j++)
+            if (piv[j] != 0)
+                for (int k = 0; k < 8; k++)
+                    if (piv[k] == -1 && fabs(A[j][k]) >= mxv) {
+                        mxv = fabs(A[j][k]);
+                        in_row = j;
+                        in_col = k;
+                    }
+        if (in_col < 0) return;   // every entry NaN: nothing the reference could pick either
+        ++piv[in_col];
+        if (in_row != in_col)
+            for (int h = 0; h < 8; h++) {
+                double t = A[in_row][h];
+                A[in_row][h] = A[in_col][h];
+                A[in_col][h] = t;
+            }
+        irow[i] = in_row;
+        icol[i] = in_col;
+        double ap = dv(1.0, A[in_col][in_col]);
+        A[in_col][in_col] = 1.0;
+        for (int h = 0; h < 8; h++) A[in_col][h] = ml(A[in_col][h], ap);
+        for (int hh = 0; hh < 8; hh++)
+            if (hh != in_col) {
+                double t = A[hh][in_col];
+                A[hh][in_col] = 0.0;
+                for (int h = 0; h < 8; h++) A[hh][h] = sb(A[hh][h], ml(A[in_col][h], t));
+            }
+    }
+    for (int h = 7; h >= 0; h--)
+        if (irow[h] != icol[h])
+            for (int k = 0; k < 8; k++) {
+                double t = A[k][irow[h]];
+                A[k][irow[h]] = A[k][icol[h]];
+                A[k][icol[h]] = t;
+            }
+}
+
+// one IMMERSED node: normal (Surface_compute_normal, Surface.c:547-615),
+// control point (Immersed_find_control_point + Surface_find_Dn_to_surface,
+// Immersed.c:891-953, Surface.c:475-541), image point (Immersed.c:1063-1150),
+// surrounding box or nearest fluid node (Immersed_find_box,
+// Immersed.c:1210-1402) and coefficients (Immersed_compute_interpolation_coef,
+// Immersed.c:122-376)
+__global__ void __launch_bounds__(128) k_ib_stencil(IbArgs a, int n, const int *__restrict__ node, GeomIb o)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const Dims &d = a.d;
+    int L = node[t];
+    int i = L % d.NX, j = (L / d.NX) % d.NY, k = L / (d.NX * d.NY);
+    const double *xq = a.xq, *yq = a.yq, *zq = a.zq;
+    double Px = xq[i], Py = yq[j], Pz = zq[k];
+    auto S = [&](int ii, int jj, int kk) { return a.sdf[d.at(ii, jj, kk)]; };
+    int iw = imx(i - 1, 0), ie = imn(i + 1, a.ni - 1);
+    int js = imx(j - 1, 0), jn = imn(j + 1, a.nj - 1);
+    int kb = imx(k - 1, 0), kf = imn(k + 1, a.nk - 1);
+    double gx = dv(sb(S(ie, j, k), S(iw, j, k)), sb(xq[ie], xq[iw]));
+    double gy = dv(sb(S(i, jn, k), S(i, js, k)), sb(yq[jn], yq[js]));
+    double gz = dv(sb(S(i, j, kf), S(i, j, kb)), sb(zq[kf], zq[kb]));
+    double an = dv(1.0, __dsqrt_rn(ad(ad(ml(gx, gx), ml(gy, gy)), ml(gz, gz))));
+    double nx = ml(gx, an), ny = ml(gy, an), nz = ml(gz, an);
+    double dn = ad(ad(ml(nx, gx), ml(ny, gy)), ml(nz, gz));
+    if (fabs(dn) < 1.0e-2 || isnan(dn)) dn = 1.0e-2;
+    double D = dv(S(i, j, k), dn);
+    double Cx = sb(Px, ml(nx, D)), Cy = sb(Py, ml(ny, D)), Cz = sb(Pz, ml(nz, D));
+    double ds = dist3(Px, Py, Pz, Cx, Cy, Cz);
+    double D2 = ml(2.0, ds);
+    double Ix = ad(Px, ml(nx, D2)), Iy = ad(Py, ml(ny, D2)), Iz = ad(Pz, ml(nz, D2));
+    // the box: the image point perturbed towards each of the 8 corners
+    const double tx = mx(ml(0.005, a.dxc[i]), 1e-12), ty = mx(ml(0.005, a.dyc[j]), 1e-12),
+                 tz = mx(ml(0.005, a.dzc[k]), 1e-12);
+    int ig = 0, jg = 0, kg = 0;
+    bool found = false;
+    for (int m = 0; m < 8 && !found; m++) {
+        double xp = ad(Ix, (m & 1) ? -tx : tx), yp = ad(Iy, (m & 2) ? -ty : ty), zp = ad(Iz, (m & 4) ? -tz : tz);
+        ig = ib_index(xq, xp, d.nx);
+        jg = ib_index(yq, yp, d.ny);
+        kg = ib_index(zq, zp, d.nz);
+        bool good = true;
+        for (int g = 0; g < 8 && good; g++) {
+            int s = ib_status(a, ig + (g & 1), jg + ((g >> 1) & 1), kg + (g >> 2));
+            good = s == T_FLUID || s == T_IMMERSED;
+        }
+        found = good && Ix >= xq[ig] && Ix <= xq[ig + 1] && Iy >= yq[jg] && Iy <= yq[jg + 1] && Iz >= zq[kg] &&
+                Iz <= zq[kg + 1];
+    }
+    int nf = 0;
+    int fi[8], fj[8], fk[8];
+    if (found) {
+        nf = 8;
+        for (int g = 0; g < 8; g++) {
+            fi[g] = ig + (g & 1);
+            fj[g] = jg + ((g >> 1) & 1);
+            fk[g] = kg + (g >> 2);
+        }
+    } else {
+        ig = imn(imx(ib_index(xq, Ix, d.nx), 0), d.nx - 1);
+        jg = imn(imx(ib_index(yq, Iy, d.ny), 0), d.ny - 1);
+        kg = imn(imx(ib_index(zq, Iz, d.nz), 0), d.nz - 1);
+        double dmin = 1e12;
+        int gf = -1;
+        for (int g = 0; g < 8; g++) {
+            int p = ig + (g & 1), q = jg + ((g >> 1) & 1), r = kg + (g >> 2);
+            if (ib_status(a, p, q, r) == T_FLUID) {
+                double dd = dist3(Ix, Iy, Iz, xq[p], yq[q], zq[r]);
+                if (dd < dmin) {
+                    dmin = dd;
+                    gf = g;
+                }
+            }
+        }
+        if (gf >= 0) {
+            nf = 1;
+            fi[0] = ig + (gf & 1);
+            fj[0] = jg + ((gf >> 1) & 1);
+            fk[0] = kg + (gf >> 2);
+        }
+    }
+    double df = dist3(Ix, Iy, Iz, Cx, Cy, Cz);
+    double coef = (fabs(ds) <= 1e-10 && fabs(df) <= 1e-10) ? 1.0 : dv(ds, df);
+    double w[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (nf == 8) {
+        double x7 = xq[fi[7]], y7 = yq[fj[7]], z7 = zq[fk[7]];
+        double x0 = xq[fi[0]], y0 = yq[fj[0]], z0 = zq[fk[0]];
+        double al = dv(sb(x7, Ix), sb(x7, x0)), be = dv(sb(y7, Iy), sb(y7, y0)), ga = dv(sb(z7, Iz), sb(z7, z0));
+        double al1 = sb(1.0, al), be1 = sb(1.0, be), ga1 = sb(1.0, ga);
+        w[0] = ml(ml(al, be), ga);
+        w[1] = ml(ml(al1, be), ga);
+        w[2] = ml(ml(al, be1), ga);
+        w[3] = ml(ml(al1, be1), ga);
+        w[4] = ml(ml(al, be), ga1);
+        w[5] = ml(ml(al1, be), ga1);
+        w[6] = ml(ml(al, be1), ga1);
+        w[7] = ml(ml(al1, be1), ga1);
+    } else if (nf == 1) {
+        w[0] = 1.0;
+    }
+    double fc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double bc;
+    if (!a.neumann) {
+        bc = ad(1.0, coef);
+        for (int g = 0; g < nf; g++) fc[g] = ml(w[g], coef);
+    } else if (nf == 1) {
+        bc = -ad(ds, df);
+        fc[0] = -w[0];
+    } else {
+        double A[8][8];
+        for (int r = 0; r < 8; r++)
+            for (int c = 0; c < 8; c++) A[r][c] = 0.0;
+        bool self = false;
+        int r = 0;
+        for (int g = 0; g < nf; g++) {
+            if (fi[g] == i && fj[g] == j && fk[g] == k) {
+                self = true;
+            } else {
+                double x = sb(xq[fi[g]], Ix), y = sb(yq[fj[g]], Iy), z = sb(zq[fk[g]], Iz);
+                A[r][0] = ml(ml(x, y), z);
+                A[r][1] = ml(x, y);
+                A[r][2] = ml(x, z);
+                A[r][3] = ml(y, z);
+                A[r][4] = x;
+                A[r][5] = y;
+                A[r][6] = z;
+                A[r][7] = 1.0;
+                r++;
+            }
+        }
+        if (self) {
+            double xc = sb(Cx, Ix), yc = sb(Cy, Iy), zc = sb(Cz, Iz);
+            A[r][0] = ad(ad(ml(ml(nx, yc), zc), ml(ml(ny, xc), zc)), ml(ml(nz, xc), yc));
+            A[r][1] = ad(ml(yc, nx), ml(xc, ny));
+            A[r][2] = ad(ml(zc, nx), ml(xc, nz));
+            A[r][3] = ad(ml(zc, ny), ml(yc, nz));
+            A[r][4] = nx;
+            A[r][5] = ny;
+            A[r][6] = nz;
+            A[r][7] = 0.0;
+        }
+        ib_gauss_jordan(A);
+        bc = ad(-ad(ds, df), self ? A[7][7] : 0.0);
+        r = 0;
+        for (int g = 0; g < nf; g++) {
+            if (fi[g] == i && fj[g] == j && fk[g] == k) {
+                fc[g] = 0.0;
+            } else {
+                fc[g] = -A[7][r];
+                r++;
+            }
+        }
+    }
+    for (int g = 0; g < nf; g++)
+        if (isnan(fc[g]) || isinf(fc[g])) {
+            fc[g] = 0.0;
+            bc = 0.0;
+        }
+    o.im[t] = L;
+    o.nf[t] = nf;
+    for (int g = 0; g < 8; g++) {
+        o.fidx[(long long)t * 8 + g] = g < nf ? (int)(((long long)fk[g] * d.NY + fj[g]) * d.NX + fi[g]) : 0;
+        o.fcoef[(long long)t * 8 + g] = g < nf ? fc[g] : 0.0;
+    }
+    o.bcoef[t] = bc;
+    if (o.pts) {
+        double *p = o.pts + (long long)t * 12;
+        p[0] = nx; p[1] = ny; p[2] = nz;
+        p[3] = Cx; p[4] = Cy; p[5] = Cz;
+        p[6] = Ix; p[7] = Iy; p[8] = Iz;
+        p[9] = Px; p[10] = Py; p[11] = Pz;
+    }
+}
+
 }  // namespace
 
 long long geom_scratch_doubles(const Dims &d)
@@ -315,5 +634,41 @@ cudaError_t geom_setup(cudaStream_t s, const GeomArgs &a, const double *ipos, do
         cudaMemcpyAsync(tmp, o->st[q], (size_t)d.n, cudaMemcpyDeviceToDevice, s);
         k_buffer<<<G, B38, 0, s>>>(d, q, 2, tmp, o->st[q]);
     }
+    return cudaGetLastError();
+}
+
+// IMMERSED nodes of one status array: row offsets (NY*NZ + 1 ints) and the count
+cudaError_t geom_ib_count(cudaStream_t s, const Dims &d, const uint8_t *st, int *rows, int *n)
+{
+    long long nr = (long long)d.NY * d.NZ;
+    k_ib_count<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(d, st, rows);
+    k_ib_scan<<<1, 1024, 0, s>>>(nr, rows);
+    cudaError_t e = cudaMemcpyAsync(n, rows + nr, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
+// Immersed_setup_q_immersed_nodes (Immersed.c:546-616) for quantity q
+// (0..3 = u, v, w, c) into o (o.n entries; node: o.n ints of scratch)
+cudaError_t geom_ib_build(cudaStream_t s, const GeomArgs &a, int q, const double *sdf, const uint8_t *st,
+                          const int *rows, int *node, const GeomIb &o)
+{
+    const Dims &d = a.d;
+    long long nr = (long long)d.NY * d.NZ;
+    if (o.n == 0) return cudaGetLastError();
+    k_ib_emit<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(d, st, rows, node);
+    IbArgs b;
+    b.d = d;
+    b.neumann = q == 3;
+    b.ni = d.nx + (q == 0);
+    b.nj = d.ny + (q == 1);
+    b.nk = d.nz + (q == 2);
+    b.xq = q == 0 ? a.xu : a.xc;
+    b.yq = q == 1 ? a.yv : a.yc;
+    b.zq = q == 2 ? a.zw : a.zc;
+    b.dxc = a.dxc; b.dyc = a.dyc; b.dzc = a.dzc;
+    b.sdf = sdf;
+    b.st = st;
+    k_ib_stencil<<<(unsigned)((o.n + 127) / 128), 128, 0, s>>>(b, o.n, node, o);
     return cudaGetLastError();
 }

@@ -175,6 +175,9 @@ struct turb_ctx {
     // restart staging: one field as big-endian words, on the device and pinned
     unsigned long long *rs_dev = nullptr;
     void *rs_host = nullptr;
+    // ghost-cell stencils made by turb_geometry (one allocation per quantity)
+    GeomIb gib[4];
+    void *gib_buf[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -994,6 +997,8 @@ int turb_destroy(turb_ctx *c)
     c->mem.release();
     if (c->hscal) cudaFreeHost(c->hscal);
     if (c->rs_host) cudaFreeHost(c->rs_host);
+    for (void *b : c->gib_buf)
+        if (b) cudaFree(b);
     cudaStreamDestroy(c->s);
     delete c;
     return TURB_OK;
@@ -1647,6 +1652,39 @@ int turb_geometry(turb_ctx *c, const double *ipos, double *const *sdf, uint8_t *
     uint8_t *tmp = (uint8_t *)q;
     cudaError_t e = cudaMemcpyAsync(dip, ipos, sizeof(double) * d.NX * d.NZ, cudaMemcpyHostToDevice, c->s);
     if (e == cudaSuccess) e = geom_setup(c->s, a, dip, scr, tmp, &o);
+    // ghost-cell stencils of u, v, w, c from the statuses and sdf just made
+    // (Immersed_setup_q_immersed_nodes for each quantity)
+    int *rows = nullptr, *node = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&rows, sizeof(int) * ((size_t)d.NY * d.NZ + 1));
+    const int sq[4] = {1, 2, 3, 0};   // sdf index of u, v, w, c
+    for (int q = 0; q < 4 && e == cudaSuccess; q++) {
+        if (c->gib_buf[q]) cudaFree(c->gib_buf[q]);
+        c->gib_buf[q] = nullptr;
+        c->gib[q] = GeomIb();
+        int n = 0;
+        e = geom_ib_count(c->s, d, o.st[q], rows, &n);
+        if (e != cudaSuccess || n == 0) continue;
+        size_t bi = sizeof(int32_t) * (size_t)n, bd = sizeof(double) * (size_t)n;
+        char *b = nullptr;
+        e = cudaMalloc(&b, 10 * bi + 21 * bd);
+        if (e != cudaSuccess) break;
+        c->gib_buf[q] = b;
+        GeomIb &g = c->gib[q];
+        g.n = n;
+        g.fcoef = (double *)b; b += 8 * bd;
+        g.bcoef = (double *)b; b += bd;
+        g.pts = (double *)b; b += 12 * bd;
+        g.im = (int32_t *)b; b += bi;
+        g.nf = (int32_t *)b; b += bi;
+        g.fidx = (int32_t *)b; b += 8 * bi;
+        if (node) cudaFree(node);
+        node = nullptr;
+        e = cudaMalloc(&node, bi);
+        if (e == cudaSuccess) e = geom_ib_build(c->s, a, q, o.sdf[sq[q]], o.st[q], rows, node, g);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    }
+    if (rows) cudaFree(rows);
+    if (node) cudaFree(node);
     for (int f = 0; f < 4 && e == cudaSuccess; f++) {
         if (sdf && sdf[f])
             e = cudaMemcpy2DAsync(sdf[f], (size_t)d.NX * 8, o.sdf[f], (size_t)d.PX * 8, (size_t)d.NX * 8,
@@ -1659,6 +1697,24 @@ int turb_geometry(turb_ctx *c, const double *ipos, double *const *sdf, uint8_t *
     cudaFree(buf);
     if (e != cudaSuccess) return TURB_ERR_CUDA;
     if (iterations) *iterations = o.iterations;
+    return TURB_OK;
+}
+
+int turb_geometry_stencils(turb_ctx *c, int q, int *n, int32_t *im, int32_t *nf, int32_t *fidx, double *fcoef,
+                           double *bcoef, double *pts)
+{
+    if (!c || q < 0 || q > 3 || !n) return TURB_ERR_ARG;
+    const GeomIb &g = c->gib[q];
+    *n = g.n;
+    if (g.n == 0) return TURB_OK;
+    size_t N = (size_t)g.n;
+    if (im) TURB_CHECK(cudaMemcpyAsync(im, g.im, 4 * N, cudaMemcpyDeviceToHost, c->s));
+    if (nf) TURB_CHECK(cudaMemcpyAsync(nf, g.nf, 4 * N, cudaMemcpyDeviceToHost, c->s));
+    if (fidx) TURB_CHECK(cudaMemcpyAsync(fidx, g.fidx, 32 * N, cudaMemcpyDeviceToHost, c->s));
+    if (fcoef) TURB_CHECK(cudaMemcpyAsync(fcoef, g.fcoef, 64 * N, cudaMemcpyDeviceToHost, c->s));
+    if (bcoef) TURB_CHECK(cudaMemcpyAsync(bcoef, g.bcoef, 8 * N, cudaMemcpyDeviceToHost, c->s));
+    if (pts) TURB_CHECK(cudaMemcpyAsync(pts, g.pts, 96 * N, cudaMemcpyDeviceToHost, c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->s));
     return TURB_OK;
 }
 

@@ -26,3 +26,16 @@ struct GeomOut {
 long long geom_scratch_doubles(const Dims &d);
 cudaError_t geom_setup(cudaStream_t s, const GeomArgs &a, const double *ipos, double *scratch, uint8_t *tmp,
                        GeomOut *o);
+
+// ghost-cell stencils of one quantity, device arrays of n (im, nf, bcoef),
+// 8n (fidx, fcoef) and 12n (pts: normal, control point, image point, node
+// point; may be null) entries; im / fidx are DA linear indices
+struct GeomIb {
+    int n = 0;
+    int32_t *im = nullptr, *nf = nullptr, *fidx = nullptr;
+    double *fcoef = nullptr, *bcoef = nullptr, *pts = nullptr;
+};
+
+cudaError_t geom_ib_count(cudaStream_t s, const Dims &d, const uint8_t *st, int *rows, int *n);
+cudaError_t geom_ib_build(cudaStream_t s, const GeomArgs &a, int q, const double *sdf, const uint8_t *st,
+                          const int *rows, int *node, const GeomIb &o);
