@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--guess", default="learned", choices=["previous", "extrapolate", "learned"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-geometry", action="store_true", help="skip timing the device geometry set-up")
     ap.add_argument("--plain-steps", type=int, default=3, help="timed steps of the plain FP64 MG-CG variant")
     ap.add_argument("--prev-steps", type=int, default=3,
                     help="timed steps of mixed MG-CG with the previous-pressure guess (learned runs)")
@@ -383,6 +384,15 @@ def main():
                              "frac_of_bf16_peak": flops / (net_ms / 1e3) / 1e12 / bf16_peak()[0],
                              "bf16_peak_source": bf16_peak()[1],
                              "guess_residual_ratio": ctx.pressure_guess_ratio()})
+    # the immersed-boundary set-up of the same bed on the device (reference
+    # level-set reinitialisation, statuses, ghost-cell stencils), timed once
+    # after the steps; the stepped case keeps its own geometry
+    geom = None
+    if not a.no_geometry:
+        from turbins_gb300 import geometry as GM
+        r = GM.device_geometry(g, case.params, GM.bed_heights(g, case.bed), apply=False, ctx=ctx)
+        geom = {"seconds": r["seconds"], "reinit_steps": r["steps"],
+                "ib_nodes": {q: int(r["stencils"][q]["n"]) for q in "uvwc"}}
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline:
         from oracle import oracle as O
@@ -405,6 +415,7 @@ def main():
                            "parallelism": "replicas" if dist.world > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "plain_fp64": plain, "mixed_previous_guess": mixed_prev, "learned": learned_info,
+                "geometry_setup": geom,
                 "solver": {"p_iters": [s["p_iters"] for s in stats], "guess_tried_taken": ctx.pressure_guess_stats(),
                            "vel_iters": stats[-1]["vel_iters"],
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}

@@ -19,6 +19,7 @@ sys.path.insert(0, ROOT)
 
 from oracle.refcheck import Reference  # noqa: E402
 from tests import _cases  # noqa: E402
+from turbins_gb300.geometry import bed_heights  # noqa: E402
 
 CASES = {
     "lock_eno2": lambda: _cases.lock_small(12, 8, 8, order=2),
@@ -264,15 +265,9 @@ GEOM_CASES = {
 }
 
 
-def bed_heights(case):
-    """interface_position [NZ][NX]: the bed height at the cell-centre columns"""
-    g = case.grid
-    return case.bed.h(g.xc[None, :], g.zc[:, None])[0]
-
-
 def dump_geom(name, case):
     g = case.grid
-    ipos = np.ascontiguousarray(bed_heights(case))
+    ipos = bed_heights(g, case.bed)
     ref = Reference(g, case.params)
     sdf, st = ref.geometry(ipos)
     out = {"ipos": ipos}

@@ -10,6 +10,7 @@
 // no contraction), so the fields and statuses are bit-identical to it; only
 // the convergence norm is summed in block order.
 #include <cmath>
+#include <utility>
 #include "turb_geom.cuh"
 
 namespace {
@@ -52,92 +53,116 @@ __global__ void k_sdf_guess(GeoIn g, const double *__restrict__ ipos, double *__
     p0[g.d.at(t.i, t.j, t.k)] = sb(g.yc[t.j], ipos[(long long)t.k * g.d.NX + t.i]);
 }
 
-// Levelset_compute_derivatives: one-sided differences, forward except on the
-// last two planes (NI = nx)
-__global__ void k_ls_deriv(GeoIn g, const double *__restrict__ p, double *__restrict__ Dx, double *__restrict__ Dy,
-                           double *__restrict__ Dz)
+// The per-point constants of Levelset_do_Godunov (Levelset.c:265-497) depend
+// on phi_0 only: sign_0 = phi_0 / sqrt(phi_0^2 + dx^2) and, next to the
+// interface (a sign change of phi_0 towards a neighbour), the distance
+// D = phi_0 / |grad phi_0| of the Russo-Smereka fix (NaN elsewhere).  They
+// are made once, with the reference's operations.
+__global__ void k_ls_prep(GeoIn g, const double *__restrict__ p0, double *__restrict__ s0, double *__restrict__ nD)
 {
     P3 t = p3(g.d);
+    const Dims &d = g.d;
+    int NI = d.nx, NJ = d.ny, NK = d.nz;
     if (!t.ok) return;
-    const Dims &d = g.d;
-    long long q = d.at(t.i, t.j, t.k);
-    int NI = d.nx, NJ = d.ny, NK = d.nz;
-    Dx[q] = t.i < NI - 1 ? ml(ml(sb(p[q + 1], p[q]), g.mxu[t.i]), g.a_dEta)
-                         : ml(ml(sb(p[q], p[q - 1]), g.mxu[t.i - 1]), g.a_dEta);
-    Dy[q] = t.j < NJ - 1 ? ml(ml(sb(p[q + d.PX], p[q]), g.myv[t.j]), g.a_dXi)
-                         : ml(ml(sb(p[q], p[q - d.PX]), g.myv[t.j - 1]), g.a_dXi);
-    Dz[q] = t.k < NK - 1 ? ml(ml(sb(p[q + d.plane], p[q]), g.mzw[t.k]), g.a_dPhi)
-                         : ml(ml(sb(p[q], p[q - d.plane]), g.mzw[t.k - 1]), g.a_dPhi);
-}
-
-// Levelset_do_Godunov, Levelset.c:267-497, on the cells i < nx, j < ny, k < nz
-__global__ void k_ls_godunov(GeoIn g, const double *__restrict__ p0, const double *__restrict__ Dx,
-                             const double *__restrict__ Dy, const double *__restrict__ Dz, double dt,
-                             double *__restrict__ p)
-{
-    P3 t = p3(g.d);
-    const Dims &d = g.d;
-    int NI = d.nx, NJ = d.ny, NK = d.nz;
-    if (!t.ok || t.i >= NI || t.j >= NJ || t.k >= NK) return;
     int i = t.i, j = t.j, k = t.k;
-    const double tol = 0.01;
     long long q = d.at(i, j, k);
+    if (i >= NI || j >= NJ || k >= NK) {
+        s0[q] = 0.0;
+        nD[q] = __longlong_as_double(0x7ff8000000000000LL);
+        return;
+    }
+    const double tol = 0.01;
     double dx = g.dxc[i];
     double pp0 = p0[q];
-    double sign_0 = dv(pp0, __dsqrt_rn(ad(ml(pp0, pp0), ml(dx, dx))));
-    double Dxp = Dx[q], Dxm = Dx[d.at(imx(0, i - 1), j, k)];
-    double Dyp = Dy[q], Dym = Dy[d.at(i, imx(0, j - 1), k)];
-    double Dzp = Dz[q], Dzm = Dz[d.at(i, j, imx(0, k - 1))];
-    double ap = mx(Dxm, 0.0), am = mn(Dxm, 0.0), bp = mx(Dxp, 0.0), bm = mn(Dxp, 0.0);
-    double cp = mx(Dym, 0.0), cm = mn(Dym, 0.0), dp = mx(Dyp, 0.0), dm = mn(Dyp, 0.0);
-    double ep = mx(Dzm, 0.0), em = mn(Dzm, 0.0), fp = mx(Dzp, 0.0), fm = mn(Dzp, 0.0);
-    double tx, ty, tz;
-    if (sign_0 > 0.0) {
-        tx = mx(ml(ap, ap), ml(bm, bm));
-        ty = mx(ml(cp, cp), ml(dm, dm));
-        tz = mx(ml(ep, ep), ml(fm, fm));
-    } else {
-        tx = mx(ml(am, am), ml(bp, bp));
-        ty = mx(ml(cm, cm), ml(dp, dp));
-        tz = mx(ml(em, em), ml(fp, fp));
-    }
-    double H = ml(sign_0, sb(__dsqrt_rn(ad(ad(tx, ty), tz)), 1.0));
-    double p_p = pp0;
+    s0[q] = dv(pp0, __dsqrt_rn(ad(ml(pp0, pp0), ml(dx, dx))));
     int ie = imn(i + 1, NI - 1), jn = imn(j + 1, NJ - 1), kf = imn(k + 1, NK - 1);
     int iw = imx(i - 1, 0), js = imx(j - 1, 0), kb = imx(k - 1, 0);
     double p_e = p0[d.at(ie, j, k)], p_n = p0[d.at(i, jn, k)], p_f = p0[d.at(i, j, kf)];
     double p_w = p0[d.at(iw, j, k)], p_s = p0[d.at(i, js, k)], p_b = p0[d.at(i, j, kb)];
     double DeltaX = sb(g.xc[ie], g.xc[iw]), DeltaY = sb(g.yc[jn], g.yc[js]), DeltaZ = sb(g.zc[kf], g.zc[kb]);
-    if (ml(p_p, p_w) < 0.0 || ml(p_p, p_e) < 0.0 || ml(p_p, p_n) < 0.0 || ml(p_p, p_s) < 0.0 ||
-        ml(p_p, p_b) < 0.0 || ml(p_p, p_f) < 0.0) {
+    double D = __longlong_as_double(0x7ff8000000000000LL);
+    if (ml(pp0, p_w) < 0.0 || ml(pp0, p_e) < 0.0 || ml(pp0, p_n) < 0.0 || ml(pp0, p_s) < 0.0 ||
+        ml(pp0, p_b) < 0.0 || ml(pp0, p_f) < 0.0) {
         double Ddx = fabs(DeltaX) > tol ? dv(sb(p_e, p_w), DeltaX) : 0.0;
         double Ddy = fabs(DeltaY) > tol ? dv(sb(p_n, p_s), DeltaY) : 0.0;
         double Ddz = fabs(DeltaZ) > tol ? dv(sb(p_f, p_b), DeltaZ) : 0.0;
         double Dt = __dsqrt_rn(ad(ad(ml(Ddx, Ddx), ml(Ddy, Ddy)), ml(Ddz, Ddz)));
         if (Dt < tol) Dt = tol;
-        double D = dv(p_p, Dt);
-        if (fabs(sign_0) < 1.0e-8) sign_0 = 0.0;
-        else if (sign_0 > 0.0) sign_0 = 1.0;
-        else sign_0 = -1.0;
-        double dy = g.dyc[j], dz = g.dzc[k];
-        double Ds = __dsqrt_rn(ad(ad(ml(dx, dx), ml(dy, dy)), ml(dz, dz)));
-        H = dv(sb(ml(sign_0, fabs(p[q])), D), Ds);
+        D = dv(pp0, Dt);
     }
-    p[q] = ad(p[q], ml(-H, dt));
+    nD[q] = D;
 }
 
-// Levelset_is_converged (NORM2) partials: sum of |p - p_old|^2 dx dy dz over
-// all DA points, per block; then Levelset_store_old_data (p_old = p)
-__global__ void k_ls_err(GeoIn g, const double *__restrict__ p, double *__restrict__ po, double *__restrict__ part)
+// One reinitialisation step, Levelset_compute_derivatives
+// (Levelset.c:154-258: one-sided differences, forward except on the last
+// two planes) fused with Levelset_do_Godunov on the cells i < nx, j < ny,
+// k < nz (the other DA points keep their value), from pc into pn; and the
+// partials of Levelset_is_converged (NORM2, Levelset.c:500-578):
+// |pn - p_old|^2 dx dy dz over all DA points, p_old = pc (0 before the
+// first step), per block.
+__global__ void __launch_bounds__(256) k_ls_step(GeoIn g, const double *__restrict__ pc, const double *__restrict__ s0,
+                                                 const double *__restrict__ nD, double dt, int first,
+                                                 double *__restrict__ pn, double *__restrict__ part)
 {
     P3 t = p3(g.d);
+    const Dims &d = g.d;
+    int NI = d.nx, NJ = d.ny, NK = d.nz;
     double e2 = 0.0;
     if (t.ok) {
-        long long q = g.d.at(t.i, t.j, t.k);
-        double pq = p[q];
-        double err = fabs(sb(pq, po[q]));
-        e2 = ml(ml(ml(ml(err, err), g.dxc[t.i]), g.dyc[t.j]), g.dzc[t.k]);
-        po[q] = pq;
+        int i = t.i, j = t.j, k = t.k;
+        long long q = d.at(i, j, k);
+        double pq = pc[q], pnew = pq;
+        if (i < NI && j < NJ && k < NK) {
+            auto DX = [&](int ii) {
+                long long r = q + (ii - i);
+                return ii < NI - 1 ? ml(ml(sb(pc[r + 1], pc[r]), g.mxu[ii]), g.a_dEta)
+                                   : ml(ml(sb(pc[r], pc[r - 1]), g.mxu[ii - 1]), g.a_dEta);
+            };
+            auto DY = [&](int jj) {
+                long long r = q + (long long)(jj - j) * d.PX;
+                return jj < NJ - 1 ? ml(ml(sb(pc[r + d.PX], pc[r]), g.myv[jj]), g.a_dXi)
+                                   : ml(ml(sb(pc[r], pc[r - d.PX]), g.myv[jj - 1]), g.a_dXi);
+            };
+            auto DZ = [&](int kk) {
+                long long r = q + (long long)(kk - k) * d.plane;
+                return kk < NK - 1 ? ml(ml(sb(pc[r + d.plane], pc[r]), g.mzw[kk]), g.a_dPhi)
+                                   : ml(ml(sb(pc[r], pc[r - d.plane]), g.mzw[kk - 1]), g.a_dPhi);
+            };
+            double Dxp = DX(i), Dxm = DX(imx(0, i - 1));
+            double Dyp = DY(j), Dym = DY(imx(0, j - 1));
+            double Dzp = DZ(k), Dzm = DZ(imx(0, k - 1));
+            double sign_0 = s0[q];
+            double H;
+            double D = nD[q];
+            if (D == D) {
+                // next to the interface: the sign function proper and the
+                // distance kept from phi_0
+                double sg = fabs(sign_0) < 1.0e-8 ? 0.0 : (sign_0 > 0.0 ? 1.0 : -1.0);
+                double dx = g.dxc[i], dy = g.dyc[j], dz = g.dzc[k];
+                double Ds = __dsqrt_rn(ad(ad(ml(dx, dx), ml(dy, dy)), ml(dz, dz)));
+                H = dv(sb(ml(sg, fabs(pq)), D), Ds);
+            } else {
+                double tx, ty, tz;
+                if (sign_0 > 0.0) {
+                    double ap = mx(Dxm, 0.0), bm = mn(Dxp, 0.0), cp = mx(Dym, 0.0), dm = mn(Dyp, 0.0);
+                    double ep = mx(Dzm, 0.0), fm = mn(Dzp, 0.0);
+                    tx = mx(ml(ap, ap), ml(bm, bm));
+                    ty = mx(ml(cp, cp), ml(dm, dm));
+                    tz = mx(ml(ep, ep), ml(fm, fm));
+                } else {
+                    double am = mn(Dxm, 0.0), bp = mx(Dxp, 0.0), cm = mn(Dym, 0.0), dp = mx(Dyp, 0.0);
+                    double em = mn(Dzm, 0.0), fp = mx(Dzp, 0.0);
+                    tx = mx(ml(am, am), ml(bp, bp));
+                    ty = mx(ml(cm, cm), ml(dp, dp));
+                    tz = mx(ml(em, em), ml(fp, fp));
+                }
+                H = ml(sign_0, sb(__dsqrt_rn(ad(ad(tx, ty), tz)), 1.0));
+            }
+            pnew = ad(pq, ml(-H, dt));
+        }
+        pn[q] = pnew;
+        double err = fabs(sb(pnew, first ? 0.0 : pq));
+        e2 = ml(ml(ml(ml(err, err), g.dxc[i]), g.dyc[j]), g.dzc[k]);
     }
     __shared__ double sm[8];
     for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
@@ -579,7 +604,7 @@ __global__ void __launch_bounds__(128) k_ib_stencil(IbArgs a, int n, const int *
 long long geom_scratch_doubles(const Dims &d)
 {
     dim3 g = g3(d);
-    return 5 * d.n + (long long)g.x * g.y * g.z + 1;
+    return 3 * d.n + (long long)g.x * g.y * g.z + 1;
 }
 
 cudaError_t geom_setup(cudaStream_t s, const GeomArgs &a, const double *ipos, double *scratch, uint8_t *tmp,
@@ -593,33 +618,32 @@ cudaError_t geom_setup(cudaStream_t s, const GeomArgs &a, const double *ipos, do
     const Dims &d = a.d;
     const dim3 G = g3(d);
     long long np = (long long)G.x * G.y * G.z;
-    // phi->G_data is the c sdf output itself
-    double *p = o->sdf[0], *po = scratch, *p0 = scratch + d.n, *Dx = scratch + 2 * d.n, *Dy = scratch + 3 * d.n,
-           *Dz = scratch + 4 * d.n, *part = scratch + 5 * d.n, *tot = part + np;
-    size_t fb = sizeof(double) * d.n;
-    // Surface_initialize (only a bottom surface): yc - interface_position
-    k_sdf_guess<<<G, B38, 0, s>>>(g, ipos, p0);
-    cudaMemcpyAsync(p, p0, fb, cudaMemcpyDeviceToDevice, s);
-    cudaMemsetAsync(po, 0, fb, s);
+    // phi ping-pongs between the c sdf output and scratch
+    double *pa = o->sdf[0], *pb = scratch, *s0 = scratch + d.n, *nD = scratch + 2 * d.n, *part = scratch + 3 * d.n,
+           *tot = part + np;
+    // Surface_initialize (only a bottom surface): phi_0 = yc - interface_position
+    k_sdf_guess<<<G, B38, 0, s>>>(g, ipos, pa);
+    k_ls_prep<<<G, B38, 0, s>>>(g, pa, s0, nD);
     // Levelset_reinitialize: stop after the step whose NORM2 change is below
     // 1e-5, or once the counter passes max_iterations + 1
     int c = 0;
     double W = 0.0;
     for (;;) {
-        k_ls_deriv<<<G, B38, 0, s>>>(g, p, Dx, Dy, Dz);
-        k_ls_godunov<<<G, B38, 0, s>>>(g, p0, Dx, Dy, Dz, a.dt, p);
-        k_ls_err<<<G, B38, 0, s>>>(g, p, po, part);
+        k_ls_step<<<G, B38, 0, s>>>(g, pa, s0, nD, a.dt, c == 0, pb, part);
         k_sum<<<1, 1024, 0, s>>>(np, part, tot);
         double e2 = 0.0;
         cudaMemcpyAsync(&e2, tot, sizeof(double), cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
+        std::swap(pa, pb);
         W = std::sqrt(e2);
         if (c > a.max_iterations + 1 || W < 1.0e-5) break;
         c++;
     }
     o->iterations = c + 1;
     o->last_error = W;
+    double *p = o->sdf[0];
+    if (pa != p) cudaMemcpyAsync(p, pa, sizeof(double) * d.n, cudaMemcpyDeviceToDevice, s);
     // Levelset_update_last_planes, then G_c_sdf = phi
     k_ls_last_x<<<dim3((unsigned)((d.NY + 127) / 128), (unsigned)d.NZ), 128, 0, s>>>(d, p);
     k_ls_last_y<<<dim3((unsigned)((d.NX + 127) / 128), (unsigned)d.NZ), 128, 0, s>>>(d, p);
