@@ -38,21 +38,42 @@ struct Cell {
     int i, j, k;
 };
 
-// (S x)_c in difference form: sum over present faces of f (x_c - x_nb) plus
-// the corner pin; an absent neighbour is redirected to the cell itself so
-// its difference vanishes
-__device__ __forceinline__ double s_apply(const MgDevLevel &L, const double *__restrict__ x, long long c, Cell q)
+// (S x)_c = dz_k [(cxy x_c - sum_xy a_n x_n)] + (dx dy) [fb (x_c - x_b) + ff (x_c - x_f)]
+// (+ the corner pin): the x and y face coefficients times the other cell
+// widths are constants of the thread's (i, j) column and are formed once;
+// absent faces have a zero coefficient (their neighbour index is redirected
+// to the cell itself).  Twelve FP64 operations per cell.
+struct SCol {
+    double axw, axe, ays, ayn, cxy, wz;
+};
+
+__device__ __forceinline__ SCol s_col(const MgDevLevel &L, int i, int j)
+{
+    SCol r;
+    double dx = L.dxd[i], dy = L.dyd[j];
+    double fxw = i > 0 ? L.rfxd[i] : 0.0, fxe = i < L.nx - 1 ? L.rfxd[i + 1] : 0.0;
+    double fys = j > 0 ? L.rfyd[j] : 0.0, fyn = j < L.ny - 1 ? L.rfyd[j + 1] : 0.0;
+    r.axw = dy * fxw;
+    r.axe = dy * fxe;
+    r.ays = dx * fys;
+    r.ayn = dx * fyn;
+    r.cxy = (r.axw + r.axe) + (r.ays + r.ayn);
+    r.wz = dx * dy;
+    return r;
+}
+
+__device__ __forceinline__ double s_apply(const MgDevLevel &L, const SCol &a, const double *__restrict__ x,
+                                          long long c, Cell q)
 {
     long long nx = L.nx, nxy = (long long)L.nx * L.ny;
     double xc = x[c];
     double xw = x[c - (q.i > 0 ? 1 : 0)], xe = x[c + (q.i < L.nx - 1 ? 1 : 0)];
     double xs = x[c - (q.j > 0 ? nx : 0)], xn = x[c + (q.j < L.ny - 1 ? nx : 0)];
     double xb = x[c - (q.k > 0 ? nxy : 0)], xf = x[c + (q.k < L.nz - 1 ? nxy : 0)];
-    double sx = fma(L.rfxd[q.i], xc - xw, L.rfxd[q.i + 1] * (xc - xe));
-    double sy = fma(L.rfyd[q.j], xc - xs, L.rfyd[q.j + 1] * (xc - xn));
+    double t = fma(a.axw, xw, fma(a.axe, xe, fma(a.ays, xs, a.ayn * xn)));
+    double xy = fma(a.cxy, xc, -t);
     double sz = fma(L.rfzd[q.k], xc - xb, L.rfzd[q.k + 1] * (xc - xf));
-    double dx = L.dxd[q.i], dy = L.dyd[q.j], dz = L.dzd[q.k];
-    double v = fma(dy * dz, sx, fma(dx * dz, sy, (dx * dy) * sz));
+    double v = fma(L.dzd[q.k], xy, a.wz * sz);
     if (q.i == L.nx - 1 && q.j == L.ny - 1 && q.k == L.nz - 1) v = fma(L.pin, xc, v);
     return v;
 }
@@ -81,16 +102,18 @@ __global__ void k_resid(MgDevLevel L, const double *__restrict__ bw, const doubl
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double acc = 0.0;
-    if (i < L.nx && j < L.ny)
+    if (i < L.nx && j < L.ny) {
+        const SCol a = s_col(L, i, j);
         for (int kk = 0; kk < KC; kk++) {
             int k = blockIdx.z * KC + kk;
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
             Cell q{i, j, k};
-            double v = bw[c] - s_apply(L, x, c, q);
+            double v = bw[c] - s_apply(L, a, x, c, q);
             r[c] = v;
             acc += v * v;
         }
+    }
     block_store(acc, part + blk3());
 }
 
@@ -99,16 +122,18 @@ __global__ void k_apply(MgDevLevel L, const double *__restrict__ p, double *__re
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double acc = 0.0;
-    if (i < L.nx && j < L.ny)
+    if (i < L.nx && j < L.ny) {
+        const SCol a = s_col(L, i, j);
         for (int kk = 0; kk < KC; kk++) {
             int k = blockIdx.z * KC + kk;
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
             Cell cc{i, j, k};
-            double v = s_apply(L, p, c, cc);
+            double v = s_apply(L, a, p, c, cc);
             q[c] = v;
             acc += p[c] * v;
         }
+    }
     block_store(acc, part + blk3());
 }
 

@@ -60,7 +60,8 @@ __device__ __forceinline__ bool is_stencil(int q, int s)
 
 // (A x)_p and the diagonal of a non-immersed row (rows of *_form_LHS_matrix
 // plus 1/dt); coefficients are products of 1-D tables, zero where absent
-__device__ __forceinline__ double helm_ax(const Dims &d, const HelmTab &h, int s, double a_dt,
+// axy = apx[i] + apy[j], formed once per (i, j) column by the caller
+__device__ __forceinline__ double helm_ax(const Dims &d, const HelmTab &h, int s, double a_dt, double axy,
                                           const double *__restrict__ x, long long p, int i, int j, int k,
                                           double &dg)
 {
@@ -69,7 +70,7 @@ __device__ __forceinline__ double helm_ax(const Dims &d, const HelmTab &h, int s
         return dg * x[p];
     }
     Nb o = nb_of(d, i, j, k);
-    dg = h.apx[i] + h.apy[j] + h.apz[k] + a_dt;
+    dg = axy + (h.apz[k] + a_dt);
     double acc = dg * x[p];
     acc = fma(h.aw[i], x[p + o.w], acc);
     acc = fma(h.ae[i], x[p + o.e], acc);
@@ -85,14 +86,15 @@ __global__ void k_helm_apply(Dims d, HelmTab h, const uint8_t *__restrict__ st, 
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= d.NX || j >= d.NY) return;
-    for (int kk = 0; kk < KC; kk++) {
+    const double axy = h.apx[i] + h.apy[j];
+        for (int kk = 0; kk < KC; kk++) {
         int k = blockIdx.z * KC + kk;
         if (k >= d.NZ) break;
         long long p = d.at(i, j, k);
         int s = st[p];
         if (s == T_IMMERSED) continue;
         double dg;
-        y[p] = helm_ax(d, h, s, a_dt, x, p, i, j, k, dg);
+        y[p] = helm_ax(d, h, s, a_dt, axy, x, p, i, j, k, dg);
     }
 }
 
@@ -116,13 +118,14 @@ __global__ void k_helm_jacobi(Dims d, HelmTab h, const uint8_t *__restrict__ st,
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double r2 = 0.0;
     if (i < d.NX && j < d.NY) {
+        const double axy = h.apx[i] + h.apy[j];
         for (int kk = 0; kk < KC; kk++) {
             int k = blockIdx.z * KC + kk;
             if (k >= d.NZ) break;
             long long p = d.at(i, j, k);
             int s = st[p];
             if (s == T_IMMERSED) continue;
-            double dg, ax = helm_ax(d, h, s, a_dt, x, p, i, j, k, dg);
+            double dg, ax = helm_ax(d, h, s, a_dt, axy, x, p, i, j, k, dg);
             double r = b[p] - ax;
             xn[p] = x[p] + r / dg;
             r2 = fma(r, r, r2);
@@ -175,13 +178,14 @@ __global__ void k_helm_resid64(Dims d, HelmTab h, const uint8_t *__restrict__ st
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     double r2 = 0.0;
     if (i < d.NX && j < d.NY) {
+        const double axy = h.apx[i] + h.apy[j];
         for (int kk = 0; kk < KC; kk++) {
             int k = blockIdx.z * KC + kk;
             if (k >= d.NZ) break;
             long long p = d.at(i, j, k);
             int s = st[p];
             if (s == T_IMMERSED) continue;
-            double dg, r = b[p] - helm_ax(d, h, s, a_dt, x, p, i, j, k, dg);
+            double dg, r = b[p] - helm_ax(d, h, s, a_dt, axy, x, p, i, j, k, dg);
             rf[p] = (float)r;
             r2 = fma(r, r, r2);
         }
