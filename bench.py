@@ -350,12 +350,11 @@ def main():
         ne = max(1, min(a.steps, 3))
         dist.barrier()
         t0 = time.perf_counter()
+        pairs = [(f, host[k]) for k, f in keys]
         for _ in range(ne):
-            for k, f in keys:
-                ctx.upload(f, host[k])
+            ctx.upload_many(pairs)
             ctx.step(dt)
-            for k, f in keys:
-                api._check(ctx.lib.turb_field_download(ctx.ctx, f, api._ptr(host[k])), "download")
+            ctx.download_many(pairs)
         ctx.synchronize()
         te = dist.allmax(time.perf_counter() - t0)
         for arr in host.values():

@@ -233,6 +233,26 @@ class Context:
         _check(self.lib.turb_field_download(self.ctx, field, _ptr(a)), "download")
         return a
 
+    def upload_many(self, pairs):
+        """turb_fields_upload: [(field, array), ...] in one overlapped call;
+        the arrays must be C-contiguous float64 of the grid's shape"""
+        n = len(pairs)
+        f = (C.c_int * n)(*[int(fi) for fi, _ in pairs])
+        for _, a in pairs:
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.grid.npts
+        h = (C.c_void_p * n)(*[a.ctypes.data for _, a in pairs])
+        _check(self.lib.turb_fields_upload(self.ctx, n, f, h), "fields_upload")
+
+    def download_many(self, pairs):
+        """turb_fields_download into [(field, array), ...] (C-contiguous
+        float64 arrays of the grid's shape)"""
+        n = len(pairs)
+        f = (C.c_int * n)(*[int(fi) for fi, _ in pairs])
+        for _, a in pairs:
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.grid.npts
+        h = (C.c_void_p * n)(*[a.ctypes.data for _, a in pairs])
+        _check(self.lib.turb_fields_download(self.ctx, n, f, h), "fields_download")
+
     def load_state(self, s):
         for k, f in (("u", F_U), ("v", F_V), ("w", F_W), ("phi", F_PHI), ("dpx", F_DPX), ("dpy", F_DPY),
                      ("dpz", F_DPZ)):

@@ -175,6 +175,11 @@ struct turb_ctx {
     // restart staging: one field as big-endian words, on the device and pinned
     unsigned long long *rs_dev = nullptr;
     void *rs_host = nullptr;
+    // host transfers: two contiguous device staging buffers of one DA field,
+    // a copy stream and the events that hand a buffer between the streams
+    double *xfer[2] = {nullptr, nullptr};
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_freed[2] = {nullptr, nullptr};
     // ghost-cell stencils made by turb_geometry (one allocation per quantity)
     GeomIb gib[4];
     void *gib_buf[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -999,6 +1004,12 @@ int turb_destroy(turb_ctx *c)
     if (c->rs_host) cudaFreeHost(c->rs_host);
     for (void *b : c->gib_buf)
         if (b) cudaFree(b);
+    for (int t = 0; t < 2; t++) {
+        if (c->xfer[t]) cudaFree(c->xfer[t]);
+        if (c->ev_copied[t]) cudaEventDestroy(c->ev_copied[t]);
+        if (c->ev_freed[t]) cudaEventDestroy(c->ev_freed[t]);
+    }
+    if (c->cs) cudaStreamDestroy(c->cs);
     cudaStreamDestroy(c->s);
     delete c;
     return TURB_OK;
@@ -1010,28 +1021,84 @@ static double *field_ptr(turb_ctx *c, int f)
     return c->fld[f];
 }
 
-int turb_field_upload(turb_ctx *c, int field, const double *h)
+void launch_da_pitch(cudaStream_t s, const Dims &d, const double *src, double *dst, int to_pitched);
+
+// transfer staging, made on first use
+static int stage_setup(turb_ctx *c)
 {
-    if (!c || !h) return TURB_ERR_ARG;
-    double *p = field_ptr(c, field);
-    if (!p) return TURB_ERR_ARG;
+    if (c->xfer[0]) return TURB_OK;
+    size_t b = sizeof(double) * (size_t)c->d.NX * c->d.NY * c->d.NZ;
+    TURB_CHECK(cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking));
+    for (int t = 0; t < 2; t++) {
+        TURB_CHECK(cudaEventCreateWithFlags(&c->ev_copied[t], cudaEventDisableTiming));
+        TURB_CHECK(cudaEventCreateWithFlags(&c->ev_freed[t], cudaEventDisableTiming));
+        TURB_CHECK(cudaMalloc(&c->xfer[t], b));
+    }
+    return TURB_OK;
+}
+
+// Host <-> device for several fields: every field moves as one contiguous
+// copy (the host DA array, no pitch) on the copy stream into / out of one of
+// two staging buffers, and a kernel on the context's stream converts between
+// the contiguous and the pitched layout, so the copy of one field overlaps
+// the conversion of the one before.  Returns when everything has landed.
+int turb_fields_upload(turb_ctx *c, int n, const int *fields, const double *const *host)
+{
+    if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
+    for (int t = 0; t < n; t++)
+        if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
+    int rc = stage_setup(c);
+    if (rc) return rc;
     const Dims &d = c->d;
-    TURB_CHECK(cudaMemcpy2DAsync(p, (size_t)d.PX * 8, h, (size_t)d.NX * 8, (size_t)d.NX * 8,
-                                 (size_t)d.NY * d.NZ, cudaMemcpyHostToDevice, c->s));
+    size_t b = sizeof(double) * (size_t)d.NX * d.NY * d.NZ;
+    // the previous work on the context's stream may still read the fields
+    TURB_CHECK(cudaEventRecord(c->ev_freed[0], c->s));
+    TURB_CHECK(cudaEventRecord(c->ev_freed[1], c->s));
+    for (int t = 0; t < n; t++) {
+        int u = t & 1;
+        TURB_CHECK(cudaStreamWaitEvent(c->cs, c->ev_freed[u], 0));
+        TURB_CHECK(cudaMemcpyAsync(c->xfer[u], host[t], b, cudaMemcpyHostToDevice, c->cs));
+        TURB_CHECK(cudaEventRecord(c->ev_copied[u], c->cs));
+        TURB_CHECK(cudaStreamWaitEvent(c->s, c->ev_copied[u], 0));
+        launch_da_pitch(c->s, d, c->xfer[u], field_ptr(c, fields[t]), 1);
+        TURB_CHECK(cudaEventRecord(c->ev_freed[u], c->s));
+    }
     TURB_CHECK(cudaStreamSynchronize(c->s));
     return TURB_OK;
 }
 
+int turb_fields_download(turb_ctx *c, int n, const int *fields, double *const *host)
+{
+    if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
+    for (int t = 0; t < n; t++)
+        if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
+    int rc = stage_setup(c);
+    if (rc) return rc;
+    const Dims &d = c->d;
+    size_t b = sizeof(double) * (size_t)d.NX * d.NY * d.NZ;
+    TURB_CHECK(cudaEventRecord(c->ev_freed[0], c->cs));
+    TURB_CHECK(cudaEventRecord(c->ev_freed[1], c->cs));
+    for (int t = 0; t < n; t++) {
+        int u = t & 1;
+        TURB_CHECK(cudaStreamWaitEvent(c->s, c->ev_freed[u], 0));
+        launch_da_pitch(c->s, d, field_ptr(c, fields[t]), c->xfer[u], 0);
+        TURB_CHECK(cudaEventRecord(c->ev_copied[u], c->s));
+        TURB_CHECK(cudaStreamWaitEvent(c->cs, c->ev_copied[u], 0));
+        TURB_CHECK(cudaMemcpyAsync(host[t], c->xfer[u], b, cudaMemcpyDeviceToHost, c->cs));
+        TURB_CHECK(cudaEventRecord(c->ev_freed[u], c->cs));
+    }
+    TURB_CHECK(cudaStreamSynchronize(c->cs));
+    return TURB_OK;
+}
+
+int turb_field_upload(turb_ctx *c, int field, const double *h)
+{
+    return turb_fields_upload(c, 1, &field, &h);
+}
+
 int turb_field_download(turb_ctx *c, int field, double *h)
 {
-    if (!c || !h) return TURB_ERR_ARG;
-    double *p = field_ptr(c, field);
-    if (!p) return TURB_ERR_ARG;
-    const Dims &d = c->d;
-    TURB_CHECK(cudaMemcpy2DAsync(h, (size_t)d.NX * 8, p, (size_t)d.PX * 8, (size_t)d.NX * 8,
-                                 (size_t)d.NY * d.NZ, cudaMemcpyDeviceToHost, c->s));
-    TURB_CHECK(cudaStreamSynchronize(c->s));
-    return TURB_OK;
+    return turb_fields_download(c, 1, &field, &h);
 }
 
 int turb_set_pressure_guess(turb_ctx *c, int mode)
@@ -2466,4 +2533,20 @@ void launch_pressure_apply(cudaStream_t s, const Dims &d, const uint8_t *st, con
                            double dPhi, const double *x, double *y)
 {
     k_pressure_apply<<<dim3((d.NX + 31) / 32, (d.NY + 7) / 8, d.NZ), dim3(32, 8), 0, s>>>(d, st, g, dEta, dXi, dPhi, x, y);
+}
+
+// contiguous DA array <-> pitched field (pad columns untouched)
+__global__ void k_da_pitch(Dims d, const double *__restrict__ src, double *__restrict__ dst, int to_pitched)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= d.NX) return;
+    long long c = ((long long)k * d.NY + j) * d.NX + i, p = d.at(i, j, k);
+    if (to_pitched) dst[p] = src[c];
+    else dst[c] = src[p];
+}
+
+void launch_da_pitch(cudaStream_t s, const Dims &d, const double *src, double *dst, int to_pitched)
+{
+    k_da_pitch<<<dim3((unsigned)((d.NX + 127) / 128), (unsigned)d.NY, (unsigned)d.NZ), 128, 0, s>>>(d, src, dst,
+                                                                                                   to_pitched);
 }
