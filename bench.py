@@ -348,20 +348,33 @@ def main():
         for arr in host.values():
             api.host_register(arr)
         ne = max(1, min(a.steps, 3))
+        pairs = [(f, host[k]) for k, f in keys]
+        # one untimed round first: the pressure mode switched back after the
+        # plain FP64 steps, and its graphs are captured again on first use
+        ctx.upload_many(pairs)
+        ctx.step(dt)
+        ctx.download_many(pairs)
         dist.barrier()
         t0 = time.perf_counter()
-        pairs = [(f, host[k]) for k, f in keys]
+        tu = ts = td = 0.0
         for _ in range(ne):
+            t1 = time.perf_counter()
             ctx.upload_many(pairs)
+            t2 = time.perf_counter()
             ctx.step(dt)
+            ctx.synchronize()
+            t3 = time.perf_counter()
             ctx.download_many(pairs)
+            t4 = time.perf_counter()
+            tu, ts, td = tu + t2 - t1, ts + t3 - t2, td + t4 - t3
         ctx.synchronize()
         te = dist.allmax(time.perf_counter() - t0)
         for arr in host.values():
             api.host_unregister(arr)
         nbytes = sum(arr.nbytes for arr in host.values())
         e2e = {"value": dist.world * nc * ne / te / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "steps": ne}
+               "d2h_bytes_per_step": nbytes, "steps": ne,
+               "ms_per_step": {"upload": 1e3 * tu / ne, "step": 1e3 * ts / ne, "download": 1e3 * td / ne}}
     # ---- roofline of the dominant kernel group -----------------------------
     peak, peak_src = hbm_peak()
     dom = max(("jacobi", "eno_yz", "eno_x"), key=lambda k: prof[k][0])
