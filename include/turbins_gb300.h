@@ -259,6 +259,11 @@ int turb_kernel_launches(turb_ctx *ctx, long long *n);
 /* page-lock caller memory for the host-buffer transfers */
 int turb_host_register(void *ptr, size_t bytes);
 int turb_host_unregister(void *ptr);
+/* page-locked host memory from the driver: transfers from and to it keep
+ * the host link's full rate however fragmented the process's own heap is
+ * (memory registered after the fact may sit on small pages) */
+int turb_host_alloc(size_t bytes, void **ptr);
+int turb_host_free(void *ptr);
 
 /* self-test: the ENO kernels' division by a grid spacing (reciprocal-based,
  * two Markstein corrections) against IEEE division on nsamples operand pairs;

@@ -18,7 +18,7 @@ def api():
     return A
 
 
-@pytest.mark.parametrize("pinned", [False, True])
+@pytest.mark.parametrize("pinned", ["pageable", "registered", "driver"])
 def test_fields_round_trip(api, pinned):
     case = _cases.bump_small(24, 12, 8)
     g = case.grid
@@ -27,7 +27,15 @@ def test_fields_round_trip(api, pinned):
     fields = [api.F_U, api.F_V, api.F_W, api.F_PHI, api.F_DPX, api.F_DPY, api.F_DPZ, api.F_C0]
     src = [np.ascontiguousarray(rng.standard_normal(g.shape)) for _ in fields]
     dst = [np.zeros(g.shape) for _ in fields]
-    if pinned:
+    if pinned == "driver":
+        src2 = []
+        for a in src:
+            b = api.host_empty(g.shape)
+            b[...] = a
+            src2.append(b)
+        src = src2
+        dst = [api.host_empty(g.shape) for _ in fields]
+    if pinned == "registered":
         for a in src + dst:
             api.host_register(a)
     try:
@@ -41,7 +49,7 @@ def test_fields_round_trip(api, pinned):
         ctx.upload(api.F_U, src[1])
         assert np.array_equal(ctx.download(api.F_U), src[1])
     finally:
-        if pinned:
+        if pinned == "registered":
             for a in src + dst:
                 api.host_unregister(a)
         ctx.close()

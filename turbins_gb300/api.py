@@ -585,6 +585,33 @@ def host_unregister(arr):
     _check(load_library().turb_host_unregister(C.c_void_p(arr.ctypes.data)), "host_unregister")
 
 
+class _PinnedBuffer:
+    def __init__(self, nbytes):
+        self.lib = load_library()
+        self.ptr = C.c_void_p()
+        _check(self.lib.turb_host_alloc(C.c_size_t(nbytes), C.byref(self.ptr)), "host_alloc")
+        self.nbytes = nbytes
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                self.lib.turb_host_free(self.ptr)
+                self.ptr = C.c_void_p()
+        except Exception:
+            pass
+
+
+def host_empty(shape, dtype=np.float64):
+    """an uninitialised C-contiguous array in page-locked host memory
+    (turb_host_alloc); the memory is released when the array is collected"""
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    buf = _PinnedBuffer(max(n, 1))
+    raw = (C.c_char * buf.nbytes).from_address(buf.ptr.value)
+    raw.owner = buf   # every view's base chain ends at raw, which keeps the memory
+    return np.frombuffer(raw, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+
+
 def selftest_division(nsamples, seed=1):
     """Bitwise mismatches of the ENO kernels' division against IEEE division."""
     bad = C.c_ulonglong()

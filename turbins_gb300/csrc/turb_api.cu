@@ -2439,6 +2439,21 @@ int turb_host_unregister(void *p)
     return TURB_OK;
 }
 
+int turb_host_alloc(size_t bytes, void **out)
+{
+    if (!bytes || !out) return TURB_ERR_ARG;
+    *out = nullptr;
+    TURB_CHECK(cudaMallocHost(out, bytes));
+    return TURB_OK;
+}
+
+int turb_host_free(void *p)
+{
+    if (!p) return TURB_ERR_ARG;
+    TURB_CHECK(cudaFreeHost(p));
+    return TURB_OK;
+}
+
 #define STEP_TRY(x)                      \
     do {                                 \
         int rc_ = (x);                   \
