@@ -132,11 +132,12 @@ int turb_create(const turb_grid_desc *grid, const turb_params *params, turb_ctx 
 int turb_destroy(turb_ctx *ctx);
 int turb_field_upload(turb_ctx *ctx, int field, const double *host_da);
 int turb_field_download(turb_ctx *ctx, int field, double *host_da);
-/* n fields in one call (host[t] <-> fields[t]): each field is one contiguous
- * copy through a device staging buffer, the copy of one field overlapping the
- * layout conversion of the one before; the call returns when every copy has
- * completed.  Host arrays registered with turb_host_register move at the
- * host link's full rate. */
+/* n fields in one call (host[t] <-> fields[t]); the call returns when every
+ * copy has completed.  Page-locked arrays (turb_host_alloc or
+ * turb_host_register, whole array) are read / written in place by the layout
+ * kernel; pageable ones move as one contiguous copy per field through a
+ * device staging buffer, the copy of one field overlapping the layout
+ * conversion of the one before. */
 int turb_fields_upload(turb_ctx *ctx, int n, const int *fields, const double *const *host_da);
 int turb_fields_download(turb_ctx *ctx, int n, const int *fields, double *const *host_da);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);

@@ -1037,16 +1037,39 @@ static int stage_setup(turb_ctx *c)
     return TURB_OK;
 }
 
-// Host <-> device for several fields: every field moves as one contiguous
-// copy (the host DA array, no pitch) on the copy stream into / out of one of
-// two staging buffers, and a kernel on the context's stream converts between
-// the contiguous and the pitched layout, so the copy of one field overlaps
-// the conversion of the one before.  Returns when everything has landed.
+// Host <-> device for several fields.  Page-locked host arrays are read or
+// written in place by the layout kernel (its loads / stores cross the host
+// link).  Pageable ones move as one contiguous copy per field on the copy
+// stream into / out of one of two staging buffers, and the kernel on the
+// context's stream converts between the contiguous and the pitched layout,
+// so the copy of one field overlaps the conversion of the one before.
+// Returns when everything has landed.
+// the device address of page-locked host memory (cudaMallocHost or
+// registered), or null for pageable memory
+static const void *host_device_ptr(const void *h)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int turb_fields_upload(turb_ctx *c, int n, const int *fields, const double *const *host)
 {
     if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
     for (int t = 0; t < n; t++)
         if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
+    // page-locked arrays: the layout kernel reads them over the host link
+    bool direct = true;
+    for (int t = 0; t < n && direct; t++) direct = host_device_ptr(host[t]) != nullptr;
+    if (direct) {
+        for (int t = 0; t < n; t++)
+            launch_da_pitch(c->s, c->d, (const double *)host_device_ptr(host[t]), field_ptr(c, fields[t]), 1);
+        TURB_CHECK(cudaStreamSynchronize(c->s));
+        return TURB_OK;
+    }
     int rc = stage_setup(c);
     if (rc) return rc;
     const Dims &d = c->d;
@@ -1072,6 +1095,14 @@ int turb_fields_download(turb_ctx *c, int n, const int *fields, double *const *h
     if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
     for (int t = 0; t < n; t++)
         if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
+    bool direct = true;
+    for (int t = 0; t < n && direct; t++) direct = host_device_ptr(host[t]) != nullptr;
+    if (direct) {
+        for (int t = 0; t < n; t++)
+            launch_da_pitch(c->s, c->d, field_ptr(c, fields[t]), (double *)host_device_ptr(host[t]), 0);
+        TURB_CHECK(cudaStreamSynchronize(c->s));
+        return TURB_OK;
+    }
     int rc = stage_setup(c);
     if (rc) return rc;
     const Dims &d = c->d;
