@@ -6,6 +6,7 @@
 // without FMA contraction.
 #include "turb_internal.cuh"
 #include "turb_kernels.cuh"
+#include "turb_div.cuh"
 
 namespace {
 
@@ -14,12 +15,15 @@ __device__ __forceinline__ double sb(double a, double b) { return __dadd_rn(a, -
 __device__ __forceinline__ double ml(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
 
-// MyMath_interpolate_quantity two-point branch, MyMath.c:22-40
-__device__ __forceinline__ double interp2(double q0, double q1, double dx, double dq, uint8_t flat)
+// MyMath_interpolate_quantity two-point branch, MyMath.c:22-40; the slope's
+// division rounds as the IEEE division in every mode (see Interp2)
+__device__ __forceinline__ double interp2(double q0, double q1, const Interp2 &T, int t)
 {
-    if (flat) return q0;
-    double m = dv(sb(q1, q0), dx);
-    return ad(ml(m, dq), q0);
+    if (T.flat[t]) return q0;
+    double a = sb(q1, q0), h = T.dx[t];
+    int mode = T.div[t];
+    double m = mode == 1 ? ml(a, T.rdx[t]) : (mode == 2 ? div_by_spacing(a, h, T.rdx[t]) : dv(a, h));
+    return ad(ml(m, T.dq[t]), q0);
 }
 
 // four-point branch, MyMath.c:54-74, weights precomputed per direction
@@ -58,9 +62,9 @@ __global__ void k_cell_center(Dims d, Interp2 ix, Interp2 iy, Interp2 iz, OpenBC
     long long p = d.at(t.i, t.j, t.k);
     double u0 = (ob.in && t.i == 0) ? ob.pl(ob.u_in, t.j, t.k) : u[p];
     double u1 = (ob.out && t.i == d.nx - 1) ? ob.pl(ob.out_f[0], t.j, t.k) : u[p + 1];
-    ubc[p] = interp2(u0, u1, ix.dx[t.i], ix.dq[t.i], ix.flat[t.i]);
-    vbc[p] = interp2(v[p], v[p + d.PX], iy.dx[t.j], iy.dq[t.j], iy.flat[t.j]);
-    wbc[p] = interp2(w[p], w[p + d.plane], iz.dx[t.k], iz.dq[t.k], iz.flat[t.k]);
+    ubc[p] = interp2(u0, u1, ix, t.i);
+    vbc[p] = interp2(v[p], v[p + d.PX], iy, t.j);
+    wbc[p] = interp2(w[p], w[p + d.plane], iz, t.k);
 }
 
 // Velocity_transpose_velocities, Velocity.c:3341-3663 (u from the inflow /
@@ -134,7 +138,7 @@ __global__ void k_rhs_vel(Dims d, int q, const uint8_t *__restrict__ st, double 
             r = ad(r, ml(ob.vw_ae[q - 1], ob.pl(ob.out_f[q], t.j, t.k)));
         }
         if (q == 1 && buoy) {
-            double c = interp2(ct[p - d.PX], ct[p], iyv.dx[t.j], iyv.dq[t.j], iyv.flat[t.j]);
+            double c = interp2(ct[p - d.PX], ct[p], iyv, t.j);
             r = sb(r, c);
         }
     }

@@ -223,17 +223,27 @@ void metrics(turb_ctx *c)
 Interp2 mk_interp2(DevBuf &m, int n, const std::vector<double> &X0, const std::vector<double> &X1,
                    const std::vector<double> &XQ, int first)
 {
-    std::vector<double> dx(n, 1.0), dq(n, 0.0);
-    std::vector<uint8_t> fl(n, 0);
+    std::vector<double> dx(n, 1.0), dq(n, 0.0), rdx(n, 1.0);
+    std::vector<uint8_t> fl(n, 0), dm(n, 0);
     for (int t = first; t < n; t++) {
         dx[t] = X1[t] - X0[t];
         dq[t] = XQ[t] - X0[t];
         fl[t] = std::fabs(X1[t] - X0[t]) < 1.0e-8;
+        // the slope's division: positive spacings in a safe exponent range
+        // take the reciprocal forms, which round exactly as the division
+        double h = dx[t];
+        int e = 0;
+        if (h > 0.0 && std::isfinite(h) && std::frexp(h, &e) && e > -500 && e < 500) {
+            rdx[t] = 1.0 / h;
+            dm[t] = std::frexp(h, &e) == 0.5 ? 1 : 2;
+        }
     }
     Interp2 o;
     o.dx = m.upload(dx);
     o.dq = m.upload(dq);
+    o.rdx = m.upload(rdx);
     o.flat = m.upload(fl);
+    o.div = m.upload(dm);
     return o;
 }
 

@@ -49,10 +49,12 @@ struct Geo {
 };
 
 // Two-point interpolation table (MyMath.c:13-43): node value at xq from
-// (x0, x1): dx = x1 - x0, dq = xq - x0, flat = |dx| < 1e-8.
+// (x0, x1): dx = x1 - x0, dq = xq - x0, flat = |dx| < 1e-8; the division by
+// dx as div = 0: IEEE division, 1: one exact multiply by rdx = 1/dx (a power
+// of two), 2: the reciprocal-based correctly rounded division (turb_div.cuh).
 struct Interp2 {
-    const double *dx, *dq;
-    const uint8_t *flat;
+    const double *dx, *dq, *rdx;
+    const uint8_t *flat, *div;
 };
 
 // Four-point bilinear weights of MyMath.c:54-74 along one direction:
