@@ -90,39 +90,24 @@ __device__ __forceinline__ double d0_at(const EnoTab &T, const double *__restric
     return ml(T.gm[gi], src == 1 ? qf : ql);
 }
 
-// The stencil choices on the integer pipe (the FP64 pipe is the bound):
-// v > 0 and |a| <= |b| decided on the bit patterns, with the IEEE results
-// for zeros, infinities and NaNs (a NaN compares false).
-__device__ __forceinline__ bool gt0(double v)
-{
-    long long b = __double_as_longlong(v);
-    return b > 0 && b <= 0x7FF0000000000000LL;
-}
-__device__ __forceinline__ bool abs_le(double a, double b)
-{
-    unsigned long long ua = (unsigned long long)__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFULL;
-    unsigned long long ub = (unsigned long long)__double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFULL;
-    return ub <= 0x7FF0000000000000ULL && ua <= ub;
-}
-
 // ENO_compute_convective_terms body for node c (ENO.c:184-244)
 template <int R>
 __device__ __forceinline__ double eno_eval(double vel, double d1m1, double d1c, double d2m1, double d2c,
                                           double d2p1, double d3m2, double d3m1, double d3c, double d3p1,
                                           const double *__restrict__ g2, const double *__restrict__ g3)
 {
-    bool up = gt0(vel);
+    bool up = vel > 0.0;
     double dQ = up ? d1m1 : d1c;
     if (R > 1) {
         double a = up ? d2m1 : d2c, b = up ? d2c : d2p1;
-        bool left = abs_le(a, b);
+        bool left = fabs(a) <= fabs(b);
         double cc = left ? a : b;
         dQ = ad(dQ, ml(cc, up ? g2[0] : g2[1]));
         if (R > 2) {
             int kso = (up ? -1 : 0) + (left ? -1 : 0);
             double e = kso == -2 ? d3m2 : (kso == -1 ? d3m1 : d3c);
             double f = kso == -2 ? d3m1 : (kso == -1 ? d3c : d3p1);
-            double cs = abs_le(e, f) ? e : f;
+            double cs = fabs(e) <= fabs(f) ? e : f;
             dQ = ad(dQ, ml(cs, g3[kso + 2]));
         }
     }
