@@ -285,6 +285,11 @@ class Context:
     def set_mg_sweeps(self, npre, npost):
         _check(self.lib.turb_set_mg_sweeps(self.ctx, npre, npost), "set_mg_sweeps")
 
+    def set_mg_coarse_sweeps(self, from_level, npre, npost):
+        """turb_set_mg_coarse_sweeps: levels >= from_level use npre / npost"""
+        _check(self.lib.turb_set_mg_coarse_sweeps(self.ctx, int(from_level), int(npre), int(npost)),
+               "set_mg_coarse_sweeps")
+
     def set_mg_split(self, on):
         """colour-split (True) or natural (False) storage of the FP32 multigrid levels"""
         _check(self.lib.turb_set_mg_split(self.ctx, int(bool(on))), "set_mg_split")

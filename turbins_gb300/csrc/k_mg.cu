@@ -475,9 +475,13 @@ void resid_lev(cudaStream_t s, const MgDevLevel &L, const T *b, const T *x, T *r
 }
 
 template <typename T>
-void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
+void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost, int cfrom, int cpre, int cpost)
 {
     const MgDevLevel &L = H.lev[l];
+    if (l >= cfrom) {
+        npre = cpre;
+        npost = cpost;
+    }
     long long n = (long long)L.nx * L.ny * L.nz;
     if (l == H.nl - 1) {
         k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
@@ -496,12 +500,12 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost)
     if (yz8) {
         if constexpr (sizeof(T) == 4) {
             k_restrict_yz8<<<g3((C.nx / 8 + 31) / 32 * 32, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
-            mg_vcycle<T>(s, H, l + 1, npre, npost);
+            mg_vcycle<T>(s, H, l + 1, npre, npost, cfrom, cpre, cpost);
             k_prolong_yz8<<<g3((L.nx / 8 + 31) / 32 * 32, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
         }
     } else {
         k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
-        mg_vcycle<T>(s, H, l + 1, npre, npost);
+        mg_vcycle<T>(s, H, l + 1, npre, npost, cfrom, cpre, cpost);
         k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
     }
     for (int it = 0; it < npost; it++) {
@@ -519,13 +523,15 @@ void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b
     k_to_double_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
 
-int mg_vcycle_launches(int nl, int npre, int npost)
+int mg_vcycle_launches(int nl, int npre, int npost, int cfrom, int cpre, int cpost)
 {
     // per non-coarsest level: 2*npre + resid + restrict + prolong + 2*npost; coarsest: 1
-    return (nl - 1) * (2 * npre + 3 + 2 * npost) + 1;
+    int n = 1;
+    for (int l = 0; l < nl - 1; l++) n += l >= cfrom ? 2 * cpre + 3 + 2 * cpost : 2 * npre + 3 + 2 * npost;
+    return n;
 }
 
 template void mg_setup_invdiag<double>(cudaStream_t, const MgDevLevel &, double *);
 template void mg_setup_invdiag<float>(cudaStream_t, const MgDevLevel &, float *);
-template void mg_vcycle<double>(cudaStream_t, const MgHier<double> &, int, int, int);
-template void mg_vcycle<float>(cudaStream_t, const MgHier<float> &, int, int, int);
+template void mg_vcycle<double>(cudaStream_t, const MgHier<double> &, int, int, int, int, int, int);
+template void mg_vcycle<float>(cudaStream_t, const MgHier<float> &, int, int, int, int, int, int);

@@ -144,6 +144,8 @@ struct turb_ctx {
     // pressure mode (FP64 V-cycles: 4 + 4; FP32 V-cycles are cheap enough that
     // 6 + 6, 8 CG iterations at 512x256x256, beats fewer sweeps)
     int mg_pre[2] = {4, 6}, mg_post[2] = {4, 6};
+    // levels from mg_cfrom on (0 = the finest) smooth with mg_cpre / mg_cpost
+    int mg_cfrom[2] = {1 << 20, 1 << 20}, mg_cpre[2] = {4, 6}, mg_cpost[2] = {4, 6};
     int mg_split = 1;   // colour-split storage of the FP32 levels
     // pressure initial guess: history of the last two solutions per RK stage
     int guess_mode = TURB_GUESS_PREVIOUS;
@@ -1237,6 +1239,19 @@ int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost)
     return TURB_OK;
 }
 
+int turb_set_mg_coarse_sweeps(turb_ctx *c, int from_level, int npre, int npost)
+{
+    if (!c || from_level < 1 || npre < 1 || npost < 1 || npre > 8 || npost > 8) return TURB_ERR_ARG;
+    int m = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
+    if (from_level != c->mg_cfrom[m] || npre != c->mg_cpre[m] || npost != c->mg_cpost[m]) {
+        if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+    }
+    c->mg_cfrom[m] = from_level;
+    c->mg_cpre[m] = npre;
+    c->mg_cpost[m] = npost;
+    return TURB_OK;
+}
+
 // ---- open boundaries ------------------------------------------------------
 int turb_set_open_boundaries(turb_ctx *c, int inflow, int outflow, double U, int transient_inflow, double time_c)
 {
@@ -2280,7 +2295,8 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     int it = 0, restart = 1, status = TURB_OK;
     const int pmi = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
     const int npre = c->mg_pre[pmi], npost = c->mg_post[pmi];
-    int vl = mg_vcycle_launches(c->H64.nl, npre, npost);
+    const int cfrom = c->mg_cfrom[pmi], cpre = c->mg_cpre[pmi], cpost = c->mg_cpost[pmi];
+    int vl = mg_vcycle_launches(pmi == 0 ? c->H64.nl : c->H32.nl, npre, npost, cfrom, cpre, cpost);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
         if (nr <= tol || it >= c->prm.p_maxit) {
@@ -2297,10 +2313,10 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         int pm = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
         auto vcycle = [&]() {
             if (pm == 0) {
-                mg_vcycle<double>(s, c->H64, 0, npre, npost);
+                mg_vcycle<double>(s, c->H64, 0, npre, npost, cfrom, cpre, cpost);
             } else {
                 mg_to_float(s, c->H32.lev[0], c->pr, c->H32.b[0]);
-                mg_vcycle<float>(s, c->H32, 0, npre, npost);
+                mg_vcycle<float>(s, c->H32, 0, npre, npost, cfrom, cpre, cpost);
                 mg_to_double(s, c->H32.lev[0], c->H32.x[0], c->pz);
             }
         };

@@ -40,8 +40,9 @@ struct MgHier {
 template <typename T>
 void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd);
 template <typename T>
-void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost);
-int mg_vcycle_launches(int nl, int npre, int npost);
+// levels l >= cfrom smooth with cpre / cpost sweeps instead of npre / npost
+void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost, int cfrom, int cpre, int cpost);
+int mg_vcycle_launches(int nl, int npre, int npost, int cfrom, int cpre, int cpost);
 
 // FP64 CG vector kernels on the compact level-0 layout (k_pcg.cu)
 struct PcgScal {
