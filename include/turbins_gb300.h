@@ -159,11 +159,11 @@ int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
  * (initial residuals; 1 when nothing was tried) */
 int turb_pressure_guess_ratio(turb_ctx *ctx, double *geo_mean);
 /* red-black Gauss-Seidel sweeps of the pressure V-cycle before / after the
- * coarse-grid correction, for the current pressure mode (defaults: 4 / 4 with
- * FP64 V-cycles, 6 / 6 with FP32 V-cycles; 1..8) */
+ * coarse-grid correction on every level, for the current pressure mode
+ * (defaults: 4 / 4 with FP64 V-cycles, 6 / 6 with FP32 V-cycles; 1..16) */
 int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
 /* levels from_level and coarser (0 = the finest, >= 1) of the current
- * pressure mode's V-cycle smooth with npre / npost sweeps (1..8) instead */
+ * pressure mode's V-cycle smooth with npre / npost sweeps (1..16) instead */
 int turb_set_mg_coarse_sweeps(turb_ctx *ctx, int from_level, int npre, int npost);
 /* storage order of the FP32 multigrid levels: 1 (default) colour-split (red
  * and black cells in separate halves, dense half sweeps), 0 natural.  The

@@ -475,13 +475,10 @@ void resid_lev(cudaStream_t s, const MgDevLevel &L, const T *b, const T *x, T *r
 }
 
 template <typename T>
-void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost, int cfrom, int cpre, int cpost)
+void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const int *post)
 {
     const MgDevLevel &L = H.lev[l];
-    if (l >= cfrom) {
-        npre = cpre;
-        npost = cpost;
-    }
+    const int npre = pre[l], npost = post[l];
     long long n = (long long)L.nx * L.ny * L.nz;
     if (l == H.nl - 1) {
         k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
@@ -500,12 +497,12 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost, i
     if (yz8) {
         if constexpr (sizeof(T) == 4) {
             k_restrict_yz8<<<g3((C.nx / 8 + 31) / 32 * 32, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
-            mg_vcycle<T>(s, H, l + 1, npre, npost, cfrom, cpre, cpost);
+            mg_vcycle<T>(s, H, l + 1, pre, post);
             k_prolong_yz8<<<g3((L.nx / 8 + 31) / 32 * 32, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
         }
     } else {
         k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
-        mg_vcycle<T>(s, H, l + 1, npre, npost, cfrom, cpre, cpost);
+        mg_vcycle<T>(s, H, l + 1, pre, post);
         k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
     }
     for (int it = 0; it < npost; it++) {
@@ -523,15 +520,15 @@ void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b
     k_to_double_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
 
-int mg_vcycle_launches(int nl, int npre, int npost, int cfrom, int cpre, int cpost)
+int mg_vcycle_launches(int nl, const int *pre, const int *post)
 {
-    // per non-coarsest level: 2*npre + resid + restrict + prolong + 2*npost; coarsest: 1
+    // per non-coarsest level: 2*pre + resid + restrict + prolong + 2*post; coarsest: 1
     int n = 1;
-    for (int l = 0; l < nl - 1; l++) n += l >= cfrom ? 2 * cpre + 3 + 2 * cpost : 2 * npre + 3 + 2 * npost;
+    for (int l = 0; l < nl - 1; l++) n += 2 * pre[l] + 3 + 2 * post[l];
     return n;
 }
 
 template void mg_setup_invdiag<double>(cudaStream_t, const MgDevLevel &, double *);
 template void mg_setup_invdiag<float>(cudaStream_t, const MgDevLevel &, float *);
-template void mg_vcycle<double>(cudaStream_t, const MgHier<double> &, int, int, int, int, int, int);
-template void mg_vcycle<float>(cudaStream_t, const MgHier<float> &, int, int, int, int, int, int);
+template void mg_vcycle<double>(cudaStream_t, const MgHier<double> &, int, const int *, const int *);
+template void mg_vcycle<float>(cudaStream_t, const MgHier<float> &, int, const int *, const int *);

@@ -143,9 +143,8 @@ struct turb_ctx {
     // red-black Gauss-Seidel sweeps before / after the coarse correction, per
     // pressure mode (FP64 V-cycles: 4 + 4; FP32 V-cycles are cheap enough that
     // 6 + 6, 8 CG iterations at 512x256x256, beats fewer sweeps)
-    int mg_pre[2] = {4, 6}, mg_post[2] = {4, 6};
-    // levels from mg_cfrom on (0 = the finest) smooth with mg_cpre / mg_cpost
-    int mg_cfrom[2] = {1 << 20, 1 << 20}, mg_cpre[2] = {4, 6}, mg_cpost[2] = {4, 6};
+    // per level (0 = the finest) and pressure mode, set in turb_create
+    int mg_pre[2][TURB_MG_MAXLEV], mg_post[2][TURB_MG_MAXLEV];
     int mg_split = 1;   // colour-split storage of the FP32 levels
     // pressure initial guess: history of the last two solutions per RK stage
     int guess_mode = TURB_GUESS_PREVIOUS;
@@ -893,6 +892,12 @@ int turb_create(const turb_grid_desc *g, const turb_params *p, turb_ctx **out)
     }
     turb_ctx *c = new turb_ctx();
     c->prm = *p;
+    // V-cycle sweeps: FP64 levels 4 + 4; FP32 levels 6 + 6 (defaults; see
+    // turb_set_mg_sweeps / turb_set_mg_coarse_sweeps)
+    for (int l = 0; l < TURB_MG_MAXLEV; l++) {
+        c->mg_pre[0][l] = c->mg_post[0][l] = 4;
+        c->mg_pre[1][l] = c->mg_post[1][l] = 6;
+    }
     Dims &d = c->d;
     d.nx = g->nx; d.ny = g->ny; d.nz = g->nz;
     d.NX = d.nx + 1; d.NY = d.ny + 1; d.NZ = d.nz + 1;
@@ -1227,29 +1232,28 @@ int turb_set_pressure_mode(turb_ctx *c, int mode)
     return TURB_OK;
 }
 
-int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost)
+// sweeps of levels [from, TURB_MG_MAXLEV) of the current pressure mode; a change
+// drops the captured V-cycle
+static int set_sweeps(turb_ctx *c, int from, int npre, int npost)
 {
-    if (!c || npre < 1 || npost < 1 || npre > 8 || npost > 8) return TURB_ERR_ARG;
+    if (!c || from < 0 || npre < 1 || npost < 1 || npre > 16 || npost > 16) return TURB_ERR_ARG;
     int m = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
-    if (npre != c->mg_pre[m] || npost != c->mg_post[m]) {   // the captured V-cycle changes
-        if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+    bool changed = false;
+    for (int l = from; l < TURB_MG_MAXLEV; l++) {
+        changed |= c->mg_pre[m][l] != npre || c->mg_post[m][l] != npost;
+        c->mg_pre[m][l] = npre;
+        c->mg_post[m][l] = npost;
     }
-    c->mg_pre[m] = npre;
-    c->mg_post[m] = npost;
+    if (changed && c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
     return TURB_OK;
 }
 
+int turb_set_mg_sweeps(turb_ctx *c, int npre, int npost) { return set_sweeps(c, 0, npre, npost); }
+
 int turb_set_mg_coarse_sweeps(turb_ctx *c, int from_level, int npre, int npost)
 {
-    if (!c || from_level < 1 || npre < 1 || npost < 1 || npre > 8 || npost > 8) return TURB_ERR_ARG;
-    int m = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
-    if (from_level != c->mg_cfrom[m] || npre != c->mg_cpre[m] || npost != c->mg_cpost[m]) {
-        if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
-    }
-    c->mg_cfrom[m] = from_level;
-    c->mg_cpre[m] = npre;
-    c->mg_cpost[m] = npost;
-    return TURB_OK;
+    if (from_level < 1) return TURB_ERR_ARG;
+    return set_sweeps(c, from_level, npre, npost);
 }
 
 // ---- open boundaries ------------------------------------------------------
@@ -2294,9 +2298,8 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     double tol = c->prm.p_rtol * nb;
     int it = 0, restart = 1, status = TURB_OK;
     const int pmi = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
-    const int npre = c->mg_pre[pmi], npost = c->mg_post[pmi];
-    const int cfrom = c->mg_cfrom[pmi], cpre = c->mg_cpre[pmi], cpost = c->mg_cpost[pmi];
-    int vl = mg_vcycle_launches(pmi == 0 ? c->H64.nl : c->H32.nl, npre, npost, cfrom, cpre, cpost);
+    const int *npre = c->mg_pre[pmi], *npost = c->mg_post[pmi];
+    int vl = mg_vcycle_launches(pmi == 0 ? c->H64.nl : c->H32.nl, npre, npost);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
         if (nr <= tol || it >= c->prm.p_maxit) {
@@ -2313,10 +2316,10 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         int pm = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
         auto vcycle = [&]() {
             if (pm == 0) {
-                mg_vcycle<double>(s, c->H64, 0, npre, npost, cfrom, cpre, cpost);
+                mg_vcycle<double>(s, c->H64, 0, npre, npost);
             } else {
                 mg_to_float(s, c->H32.lev[0], c->pr, c->H32.b[0]);
-                mg_vcycle<float>(s, c->H32, 0, npre, npost, cfrom, cpre, cpost);
+                mg_vcycle<float>(s, c->H32, 0, npre, npost);
                 mg_to_double(s, c->H32.lev[0], c->H32.x[0], c->pz);
             }
         };

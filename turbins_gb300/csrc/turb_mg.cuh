@@ -40,9 +40,9 @@ struct MgHier {
 template <typename T>
 void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd);
 template <typename T>
-// levels l >= cfrom smooth with cpre / cpost sweeps instead of npre / npost
-void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, int npre, int npost, int cfrom, int cpre, int cpost);
-int mg_vcycle_launches(int nl, int npre, int npost, int cfrom, int cpre, int cpost);
+// level l smooths with pre[l] / post[l] red-black sweeps
+void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const int *post);
+int mg_vcycle_launches(int nl, const int *pre, const int *post);
 
 // FP64 CG vector kernels on the compact level-0 layout (k_pcg.cu)
 struct PcgScal {
