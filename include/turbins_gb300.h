@@ -160,7 +160,8 @@ int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
 int turb_pressure_guess_ratio(turb_ctx *ctx, double *geo_mean);
 /* red-black Gauss-Seidel sweeps of the pressure V-cycle before / after the
  * coarse-grid correction on every level, for the current pressure mode
- * (defaults: 4 / 4 with FP64 V-cycles, 6 / 6 with FP32 V-cycles; 1..16) */
+ * (1..16; defaults: 4 / 4 with FP64 V-cycles; with FP32 V-cycles 4 / 4 on the
+ * finest level, 5 / 5 on the next and 12 / 12 on the coarser ones) */
 int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
 /* levels from_level and coarser (0 = the finest, >= 1) of the current
  * pressure mode's V-cycle smooth with npre / npost sweeps (1..16) instead */
