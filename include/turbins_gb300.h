@@ -170,7 +170,9 @@ int turb_set_mg_coarse_sweeps(turb_ctx *ctx, int from_level, int npre, int npost
  * and black cells in separate halves, dense half sweeps), 0 natural.  The
  * arithmetic is the same, so results are bit-identical either way. */
 int turb_set_mg_split(turb_ctx *ctx, int on);
-/* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b|| */
+/* both modes stop on the FP64 residual ||b - A x|| <= vel_rtol ||b||;
+ * inner_sweeps: FP32 Jacobi sweeps per defect-correction step of the mixed
+ * mode (1..64, default 5) */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 1 (default) divides by a grid spacing through its
  * precomputed reciprocal with two correction steps (FP64: 1 multiply + 4 FMA,

@@ -457,7 +457,7 @@ class Context:
         _check(self.lib.turb_resume_read(self.ctx, os.fsencode(dirname), C.byref(q), flags), "resume_read")
         return q.as_dict()
 
-    def set_helmholtz_mode(self, mode, inner_sweeps=6):
+    def set_helmholtz_mode(self, mode, inner_sweeps=5):
         _check(self.lib.turb_set_helmholtz_mode(self.ctx, mode, inner_sweeps), "set_helmholtz_mode")
 
     def set_eno_division(self, fast):

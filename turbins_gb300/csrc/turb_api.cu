@@ -112,7 +112,7 @@ struct turb_ctx {
     IbDevF ibf[4];
     float *hrf = nullptr, *he0 = nullptr, *he1 = nullptr;   // defect-correction buffers
     int hmode = TURB_HMODE_MIXED;
-    int hinner = 6;
+    int hinner = 5;   // FP32 Jacobi sweeps per defect-correction step (5: the fewest that keep 2 outer steps at 512x256x256)
     const double *pcx, *pcy, *pcz;
     ProjArgs proj;
     // pressure
