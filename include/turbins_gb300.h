@@ -166,6 +166,10 @@ int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
 /* levels from_level and coarser (0 = the finest, >= 1) of the current
  * pressure mode's V-cycle smooth with npre / npost sweeps (1..16) instead */
 int turb_set_mg_coarse_sweeps(turb_ctx *ctx, int from_level, int npre, int npost);
+/* the V-cycle from the first level of at most max_cells cells (default
+ * 32768; 0: never) down to the coarsest and back runs as one single-block
+ * kernel instead of a launch per half sweep; results are bit-identical */
+int turb_set_mg_tail(turb_ctx *ctx, long long max_cells);
 /* storage order of the FP32 multigrid levels: 1 (default) colour-split (red
  * and black cells in separate halves, dense half sweeps), 0 natural.  The
  * arithmetic is the same, so results are bit-identical either way. */

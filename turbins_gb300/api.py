@@ -285,6 +285,10 @@ class Context:
     def set_mg_sweeps(self, npre, npost):
         _check(self.lib.turb_set_mg_sweeps(self.ctx, npre, npost), "set_mg_sweeps")
 
+    def set_mg_tail(self, max_cells):
+        """turb_set_mg_tail: single-block V-cycle below max_cells cells (0: off)"""
+        _check(self.lib.turb_set_mg_tail(self.ctx, C.c_longlong(int(max_cells))), "set_mg_tail")
+
     def set_mg_coarse_sweeps(self, from_level, npre, npost):
         """turb_set_mg_coarse_sweeps: levels >= from_level use npre / npost"""
         _check(self.lib.turb_set_mg_coarse_sweeps(self.ctx, int(from_level), int(npre), int(npost)),

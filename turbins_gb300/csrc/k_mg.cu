@@ -103,8 +103,20 @@ __global__ void k_invdiag(MgDevLevel Ld, T *__restrict__ invd)
     }
 }
 
-// red-black Gauss-Seidel half sweep; zero_init: x taken as 0 on entry (first
-// sweep of a cycle, colour 0 only)
+// one cell of a red-black Gauss-Seidel half sweep; zero_init: x taken as 0
+// on entry (first sweep of a cycle, colour 0 only)
+template <typename T>
+__device__ __forceinline__ void rb_cell(const LevelT<T> &L, int zero_init, const T *__restrict__ b,
+                                        const T *__restrict__ invd, T *__restrict__ x, int i, int j, int k)
+{
+    long long c = ((long long)k * L.ny + j) * L.nx + i;
+    long long o = L.at(c, i, j, k);
+    if (zero_init) { x[o] = rmul(b[o], invd[o]); return; }
+    T off, dg;
+    s_row<T>(L, x, i, j, k, off, dg);
+    x[o] = rmul(radd(b[o], off), invd[o]);
+}
+
 template <typename T>
 __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restrict__ b, const T *__restrict__ invd,
                        T *__restrict__ x)
@@ -114,12 +126,7 @@ __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restr
     if (j >= L.ny) return;
     int i = 2 * i2 + ((j + k + color) & 1);
     if (i >= L.nx) return;
-    long long c = ((long long)k * L.ny + j) * L.nx + i;
-    long long o = L.at(c, i, j, k);
-    if (zero_init) { x[o] = rmul(b[o], invd[o]); return; }
-    T off, dg;
-    s_row<T>(L, x, i, j, k, off, dg);
-    x[o] = rmul(radd(b[o], off), invd[o]);
+    rb_cell<T>(L, zero_init, b, invd, x, i, j, k);
 }
 
 // The same half sweep on colour-split FP32 storage, four cells of one row per
@@ -182,16 +189,23 @@ __global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__
 }
 
 template <typename T>
-__global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r)
+__device__ __forceinline__ void resid_cell(const LevelT<T> &L, const T *__restrict__ b, const T *__restrict__ x,
+                                           T *__restrict__ r, int i, int j, int k)
 {
-    LevelT<T> L = lev_of<T>(Ld);
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
-    if (i >= L.nx || j >= L.ny) return;
     long long c = ((long long)k * L.ny + j) * L.nx + i;
     T off, dg;
     s_row<T>(L, x, i, j, k, off, dg);
     long long o = L.at(c, i, j, k);
     r[c] = radd(b[o], -rfma(dg, x[o], -off));
+}
+
+template <typename T>
+__global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r)
+{
+    LevelT<T> L = lev_of<T>(Ld);
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= L.nx || j >= L.ny) return;
+    resid_cell<T>(L, b, x, r, i, j, k);
 }
 
 // residual r = b - S x of a colour-split FP32 level (nx a multiple of 8),
@@ -270,11 +284,13 @@ __device__ __forceinline__ const float *pw1_of<float>(const Xfer1D &t) { return 
 
 // restriction = transpose of the linear prolongation (gather over <= 4 fine
 // cells per coarsened direction)
+// full-weighting restriction to coarse cell (I, J, K) and linear
+// prolongation (stretching-aware weights) added to fine cell (i, j, k);
+// explicitly rounded, so the kernels and the fused tail agree bit for bit
 template <typename T>
-__global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ rf, T *__restrict__ bc)
+__device__ __forceinline__ void restrict_cell(const MgDevLevel &Lf, const MgDevLevel &Lc, const T *__restrict__ rf,
+                                              T *__restrict__ bc, int I, int J, int K)
 {
-    int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
-    if (I >= Lc.nx || J >= Lc.ny) return;
     long long c = ((long long)K * Lc.ny + J) * Lc.nx + I;
     const T *rwx = rw_of<T>(Lf.tx), *rwy = rw_of<T>(Lf.ty), *rwz = rw_of<T>(Lf.tz);
     int nxx = Lf.tx.rcnt[I], nyy = Lf.ty.rcnt[J], nzz = Lf.tz.rcnt[K];
@@ -284,20 +300,18 @@ __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ r
         T wz = rwz[4 * K + c3];
         for (int b = 0; b < nyy; b++) {
             int j = Lf.ty.rf[4 * J + b];
-            T wyz = wz * rwy[4 * J + b];
+            T wyz = rmul(wz, rwy[4 * J + b]);
             const T *row = rf + ((long long)k * Lf.ny + j) * Lf.nx;
-            for (int a = 0; a < nxx; a++) s += wyz * rwx[4 * I + a] * row[Lf.tx.rf[4 * I + a]];
+            for (int a = 0; a < nxx; a++) s = rfma(rmul(wyz, rwx[4 * I + a]), row[Lf.tx.rf[4 * I + a]], s);
         }
     }
     bc[lev_at(Lc, c, I, J, K)] = s;
 }
 
-// linear prolongation (stretching-aware weights), added to the fine iterate
 template <typename T>
-__global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc, T *__restrict__ xf)
+__device__ __forceinline__ void prolong_cell(const MgDevLevel &Lf, const MgDevLevel &Lc, const T *__restrict__ xc,
+                                             T *__restrict__ xf, int i, int j, int k)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
-    if (i >= Lf.nx || j >= Lf.ny) return;
     long long c = ((long long)k * Lf.ny + j) * Lf.nx + i;
     int Ix[2] = {Lf.tx.I0[i], Lf.tx.I1[i]}, Iy[2] = {Lf.ty.I0[j], Lf.ty.I1[j]}, Iz[2] = {Lf.tz.I0[k], Lf.tz.I1[k]};
     T wx[2] = {pw0_of<T>(Lf.tx)[i], pw1_of<T>(Lf.tx)[i]};
@@ -311,13 +325,30 @@ __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc
         for (int b = 0; b < 2; b++) {
             if (wy[b] == T(0)) continue;
             long long row = ((long long)Iz[d] * Lc.ny + Iy[b]) * Lc.nx;
-            T wyz = wz[d] * wy[b];
+            T wyz = rmul(wz[d], wy[b]);
 #pragma unroll
             for (int a = 0; a < 2; a++)
-                if (wx[a] != T(0)) acc += wyz * wx[a] * xc[lev_at(Lc, row + Ix[a], Ix[a], Iy[b], Iz[d])];
+                if (wx[a] != T(0)) acc = rfma(rmul(wyz, wx[a]), xc[lev_at(Lc, row + Ix[a], Ix[a], Iy[b], Iz[d])], acc);
         }
     }
-    xf[lev_at(Lf, c, i, j, k)] += acc;
+    long long o = lev_at(Lf, c, i, j, k);
+    xf[o] = radd(xf[o], acc);
+}
+
+template <typename T>
+__global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ rf, T *__restrict__ bc)
+{
+    int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
+    if (I >= Lc.nx || J >= Lc.ny) return;
+    restrict_cell<T>(Lf, Lc, rf, bc, I, J, K);
+}
+
+template <typename T>
+__global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc, T *__restrict__ xf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (i >= Lf.nx || j >= Lf.ny) return;
+    prolong_cell<T>(Lf, Lc, xc, xf, i, j, k);
 }
 
 // eight consecutive values (cells i0..i0+7 of row (j, k)) of a level's FP32
@@ -408,13 +439,95 @@ __global__ void k_prolong_yz8(MgDevLevel Lf, MgDevLevel Lc, const float *__restr
 }
 
 template <typename T>
+__device__ __forceinline__ void coarse_row(int n, const double *__restrict__ ainv, const T *__restrict__ b,
+                                           T *__restrict__ x, int r)
+{
+    double s = 0.0;
+    for (int c = 0; c < n; c++) s = __fma_rn(ainv[r * n + c], (double)b[c], s);
+    x[r] = (T)s;
+}
+
+template <typename T>
 __global__ void k_coarse(int n, const double *__restrict__ ainv, const T *__restrict__ b, T *__restrict__ x)
 {
     int r = threadIdx.x;
     if (r >= n) return;
-    double s = 0.0;
-    for (int c = 0; c < n; c++) s += ainv[r * n + c] * (double)b[c];
-    x[r] = (T)s;
+    coarse_row<T>(n, ainv, b, x, r);
+}
+
+// The V-cycle from level l0 down to the coarsest and back in one block of
+// TAIL_THREADS threads (levels small enough that a launch per half sweep
+// costs more than the sweep): the same per-cell operations as the kernels,
+// phases separated by block barriers.
+constexpr int TAIL_THREADS = 1024;
+
+template <typename T>
+struct TailArgs {
+    int nlev;                                         // levels l0 .. coarsest
+    MgDevLevel L[MG_TAIL_MAXLEV];
+    T *x[MG_TAIL_MAXLEV], *b[MG_TAIL_MAXLEV], *r[MG_TAIL_MAXLEV];
+    const T *invd[MG_TAIL_MAXLEV];
+    int pre[MG_TAIL_MAXLEV], post[MG_TAIL_MAXLEV];
+    const double *coarse_inv;
+};
+
+template <typename T>
+__device__ void tail_half(const MgDevLevel &Ld, int color, int zero_init, const T *b, const T *invd, T *x)
+{
+    LevelT<T> L = lev_of<T>(Ld);
+    int hx = (L.nx + 1) >> 1;
+    long long n2 = (long long)hx * L.ny * L.nz;
+    for (long long t = threadIdx.x; t < n2; t += TAIL_THREADS) {
+        int i2 = (int)(t % hx);
+        long long q = t / hx;
+        int j = (int)(q % L.ny), k = (int)(q / L.ny);
+        int i = 2 * i2 + ((j + k + color) & 1);
+        if (i < L.nx) rb_cell<T>(L, zero_init, b, invd, x, i, j, k);
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TAIL_THREADS) k_vcycle_tail(const TailArgs<T> a)
+{
+    const int last = a.nlev - 1;
+    for (int l = 0; l < last; l++) {
+        const MgDevLevel &Ld = a.L[l];
+        for (int it = 0; it < a.pre[l]; it++) {
+            tail_half<T>(Ld, 0, it == 0, a.b[l], a.invd[l], a.x[l]);
+            tail_half<T>(Ld, 1, 0, a.b[l], a.invd[l], a.x[l]);
+        }
+        LevelT<T> L = lev_of<T>(Ld);
+        long long n = (long long)L.nx * L.ny * L.nz;
+        for (long long c = threadIdx.x; c < n; c += TAIL_THREADS)
+            resid_cell<T>(L, a.b[l], a.x[l], a.r[l], (int)(c % L.nx), (int)((c / L.nx) % L.ny),
+                          (int)(c / ((long long)L.nx * L.ny)));
+        __syncthreads();
+        const MgDevLevel &C = a.L[l + 1];
+        long long nc = (long long)C.nx * C.ny * C.nz;
+        for (long long c = threadIdx.x; c < nc; c += TAIL_THREADS)
+            restrict_cell<T>(Ld, C, a.r[l], a.b[l + 1], (int)(c % C.nx), (int)((c / C.nx) % C.ny),
+                             (int)(c / ((long long)C.nx * C.ny)));
+        __syncthreads();
+    }
+    {
+        const MgDevLevel &C = a.L[last];
+        int n = C.nx * C.ny * C.nz;
+        for (int r = threadIdx.x; r < n; r += TAIL_THREADS) coarse_row<T>(n, a.coarse_inv, a.b[last], a.x[last], r);
+        __syncthreads();
+    }
+    for (int l = last - 1; l >= 0; l--) {
+        const MgDevLevel &Ld = a.L[l], &C = a.L[l + 1];
+        long long n = (long long)Ld.nx * Ld.ny * Ld.nz;
+        for (long long c = threadIdx.x; c < n; c += TAIL_THREADS)
+            prolong_cell<T>(Ld, C, a.x[l + 1], a.x[l], (int)(c % Ld.nx), (int)((c / Ld.nx) % Ld.ny),
+                            (int)(c / ((long long)Ld.nx * Ld.ny)));
+        __syncthreads();
+        for (int it = 0; it < a.post[l]; it++) {
+            tail_half<T>(Ld, 1, 0, a.b[l], a.invd[l], a.x[l]);
+            tail_half<T>(Ld, 0, 0, a.b[l], a.invd[l], a.x[l]);
+        }
+    }
 }
 
 // FP64 <-> FP32 between the natural order and a level's storage order
@@ -480,6 +593,22 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
     const MgDevLevel &L = H.lev[l];
     const int npre = pre[l], npost = post[l];
     long long n = (long long)L.nx * L.ny * L.nz;
+    if (H.tail_from >= 0 && l == H.tail_from && H.nl - l <= MG_TAIL_MAXLEV && l < H.nl - 1) {
+        TailArgs<T> a;
+        a.nlev = H.nl - l;
+        for (int t = 0; t < a.nlev; t++) {
+            a.L[t] = H.lev[l + t];
+            a.x[t] = H.x[l + t];
+            a.b[t] = H.b[l + t];
+            a.r[t] = H.r[l + t];
+            a.invd[t] = H.invd[l + t];
+            a.pre[t] = pre[l + t];
+            a.post[t] = post[l + t];
+        }
+        a.coarse_inv = H.coarse_inv;
+        k_vcycle_tail<T><<<1, TAIL_THREADS, 0, s>>>(a);
+        return;
+    }
     if (l == H.nl - 1) {
         k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
         return;
@@ -520,11 +649,15 @@ void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b
     k_to_double_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
 
-int mg_vcycle_launches(int nl, const int *pre, const int *post)
+int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from)
 {
-    // per non-coarsest level: 2*pre + resid + restrict + prolong + 2*post; coarsest: 1
+    // per non-coarsest level: 2*pre + resid + restrict + prolong + 2*post;
+    // coarsest: 1; the fused tail from tail_from on: 1
     int n = 1;
-    for (int l = 0; l < nl - 1; l++) n += 2 * pre[l] + 3 + 2 * post[l];
+    for (int l = 0; l < nl - 1; l++) {
+        if (tail_from >= 0 && l == tail_from && nl - l <= MG_TAIL_MAXLEV) return n;
+        n += 2 * pre[l] + 3 + 2 * post[l];
+    }
     return n;
 }
 

@@ -756,6 +756,16 @@ int build_mg(turb_ctx *c)
     c->H64.x[0] = c->pz;   // FP64 V-cycle writes z directly
     c->H64.b[0] = c->pr;   // and reads r directly
     c->sc = c->mem.alloc<PcgScal>(1);
+    // levels of at most 32768 cells finish the V-cycle in one block
+    // (turb_set_mg_tail)
+    c->H64.tail_from = c->H32.tail_from = -1;
+    for (int l = 0; l + 1 < nl; l++) {
+        const MgDevLevel &m = c->H32.lev[l];
+        if ((long long)m.nx * m.ny * m.nz <= 32768 && nl - l <= MG_TAIL_MAXLEV) {
+            c->H64.tail_from = c->H32.tail_from = l;
+            break;
+        }
+    }
     return c->mem.err == cudaSuccess ? TURB_OK : TURB_ERR_ALLOC;
 }
 
@@ -1494,6 +1504,27 @@ int turb_Outflow_copy_data_into_2D_array(turb_ctx *c, char which, int ic)
     launch_field_to_plane(c->s, c->d, q, c->pl_out[f]);
     c->launches += 1;
     return check_launch(c);
+}
+
+// the first level with at most max_cells cells (and at most MG_TAIL_MAXLEV
+// levels from it to the coarsest) runs the rest of the V-cycle in one block
+static void set_tail(turb_ctx *c, long long max_cells)
+{
+    int from = -1;
+    for (int l = 0; l + 1 < c->H32.nl && max_cells > 0; l++) {
+        const MgDevLevel &m = c->H32.lev[l];
+        if ((long long)m.nx * m.ny * m.nz <= max_cells && c->H32.nl - l <= MG_TAIL_MAXLEV) { from = l; break; }
+    }
+    c->H32.tail_from = c->H64.tail_from = from;
+    for (int m = 0; m < 2; m++)
+        if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+}
+
+int turb_set_mg_tail(turb_ctx *c, long long max_cells)
+{
+    if (!c || max_cells < 0) return TURB_ERR_ARG;
+    set_tail(c, max_cells);
+    return TURB_OK;
 }
 
 int turb_set_mg_split(turb_ctx *c, int on)
@@ -2300,7 +2331,8 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     int it = 0, restart = 1, status = TURB_OK;
     const int pmi = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
     const int *npre = c->mg_pre[pmi], *npost = c->mg_post[pmi];
-    int vl = mg_vcycle_launches(pmi == 0 ? c->H64.nl : c->H32.nl, npre, npost);
+    int vl = pmi == 0 ? mg_vcycle_launches(c->H64.nl, npre, npost, c->H64.tail_from)
+                      : mg_vcycle_launches(c->H32.nl, npre, npost, c->H32.tail_from);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
         if (nr <= tol || it >= c->prm.p_maxit) {

@@ -3,6 +3,7 @@
 #include "turb_internal.cuh"
 
 #define TURB_MG_MAXLEV 24
+#define MG_TAIL_MAXLEV 6   // levels a fused single-block V-cycle tail may hold
 
 // 1-D transfer tables between a level and the next coarser one along one
 // direction: prolongation weights per fine index (two coarse cells) and the
@@ -35,6 +36,9 @@ struct MgHier {
     MgDevLevel lev[TURB_MG_MAXLEV];
     T *x[TURB_MG_MAXLEV], *b[TURB_MG_MAXLEV], *r[TURB_MG_MAXLEV], *invd[TURB_MG_MAXLEV];
     const double *coarse_inv;
+    // from this level on (-1: never) the V-cycle runs as one single-block
+    // kernel (k_vcycle_tail); it must leave at most MG_TAIL_MAXLEV levels
+    int tail_from = -1;
 };
 
 template <typename T>
@@ -42,7 +46,7 @@ void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd);
 template <typename T>
 // level l smooths with pre[l] / post[l] red-black sweeps
 void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const int *post);
-int mg_vcycle_launches(int nl, const int *pre, const int *post);
+int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from);
 
 // FP64 CG vector kernels on the compact level-0 layout (k_pcg.cu)
 struct PcgScal {
