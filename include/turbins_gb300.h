@@ -167,7 +167,7 @@ int turb_set_mg_sweeps(turb_ctx *ctx, int npre, int npost);
  * pressure mode's V-cycle smooth with npre / npost sweeps (1..16) instead */
 int turb_set_mg_coarse_sweeps(turb_ctx *ctx, int from_level, int npre, int npost);
 /* the V-cycle from the first level of at most max_cells cells (default
- * 32768; 0: never) down to the coarsest and back runs as one single-block
+ * 4096; 0: never) down to the coarsest and back runs as one single-block
  * kernel instead of a launch per half sweep; results are bit-identical */
 int turb_set_mg_tail(turb_ctx *ctx, long long max_cells);
 /* storage order of the FP32 multigrid levels: 1 (default) colour-split (red

@@ -756,12 +756,13 @@ int build_mg(turb_ctx *c)
     c->H64.x[0] = c->pz;   // FP64 V-cycle writes z directly
     c->H64.b[0] = c->pr;   // and reads r directly
     c->sc = c->mem.alloc<PcgScal>(1);
-    // levels of at most 32768 cells finish the V-cycle in one block
-    // (turb_set_mg_tail)
+    // levels of at most 4096 cells finish the V-cycle in one block
+    // (turb_set_mg_tail; at 512x256x256 larger tails ran slower than a
+    // launch per half sweep, one SM having too little memory parallelism)
     c->H64.tail_from = c->H32.tail_from = -1;
     for (int l = 0; l + 1 < nl; l++) {
         const MgDevLevel &m = c->H32.lev[l];
-        if ((long long)m.nx * m.ny * m.nz <= 32768 && nl - l <= MG_TAIL_MAXLEV) {
+        if ((long long)m.nx * m.ny * m.nz <= 4096 && nl - l <= MG_TAIL_MAXLEV) {
             c->H64.tail_from = c->H32.tail_from = l;
             break;
         }
