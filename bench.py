@@ -384,9 +384,16 @@ def main():
     gms, gnl = prof[dom]
     bpl = algorithmic_bytes(dom, npts)
     ach = bpl / (gms / gnl / 1e3) / 1e9 if gnl else None
+    # DRAM traffic per launch of the ENO y/z pass from one ncu capture of a
+    # y pass at 256x128x128 (dram__bytes_read.sum + dram__bytes_write.sum =
+    # 68.73 MB + 0.89 MB for 257*129*129 points), scaled by the points of a
+    # launch here; at that size the conv writes still sat in L2 when the
+    # kernel ended, so the figure counts reads
+    traffic = (68.734720e6 + 0.888064e6) / (257 * 129 * 129) * npts if dom == "eno_yz" else None
     roof = {"bound": "hbm", "kernel_group": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
             "frac": (ach / peak) if ach else None, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": None, "bytes_per_launch": bpl, "launches": gnl, "ms_per_launch": gms / gnl if gnl else None,
+            "traffic": traffic, "traffic_source": "ncu, one y pass at 256x128x128, scaled by points"
+            if traffic else None, "bytes_per_launch": bpl, "launches": gnl, "ms_per_launch": gms / gnl if gnl else None,
             "groups_ms": {k: v[0] for k, v in prof.items()}, "groups_launches": {k: v[1] for k, v in prof.items()}}
     if learned_info is not None and prof["net"][1]:
         # the network's tensor-core work: 2 * 27 * cin * cout FLOP per voxel and conv
