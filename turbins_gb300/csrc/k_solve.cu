@@ -170,12 +170,21 @@ __global__ void k_add_corr(long long n, const double *__restrict__ x, const floa
         xn[p] = x[p] + (double)e[p];
 }
 
-// r = b - A x in FP64, rounded to FP32 for the inner solve; |r|^2 partials
+// r = b - A x in FP64, rounded to FP32 for the inner solve; |r|^2 partials.
+// The FP64 pipe bounds this kernel, so the row is accumulated as
+// -(diag x - b + sum a_nb x_nb) (no separate subtraction) and apz[k] + 1/dt
+// is formed once per plane of the block: nine FP64 operations per point
 __global__ void k_helm_resid64(Dims d, HelmTab h, const uint8_t *__restrict__ st, double a_dt,
                                const double *__restrict__ b, const double *__restrict__ x,
                                float *__restrict__ rf, double *__restrict__ part)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    __shared__ double zdt[KC];
+    {
+        int t = threadIdx.y * blockDim.x + threadIdx.x, k = blockIdx.z * KC + t;
+        if (t < KC) zdt[t] = k < d.NZ ? h.apz[k] + a_dt : 0.0;
+    }
+    __syncthreads();
     double r2 = 0.0;
     if (i < d.NX && j < d.NY) {
         const double axy = h.apx[i] + h.apy[j];
@@ -185,7 +194,20 @@ __global__ void k_helm_resid64(Dims d, HelmTab h, const uint8_t *__restrict__ st
             long long p = d.at(i, j, k);
             int s = st[p];
             if (s == T_IMMERSED) continue;
-            double dg, r = b[p] - helm_ax(d, h, s, a_dt, axy, x, p, i, j, k, dg);
+            double r;
+            if (!is_stencil(h.q, s)) {
+                r = b[p] - (h.ap_solid + a_dt) * x[p];
+            } else {
+                Nb o = nb_of(d, i, j, k);
+                double acc = fma(axy + zdt[kk], x[p], -b[p]);
+                acc = fma(h.aw[i], x[p + o.w], acc);
+                acc = fma(h.ae[i], x[p + o.e], acc);
+                acc = fma(h.as[j], x[p + o.s], acc);
+                acc = fma(h.an[j], x[p + o.n], acc);
+                acc = fma(h.ab[k], x[p + o.b], acc);
+                acc = fma(h.af[k], x[p + o.f], acc);
+                r = -acc;
+            }
             rf[p] = (float)r;
             r2 = fma(r, r, r2);
         }
