@@ -87,7 +87,7 @@ __global__ void k_helm_apply(Dims d, HelmTab h, const uint8_t *__restrict__ st, 
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= d.NX || j >= d.NY) return;
     const double axy = h.apx[i] + h.apy[j];
-    for (int kk = 0; kk < KC; kk++) {
+        for (int kk = 0; kk < KC; kk++) {
         int k = blockIdx.z * KC + kk;
         if (k >= d.NZ) break;
         long long p = d.at(i, j, k);
@@ -252,14 +252,6 @@ __global__ void k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st
     const float aev[4] = {ae.x, ae.y, ae.z, ae.w};
     const float apyj = h.apy[j], asj = h.as[j], anj = h.an[j];
     const int nvalid = min(4, d.NX - i0);
-    // e on planes k-1, k, k+1 of this thread's column, carried from one
-    // plane to the next (a missing neighbour plane is the cell itself)
-    float4 eb = make_float4(0.f, 0.f, 0.f, 0.f), ec = eb;
-    if (!first && blockIdx.z * KC < d.NZ) {
-        const long long p0 = d.at(i0, j, blockIdx.z * KC);
-        ec = *reinterpret_cast<const float4 *>(e + p0);
-        eb = blockIdx.z * KC > 0 ? *reinterpret_cast<const float4 *>(e + p0 - d.plane) : ec;
-    }
     for (int kk = 0; kk < KC; kk++) {
         const int k = blockIdx.z * KC + kk;
         if (k >= d.NZ) break;
@@ -279,16 +271,14 @@ __global__ void k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st
                 out[t] = __fmul_rn(rv[t], __frcp_rn(dg));
             }
         } else {
-            const float4 e4 = ec;
+            const float4 e4 = *reinterpret_cast<const float4 *>(e + p);
             const float ev[4] = {e4.x, e4.y, e4.z, e4.w};
             const float xw = i0 > 0 ? e[p - 1] : ev[0];
             const float xe = i0 + 4 < d.NX ? e[p + 4] : ev[3];
             const float4 s_ = j > 0 ? *reinterpret_cast<const float4 *>(e + p - d.PX) : e4;
             const float4 n_ = j < d.NY - 1 ? *reinterpret_cast<const float4 *>(e + p + d.PX) : e4;
-            const float4 b_ = eb;
+            const float4 b_ = k > 0 ? *reinterpret_cast<const float4 *>(e + p - d.plane) : e4;
             const float4 f_ = k < d.NZ - 1 ? *reinterpret_cast<const float4 *>(e + p + d.plane) : e4;
-            eb = ec;
-            ec = f_;
             const float sv_[4] = {s_.x, s_.y, s_.z, s_.w}, nv_[4] = {n_.x, n_.y, n_.z, n_.w};
             const float bv_[4] = {b_.x, b_.y, b_.z, b_.w}, fv_[4] = {f_.x, f_.y, f_.z, f_.w};
 #pragma unroll
