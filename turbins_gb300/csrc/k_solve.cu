@@ -87,7 +87,7 @@ __global__ void k_helm_apply(Dims d, HelmTab h, const uint8_t *__restrict__ st, 
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= d.NX || j >= d.NY) return;
     const double axy = h.apx[i] + h.apy[j];
-        for (int kk = 0; kk < KC; kk++) {
+    for (int kk = 0; kk < KC; kk++) {
         int k = blockIdx.z * KC + kk;
         if (k >= d.NZ) break;
         long long p = d.at(i, j, k);
