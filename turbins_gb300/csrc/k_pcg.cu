@@ -38,11 +38,12 @@ struct Cell {
     int i, j, k;
 };
 
-// (S x)_c = dz_k [(cxy x_c - sum_xy a_n x_n)] + (dx dy) [fb (x_c - x_b) + ff (x_c - x_f)]
+// (S x)_c = dz_k [cxy x_c - sum_xy a_n x_n] + (dx dy) [zs x_c - zb x_b - zf x_f]
 // (+ the corner pin): the x and y face coefficients times the other cell
-// widths are constants of the thread's (i, j) column and are formed once;
-// absent faces have a zero coefficient (their neighbour index is redirected
-// to the cell itself).  Twelve FP64 operations per cell.
+// widths are constants of the thread's (i, j) column and are formed once,
+// the z ones are constants of a plane; absent faces have a zero coefficient
+// (their neighbour index is redirected to the cell itself).  Eleven FP64
+// operations per cell.
 struct SCol {
     double axw, axe, ays, ayn, cxy, wz;
 };
@@ -62,8 +63,23 @@ __device__ __forceinline__ SCol s_col(const MgDevLevel &L, int i, int j)
     return r;
 }
 
-__device__ __forceinline__ double s_apply(const MgDevLevel &L, const SCol &a, const double *__restrict__ x,
-                                          long long c, Cell q)
+// z face coefficients of one plane (zero for an absent face) and their sum
+struct SPlane {
+    double zb, zf, zs, dz;
+};
+
+__device__ __forceinline__ SPlane s_plane(const MgDevLevel &L, int k)
+{
+    SPlane r;
+    r.zb = k > 0 ? L.rfzd[k] : 0.0;
+    r.zf = k < L.nz - 1 ? L.rfzd[k + 1] : 0.0;
+    r.zs = r.zb + r.zf;
+    r.dz = L.dzd[k];
+    return r;
+}
+
+__device__ __forceinline__ double s_apply(const MgDevLevel &L, const SCol &a, const SPlane &z,
+                                          const double *__restrict__ x, long long c, Cell q)
 {
     long long nx = L.nx, nxy = (long long)L.nx * L.ny;
     double xc = x[c];
@@ -72,8 +88,8 @@ __device__ __forceinline__ double s_apply(const MgDevLevel &L, const SCol &a, co
     double xb = x[c - (q.k > 0 ? nxy : 0)], xf = x[c + (q.k < L.nz - 1 ? nxy : 0)];
     double t = fma(a.axw, xw, fma(a.axe, xe, fma(a.ays, xs, a.ayn * xn)));
     double xy = fma(a.cxy, xc, -t);
-    double sz = fma(L.rfzd[q.k], xc - xb, L.rfzd[q.k + 1] * (xc - xf));
-    double v = fma(L.dzd[q.k], xy, a.wz * sz);
+    double sz = fma(z.zs, xc, -fma(z.zb, xb, z.zf * xf));
+    double v = fma(z.dz, xy, a.wz * sz);
     if (q.i == L.nx - 1 && q.j == L.ny - 1 && q.k == L.nz - 1) v = fma(L.pin, xc, v);
     return v;
 }
@@ -109,7 +125,7 @@ __global__ void k_resid(MgDevLevel L, const double *__restrict__ bw, const doubl
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
             Cell q{i, j, k};
-            double v = bw[c] - s_apply(L, a, x, c, q);
+            double v = bw[c] - s_apply(L, a, s_plane(L, k), x, c, q);
             r[c] = v;
             acc += v * v;
         }
@@ -129,7 +145,7 @@ __global__ void k_apply(MgDevLevel L, const double *__restrict__ p, double *__re
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
             Cell cc{i, j, k};
-            double v = s_apply(L, a, p, c, cc);
+            double v = s_apply(L, a, s_plane(L, k), p, c, cc);
             q[c] = v;
             acc += p[c] * v;
         }
