@@ -78,6 +78,14 @@ __device__ __forceinline__ SPlane s_plane(const MgDevLevel &L, int k)
     return r;
 }
 
+// the KC planes of a block, formed once by its first threads
+__device__ __forceinline__ void s_planes(const MgDevLevel &L, SPlane *sp)
+{
+    int t = threadIdx.y * blockDim.x + threadIdx.x, k = blockIdx.z * KC + t;
+    if (t < KC && k < L.nz) sp[t] = s_plane(L, k);
+    __syncthreads();
+}
+
 __device__ __forceinline__ double s_apply(const MgDevLevel &L, const SCol &a, const SPlane &z,
                                           const double *__restrict__ x, long long c, Cell q)
 {
@@ -117,6 +125,8 @@ __global__ void k_resid(MgDevLevel L, const double *__restrict__ bw, const doubl
                         double *__restrict__ r, double *__restrict__ part)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    __shared__ SPlane sp[KC];
+    s_planes(L, sp);
     double acc = 0.0;
     if (i < L.nx && j < L.ny) {
         const SCol a = s_col(L, i, j);
@@ -125,7 +135,7 @@ __global__ void k_resid(MgDevLevel L, const double *__restrict__ bw, const doubl
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
             Cell q{i, j, k};
-            double v = bw[c] - s_apply(L, a, s_plane(L, k), x, c, q);
+            double v = bw[c] - s_apply(L, a, sp[kk], x, c, q);
             r[c] = v;
             acc += v * v;
         }
@@ -137,6 +147,8 @@ __global__ void k_resid(MgDevLevel L, const double *__restrict__ bw, const doubl
 __global__ void k_apply(MgDevLevel L, const double *__restrict__ p, double *__restrict__ q, double *__restrict__ part)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    __shared__ SPlane sp[KC];
+    s_planes(L, sp);
     double acc = 0.0;
     if (i < L.nx && j < L.ny) {
         const SCol a = s_col(L, i, j);
@@ -145,7 +157,7 @@ __global__ void k_apply(MgDevLevel L, const double *__restrict__ p, double *__re
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
             Cell cc{i, j, k};
-            double v = s_apply(L, a, s_plane(L, k), p, c, cc);
+            double v = s_apply(L, a, sp[kk], p, c, cc);
             q[c] = v;
             acc += p[c] * v;
         }
