@@ -24,11 +24,11 @@ __device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b
 // a / h[b] rounded to nearest: IEEE division or the reciprocal-based form;
 // for a power-of-two spacing (flag bit `bit` of T.p2[b]) one exact scaling
 __device__ __forceinline__ double dd(const EnoTab &T, double a, const double *__restrict__ h,
-                                     const double *__restrict__ rh, int b, int bit)
+                                     const double *__restrict__ rh, const double *__restrict__ rl, int b, int bit)
 {
     if (!T.fastdiv) return dv(a, h[b]);
     if (T.p2[b] & bit) return __dmul_rn(a, rh[b]);
-    return div_by_spacing(a, h[b], rh[b]);
+    return div_by_spacing(a, h[b], rh[b], rl[b]);
 }
 
 __device__ __forceinline__ double interp4(double q0, double q1, double q2, double q3, double wx0,
@@ -128,14 +128,14 @@ __global__ void k_eno_x(Dims d, EnoTab T, const double *__restrict__ q, AdvSrc a
     const long long line = (long long)k * T.gNY + j;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) s0[b] = d0_at(T, q, base, 1, b, qf, ql, line);
     __syncthreads();
-    for (int b = threadIdx.x; b < nb - 1; b += blockDim.x) s1[b] = dd(T, sb(s0[b + 1], s0[b]), T.h1, T.rh1, b, 1);
+    for (int b = threadIdx.x; b < nb - 1; b += blockDim.x) s1[b] = dd(T, sb(s0[b + 1], s0[b]), T.h1, T.rh1, T.rl1, b, 1);
     __syncthreads();
     if (R > 1) {
-        for (int b = 1 + threadIdx.x; b < nb - 1; b += blockDim.x) s2[b] = dd(T, sb(s1[b], s1[b - 1]), T.h2, T.rh2, b, 2);
+        for (int b = 1 + threadIdx.x; b < nb - 1; b += blockDim.x) s2[b] = dd(T, sb(s1[b], s1[b - 1]), T.h2, T.rh2, T.rl2, b, 2);
         __syncthreads();
     }
     if (R > 2) {
-        for (int b = 1 + threadIdx.x; b < nb - 2; b += blockDim.x) s3[b] = dd(T, sb(s2[b + 1], s2[b]), T.h3, T.rh3, b, 4);
+        for (int b = 1 + threadIdx.x; b < nb - 2; b += blockDim.x) s3[b] = dd(T, sb(s2[b + 1], s2[b]), T.h3, T.rh3, T.rl3, b, 4);
         __syncthreads();
     }
     for (int c = R + threadIdx.x; c < nb - R; c += blockDim.x) {
@@ -166,14 +166,14 @@ __global__ void k_eno_yz(Dims d, int dir, EnoTab T, const double *__restrict__ q
 #pragma unroll
     for (int t = 0; t < W; t++) w0[t] = d0_at(T, q, base, stride, t, qf, ql);
 #pragma unroll
-    for (int t = 0; t < 2 * R; t++) w1[t] = dd(T, sb(w0[t + 1], w0[t]), T.h1, T.rh1, t, 1);
+    for (int t = 0; t < 2 * R; t++) w1[t] = dd(T, sb(w0[t + 1], w0[t]), T.h1, T.rh1, T.rl1, t, 1);
     if (R > 1) {
 #pragma unroll
-        for (int t = 0; t < 2 * R - 1; t++) w2[t] = dd(T, sb(w1[t + 1], w1[t]), T.h2, T.rh2, t + 1, 2);
+        for (int t = 0; t < 2 * R - 1; t++) w2[t] = dd(T, sb(w1[t + 1], w1[t]), T.h2, T.rh2, T.rl2, t + 1, 2);
     }
     if (R > 2) {
 #pragma unroll
-        for (int t = 0; t < 2 * R - 2; t++) w3[t] = dd(T, sb(w2[t + 1], w2[t]), T.h3, T.rh3, t + 1, 4);
+        for (int t = 0; t < 2 * R - 2; t++) w3[t] = dd(T, sb(w2[t + 1], w2[t]), T.h3, T.rh3, T.rl3, t + 1, 4);
     }
     for (int c = R; c < T.nb - R; c++) {
         int m = c - R + T.s0;
@@ -192,16 +192,16 @@ __global__ void k_eno_yz(Dims d, int dir, EnoTab T, const double *__restrict__ q
             w0[W - 1] = d0_at(T, q, base, stride, c + 1 + R, qf, ql);
 #pragma unroll
             for (int t = 0; t < 2 * R - 1; t++) w1[t] = w1[t + 1];
-            w1[2 * R - 1] = dd(T, sb(w0[W - 1], w0[W - 2]), T.h1, T.rh1, c + R, 1);
+            w1[2 * R - 1] = dd(T, sb(w0[W - 1], w0[W - 2]), T.h1, T.rh1, T.rl1, c + R, 1);
             if (R > 1) {
 #pragma unroll
                 for (int t = 0; t < 2 * R - 2; t++) w2[t] = w2[t + 1];
-                w2[2 * R - 2] = dd(T, sb(w1[2 * R - 1], w1[2 * R - 2]), T.h2, T.rh2, c + R, 2);
+                w2[2 * R - 2] = dd(T, sb(w1[2 * R - 1], w1[2 * R - 2]), T.h2, T.rh2, T.rl2, c + R, 2);
             }
             if (R > 2) {
 #pragma unroll
                 for (int t = 0; t < 2 * R - 3; t++) w3[t] = w3[t + 1];
-                w3[2 * R - 3] = dd(T, sb(w2[2 * R - 2], w2[2 * R - 3]), T.h3, T.rh3, c + R - 1, 4);
+                w3[2 * R - 3] = dd(T, sb(w2[2 * R - 2], w2[2 * R - 3]), T.h3, T.rh3, T.rl3, c + R - 1, 4);
             }
         }
     }

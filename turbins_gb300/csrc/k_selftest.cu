@@ -53,7 +53,7 @@ __global__ void k_selftest(long long n, unsigned long long seed, unsigned long l
             break;
         }
         }
-        double q1 = div_by_spacing(a, h, y), q2 = __ddiv_rn(a, h);
+        double q1 = div_by_spacing(a, h, y, recip_low(h, y)), q2 = __ddiv_rn(a, h);
         if (__double_as_longlong(q1) != __double_as_longlong(q2)) {
             nbad++;
             ex[0] = a; ex[1] = h;

@@ -15,6 +15,7 @@
 #include "turb_internal.cuh"
 #include "turb_diag.cuh"
 #include "turb_geom.cuh"
+#include "turb_div.cuh"
 
 // open boundaries (k_open.cu)
 int open_parts(const Dims &d);
@@ -222,7 +223,7 @@ void metrics(turb_ctx *c)
 Interp2 mk_interp2(DevBuf &m, int n, const std::vector<double> &X0, const std::vector<double> &X1,
                    const std::vector<double> &XQ, int first)
 {
-    std::vector<double> dx(n, 1.0), dq(n, 0.0), rdx(n, 1.0);
+    std::vector<double> dx(n, 1.0), dq(n, 0.0), rdx(n, 1.0), rdxl(n, 0.0);
     std::vector<uint8_t> fl(n, 0), dm(n, 0);
     for (int t = first; t < n; t++) {
         dx[t] = X1[t] - X0[t];
@@ -234,6 +235,7 @@ Interp2 mk_interp2(DevBuf &m, int n, const std::vector<double> &X0, const std::v
         int e = 0;
         if (h > 0.0 && std::isfinite(h) && std::frexp(h, &e) && e > -500 && e < 500) {
             rdx[t] = 1.0 / h;
+            rdxl[t] = recip_low(h, rdx[t]);
             dm[t] = std::frexp(h, &e) == 0.5 ? 1 : 2;
         }
     }
@@ -241,6 +243,7 @@ Interp2 mk_interp2(DevBuf &m, int n, const std::vector<double> &X0, const std::v
     o.dx = m.upload(dx);
     o.dq = m.upload(dq);
     o.rdx = m.upload(rdx);
+    o.rdxl = m.upload(rdxl);
     o.flat = m.upload(fl);
     o.div = m.upload(dm);
     return o;
@@ -319,11 +322,17 @@ EnoTab mk_eno(DevBuf &m, int r, const std::vector<double> &pos, int s0, int e0, 
     T.h1 = m.upload(h1);
     T.h2 = m.upload(h2);
     T.h3 = m.upload(h3);
-    std::vector<double> r1(nb), r2(nb), r3(nb);
-    for (int b = 0; b < nb; b++) { r1[b] = 1.0 / h1[b]; r2[b] = 1.0 / h2[b]; r3[b] = 1.0 / h3[b]; }
+    std::vector<double> r1(nb), r2(nb), r3(nb), l1(nb), l2(nb), l3(nb);
+    for (int b = 0; b < nb; b++) {
+        r1[b] = 1.0 / h1[b]; r2[b] = 1.0 / h2[b]; r3[b] = 1.0 / h3[b];
+        l1[b] = recip_low(h1[b], r1[b]); l2[b] = recip_low(h2[b], r2[b]); l3[b] = recip_low(h3[b], r3[b]);
+    }
     T.rh1 = m.upload(r1);
     T.rh2 = m.upload(r2);
     T.rh3 = m.upload(r3);
+    T.rl1 = m.upload(l1);
+    T.rl2 = m.upload(l2);
+    T.rl3 = m.upload(l3);
     T.fastdiv = 1;   // reciprocal-based, correctly rounded (turb_div.cuh); 0 = IEEE division
     // power-of-two spacings (uniform grids with 2^k cells per unit length):
     // the reciprocal is exact and a/h = a*(1/h) is the same real number, so

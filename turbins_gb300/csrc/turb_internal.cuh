@@ -51,9 +51,10 @@ struct Geo {
 // Two-point interpolation table (MyMath.c:13-43): node value at xq from
 // (x0, x1): dx = x1 - x0, dq = xq - x0, flat = |dx| < 1e-8; the division by
 // dx as div = 0: IEEE division, 1: one exact multiply by rdx = 1/dx (a power
-// of two), 2: the reciprocal-based correctly rounded division (turb_div.cuh).
+// of two), 2: the reciprocal-based correctly rounded division (turb_div.cuh,
+// rdxl its correction term).
 struct Interp2 {
-    const double *dx, *dq, *rdx;
+    const double *dx, *dq, *rdx, *rdxl;
     const uint8_t *flat, *div;
 };
 
@@ -76,6 +77,7 @@ struct EnoTab {
     const double *g2;    // [nb*2]: k=b-1, k=b  -> (x_i-x_k)+(x_i-x_k1)
     const double *g3;    // [nb*3]: kstar=b-2,b-1,b -> three-product sum
     const double *rh1, *rh2, *rh3;   // RN(1/h*) for the reciprocal-based division
+    const double *rl1, *rl2, *rl3;   // and its correction RN((1 - RN(1/h) h)/h)
     int fastdiv;         // 1: div_by_spacing (turb_div.cuh), 0: IEEE division
     const uint8_t *p2;   // per b: bit 0/1/2 set when h1/h2/h3 is a power of two, so that
                          // a/h = a*RN(1/h) exactly (fastdiv only)
