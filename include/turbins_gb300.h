@@ -179,9 +179,9 @@ int turb_set_mg_split(turb_ctx *ctx, int on);
  * mode (1..64, default 5) */
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 1 (default) divides by a grid spacing through its
- * precomputed reciprocal with two correction steps (FP64: 1 multiply + 4 FMA,
- * range tests on the integer pipe), 0 uses IEEE division; both round to
- * nearest, so the results are the same bits */
+ * precomputed two-term reciprocal and one correction step (FP64: 1 multiply +
+ * 3 FMA, range tests on the integer pipe), 0 uses IEEE division; both round
+ * to nearest, so the results are the same bits */
 int turb_set_eno_division(turb_ctx *ctx, int fast);
 int turb_synchronize(turb_ctx *ctx);
 const char *turb_status_string(int status);
@@ -276,8 +276,9 @@ int turb_host_unregister(void *ptr);
 int turb_host_alloc(size_t bytes, void **ptr);
 int turb_host_free(void *ptr);
 
-/* self-test: the ENO kernels' division by a grid spacing (reciprocal-based,
- * two Markstein corrections) against IEEE division on nsamples operand pairs;
+/* self-test: the ENO kernels' division by a grid spacing (two-term
+ * reciprocal, one Markstein correction) against IEEE division on nsamples
+ * operand pairs;
  * returns the number of bitwise mismatches (and one offending (a, h)) */
 int turb_selftest_division(long long nsamples, unsigned long long seed,
                            unsigned long long *mismatches, double *example);
