@@ -106,6 +106,25 @@ def bf16_peak():
         return 1900.0, "fallback"
 
 
+def host_cpu():
+    """the host's core count and CPU model (model name, or the Arm part
+    number, from /proc/cpuinfo)"""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read().splitlines()
+        for key in ("model name", "CPU part"):
+            for line in info:
+                if line.lower().startswith(key.lower()):
+                    model = line.split(":", 1)[1].strip()
+                    break
+            if model:
+                break
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count(), "model": model}
+
+
 def hbm_peak():
     try:
         with open(PEAKS) as f:
@@ -222,7 +241,7 @@ def run_reference(a, dist):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "turbidity current, 16 seeded Gaussian bumps, 2 fractions, Re=5000, dt=2.5e-4, "
                                    "sampled at %dx%dx%d per host process" % (nx, ny, nz)},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port", "host": host_cpu(),
                              "sample": "one step of the %dx%dx%d version of the workload in each of %d processes "
                                        "(the reference parallelises over MPI ranks only)" % (nx, ny, nz, procs)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -421,7 +440,7 @@ def main():
         O.build()
         v, dtc = cpu_sample_throughput(1, 1)
         nx, ny, nz = SAMPLE
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
                "sample": "one TVD-RK2 step of the %dx%dx%d version of the same workload (%.1f s)" % (nx, ny, nz, dtc)}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
