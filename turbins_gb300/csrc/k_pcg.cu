@@ -186,52 +186,6 @@ __global__ void k_dot2(long long n, const double *__restrict__ r, const double *
     block_store(b, part + NP + blockIdx.x);
 }
 
-// the FP32 V-cycle's result z at cell c, read from the level-0 storage
-// (colour-split or natural) and widened, as the FP64 copy would hold it
-__device__ __forceinline__ double z32_at(const MgDevLevel &L, const float *__restrict__ z, long long c, int i, int j,
-                                         int k)
-{
-    long long o = L.split ? (long long)((i + j + k) & 1) * (((long long)L.nx * L.ny * L.nz) >> 1) + (c >> 1) : c;
-    return (double)z[o];
-}
-
-// k_dot2 with z from the FP32 V-cycle (3-D launch, KC planes per thread):
-// r.z at part[blk], r_old.z at part[nblk + blk]
-__global__ void k_dot2_32(MgDevLevel L, const double *__restrict__ r, const float *__restrict__ z,
-                          const double *__restrict__ ro, double *__restrict__ part)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    double a = 0.0, b = 0.0;
-    if (i < L.nx && j < L.ny)
-        for (int kk = 0; kk < KC; kk++) {
-            int k = blockIdx.z * KC + kk;
-            if (k >= L.nz) break;
-            long long c = ((long long)k * L.ny + j) * L.nx + i;
-            double zc = z32_at(L, z, c, i, j, k);
-            a += r[c] * zc;
-            b += ro[c] * zc;
-        }
-    long long nblk = (long long)gridDim.x * gridDim.y * gridDim.z;
-    block_store(a, part + blk3());
-    block_store(b, part + nblk + blk3());
-}
-
-// k_pupdate with z from the FP32 V-cycle
-__global__ void k_pupdate_32(MgDevLevel L, const float *__restrict__ z, double *__restrict__ p, const PcgScal *sc,
-                             int first)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= L.nx || j >= L.ny) return;
-    double beta = first ? 0.0 : sc->beta;
-    for (int kk = 0; kk < KC; kk++) {
-        int k = blockIdx.z * KC + kk;
-        if (k >= L.nz) break;
-        long long c = ((long long)k * L.ny + j) * L.nx + i;
-        double zc = z32_at(L, z, c, i, j, k);
-        p[c] = first ? zc : zc + beta * p[c];
-    }
-}
-
 __global__ void k_reduce(const double *__restrict__ part, int nvals, int nper, double *__restrict__ dst)
 {
     for (int v = 0; v < nvals; v++) {
@@ -348,17 +302,6 @@ void pcg_dot2(cudaStream_t s, long long n, const double *r, const double *z, con
 void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst, int nper)
 {
     k_reduce<<<1, 1024, 0, s>>>(part, nvals, nper > 0 ? nper : NP, dst);
-}
-
-void pcg_dot2_32(cudaStream_t s, const MgDevLevel &L0, const double *r, const float *z, const double *rold,
-                 double *part)
-{
-    k_dot2_32<<<g3k(L0), dim3(32, 8), 0, s>>>(L0, r, z, rold, part);
-}
-
-void pcg_pupdate_32(cudaStream_t s, const MgDevLevel &L0, const float *z, double *p, const PcgScal *sc, int first)
-{
-    k_pupdate_32<<<g3k(L0), dim3(32, 8), 0, s>>>(L0, z, p, sc, first);
 }
 
 void pcg_pupdate(cudaStream_t s, long long n, const double *z, double *p, const PcgScal *sc, int first)

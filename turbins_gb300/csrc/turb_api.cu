@@ -137,7 +137,7 @@ struct turb_ctx {
     // CUDA graphs: V-cycle per pressure mode, CG vector step (restart / not),
     // FP32 inner sweeps of each Helmholtz field
     cudaGraphExec_t g_mg[2] = {nullptr, nullptr};
-    cudaGraphExec_t g_pcg[4] = {nullptr, nullptr, nullptr, nullptr};   // [pressure mode * 2 + restart]
+    cudaGraphExec_t g_pcg[2] = {nullptr, nullptr};
     cudaGraphExec_t g_inner[3 + TURB_MAXCONC] = {nullptr};
     int g_inner_n[3 + TURB_MAXCONC] = {0};
     int use_graphs = 1;
@@ -1546,11 +1546,7 @@ int turb_set_mg_split(turb_ctx *c, int on)
         m.split = c->mg_split && (m.nx % 2 == 0) && l + 1 < c->H32.nl;
         mg_setup_invdiag<float>(c->s, m, c->H32.invd[l]);
     }
-    // the V-cycle and the mixed-mode CG step (which reads z in the level-0
-    // storage order) are captured again
     if (c->g_mg[1]) { cudaGraphExecDestroy(c->g_mg[1]); c->g_mg[1] = nullptr; }
-    for (int g = 2; g < 4; g++)
-        if (c->g_pcg[g]) { cudaGraphExecDestroy(c->g_pcg[g]); c->g_pcg[g] = nullptr; }
     return check_launch(c);
 }
 
@@ -2366,27 +2362,22 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
                 mg_vcycle<double>(s, c->H64, 0, npre, npost);
             } else {
                 mg_to_float(s, c->H32.lev[0], c->pr, c->H32.b[0]);
-                mg_vcycle<float>(s, c->H32, 0, npre, npost);   // z stays FP32: the CG step reads it
+                mg_vcycle<float>(s, c->H32, 0, npre, npost);
+                mg_to_double(s, c->H32.lev[0], c->H32.x[0], c->pz);
             }
         };
         auto cgstep = [&](int rs) {
-            if (pm == 0) {
-                pcg_dot2(s, n0, c->pr, c->pz, c->pro, c->part);
-                pcg_reduce(s, c->part, 2, dsc + 2);   // rz and z.r_old
-            } else {
-                pcg_dot2_32(s, c->H32.lev[0], c->pr, c->H32.x[0], c->pro, c->part);
-                pcg_reduce(s, c->part, 2, dsc + 2, nsp);
-            }
+            pcg_dot2(s, n0, c->pr, c->pz, c->pro, c->part);
+            pcg_reduce(s, c->part, 2, dsc + 2);   // rz and z.r_old
             if (!rs) pcg_scalars(s, sc, 0);
-            if (pm == 0) pcg_pupdate(s, n0, c->pz, c->pp, sc, rs);
-            else pcg_pupdate_32(s, c->H32.lev[0], c->H32.x[0], c->pp, sc, rs);
+            pcg_pupdate(s, n0, c->pz, c->pp, sc, rs);
             pcg_apply(s, L0, c->pp, c->pq, c->part);
             pcg_reduce(s, c->part, 1, dsc + 5, nsp);
             pcg_scalars(s, sc, 1);
             pcg_xrupdate(s, n0, c->px, c->pr, c->pro, c->pp, c->pq, sc, c->part);
             pcg_reduce(s, c->part, 1, dsc + 1);
         };
-        int nmg = vl + (pm ? 1 : 0), ncg = 8 + (restart ? 0 : 1);
+        int nmg = vl + (pm ? 2 : 0), ncg = 8 + (restart ? 0 : 1);
         int ph = prof_begin(c, TURB_PROF_MG);
         if (c->use_graphs) {
             if (!c->g_mg[pm]) { int rc = capture(c, &c->g_mg[pm], vcycle); if (rc) return rc; }
@@ -2397,13 +2388,12 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         prof_end(c, ph, nmg);
         ph = prof_begin(c, TURB_PROF_PCG);
         if (c->use_graphs) {
-            int gi = pm * 2 + restart;
-            if (!c->g_pcg[gi]) {
+            if (!c->g_pcg[restart]) {
                 int rs = restart;
-                int rc = capture(c, &c->g_pcg[gi], [&]() { cgstep(rs); });
+                int rc = capture(c, &c->g_pcg[restart], [&]() { cgstep(rs); });
                 if (rc) return rc;
             }
-            TURB_CHECK(cudaGraphLaunch(c->g_pcg[gi], s));
+            TURB_CHECK(cudaGraphLaunch(c->g_pcg[restart], s));
         } else {
             cgstep(restart);
         }

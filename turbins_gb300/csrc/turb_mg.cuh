@@ -62,11 +62,6 @@ void pcg_dot2(cudaStream_t s, long long n, const double *r, const double *z, con
 void pcg_reduce(cudaStream_t s, const double *part, int nvals, double *dst, int nper = 0);
 int pcg_stencil_parts(const MgDevLevel &L);
 void pcg_pupdate(cudaStream_t s, long long n, const double *z, double *p, const PcgScal *sc, int first);
-// the same with z read from the FP32 V-cycle's level-0 storage (3-D launch;
-// dot2 leaves pcg_stencil_parts(L0) partials per value)
-void pcg_dot2_32(cudaStream_t s, const MgDevLevel &L0, const double *r, const float *z, const double *rold,
-                 double *part);
-void pcg_pupdate_32(cudaStream_t s, const MgDevLevel &L0, const float *z, double *p, const PcgScal *sc, int first);
 void pcg_xrupdate(cudaStream_t s, long long n, double *x, double *r, double *rold, const double *p,
                   const double *q, const PcgScal *sc, double *part);
 void pcg_scalars(cudaStream_t s, PcgScal *sc, int what);
