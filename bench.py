@@ -122,6 +122,9 @@ def host_cpu():
                 break
     except OSError:
         pass
+    arm = {"0xd4f": "Arm Neoverse-V2", "0xd40": "Arm Neoverse-V1", "0xd0c": "Arm Neoverse-N1"}
+    if model in arm:
+        model = "%s (CPU part %s)" % (arm[model], model)
     return {"nproc": os.cpu_count(), "model": model}
 
 
