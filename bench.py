@@ -25,6 +25,7 @@ import multiprocessing as mp
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -145,7 +146,9 @@ class Clocks:
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        # raw samples: $TURB_CLOCKS_DIR if set, else the system's temporary directory
+        self.path = os.path.join(os.environ.get("TURB_CLOCKS_DIR", tempfile.gettempdir()),
+                                 "clocks_bench_%d.csv" % os.getpid())
 
     def start(self):
         try:
