@@ -15,6 +15,7 @@
 namespace {
 
 constexpr int HBX = 32, HBY = 8, KC = 4;   // 32x8 threads over (i, j), KC planes per thread
+constexpr int KCJ = 2;                      // planes per thread of the FP32 Jacobi sweep
 
 __device__ __forceinline__ double block_sum(double v)
 {
@@ -252,8 +253,8 @@ __global__ void k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st
     const float aev[4] = {ae.x, ae.y, ae.z, ae.w};
     const float apyj = h.apy[j], asj = h.as[j], anj = h.an[j];
     const int nvalid = min(4, d.NX - i0);
-    for (int kk = 0; kk < KC; kk++) {
-        const int k = blockIdx.z * KC + kk;
+    for (int kk = 0; kk < KCJ; kk++) {
+        const int k = blockIdx.z * KCJ + kk;
         if (k >= d.NZ) break;
         const long long p = d.at(i0, j, k);
         const uchar4 s4 = *reinterpret_cast<const uchar4 *>(st + p);
@@ -422,7 +423,7 @@ void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const u
                        const float *r, const float *e, float *en, const IbDevF &ib, int first)
 {
     dim3 g((unsigned)((d.NX + 4 * HBX - 1) / (4 * HBX)), (unsigned)((d.NY + HBY - 1) / HBY),
-           (unsigned)((d.NZ + KC - 1) / KC));
+           (unsigned)((d.NZ + KCJ - 1) / KCJ));
     k_helm_jac32v<<<g, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
     if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
 }
