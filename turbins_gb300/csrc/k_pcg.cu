@@ -7,7 +7,7 @@
 
 namespace {
 
-constexpr int NP = 1024;   // blocks of the grid-stride reductions
+constexpr int NP = 4096;   // blocks of the grid-stride reductions
 constexpr int BS = 256;
 
 __device__ __forceinline__ double warp_sum(double v)
