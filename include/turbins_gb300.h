@@ -226,20 +226,26 @@ int turb_store_old_data(turb_ctx *ctx);
 /* Velocity_rk_average / Conc_rk_average, Velocity.c:2047, Conc.c:1007 */
 int turb_rk_average(turb_ctx *ctx, double old_frac, double new_frac);
 /* No reference counterpart: the divergence check of
- * Pressure_compute_velocity_divergence for callers that cannot allocate GPU
- * memory (a step replayed inside a CUDA graph capture, a host under a fixed
- * memory budget, a plugin that only receives device buffers).  Every argument
- * is caller-owned: u, v, w (FP64, DA order with rows of `pitch` doubles),
- * c_status (uint8), the metrics mxc/myc/mzc (nx+1/ny+1/nz+1 doubles) and the
- * output div on the device, div_max on the host.  The only scratch is a
- * file-scope __device__ array of TURB_NOALLOC_MAX_BLOCKS doubles (512 KB) that
- * every GPU loading this library holds until exit; grids needing more than
- * TURB_NOALLOC_MAX_BLOCKS blocks of 32 x 8 x 8 points return
- * TURB_ERR_SCRATCH_LIMIT.  Nothing is allocated: the first call on a device
- * resolves the array's device address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU (different streams, no ordering) race.  The call
- * synchronizes `stream` (a cudaStream_t, 0 = legacy default stream). */
+ * Pressure_compute_velocity_divergence on a closed box (no inflow / outflow
+ * faces) for callers that cannot allocate GPU memory (a host under a fixed
+ * device memory budget, a plugin that only receives device buffers from its
+ * host application).  Every argument is caller-owned: u, v, w (FP64, DA order
+ * with rows of `pitch` doubles, pitch >= nx+1), c_status (uint8, same pitch),
+ * the metrics mxc/myc/mzc (nx+1/ny+1/nz+1 doubles) and the output div on the
+ * device, div_max on the host.  c_status must mark the last layers i = nx,
+ * j = ny and k = nz BOUNDARY (7), as the reference's DA does; those
+ * layers are never evaluated, so no read leaves the buffers whatever the
+ * status holds.  A NaN in the fields gives a NaN div_max and TURB_ERR_NAN.
+ * The only scratch is a file-scope __device__ array of
+ * TURB_NOALLOC_MAX_BLOCKS doubles (512 KB) that every GPU loading this
+ * library holds until exit; grids needing more than TURB_NOALLOC_MAX_BLOCKS
+ * blocks of 32 x 8 x 8 points return TURB_ERR_SCRATCH_LIMIT.  Nothing is
+ * allocated: the first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress); cudaDeviceReset after it is not supported.  All
+ * calls share the array, so calls that overlap on the GPU (different
+ * streams, no ordering) race.  The call copies div_max to the host and
+ * synchronizes `stream` (a cudaStream_t, 0 = legacy default stream), so it
+ * is made outside any stream capture. */
 #define TURB_NOALLOC_MAX_BLOCKS 65536
 int turb_velocity_divergence_noalloc(int nx, int ny, int nz, long long pitch, const double *u,
                                      const double *v, const double *w, const uint8_t *c_status,

@@ -261,6 +261,36 @@ void ref_lhs_apply(ref_case *r, char q, int ic, double dt, const double *x, doub
     shim_mat_mult(A, x, y);
 }
 
+/* y = A x with A assembled once and its diagonal updated by the reference's
+ * modify_diagonal routine for each time step of dts in turn (dt_old = 0 for
+ * the first, then the previous entry), as a run whose dt changes does: the
+ * diagonal accumulates 1/dt0 + (1/dt1 - 1/dt0) + ..., a change of 1/dt of at
+ * most 1e-10 is skipped, and IMMERSED rows never get the term
+ * (Velocity.c:374-443, Conc.c:293-354) */
+void ref_lhs_apply_dts(ref_case *r, char q, int ic, int ndt, const double *dts, const double *x, double *y)
+{
+    Mat A;
+    int t;
+    if (q == 'c') {
+        Concentration *c = r->c[ic];
+        MatDestroy(c->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &c->A);
+        Conc_form_LHS_matrix(c, r->g, r->p);
+        for (t = 0; t < ndt; t++) Conc_modify_diagonal(c, r->g, dts[t], t ? dts[t - 1] : 0.0);
+        A = c->A;
+    } else {
+        Velocity *V = vel_of(r, q);
+        MatDestroy(V->A);
+        DAGetMatrix(r->g->DA_3D_Lsys, MATMPIAIJ, &V->A);
+        if (q == 'u') Velocity_u_form_LHS_matrix(V, r->g, r->p);
+        else if (q == 'v') Velocity_v_form_LHS_matrix(V, r->g, r->p);
+        else Velocity_w_form_LHS_matrix(V, r->g, r->p);
+        for (t = 0; t < ndt; t++) Velocity_modify_diagonal(V, r->g, r->p, dts[t], t ? dts[t - 1] : 0.0);
+        A = V->A;
+    }
+    shim_mat_mult(A, x, y);
+}
+
 /* the reference's linear solves (the shim's KSPSolve is BiCGStab without a
  * preconditioner, Solver.c's KSPIBCGS; for the pressure it stands in for
  * GMRES(20) + BoomerAMG): LHS formed and diagonal modified as ref_lhs_apply,

@@ -15,7 +15,9 @@ import subprocess
 import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("TURB_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: TURB_REFERENCE_ROOT, else a checkout named
+# "reference" beside this repository
+REF = os.environ.get("TURB_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 SRC = os.path.join(REF, "src")
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libturbins_ref.so")

@@ -182,6 +182,15 @@ class Reference:
                                _p(np.ascontiguousarray(x)), _p(y))
         return y
 
+    def lhs_apply_dts(self, q, ic, dts, x):
+        """A x after the reference's diagonal updates for the time steps dts
+        in turn (matrix assembled once, as in a run whose dt changes)"""
+        y = self._z()
+        d = np.ascontiguousarray(dts, dtype=np.float64)
+        self.lib.ref_lhs_apply_dts(self.h, C.c_char(q.encode()), C.c_int(ic), C.c_int(len(d)), _p(d),
+                                   _p(np.ascontiguousarray(x)), _p(y))
+        return y
+
     def pressure_apply(self, x):
         y = self._z()
         self.lib.ref_pressure_apply(self.h, _p(np.ascontiguousarray(x)), _p(y))

@@ -216,3 +216,26 @@ def to_blocked(a):
 def from_blocked(b, C):
     nb, Z, Y, X, _ = b.shape
     return np.ascontiguousarray(b.transpose(0, 4, 1, 2, 3).reshape(C, Z, Y, X))
+
+
+class Adam:
+    """Adam (Kingma & Ba 2015) on the flat FP32 parameter vector, in float64:
+    m = b1 m + (1 - b1) g, v = b2 v + (1 - b2) g^2,
+    p -= lr (m / (1 - b1^t)) / (sqrt(v / (1 - b2^t)) + eps), with the
+    library's constants b1 = 0.9, b2 = 0.999, eps = 1e-8 and the step count t
+    restarting at 1 after new parameters are loaded."""
+
+    def __init__(self, n, b1=0.9, b2=0.999, eps=1e-8):
+        self.m = np.zeros(n)
+        self.v = np.zeros(n)
+        self.t = 0
+        self.b1, self.b2, self.eps = b1, b2, eps
+
+    def step(self, p, g, lr):
+        self.t += 1
+        g = np.asarray(g, dtype=np.float64)
+        self.m = self.b1 * self.m + (1.0 - self.b1) * g
+        self.v = self.b2 * self.v + (1.0 - self.b2) * g * g
+        c1 = 1.0 - self.b1 ** self.t
+        c2 = 1.0 - self.b2 ** self.t
+        return np.asarray(p, dtype=np.float64) - lr * (self.m / c1) / (np.sqrt(self.v / c2) + self.eps)

@@ -284,7 +284,54 @@ def dump_geom(name, case):
     np.savez_compressed(os.path.join(HERE, "geom", "geom_%s.npz" % name), meta=np.array(json.dumps(meta)), **out)
 
 
+# a run whose time step changes: operators after the reference's diagonal
+# updates for several dt sequences (one change above the 1e-10 threshold of
+# Velocity_modify_diagonal / Conc_modify_diagonal, one below it, several in
+# a row) and three steps with dt = dt0, 0.7 dt0, 1.3 dt0 through the
+# reference's routines
+DT_SEQS = {"up": (1.0, 0.7), "tiny": (1.0, 1.0 + 1e-14), "many": (1.0, 0.7, 1.3, 1.3, 1.0)}
+DT_STEPS = (1.0, 0.7, 1.3)
+
+
+def dt_case():
+    return _cases.bump_small(24, 12, 8)
+
+
+def dump_dt():
+    case = dt_case()
+    g, p = case.grid, case.params
+    s = _cases.random_state(case, seed=23)
+    ref = Reference(g, p)
+    dt0 = case.dt
+    out = {}
+    x = s["phi"]
+    for nm, seq in DT_SEQS.items():
+        dts = [dt0 * f for f in seq]
+        out["dts_" + nm] = np.array(dts)
+        for q in "uvw":
+            out["ref_lhs_%s_%s" % (nm, q)] = ref.lhs_apply_dts(q, 0, dts, x)
+        for ic in range(p.nconc):
+            out["ref_lhs_%s_c%d" % (nm, ic)] = ref.lhs_apply_dts("c", ic, dts, x)
+    keys = ["u", "v", "w", "phi", "dpx", "dpy", "dpz"] + ["c%d" % i for i in range(p.nconc)]
+    for k in keys:
+        out["in_" + k] = s[k]
+    st = {k: s[k].copy() for k in keys}
+    for n, f in enumerate(DT_STEPS):
+        ref.step(st, dt0 * f)
+        for k in keys:
+            out["ref_step%d_%s" % (n + 1, k)] = st[k].copy()
+    meta = dict(dt0=dt0, steps=list(DT_STEPS))
+    os.makedirs(os.path.join(HERE, "dt"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "dt", "dt_change.npz"), meta=np.array(json.dumps(meta)), **out)
+
+
 if __name__ == "__main__":
+    if sys.argv[1:] == ["dt"]:          # only the dt-change fixture
+        dump_dt()
+        print("wrote dt_change")
+        sys.exit(0)
+    dump_dt()
+    print("wrote dt_change")
     for nm, mk in CASES.items():
         dump(nm, mk())
         print("wrote", nm)

@@ -146,3 +146,33 @@ def test_net_forward_backward_vs_oracle(netmod, dims):
         assert e_w < 1e-2 and e_b < 1e-2, (l, e_w, e_b)
     assert _rel(g[hw:hw + 17], ref_g[hw:hw + 17]) < 1e-4
     net.close()
+
+
+def test_adam_matches_oracle(netmod):
+    """Three Adam steps of the library (k_adam, FP32) on the gradients of its
+    own backward pass against the oracle's Adam in float64: each parameter
+    within 1e-3 of the step size lr plus 4 FP32 ulps of its value."""
+    nx, ny, nz = 32, 16, 16
+    rng = np.random.default_rng(3)
+    net = netmod.Net(nx, ny, nz, train=True)
+    p = U.init_params(2).astype(np.float32)
+    net.set_params(p)
+    opt = U.Adam(p.size)
+    ref = p.astype(np.float64)
+    out = torch.zeros((nz, ny, nx), dtype=torch.float32, device="cuda")
+    for step, lr in enumerate((1e-3, 1e-3, 2.5e-4)):
+        in3 = torch.from_numpy(rng.normal(size=(3, nz, ny, nx)).astype(np.float32)).cuda()
+        gout = torch.from_numpy((1.0 + rng.normal(size=(nz, ny, nx))).astype(np.float32)).cuda()
+        net.forward(in3, out)
+        net.backward(gout)
+        g = net.get_grads()
+        assert np.count_nonzero(g) > g.size // 2
+        net.adam(lr)
+        got = net.get_params().astype(np.float64)
+        ref = opt.step(ref, g, lr)
+        tol = 1e-3 * lr + 4 * np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+        bad = np.abs(got - ref) > tol
+        assert not bad.any(), (step, int(bad.sum()), float(np.abs(got - ref).max()))
+        ref = got          # continue from the library's FP32 parameters
+    assert opt.t == 3
+    net.close()

@@ -1,18 +1,22 @@
 // k_noalloc.cu -- the velocity-divergence check (Pressure_compute_velocity_divergence,
-// Pressure.c:462-586) for callers that cannot allocate GPU memory.
+// Pressure.c:462-586, closed box) for callers that cannot allocate GPU memory.
 //
-// Some callers cannot call cudaMalloc: a solver step replayed inside a CUDA
-// graph capture, a host that runs under a fixed memory budget, or a plugin
-// that gets device buffers from its host application and may not create its
-// own.  turb_velocity_divergence_noalloc takes every input and output as
-// caller-owned device memory and keeps the only scratch it needs -- one
-// partial maximum per thread block -- in a file-scope __device__ array of
-// fixed size, so no call allocates.  The array is part of the library image:
-// every GPU that loads the library holds it (TURB_NOALLOC_MAX_BLOCKS doubles,
-// 512 KB) until the process exits.
+// Some callers cannot call cudaMalloc: a host that runs under a fixed device
+// memory budget, or a plugin that gets its device buffers from a host
+// application and may not create its own.  turb_velocity_divergence_noalloc
+// takes every input and output as caller-owned device memory and keeps the
+// only scratch it needs -- one partial maximum per thread block -- in a
+// file-scope __device__ array of fixed size, so no call allocates.  The array
+// is part of the library image: every GPU that loads the library holds it
+// (TURB_NOALLOC_MAX_BLOCKS doubles, 512 KB) until the process exits.
 //
-// The arithmetic is that of k_divergence (k_stencil.cu), so both entry points
-// return the same bits.
+// The call copies the maximum to the host and synchronizes its stream, so it
+// is made outside any stream capture.  Its first call on a device resolves
+// the array's device address; cudaDeviceReset after that call is not
+// supported (the cached address would belong to the old context).
+//
+// The arithmetic is that of k_divergence (k_stencil.cu) without the open-face
+// branches, so on a closed box both entry points return the same bits.
 #include <mutex>
 
 #include "../../include/turbins_gb300.h"
@@ -33,12 +37,12 @@ __device__ __forceinline__ double block_max(double m)
 {
     __shared__ double sm[32];
     int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((lt & 31) == 0) sm[lt >> 5] = m;
     __syncthreads();
     if (lt < 32) {
         m = (lt < (nt >> 5)) ? sm[lt] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     }
     return m;
 }
@@ -58,14 +62,17 @@ __global__ void k_div_noalloc(int NX, int NY, int NZ, long long PX, const double
             if (k >= NZ) break;
             long long p = ((long long)k * NY + j) * PX + i;
             double dc = 0.0;
-            if (st[p] != T_BOUNDARY) {
+            // the last layer i = nx, j = ny, k = nz is BOUNDARY in a valid
+            // status array; the index test keeps every neighbour read inside
+            // the caller's buffers even when it is not
+            if (st[p] != T_BOUNDARY && i < NX - 1 && j < NY - 1 && k < NZ - 1) {
                 double dudx = ml(ml(sb(u[p + 1], u[p]), a_dEta), mxc[i]);
                 double dvdy = ml(ml(sb(v[p + PX], v[p]), a_dXi), myc[j]);
                 double dwdz = ml(ml(sb(w[p + plane], w[p]), a_dPhi), mzc[k]);
                 dc = fabs(ad(ad(dudx, dvdy), dwdz));
             }
             div[p] = dc;
-            m = fmax(m, dc);
+            m = turb_nanmax(m, dc);
         }
     m = block_max(m);
     if (threadIdx.x == 0 && threadIdx.y == 0)
@@ -75,7 +82,7 @@ __global__ void k_div_noalloc(int NX, int NY, int NZ, long long PX, const double
 __global__ void k_max_noalloc(int nparts, double *__restrict__ part)
 {
     double m = 0.0;
-    for (int t = threadIdx.x; t < nparts; t += blockDim.x) m = fmax(m, part[t]);
+    for (int t = threadIdx.x; t < nparts; t += blockDim.x) m = turb_nanmax(m, part[t]);
     m = block_max(m);
     if (threadIdx.x == 0) part[TURB_NOALLOC_MAX_BLOCKS] = m;
 }
@@ -122,10 +129,14 @@ extern "C" int turb_velocity_divergence_noalloc(int nx, int ny, int nz, long lon
     cudaStream_t s = (cudaStream_t)stream;
     k_div_noalloc<<<g, dim3(32, 8), 0, s>>>(NX, NY, NZ, pitch, u, v, w, c_status, mxc, myc, mzc, 1.0 / (1.0 / nx),
                                             1.0 / (1.0 / ny), 1.0 / (1.0 / nz), div, part);
-    k_max_noalloc<<<1, 1024, 0, s>>>((int)nparts, part);
-    cudaError_t e = cudaMemcpyAsync(div_max, part + TURB_NOALLOC_MAX_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_max_noalloc<<<1, 1024, 0, s>>>((int)nparts, part);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(div_max, part + TURB_NOALLOC_MAX_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
-    return TURB_OK;
+    return (*div_max != *div_max) ? TURB_ERR_NAN : TURB_OK;
 }

@@ -113,6 +113,10 @@ struct turb_ctx {
     IbDevF ibf[4];
     float *hrf = nullptr, *he0 = nullptr, *he1 = nullptr;   // defect-correction buffers
     int hmode = TURB_HMODE_MIXED;
+    // the 1/dt term of each Helmholtz diagonal (u, v, w, c_0..) and the dt it
+    // was last updated for (0: not yet)
+    double adt[3 + TURB_MAXCONC] = {};
+    double adt_dt[3 + TURB_MAXCONC] = {};
     int hinner = 5;   // FP32 Jacobi sweeps per defect-correction step (5: the fewest that keep 2 outer steps at 512x256x256)
     const double *pcx, *pcy, *pcz;
     ProjArgs proj;
@@ -2117,12 +2121,31 @@ int turb_Conc_set_RHS(turb_ctx *c, int ic, double dt)
     return check_launch(c);
 }
 
+// The 1/dt term of the diagonal of Helmholtz system sys (0..2 u, v, w;
+// 3 + ic the fractions), kept as Velocity_modify_diagonal /
+// Conc_modify_diagonal keep it (Velocity.c:384-396, Conc.c:304-314): the
+// first call sets 1/dt; a later call with a new dt adds 1/dt - 1/dt_old
+// (dt_old = the dt of the previous call) only when that exceeds 1e-10 in
+// magnitude.  IMMERSED rows never carry it (the kernels skip them).
+static double diag_term(turb_ctx *c, int sys, double dt)
+{
+    double &a = c->adt[sys], &last = c->adt_dt[sys];
+    if (!(last > 0.0)) {
+        a = 1.0 / dt;
+    } else {
+        double mod = 1.0 / dt - 1.0 / last;
+        if (std::fabs(mod) > 1.0e-10) a = a + mod;
+    }
+    last = dt;
+    return a;
+}
+
 static int helm_solve_fp64(turb_ctx *c, int q, int ic, int fx, int fb, double dt, int *iters)
 {
     const Dims &d = c->d;
     const HelmTab &h = q < 3 ? c->helm[q] : c->helm_c[ic];
     const IbDev &ib = c->ib[q];
-    double a_dt = 1.0 / dt;
+    double a_dt = diag_term(c, q < 3 ? q : 3 + ic, dt);
     double *b = c->fld[fb];
     launch_norm2(c->s, d.n, b, c->part, norm_parts(), c->dscal);
     int rc = fetch_scalars(c, 1);
@@ -2163,7 +2186,7 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
     const HelmTabF &hf = q < 3 ? c->helmf[q] : c->helmf_c[ic];
     const IbDev &ib = c->ib[q];
     const IbDevF &ibf = c->ibf[q];
-    double a_dt = 1.0 / dt;
+    double a_dt = diag_term(c, q < 3 ? q : 3 + ic, dt);
     double *b = c->fld[fb];
     launch_norm2(c->s, d.n, b, c->part, norm_parts(), c->dscal);
     int rc = fetch_scalars(c, 1);
@@ -2261,8 +2284,8 @@ int turb_helmholtz_apply(turb_ctx *c, char which, int ic, double dt, int fx, int
     int q = qidx(which);
     if (!c || q < 0 || !(dt > 0.0) || !field_ptr(c, fx) || !field_ptr(c, fy)) return TURB_ERR_ARG;
     if (q == 3 && (ic < 0 || ic >= c->prm.nconc)) return TURB_ERR_ARG;
-    launch_helm_apply(c->s, c->d, q < 3 ? c->helm[q] : c->helm_c[ic], c->st[q], 1.0 / dt, c->fld[fx], c->fld[fy],
-                      c->ib[q]);
+    launch_helm_apply(c->s, c->d, q < 3 ? c->helm[q] : c->helm_c[ic], c->st[q], diag_term(c, q < 3 ? q : 3 + ic, dt),
+                      c->fld[fx], c->fld[fy], c->ib[q]);
     c->launches += 2;
     return check_launch(c);
 }
@@ -2461,6 +2484,7 @@ int turb_Pressure_compute_velocity_divergence(turb_ctx *c, double *div_max)
         rc = fetch_scalars(c, 1);
         if (rc) return rc;
         *div_max = c->hscal[0];
+        if (*div_max != *div_max) return TURB_ERR_NAN;   // the maximum keeps a NaN
     }
     return TURB_OK;
 }

@@ -127,6 +127,13 @@ struct MgLevel {
     double pin;                     // corner east-face coefficient
 };
 
+// Maximum of two non-negative values that keeps a NaN: fmax drops a NaN
+// operand, which would let a non-finite field pass a divergence gate.
+__device__ __forceinline__ double turb_nanmax(double a, double b)
+{
+    return (a != a || a > b) ? a : b;
+}
+
 #define TURB_CHECK(x)                                                          \
     do {                                                                       \
         cudaError_t e_ = (x);                                                  \

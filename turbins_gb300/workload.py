@@ -434,3 +434,46 @@ def multi_bump_case(nx=512, ny=256, nz=256, seed=4, lx=32.0, lz=2.0, nbump=16):
     s["c0"] = c.copy()
     s["c1"] = c.copy()
     return Case("multi_bump_%dx%dx%d" % (nx, ny, nz), g, p, 2.5e-4, 500, s, bed)
+
+
+def poisson_case(nx, ny, nz, lengths, ystretch=None):
+    """Closed box with Neumann walls and no immersed body, for pressure
+    solves alone (every c node FLUID except the BOUNDARY ring)."""
+    g = make_grid(nx, ny, nz, lengths, ystretch=ystretch)
+    tag_status(g, None)
+    build_immersed(g, None)
+    p = Params(nx, ny, nz, eno_order=2, re=2000.0, nconc=1, pe=[2000.0], vs0=[0.0], alpha=[1.0],
+               ctype=[SALINITY], p_rtol=1e-10, p_maxit=400)
+    return Case("poisson_%dx%dx%d%s" % (nx, ny, nz, "_ystretch" if ystretch else ""), g, p, 1.0, 0,
+                _zero_state(g, 1))
+
+
+def fourier_velocity(g, seed, kmax=8, slope=-5.0 / 3.0):
+    """Seeded random-Fourier-mode velocity on the MAC grid: each component is
+    Re sum_k C_k exp(2 pi i (kx x/Lx + ky y/Ly + kz z/Lz)) over the integer
+    wave vectors 1 <= |k| <= kmax, C_k = |k|^slope (a + i b)/sqrt(2) with a, b
+    standard normal (PCG64(seed)), evaluated at the component's own nodes and
+    set to zero on its BOUNDARY nodes (impermeable walls, so the divergence
+    sums to zero).  No k = 0 mode: zero mean.  Separable evaluation: one
+    contraction per direction."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ks = np.arange(-kmax, kmax + 1)
+    KZ, KY, KX = np.meshgrid(ks, ks, ks, indexing="ij")
+    kk = np.sqrt(KX * KX + KY * KY + KZ * KZ)
+    mask = (kk >= 1.0) & (kk <= kmax)
+    amp = np.where(mask, np.where(mask, kk, 1.0) ** slope, 0.0)
+    lx, ly, lz = g.xu[-1] - g.xu[0], g.yv[-1] - g.yv[0], g.zw[-1] - g.zw[0]
+    out = {}
+    for q in "uvw":
+        cz = amp * (rng.standard_normal(amp.shape) + 1j * rng.standard_normal(amp.shape)) / np.sqrt(2.0)
+        x, y, z = g.coords(q)
+        ex = np.exp(2j * np.pi * np.outer(ks, (x - g.xu[0]) / lx))      # [k, NX]
+        ey = np.exp(2j * np.pi * np.outer(ks, (y - g.yv[0]) / ly))      # [k, NY]
+        ez = np.exp(2j * np.pi * np.outer((z - g.zw[0]) / lz, ks))      # [NZ, k]
+        t1 = cz @ ex                                                    # [kz, ky, NX]
+        t2 = np.einsum("jb,abi->aji", ey.T, t1)                         # [kz, NY, NX]
+        n = len(ks)
+        f = (ez @ t2.reshape(n, -1)).real.reshape(g.shape)
+        f[g.status[q] == BOUNDARY] = 0.0
+        out[q] = f
+    return out
