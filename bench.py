@@ -53,10 +53,12 @@ def parse():
     ap.add_argument("--guess", default="learned", choices=["previous", "extrapolate", "learned"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-geometry", action="store_true", help="skip timing the device geometry set-up")
-    ap.add_argument("--plain-steps", type=int, default=3, help="timed steps of the plain FP64 MG-CG variant")
-    ap.add_argument("--prev-steps", type=int, default=3,
-                    help="timed steps of mixed MG-CG with the previous-pressure guess (learned runs)")
+    ap.add_argument("--analytic-geometry", action="store_true",
+                    help="keep the analytic-sdf immersed geometry instead of the reference construction")
+    ap.add_argument("--cmp-steps", type=int, default=5,
+                    help="rounds of one step per arm (learned, previous guess, plain FP64) timed in turn")
+    ap.add_argument("--poisson-rhs", type=int, default=16,
+                    help="Fourier right-hand sides per grid for the Poisson-alone comparison (0: skip)")
     ap.add_argument("--train-seeds", type=int, default=8, help="learned guess: training runs (one bump field each)")
     ap.add_argument("--train-steps", type=int, default=125, help="learned guess: steps per training run")
     ap.add_argument("--guess-stages", type=int, default=2,
@@ -195,7 +197,7 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # CPU legs (the oracle port of the same step; never part of the GPU path)
 # ---------------------------------------------------------------------------
-def _cpu_sample_step(args):
+def _cpu_sample_step(args, keep=False):
     nx, ny, nz, nsteps = args
     from oracle.oracle import Oracle
     from turbins_gb300 import workload as W
@@ -206,16 +208,20 @@ def _cpu_sample_step(args):
     t = time.perf_counter()
     for _ in range(nsteps):
         o.step(s, case.dt)
-    return time.perf_counter() - t
+    el = time.perf_counter() - t
+    return (el, s) if keep else el
 
 
-def cpu_sample_throughput(procs, nsteps=1):
+def cpu_sample_throughput(procs, nsteps=1, keep=None):
     """Mcell-steps/s of `procs` concurrent oracle processes, each running
-    `nsteps` steps of the SAMPLE-size version of the workload."""
+    `nsteps` steps of the SAMPLE-size version of the workload (after one
+    untimed step).  keep (procs == 1): a dict that receives the final state."""
     nx, ny, nz = SAMPLE
     nc = nx * ny * nz
     if procs == 1:
-        dt = _cpu_sample_step((nx, ny, nz, nsteps))
+        dt, s = _cpu_sample_step((nx, ny, nz, nsteps), keep=True)
+        if keep is not None:
+            keep.update(s)
         return nc * nsteps / dt / 1e6, dt
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
@@ -257,16 +263,43 @@ def run_reference(a, dist):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def algorithmic_bytes(group, npts, nl_levels=None):
-    """Algorithmic bytes of ONE launch of the group's kernel (each array read
-    or written once per launch; status masks at 1 byte)."""
-    if group == "jacobi":     # read x, b, status; write x_new
-        return npts * (8 + 8 + 1 + 8)
-    if group == "eno_yz":     # read q, advecting velocity, conv; write conv
-        return npts * (8 + 8 + 8 + 8)
-    if group == "eno_x":      # read q, advecting velocity; write conv
-        return npts * (8 + 8 + 8)
-    return None
+# FP64 pipe instructions (thread-level DADD / DMUL / DFMA) per point of one
+# launch, from ncu counters of the kernel (smsp__sass_thread_inst_executed_op_
+# {dadd,dmul,dfma}_pred_on.sum divided by the points of the launch); see
+# profiles/fp64_ops_multi_bump_256x128x128.md.  None: not measured.
+FP64_OPS = {"eno_yz": None, "jacobi": None, "pcg": None}
+
+
+def step_arm(ctx, api, dt, mode, guess, guess_stages=None):
+    """one step of an arm, timed with events on the context stream"""
+    ctx.set_pressure_mode(mode)
+    ctx.set_pressure_guess(guess)
+    if guess_stages is not None:
+        ctx.set_guess_stages(guess_stages)
+    api.event_record(ctx, 2)
+    st = ctx.step(dt)
+    api.event_record(ctx, 3)
+    return api.event_elapsed(ctx, 2, 3), st
+
+
+def group_table(prof, pbytes, peak_hbm, fp64_rate, npts, ncell):
+    """per kernel group: event ms, launches, algorithmic GB, GB/s and the
+    fraction of the HBM peak; for FP64-bound groups with measured op counts,
+    the fraction of the FP64 pipe rate"""
+    out = {}
+    for g_, (ms, nl) in prof.items():
+        gb = pbytes.get(g_, 0.0) / 1e9
+        row = {"ms": ms, "launches": nl, "gbytes": gb}
+        if ms > 0 and gb > 0:
+            row["gbs"] = gb / (ms / 1e3)
+            row["hbm_frac"] = row["gbs"] / peak_hbm
+        ops = FP64_OPS.get(g_)
+        if ops and ms > 0 and fp64_rate:
+            pts = ncell if g_ == "pcg" else npts
+            units = nl / (2 if g_ == "eno_yz" else 1)
+            row["fp64_frac"] = ops * pts * units / (ms / 1e3) / fp64_rate
+        out[g_] = row
+    return out
 
 
 def main():
@@ -302,12 +335,19 @@ def main():
                 np.save(a.save_net_params, params)
         learned_info["guess_stages"] = a.guess_stages
     case = W.multi_bump_case(a.nx, a.ny, a.nz)
+    # the immersed-boundary geometry of the reference's own construction
+    # (level-set reinitialised sdf, Immersed.c stencils), built on the GPU
+    geom = None
+    if not a.analytic_geometry:
+        from turbins_gb300 import geometry as GM
+        geom = GM.reference_geometry(case)
     g = case.grid
     nc = g.nx * g.ny * g.nz
     npts = g.npts
     ctx = api.Context(g, case.params)
     ctx.load_state(case.state)
-    ctx.set_pressure_mode(api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64)
+    pmode = api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64
+    ctx.set_pressure_mode(pmode)
     guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED}[a.guess]
     net = None
     if guess == api.GUESS_LEARNED:
@@ -315,6 +355,7 @@ def main():
         ctx.set_guess_stages(a.guess_stages)
     elif guess != api.GUESS_PREVIOUS:
         ctx.set_pressure_guess(guess)
+    fp64_rate = api.measure_fp64_rate()
     dt = case.dt
     for _ in range(a.warmup):
         ctx.step(dt)
@@ -336,37 +377,35 @@ def main():
     dist.barrier()
     launches = api.kernel_launches(ctx) - l0
     prof = api.profile_read(ctx)
+    pbytes = api.profile_bytes(ctx)
     api.profile_enable(ctx, False)
     ms_max = dist.allmax(ms)
     value = dist.world * nc * a.steps / (ms_max / 1e3) / 1e6
     divmax = max(max(s["div_max"]) for s in stats)
     assert divmax <= 1e-10, "divergence gate failed: %g" % divmax
-    # ---- mixed MG-CG with the previous-pressure guess (what the network adds) --
-    mixed_prev = None
-    if guess == api.GUESS_LEARNED and a.prev_steps > 0:
-        ctx.set_pressure_guess(api.GUESS_PREVIOUS)
-        ctx.step(dt)
-        api.event_record(ctx, 4)
-        mst = [ctx.step(dt) for _ in range(a.prev_steps)]
-        api.event_record(ctx, 5)
-        mms = dist.allmax(api.event_elapsed(ctx, 4, 5))
-        mixed_prev = {"value": dist.world * nc * a.prev_steps / (mms / 1e3) / 1e6, "ms_per_step": mms / a.prev_steps,
-                      "p_iters": [s["p_iters"] for s in mst], "steps": a.prev_steps}
+    # ---- the arms side by side: one step of each in turn, cmp_steps rounds --
+    arms = [("mixed_previous_guess", api.PMODE_MIXED, api.GUESS_PREVIOUS, None),
+            ("plain_fp64", api.PMODE_FP64, api.GUESS_PREVIOUS, None)]
+    if guess == api.GUESS_LEARNED:
+        arms.insert(0, ("learned_mixed", api.PMODE_MIXED, api.GUESS_LEARNED, a.guess_stages))
+    cmp = {}
+    if a.cmp_steps > 0:
+        for nm, md, gs, stg in arms:            # each arm once untimed (graphs of its mode)
+            step_arm(ctx, api, dt, md, gs, stg)
+        rec = {nm: [] for nm, _, _, _ in arms}
+        for _ in range(a.cmp_steps):
+            for nm, md, gs, stg in arms:
+                rec[nm].append(step_arm(ctx, api, dt, md, gs, stg))
+        for nm, lst in rec.items():
+            t = dist.allmax(sum(x[0] for x in lst))
+            cmp[nm] = {"value": dist.world * nc * len(lst) / (t / 1e3) / 1e6, "ms_per_step": t / len(lst),
+                       "steps": len(lst), "p_iters": [x[1]["p_iters"] for x in lst],
+                       "div_max": max(max(x[1]["div_max"]) for x in lst)}
+            assert cmp[nm]["div_max"] <= 1e-10, (nm, cmp[nm]["div_max"])
+        ctx.set_pressure_mode(pmode)
         ctx.set_pressure_guess(guess)
-    # ---- plain FP64 MG-CG on the same state --------------------------------
-    plain = None
-    if a.plain_steps > 0:
-        ctx.set_pressure_mode(api.PMODE_FP64)
-        ctx.set_pressure_guess(api.GUESS_PREVIOUS)   # the plain method: previous-pressure guess
-        ctx.step(dt)
-        api.event_record(ctx, 2)
-        pst = [ctx.step(dt) for _ in range(a.plain_steps)]
-        api.event_record(ctx, 3)
-        pms = dist.allmax(api.event_elapsed(ctx, 2, 3))
-        plain = {"value": dist.world * nc * a.plain_steps / (pms / 1e3) / 1e6, "ms_per_step": pms / a.plain_steps,
-                 "p_iters": [s["p_iters"] for s in pst], "steps": a.plain_steps}
-        ctx.set_pressure_mode(api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64)
-        ctx.set_pressure_guess(guess)
+        if guess == api.GUESS_LEARNED:
+            ctx.set_guess_stages(a.guess_stages)
     # ---- end to end through the C ABI with host buffers ---------------------
     e2e = None
     if not a.no_e2e:
@@ -379,8 +418,7 @@ def main():
             ctx.download_many([(f, host[k])])
         ne = max(1, min(a.steps, 3))
         pairs = [(f, host[k]) for k, f in keys]
-        # one untimed round first: the pressure mode switched back after the
-        # plain FP64 steps, and its graphs are captured again on first use
+        # one untimed round first (the arms above switched modes)
         ctx.upload_many(pairs)
         ctx.step(dt)
         ctx.download_many(pairs)
@@ -403,23 +441,17 @@ def main():
         e2e = {"value": dist.world * nc * ne / te / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "steps": ne,
                "ms_per_step": {"upload": 1e3 * tu / ne, "step": 1e3 * ts / ne, "download": 1e3 * td / ne}}
-    # ---- roofline of the dominant kernel group -----------------------------
+    # ---- roofline: every group, and the dominant one -------------------------
     peak, peak_src = hbm_peak()
-    dom = max(("jacobi", "eno_yz", "eno_x"), key=lambda k: prof[k][0])
-    gms, gnl = prof[dom]
-    bpl = algorithmic_bytes(dom, npts)
-    ach = bpl / (gms / gnl / 1e3) / 1e9 if gnl else None
-    # DRAM traffic per launch of the ENO y/z pass from one ncu capture of a
-    # y pass at 256x128x128 (dram__bytes_read.sum + dram__bytes_write.sum =
-    # 68.73 MB + 0.89 MB for 257*129*129 points), scaled by the points of a
-    # launch here; at that size the conv writes still sat in L2 when the
-    # kernel ended, so the figure counts reads
-    traffic = (68.734720e6 + 0.888064e6) / (257 * 129 * 129) * npts if dom == "eno_yz" else None
-    roof = {"bound": "hbm", "kernel_group": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
-            "frac": (ach / peak) if ach else None, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": traffic, "traffic_source": "ncu, one y pass at 256x128x128, scaled by points"
-            if traffic else None, "bytes_per_launch": bpl, "launches": gnl, "ms_per_launch": gms / gnl if gnl else None,
-            "groups_ms": {k: v[0] for k, v in prof.items()}, "groups_launches": {k: v[1] for k, v in prof.items()}}
+    groups = group_table(prof, pbytes, peak, fp64_rate, npts, nc)
+    dom = max(groups, key=lambda k: groups[k]["ms"])
+    d = groups[dom]
+    roof = {"bound": "tensor" if dom == "net" else "hbm", "kernel_group": dom,
+            "achieved": d.get("gbs"), "peak": peak, "unit": "GB/s", "frac": d.get("hbm_frac"),
+            "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_src,
+            "traffic": None, "algorithmic_bytes_per_launch": pbytes.get(dom, 0.0) / max(d["launches"], 1),
+            "ms_per_launch": d["ms"] / max(d["launches"], 1), "launches": d["launches"],
+            "fp64_rate_dfma_per_s": fp64_rate, "groups": groups}
     if learned_info is not None and prof["net"][1]:
         # the network's tensor-core work: 2 * 27 * cin * cout FLOP per voxel and conv
         # (25920 MAC per finest cell over the 11 convolutions), per guess
@@ -431,23 +463,40 @@ def main():
                              "frac_of_bf16_peak": flops / (net_ms / 1e3) / 1e12 / bf16_peak()[0],
                              "bf16_peak_source": bf16_peak()[1],
                              "guess_residual_ratio": ctx.pressure_guess_ratio()})
-    # the immersed-boundary set-up of the same bed on the device (reference
-    # level-set reinitialisation, statuses, ghost-cell stencils), timed once
-    # after the steps; the stepped case keeps its own geometry
-    geom = None
-    if not a.no_geometry:
-        from turbins_gb300 import geometry as GM
-        r = GM.device_geometry(g, case.params, GM.bed_heights(g, case.bed), apply=False, ctx=ctx)
-        geom = {"seconds": r["seconds"], "reinit_steps": r["steps"],
-                "ib_nodes": {q: int(r["stencils"][q]["n"]) for q in "uvwc"}}
-    cpu = None
+    ctx.close()
+    if net is not None:
+        net.close()
+    # ---- pressure solves alone: mixed vs plain FP64 on Fourier divergences --
+    poisson = None
+    if a.poisson_rhs > 0 and dist.rank == 0:
+        from turbins_gb300 import poisson as PS
+        poisson = {}
+        for nm, ((px, py, pz), lens, q) in PS.SHAPES.items():
+            recs = PS.solve_set(W.poisson_case(px, py, pz, lens, q), range(a.poisson_rhs))
+            poisson[nm] = PS.summary(recs)
+    # ---- CPU baseline, and the GPU on the same sample from the same state ---
+    cpu, parity = None, None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline:
         from oracle import oracle as O
         O.build()
-        v, dtc = cpu_sample_throughput(1, 1)
-        nx, ny, nz = SAMPLE
+        ref = {}
+        v, dtc = cpu_sample_throughput(1, 1, keep=ref)
+        sx, sy, sz = SAMPLE
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
-               "sample": "one TVD-RK2 step of the %dx%dx%d version of the same workload (%.1f s)" % (nx, ny, nz, dtc)}
+               "sample": "one TVD-RK2 step of the %dx%dx%d version of the same workload (%.1f s)" % (sx, sy, sz, dtc)}
+        sc = W.multi_bump_case(sx, sy, sz)
+        sctx = api.Context(sc.grid, sc.params)
+        sctx.set_pressure_mode(api.PMODE_MIXED)
+        sctx.load_state(sc.state)
+        for _ in range(2):               # the oracle's untimed and timed steps
+            sctx.step(sc.dt)
+        got = sctx.state()
+        sctx.close()
+        vsc = max(np.abs(ref[k]).max() for k in "uvw")
+        parity = {"sample": "%dx%dx%d, 2 steps from the same state" % (sx, sy, sz),
+                  "max_abs_diff_rel": {k: float(np.abs(got[k] - ref[k]).max() / (vsc if k in "uvw" else
+                                                                                    max(np.abs(ref[k]).max(), 1.0)))
+                                       for k in ["u", "v", "w"] + ["c%d" % i for i in range(sc.params.nconc)]}}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
@@ -455,21 +504,20 @@ def main():
                 "config": {"workload": "turbidity current %dx%dx%d y-stretched (tanh 1.5), 16 seeded Gaussian bumps "
                                        "(immersed), 2 fractions (Vs 0.005, 0.02), Re=5000, dt=2.5e-4, ENO-3"
                                        % (a.nx, a.ny, a.nz),
+                           "geometry": "analytic sdf" if geom is None else
+                                       "reference construction on the GPU (level-set sdf, Immersed.c stencils)",
                            "pressure": "%s MG-CG (FP64 CG, %s V-cycles), rtol 1e-10" % (
                                a.pmode, "FP32" if a.pmode == "mixed" else "FP64"),
                            "learned_warm_start": a.guess == "learned", "pressure_guess": a.guess,
                            "l2": "inputs larger than L2: each FP64 field is %.0f MB" % (npts * 8 / 1e6),
                            "parallelism": "replicas" if dist.world > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "plain_fp64": plain, "mixed_previous_guess": mixed_prev, "learned": learned_info,
-                "geometry_setup": geom,
-                "solver": {"p_iters": [s["p_iters"] for s in stats], "guess_tried_taken": ctx.pressure_guess_stats(),
-                           "vel_iters": stats[-1]["vel_iters"],
+                "clocks": clk, "arms": cmp, "plain_fp64": cmp.get("plain_fp64"),
+                "mixed_previous_guess": cmp.get("mixed_previous_guess"), "learned": learned_info,
+                "geometry_setup": geom, "poisson_alone": poisson, "parity": parity,
+                "solver": {"p_iters": [s["p_iters"] for s in stats], "vel_iters": stats[-1]["vel_iters"],
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}
         print(json.dumps(line))
-    ctx.close()
-    if net is not None:
-        net.close()
     dist.close()
 
 

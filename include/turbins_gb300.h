@@ -268,6 +268,10 @@ int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
 #define TURB_PROF_NGROUPS 7
 int turb_profile_enable(turb_ctx *ctx, int on);
 int turb_profile_read(turb_ctx *ctx, double *ms, long long *launches);
+/* algorithmic bytes of the timed launches per group since profiling was
+ * enabled (each array a kernel reads or writes counted once per launch;
+ * TURB_PROF_NGROUPS values, 0 for the network) */
+int turb_profile_bytes(turb_ctx *ctx, double *bytes);
 /* events 0..7 on the context stream; elapsed waits for event b */
 int turb_event_record(turb_ctx *ctx, int slot);
 int turb_event_elapsed(turb_ctx *ctx, int a, int b, double *ms);
@@ -286,6 +290,10 @@ int turb_host_free(void *ptr);
  * reciprocal, one Markstein correction) against IEEE division on nsamples
  * operand pairs;
  * returns the number of bitwise mismatches (and one offending (a, h)) */
+/* FP64 FMA instructions per second of the current GPU (thread-level;
+ * FLOP/s = 2x), measured with CUDA events on a DFMA-only kernel over every SM;
+ * the denominator of the FP64-pipe fractions */
+int turb_measure_fp64_rate(double *dfma_per_s);
 int turb_selftest_division(long long nsamples, unsigned long long seed,
                            unsigned long long *mismatches, double *example);
 

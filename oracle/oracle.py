@@ -24,11 +24,35 @@ def build(force=False):
     """Compile turb_oracle.c with the reference's rounding rules (no FMA
     contraction, no fast-math)."""
     src = os.path.join(HERE, "turb_oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    deps = [src, os.path.join(HERE, "turb_oracle.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in deps):
         return LIB
-    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-                           "-o", LIB, src, "-lm"])
+    base = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-o", LIB + ".tmp", src]
+    try:
+        subprocess.check_call(base + ["-fopenmp", "-lm"])
+    except subprocess.CalledProcessError:
+        subprocess.check_call(base + ["-lm"])      # no OpenMP: the loops run serially
+    os.replace(LIB + ".tmp", LIB)
     return LIB
+
+
+_LOADED = None
+
+
+def _lib():
+    """the oracle library, loaded once; its parallel loops start with
+    TURB_ORACLE_THREADS threads (default 1)"""
+    global _LOADED
+    if _LOADED is None:
+        _LOADED = C.CDLL(build())
+        _LOADED.to_set_threads(int(os.environ.get("TURB_ORACLE_THREADS", "1")))
+    return _LOADED
+
+
+def set_threads(n):
+    """threads of the oracle's parallel loops (results are the same bits for
+    any count)"""
+    _lib().to_set_threads(int(n))
 
 
 class _Params(C.Structure):
@@ -85,7 +109,7 @@ class Oracle:
     """Holds one grid + parameter set in the oracle's C layout."""
 
     def __init__(self, grid, params):
-        self.lib = C.CDLL(build())
+        self.lib = _lib()
         L = self.lib
         L.to_divergence.restype = C.c_double
         self.g = grid

@@ -1,17 +1,32 @@
 /*
  * turb_oracle.c -- CPU oracle (TEST INFRASTRUCTURE ONLY) for the TURBINS
- * fractional-step hot path: a single-threaded plain-C restatement of the
- * reference arithmetic, cited routine by routine.  Used by tests/ as the
- * checker of the CUDA path and by bench.py as the timed CPU baseline
- * ("kind": "port").  The product never links or calls it.
+ * fractional-step hot path: a plain-C restatement of the reference
+ * arithmetic, cited routine by routine.  Used by tests/ as the checker of the
+ * CUDA path and by bench.py as the timed CPU baseline ("kind": "port").  The
+ * product never links or calls it.
  *
  * Build with -O2 -ffp-contract=off (no fused multiply-add, no fast-math) so
  * that every rounding matches the reference's own C compiled the same way.
+ * With OpenMP, loops whose iterations write disjoint outputs run on
+ * to_set_threads() threads (default 1); every sum stays serial, so results
+ * are the same bits for any thread count.
  */
 #include "turb_oracle.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+
+void to_set_threads(int n)
+{
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : 1);
+#else
+    (void)n;
+#endif
+}
 
 #define IDX(g, i, j, k) (((size_t)(k) * (g)->NY + (size_t)(j)) * (g)->NX + (size_t)(i))
 #define NPTS(g) ((size_t)(g)->NX * (g)->NY * (g)->NZ)
@@ -110,6 +125,7 @@ void to_cell_center(const to_grid *g, const double *u, const double *v,
                     const double *w, double *ubc, double *vbc, double *wbc)
 {
     int i, j, k;
+#pragma omp parallel for private(i, j) schedule(static)
     for (k = 0; k < g->nz; k++)
         for (j = 0; j < g->ny; j++)
             for (i = 0; i < g->nx; i++) {
@@ -128,6 +144,7 @@ void to_transpose(const to_grid *g, char which, const double *u,
 {
     int i, j, k, q = (which == 'u') ? 0 : (which == 'v') ? 1 : 2;
     const double *xc = g->xc, *yc = g->yc, *zc = g->zc, *xu = g->xu, *yv = g->yv, *zw = g->zw;
+#pragma omp parallel for private(i, j) schedule(static)
     for (k = 0; k < g->NZ; k++)
         for (j = 0; j < g->NY; j++)
             for (i = 0; i < g->NX; i++) {
@@ -206,11 +223,15 @@ static void conv_dir(const to_grid *g, int order, int dir, const double *q,
                      int r1a, int r1b, int r2a, int r2b, ghost_rule lo,
                      ghost_rule hi, double *conv, int first)
 {
-    int nint = e0 - s0 + 1, n = nint + 2 * order, a, b, m;
+    int nint = e0 - s0 + 1, n = nint + 2 * order;
+#pragma omp parallel
+    {
+    int a, b, m;
     double *D0 = (double *)malloc(sizeof(double) * n);
     double *P = (double *)malloc(sizeof(double) * n);
     double *V = (double *)calloc((size_t)n, sizeof(double));
     double *O = (double *)calloc((size_t)n, sizeof(double));
+#pragma omp for schedule(static)
     for (b = r2a; b <= r2b; b++)
         for (a = r1a; a <= r1b; a++) {
             for (m = s0; m <= e0; m++) {
@@ -228,6 +249,7 @@ static void conv_dir(const to_grid *g, int order, int dir, const double *q,
             }
         }
     free(D0); free(P); free(V); free(O);
+    }
 }
 
 static double slip(int noslip) { return noslip ? -1.0 : 1.0; }
@@ -500,6 +522,7 @@ void to_helmholtz_apply(const to_grid *g, const to_params *p, char which,
     double a_dt = 1.0 / dt;
     double aps = ap_solid_of(g, q == 3 ? p->pe[ic] : p->re);
     size_t NX = g->NX, NXY = (size_t)g->NX * g->NY;
+#pragma omp parallel for private(i, j) schedule(static)
     for (k = 0; k < g->NZ; k++)
         for (j = 0; j < g->NY; j++)
             for (i = 0; i < g->NX; i++) {
@@ -525,11 +548,21 @@ void to_helmholtz_apply(const to_grid *g, const to_params *p, char which,
     ib_rows_apply(g, q, aps, x, y);
 }
 
+/* dot product summed in 64 fixed chunks (each serially, then the chunk sums
+ * in order): the same bits for any thread count */
+#define DOT_CHUNKS 64
 static double dot(size_t n, const double *a, const double *b)
 {
-    double s = 0.0;
-    size_t i;
-    for (i = 0; i < n; i++) s += a[i] * b[i];
+    double part[DOT_CHUNKS], s = 0.0;
+    int c;
+#pragma omp parallel for schedule(static)
+    for (c = 0; c < DOT_CHUNKS; c++) {
+        size_t i, lo = n * (size_t)c / DOT_CHUNKS, hi = n * (size_t)(c + 1) / DOT_CHUNKS;
+        double t = 0.0;
+        for (i = lo; i < hi; i++) t += a[i] * b[i];
+        part[c] = t;
+    }
+    for (c = 0; c < DOT_CHUNKS; c++) s += part[c];
     return s;
 }
 
@@ -586,15 +619,18 @@ int to_helmholtz_solve(const to_grid *g, const to_params *p, char which, int ic,
             double rho1 = dot(n, rh, r), beta;
             if (rho1 == 0.0) break;
             beta = (rho1 / rho) * (alpha / omega);
+#pragma omp parallel for schedule(static)
             for (t = 0; t < n; t++) pv[t] = r[t] + beta * (pv[t] - omega * v[t]);
             to_helmholtz_apply(g, p, which, ic, dt, pv, v);
             alpha = rho1 / dot(n, rh, v);
+#pragma omp parallel for schedule(static)
             for (t = 0; t < n; t++) s[t] = r[t] - alpha * v[t];
             to_helmholtz_apply(g, p, which, ic, dt, s, tv);
             {
                 double tt = dot(n, tv, tv);
                 omega = tt > 0.0 ? dot(n, tv, s) / tt : 0.0;
             }
+#pragma omp parallel for schedule(static)
             for (t = 0; t < n; t++) {
                 x[t] += alpha * pv[t] + omega * s[t];
                 r[t] = s[t] - omega * tv[t];
@@ -729,6 +765,7 @@ static double mg_offsum(const mg_lev *l, const double *x, int i, int j, int k)
 static void mg_apply(const mg_lev *l, const double *x, double *y)
 {
     int i, j, k;
+#pragma omp parallel for private(i, j) schedule(static)
     for (k = 0; k < l->nz; k++)
         for (j = 0; j < l->ny; j++)
             for (i = 0; i < l->nx; i++) {
@@ -740,6 +777,9 @@ static void mg_apply(const mg_lev *l, const double *x, double *y)
 static void mg_rbgs(const mg_lev *l, double *x, const double *b, int color)
 {
     int i, j, k;
+    /* the cells of one colour have no neighbour of that colour: updated in
+     * any order (or in parallel) they give the same bits */
+#pragma omp parallel for private(i, j) schedule(static)
     for (k = 0; k < l->nz; k++)
         for (j = 0; j < l->ny; j++)
             for (i = ((j + k + color) & 1); i < l->nx; i += 2) {
@@ -921,6 +961,9 @@ static void mg_transfer(const mg_lev *f, const mg_lev *c, double *xf, double *xc
     pw_build(f->DY, f->ny, c->DY, c->ny, f->cy, &ty);
     pw_build(f->DZ, f->nz, c->DZ, c->nz, f->cz, &tz);
     if (restrict_) memset(xc, 0, sizeof(double) * (size_t)c->nx * c->ny * c->nz);
+    /* prolongation writes each fine cell once (parallel); restriction
+     * scatters into shared coarse cells and stays serial */
+#pragma omp parallel for private(i, j, a, b, d) schedule(static) if (!restrict_)
     for (k = 0; k < f->nz; k++)
         for (j = 0; j < f->ny; j++)
             for (i = 0; i < f->nx; i++) {
@@ -968,6 +1011,7 @@ static void mg_vcycle(mg_hier *H, int lev)
     memset(L->x, 0, nc * sizeof(double));
     for (s = 0; s < g_npre; s++) { mg_rbgs(L, L->x, L->b, 0); mg_rbgs(L, L->x, L->b, 1); }
     mg_apply(L, L->x, L->r);
+#pragma omp parallel for schedule(static)
     for (t = 0; t < nc; t++) L->r[t] = L->b[t] - L->r[t];
     mg_restrict(L, L->r, &H->L[lev + 1], H->L[lev + 1].b);
     mg_vcycle(H, lev + 1);
@@ -1020,11 +1064,16 @@ int to_pressure_solve(const to_grid *g, const to_params *p, const double *b,
             memcpy(z, L0->x, nc * sizeof(double));
             rz1 = dot(nc, r, z);
             if (restart) memcpy(pv, z, nc * sizeof(double));
-            else { double beta = rz1 / rz; for (t = 0; t < nc; t++) pv[t] = z[t] + beta * pv[t]; }
+            else {
+                double beta = rz1 / rz;
+#pragma omp parallel for schedule(static)
+                for (t = 0; t < nc; t++) pv[t] = z[t] + beta * pv[t];
+            }
             restart = 0;
             rz = rz1;
             mg_apply(L0, pv, q);
             alpha = rz / dot(nc, pv, q);
+#pragma omp parallel for schedule(static)
             for (t = 0; t < nc; t++) { x[t] += alpha * pv[t]; r[t] -= alpha * q[t]; }
             nr = sqrt(dot(nc, r, r));
             it++;

@@ -158,6 +158,9 @@ void to_diagnostics(const to_grid *g, const to_params *p, const double *u,
 int to_step(const to_grid *g, const to_params *p, to_state *s, double dt,
             to_step_stats *stats);
 
+/* threads of the parallel loops (OpenMP builds; results do not depend on it) */
+void to_set_threads(int n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,3 +170,21 @@ def test_projection_gate_and_nonconvergence(oracle_mod):
     o = oracle_mod.Oracle(case.grid, case.params)
     phi, it, rr = o.pressure_solve(b, np.zeros(case.grid.shape))
     assert it == 1 and rr > 1e-12
+
+
+def test_oracle_threads_give_same_bits(oracle_mod):
+    """the oracle's parallel loops write disjoint outputs and its sums stay
+    serial: two steps on 1 and on 4 threads give the same bits"""
+    from tests import _cases
+    case = _cases.multi_small(32, 16, 8)
+    out = []
+    for nt in (1, 4):
+        oracle_mod.set_threads(nt)
+        o = oracle_mod.Oracle(case.grid, case.params)
+        s = {k: v.copy() for k, v in _cases.random_state(case, seed=3).items()}
+        for _ in range(2):
+            o.step(s, case.dt)
+        out.append(s)
+    oracle_mod.set_threads(1)
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k

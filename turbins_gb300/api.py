@@ -628,3 +628,17 @@ def selftest_division(nsamples, seed=1):
     _check(load_library().turb_selftest_division(C.c_longlong(nsamples), C.c_ulonglong(seed), C.byref(bad), ex),
            "selftest_division")
     return bad.value, (ex[0], ex[1])
+
+
+def measure_fp64_rate():
+    """FP64 FMA instructions per second of the current GPU (turb_measure_fp64_rate)"""
+    r = C.c_double()
+    _check(load_library().turb_measure_fp64_rate(C.byref(r)), "measure_fp64_rate")
+    return r.value
+
+
+def profile_bytes(ctx):
+    """algorithmic bytes of the timed launches per group (turb_profile_bytes)"""
+    b = (C.c_double * len(PROF_GROUPS))()
+    _check(ctx.lib.turb_profile_bytes(ctx.ctx, b), "profile_bytes")
+    return {g: b[i] for i, g in enumerate(PROF_GROUPS)}

@@ -649,6 +649,43 @@ void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b
     k_to_double_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
 
+// Algorithmic bytes of one V-cycle from level l (each array a kernel reads
+// or writes counted once per launch): a half sweep of a colour reads b, invd
+// and the other colour's x and writes its own x (the first one of a cycle
+// reads b and invd only); the residual reads b, x and writes r; restriction
+// reads r and writes the coarse b; prolongation reads the coarse x and
+// reads and writes the fine x; the coarsest solve and the single-block tail
+// read b and write x of their levels (their sweeps stay in L1/L2).
+template <typename T>
+double mg_vcycle_bytes(const MgHier<T> &H, int l, const int *pre, const int *post)
+{
+    const double e = (double)sizeof(T);
+    double total = 0.0;
+    for (; l < H.nl; l++) {
+        const MgDevLevel &L = H.lev[l];
+        double n = (double)L.nx * L.ny * L.nz;
+        bool tail = H.tail_from >= 0 && l == H.tail_from && H.nl - l <= MG_TAIL_MAXLEV && l < H.nl - 1;
+        if (tail || l == H.nl - 1) {
+            for (int t = l; t < H.nl; t++) {
+                const MgDevLevel &M = H.lev[t];
+                total += 2.0 * e * (double)M.nx * M.ny * M.nz;
+            }
+            break;
+        }
+        const MgDevLevel &C = H.lev[l + 1];
+        double nc = (double)C.nx * C.ny * C.nz;
+        int halves = 2 * pre[l] + 2 * post[l];
+        total += (halves > 0 ? 1.5 * e * n : 0.0) + (halves > 1 ? (halves - 1) * 2.0 * e * n : 0.0);
+        total += 3.0 * e * n;                 // residual
+        total += e * n + e * nc;              // restriction
+        total += e * nc + 2.0 * e * n;        // prolongation
+    }
+    return total;
+}
+
+template double mg_vcycle_bytes<double>(const MgHier<double> &, int, const int *, const int *);
+template double mg_vcycle_bytes<float>(const MgHier<float> &, int, const int *, const int *);
+
 int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from)
 {
     // per non-coarsest level: 2*pre + resid + restrict + prolong + 2*post;

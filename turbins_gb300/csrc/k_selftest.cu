@@ -1,6 +1,7 @@
 // k_selftest.cu -- on-device self-tests of arithmetic building blocks.
 // turb_selftest_division compares div_by_spacing (turb_div.cuh) with the IEEE
 // division __ddiv_rn bit for bit on random and adversarial operands.
+#include <algorithm>
 #include <cstdint>
 #include "../../include/turbins_gb300.h"
 #include "turb_div.cuh"
@@ -62,7 +63,61 @@ __global__ void k_selftest(long long n, unsigned long long seed, unsigned long l
     if (nbad) atomicAdd(bad, nbad);
 }
 
+// FP64 pipe throughput: eight independent FMA chains per thread (the chains
+// hide the FMA latency), values kept near 1 so no operand turns subnormal
+__global__ void k_dfma_rate(int iters, double b, double c, double *out)
+{
+    double a[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) a[t] = 1.0 + 1e-3 * (threadIdx.x + t);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int t = 0; t < 8; t++) a[t] = fma(a[t], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) s += a[t];
+    if (s == 12345.678) out[0] = s;   // never true: keeps the chains live
+}
+
 }  // namespace
+
+// FP64 FMA instructions per second of this GPU (thread-level, so one DFMA of
+// one thread counts once; FLOP/s is twice this): a fixed number of DFMAs on
+// every SM, timed with CUDA events on the legacy stream after one untimed
+// launch.  Reports the larger of two timed launches' rates.
+extern "C" int turb_measure_fp64_rate(double *dfma_per_s)
+{
+    if (!dfma_per_s) return TURB_ERR_ARG;
+    int dev = 0, nsm = 0;
+    TURB_CHECK(cudaGetDevice(&dev));
+    TURB_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    double *dout = nullptr;
+    TURB_CHECK(cudaMalloc(&dout, sizeof(double)));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = nsm * 8, threads = 256, iters = 4096;
+    double best = 0.0;
+    cudaError_t e = cudaSuccess;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+        cudaEventRecord(e0, 0);
+        k_dfma_rate<<<blocks, threads>>>(iters, 1.0000000001, 1e-12, dout);
+        cudaEventRecord(e1, 0);
+        e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        double ops = (double)blocks * threads * iters * 8.0;
+        if (rep > 0 && ms > 0.0f) best = std::max(best, ops / (ms * 1e-3));
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(dout);
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    *dfma_per_s = best;
+    return TURB_OK;
+}
 
 extern "C" int turb_selftest_division(long long nsamples, unsigned long long seed, unsigned long long *mismatches,
                                       double *example)

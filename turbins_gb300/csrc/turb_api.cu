@@ -91,6 +91,19 @@ struct DevBuf {
 
 }  // namespace
 
+// Algorithmic bytes per DA point of one launch of the step's kernels (each
+// array a kernel reads or writes counted once, status masks at 1 byte):
+// ENO x pass: q, advecting velocity read, conv written; y / z passes also
+// read conv.  FP64 Jacobi sweep: x, b, status read, x' written; FP64
+// Helmholtz residual: x, b, status read, FP32 r written; FP32 Jacobi sweep:
+// r, e, status read, e' written (the first sweep starts from e = 0).  An
+// immersed row: its diagonal, count, eight columns, values and x entries, b
+// and the row's result.
+constexpr double ENO_X_BYTES = 24.0, ENO_YZ_BYTES = 32.0;
+constexpr double HELM_JACOBI_BYTES = 25.0, HELM_RESID64_BYTES = 21.0;
+constexpr double HELM_JAC32_FIRST_BYTES = 9.0, HELM_JAC32_BYTES = 13.0;
+constexpr double IB_ROW_BYTES = 8.0 + 4.0 + 8.0 * (4.0 + 8.0 + 8.0) + 8.0 + 8.0;
+
 struct turb_ctx {
     Dims d;
     turb_params prm;
@@ -132,11 +145,12 @@ struct turb_ctx {
     long long launches = 0;
     // per-group CUDA-event timing (turb_profile_*)
     int prof = 0;
-    struct Rec { int g, nl; cudaEvent_t a, b; };
+    struct Rec { int g, nl; double bytes; cudaEvent_t a, b; };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
     double prof_ms[TURB_PROF_NGROUPS] = {0};
     long long prof_nl[TURB_PROF_NGROUPS] = {0};
+    double prof_bytes[TURB_PROF_NGROUPS] = {0};   // algorithmic bytes of the timed launches
     cudaEvent_t user_ev[8] = {nullptr};
     // CUDA graphs: V-cycle per pressure mode, CG vector step (restart / not),
     // FP32 inner sweeps of each Helmholtz field
@@ -828,6 +842,7 @@ int prof_begin(turb_ctx *c, int g)
     turb_ctx::Rec r;
     r.g = g;
     r.nl = 0;
+    r.bytes = 0.0;
     r.a = prof_event(c);
     r.b = prof_event(c);
     cudaEventRecord(r.a, c->s);
@@ -835,11 +850,14 @@ int prof_begin(turb_ctx *c, int g)
     return (int)c->recs.size() - 1;
 }
 
-void prof_end(turb_ctx *c, int h, int nlaunch)
+// bytes: the algorithmic bytes of the launches in the group (each array a
+// kernel reads or writes counted once per launch)
+void prof_end(turb_ctx *c, int h, int nlaunch, double bytes = 0.0)
 {
     if (h < 0) return;
     cudaEventRecord(c->recs[h].b, c->s);
     c->recs[h].nl = nlaunch;
+    c->recs[h].bytes = bytes;
 }
 
 void prof_collect(turb_ctx *c)
@@ -850,6 +868,7 @@ void prof_collect(turb_ctx *c)
         cudaEventElapsedTime(&ms, r.a, r.b);
         c->prof_ms[r.g] += ms;
         c->prof_nl[r.g] += r.nl;
+        c->prof_bytes[r.g] += r.bytes;
         c->pool.push_back(r.a);
         c->pool.push_back(r.b);
     }
@@ -2066,13 +2085,14 @@ int turb_Velocity_convective_terms(turb_ctx *c, char which)
         az = adv_of(0, w, z, z);
     }
     cudaMemsetAsync(conv, 0, d.n * 8, c->s);
+    const double npts = (double)d.NX * d.NY * d.NZ;
     int h = prof_begin(c, TURB_PROF_ENO_X);
     launch_eno_pass(c->s, d, 0, c->eno[q][0], self, ax, j0, ny - 1, k0, nz - 1, 1, conv);
-    prof_end(c, h, 1);
+    prof_end(c, h, 1, ENO_X_BYTES * npts);
     h = prof_begin(c, TURB_PROF_ENO_YZ);
     launch_eno_pass(c->s, d, 1, c->eno[q][1], self, ay, i0, nx - 1, k0, nz - 1, 0, conv);
     launch_eno_pass(c->s, d, 2, c->eno[q][2], self, az, i0, nx - 1, j0, ny - 1, 0, conv);
-    prof_end(c, h, 2);
+    prof_end(c, h, 2, 2.0 * ENO_YZ_BYTES * npts);
     c->launches += 3;
     return check_launch(c);
 }
@@ -2089,14 +2109,15 @@ int turb_Conc_convective_terms(turb_ctx *c, int ic)
                                                   : adv_of(0, c->fld[TURB_F_VBC], z, z);
     AdvSrc az = adv_of(0, c->fld[TURB_F_WBC], z, z);
     cudaMemsetAsync(conv, 0, d.n * 8, c->s);
+    const double npts = (double)d.NX * d.NY * d.NZ;
     int h = prof_begin(c, TURB_PROF_ENO_X);
     launch_eno_pass(c->s, d, 0, c->ob.in || c->ob.out ? c->eno_cx[ic] : c->eno[3][0], cf, ax, 0, d.ny - 1, 0,
                     d.nz - 1, 1, conv);
-    prof_end(c, h, 1);
+    prof_end(c, h, 1, ENO_X_BYTES * npts);
     h = prof_begin(c, TURB_PROF_ENO_YZ);
     launch_eno_pass(c->s, d, 1, c->eno_cy[ic], cf, ay, 0, d.nx - 1, 0, d.nz - 1, 0, conv);
     launch_eno_pass(c->s, d, 2, c->eno[3][2], cf, az, 0, d.nx - 1, 0, d.ny - 1, 0, conv);
-    prof_end(c, h, 2);
+    prof_end(c, h, 2, 2.0 * ENO_YZ_BYTES * npts);
     c->launches += 3;
     return check_launch(c);
 }
@@ -2159,7 +2180,7 @@ static int helm_solve_fp64(turb_ctx *c, int q, int ic, int fx, int fb, double dt
         double *x = c->fld[fx];
         int ph = prof_begin(c, TURB_PROF_JACOBI);
         launch_helm_jacobi(c->s, d, h, c->st[q], a_dt, b, x, c->jtmp, ib, c->part, hp);
-        prof_end(c, ph, 1);
+        prof_end(c, ph, 1, HELM_JACOBI_BYTES * ((double)d.NX * d.NY * d.NZ) + IB_ROW_BYTES * ib.n);
         launch_sum_final(c->s, np, c->part, c->dscal);
         c->launches += 2 + (ib.n > 0);
         rc = fetch_scalars(c, 1);
@@ -2205,7 +2226,7 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
         }
         int ph = prof_begin(c, TURB_PROF_JACOBI);
         launch_helm_resid64(c->s, d, h, c->st[q], a_dt, b, c->fld[fx], c->hrf, ib, c->part, hp);
-        prof_end(c, ph, 1);
+        prof_end(c, ph, 1, HELM_RESID64_BYTES * ((double)d.NX * d.NY * d.NZ) + IB_ROW_BYTES * ib.n);
         launch_sum_final(c->s, np, c->part, c->dscal);
         c->launches += 2 + (ib.n > 0);
         rc = fetch_scalars(c, 1);
@@ -2234,7 +2255,9 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
         // an even number of sweeps
         e = (c->hinner % 2 == 0) ? c->he0 : c->he1;
         en = (e == c->he0) ? c->he1 : c->he0;
-        prof_end(c, ph, c->hinner);
+        prof_end(c, ph, c->hinner,
+                 (HELM_JAC32_FIRST_BYTES + HELM_JAC32_BYTES * (c->hinner - 1)) * ((double)d.NX * d.NY * d.NZ) +
+                     IB_ROW_BYTES * 0.5 * ibf.n * c->hinner);
         c->launches += c->hinner * (1 + (ib.n > 0));
         it++;
     }
@@ -2408,7 +2431,9 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         } else {
             vcycle();
         }
-        prof_end(c, ph, nmg);
+        prof_end(c, ph, nmg,
+                 pm == 0 ? mg_vcycle_bytes<double>(c->H64, 0, npre, npost)
+                         : mg_vcycle_bytes<float>(c->H32, 0, npre, npost) + 24.0 * n0);
         ph = prof_begin(c, TURB_PROF_PCG);
         if (c->use_graphs) {
             if (!c->g_pcg[restart]) {
@@ -2420,7 +2445,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         } else {
             cgstep(restart);
         }
-        prof_end(c, ph, ncg);
+        prof_end(c, ph, ncg, (restart ? 112.0 : 120.0) * n0);
         c->launches += nmg + ncg;
         TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
         TURB_CHECK(cudaStreamSynchronize(s));
@@ -2434,7 +2459,9 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         int rc = net_snapshot_finish(c->snaps, s, L0, c->H64.invd[0], c->px, status == TURB_OK);
         if (rc) return rc;
     }
-    if (status == TURB_OK && (c->guess_mode != TURB_GUESS_PREVIOUS || c->snaps)) {
+    // the per-stage history of converged pressures (what the extrapolated and
+    // learned guesses start from) is kept whenever a guess could use it
+    if (status == TURB_OK && (c->guess_mode != TURB_GUESS_PREVIOUS || c->snaps || c->net)) {
         if (!c->ph[st][0]) {
             c->ph[st][0] = c->mem.alloc<double>(n0);
             c->ph[st][1] = c->mem.alloc<double>(n0);
@@ -2514,7 +2541,7 @@ int turb_profile_enable(turb_ctx *c, int on)
 {
     if (!c) return TURB_ERR_ARG;
     prof_collect(c);
-    for (int g = 0; g < TURB_PROF_NGROUPS; g++) { c->prof_ms[g] = 0.0; c->prof_nl[g] = 0; }
+    for (int g = 0; g < TURB_PROF_NGROUPS; g++) { c->prof_ms[g] = 0.0; c->prof_nl[g] = 0; c->prof_bytes[g] = 0.0; }
     c->prof = on ? 1 : 0;
     return TURB_OK;
 }
@@ -2524,6 +2551,14 @@ int turb_profile_read(turb_ctx *c, double *ms, long long *nlaunch)
     if (!c || !ms || !nlaunch) return TURB_ERR_ARG;
     prof_collect(c);
     for (int g = 0; g < TURB_PROF_NGROUPS; g++) { ms[g] = c->prof_ms[g]; nlaunch[g] = c->prof_nl[g]; }
+    return TURB_OK;
+}
+
+int turb_profile_bytes(turb_ctx *c, double *bytes)
+{
+    if (!c || !bytes) return TURB_ERR_ARG;
+    prof_collect(c);
+    for (int g = 0; g < TURB_PROF_NGROUPS; g++) bytes[g] = c->prof_bytes[g];
     return TURB_OK;
 }
 

@@ -47,6 +47,8 @@ template <typename T>
 // level l smooths with pre[l] / post[l] red-black sweeps
 void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const int *post);
 int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from);
+template <typename T>
+double mg_vcycle_bytes(const MgHier<T> &H, int l, const int *pre, const int *post);
 
 // FP64 CG vector kernels on the compact level-0 layout (k_pcg.cu)
 struct PcgScal {

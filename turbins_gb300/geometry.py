@@ -54,6 +54,26 @@ def device_geometry(grid, params, heights, apply=True, ctx=None):
     return dict(sdf=sdf, status=st, stencils=ib, steps=steps, seconds=sec)
 
 
+def reference_geometry(case):
+    """Replace a workload case's analytic-sdf statuses and stencils with the
+    reference's construction run on the GPU (level-set reinitialised sdf,
+    Immersed.c stencils; bit-identical to the reference's set-up), and zero
+    the concentration at the new SOLID / BOUNDARY c nodes as the lock
+    initial condition does.  Returns the set-up record (seconds, reinit
+    steps, IMMERSED nodes per quantity)."""
+    g = case.grid
+    if case.bed is None:
+        return None
+    r = device_geometry(g, case.params, bed_heights(g, case.bed), apply=True)
+    st = g.status["c"]
+    for k in case.state:
+        if k.startswith("c"):
+            case.state[k] = case.state[k].copy()
+            case.state[k][(st == W.BOUNDARY) | (st == W.SOLID)] = 0.0
+    return {"seconds": r["seconds"], "reinit_steps": r["steps"],
+            "ib_nodes": {q: int(r["stencils"][q]["n"]) for q in "uvwc"}}
+
+
 def main(argv):
     nx, ny, nz = (int(a) for a in argv[:3]) if len(argv) >= 3 else (512, 256, 256)
     case = W.multi_bump_case(nx, ny, nz)
