@@ -225,6 +225,11 @@ int turb_Pressure_compute_velocity_divergence(turb_ctx *ctx, double *div_max);
 int turb_store_old_data(turb_ctx *ctx);
 /* Velocity_rk_average / Conc_rk_average, Velocity.c:2047, Conc.c:1007 */
 int turb_rk_average(turb_ctx *ctx, double old_frac, double new_frac);
+/* the same for one state field (TURB_F_U..TURB_F_W or TURB_F_C0 + ic):
+ * Velocity_store_old_data / Conc_store_old_data and Velocity_rk_average /
+ * Conc_rk_average of a single Velocity or Concentration */
+int turb_store_old_field(turb_ctx *ctx, int field);
+int turb_rk_average_field(turb_ctx *ctx, int field, double old_frac, double new_frac);
 /* No reference counterpart: the divergence check of
  * Pressure_compute_velocity_divergence on a closed box (no inflow / outflow
  * faces) for callers that cannot allocate GPU memory (a host under a fixed

@@ -101,6 +101,9 @@ int DAGetInfo(DA da, int *dim, int *M, int *N, int *P, int *m, int *n, int *p, i
               DAPeriodicType *wrap, DAStencilType *st);
 int DAGetOwnershipRanges(DA da, const int **lx, const int **ly, const int **lz);
 int DAGetMatrix(DA da, MatType t, Mat *A);
+int VecGetArray(Vec v, PetscScalar **a);
+int VecRestoreArray(Vec v, PetscScalar **a);
+int VecGetSize(Vec v, PetscInt *n);
 int DAVecGetArray(DA da, Vec v, void *array);
 int DAVecRestoreArray(DA da, Vec v, void *array);
 int DAGlobalToLocalBegin(DA da, Vec g, InsertMode mode, Vec l);

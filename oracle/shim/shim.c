@@ -153,6 +153,10 @@ int DAVecGetArray(DA da, Vec v, void *array)
     return 0;
 }
 int DAVecRestoreArray(DA da, Vec v, void *array) { (void)da; (void)v; (void)array; return 0; }
+/* contiguous storage of a (single-rank) vector, DA order */
+int VecGetArray(Vec v, PetscScalar **a) { *a = v->a; return 0; }
+int VecRestoreArray(Vec v, PetscScalar **a) { (void)v; if (a) *a = NULL; return 0; }
+int VecGetSize(Vec v, PetscInt *n) { *n = (PetscInt)v->n; return 0; }
 int DAGlobalToLocalBegin(DA da, Vec g, InsertMode mode, Vec l)
 {
     long t;

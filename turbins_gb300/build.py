@@ -1,6 +1,9 @@
 """Build recipe of libturbgpu.so: every CUDA source under csrc/ is compiled for
 sm_103a only (one -gencode), in parallel, and linked into an in-tree shared
-library next to this file (turbins_gb300/lib/)."""
+library next to this file (turbins_gb300/lib/).  libturbdropin.so, the layer
+that takes the reference's own routine names (dropin/turbins_dropin.c), is
+compiled with gcc beside it and linked to libturbgpu.so; its PETSc vector
+calls resolve in the host program."""
 from __future__ import annotations
 
 import concurrent.futures as cf
@@ -31,7 +34,31 @@ def _compile(src, obj, verbose):
     return r.stderr
 
 
+DROPIN_SRC = os.path.join(HERE, "dropin", "turbins_dropin.c")
+DROPIN = os.path.join(OUT, "libturbdropin.so")
+
+
+def build_dropin(force=False):
+    deps = [DROPIN_SRC, LIB, os.path.join(HERE, "..", "include", "turbins_dropin.h")]
+    if not force and os.path.exists(DROPIN) and all(os.path.getmtime(d) <= os.path.getmtime(DROPIN) for d in deps):
+        return DROPIN
+    tmp = DROPIN + ".tmp"
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-Wall", "-o", tmp, DROPIN_SRC, "-L" + OUT, "-lturbgpu",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("drop-in layer build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, DROPIN)
+    return DROPIN
+
+
 def build(force=False, verbose=False):
+    lib = _build_gpu(force, verbose)
+    build_dropin(force)
+    return lib
+
+
+def _build_gpu(force=False, verbose=False):
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     deps = srcs + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         [os.path.join(HERE, "..", "include", "turbins_gb300.h")]

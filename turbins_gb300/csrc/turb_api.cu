@@ -2537,6 +2537,33 @@ int turb_rk_average(turb_ctx *c, double old_frac, double new_frac)
     return check_launch(c);
 }
 
+// the old-data slot of a state field (u, v, w, c_i), -1 for others
+static int old_slot(const turb_ctx *c, int field)
+{
+    if (field >= TURB_F_U && field <= TURB_F_W) return field - TURB_F_U;
+    if (field >= TURB_F_C0 && field < TURB_F_C0 + c->prm.nconc) return 3 + field - TURB_F_C0;
+    return -1;
+}
+
+int turb_store_old_field(turb_ctx *c, int field)
+{
+    if (!c) return TURB_ERR_ARG;
+    int o = old_slot(c, field);
+    if (o < 0) return TURB_ERR_ARG;
+    TURB_CHECK(cudaMemcpyAsync(c->old[o], c->fld[field], c->d.n * 8, cudaMemcpyDeviceToDevice, c->s));
+    return TURB_OK;
+}
+
+int turb_rk_average_field(turb_ctx *c, int field, double old_frac, double new_frac)
+{
+    if (!c) return TURB_ERR_ARG;
+    int o = old_slot(c, field);
+    if (o < 0) return TURB_ERR_ARG;
+    launch_axpby(c->s, c->d.n, old_frac, c->old[o], new_frac, c->fld[field]);
+    c->launches += 1;
+    return check_launch(c);
+}
+
 int turb_profile_enable(turb_ctx *c, int on)
 {
     if (!c) return TURB_ERR_ARG;
