@@ -15,9 +15,14 @@ Both sides iterate every solve to the same relative residuals (Helmholtz
 oracle's BiCGStab / MG-PCG in another order), so fields differ by the
 solvers' tolerance and that difference is carried along by the flow.  The
 tolerances below bound it with room for 100 steps: velocities within
-DRIFT_VEL of the velocity scale, concentrations within DRIFT_C, the
-mean-removed pressure within DRIFT_PHI of its scale, and every step's
-max|div u| <= 1e-10 on the GPU.
+DRIFT_VEL of the velocity scale, concentrations within DRIFT_C, the pressure
+gradients dp_dx, dp_dy, dp_dz (the pressure state TURBINS carries) within
+DRIFT_DP of their scale, and every step's max|div u| <= 1e-10 on the GPU.
+The projection potential phi of the last solve is compared mean-removed
+within DRIFT_PHI: a relative residual of 1e-10 fixes it only to about
+1e-10 times the condition number of the Poisson operator (about 5e4 on the
+64x32x32 box), while its gradient, which is all the step uses, agrees to
+the velocities' tolerance.
 """
 import json
 import os
@@ -29,7 +34,8 @@ pytestmark = pytest.mark.gpu
 
 DRIFT_VEL = 1e-7
 DRIFT_C = 1e-6
-DRIFT_PHI = 1e-6
+DRIFT_DP = 1e-6
+DRIFT_PHI = 1e-4
 
 
 def _diffs(got, ref, nconc, g):
@@ -38,6 +44,9 @@ def _diffs(got, ref, nconc, g):
     for i in range(nconc):
         k = "c%d" % i
         out[k] = float(np.abs(got[k] - ref[k]).max() / max(np.abs(ref[k]).max(), 1.0))
+    dscale = max(np.abs(ref[k]).max() for k in ("dpx", "dpy", "dpz"))
+    for k in ("dpx", "dpy", "dpz"):
+        out[k] = float(np.abs(got[k] - ref[k]).max() / max(dscale, 1e-300))
     m = (slice(0, g.nz), slice(0, g.ny), slice(0, g.nx))
     a = got["phi"][m] - got["phi"][m].mean()
     b = ref["phi"][m] - ref["phi"][m].mean()
@@ -47,7 +56,8 @@ def _diffs(got, ref, nconc, g):
 
 def _check(d, step):
     for k, v in d.items():
-        tol = DRIFT_VEL if k in "uvw" else DRIFT_PHI if k == "phi" else DRIFT_C
+        tol = (DRIFT_VEL if k in ("u", "v", "w") else DRIFT_PHI if k == "phi" else
+               DRIFT_DP if k.startswith("dp") else DRIFT_C)
         assert v <= tol, (step, k, v, tol)
 
 
