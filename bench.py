@@ -50,7 +50,9 @@ def parse():
     ap.add_argument("--ny", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
     ap.add_argument("--pmode", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--guess", default="learned", choices=["previous", "extrapolate", "learned"])
+    ap.add_argument("--guess", default="learned", choices=["previous", "extrapolate", "learned", "project"])
+    ap.add_argument("--galerkin", type=int, default=1,
+                    help="learned guess: fit the network candidate together with the stage's last two solutions")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--analytic-geometry", action="store_true",
@@ -346,13 +348,18 @@ def main():
     npts = g.npts
     ctx = api.Context(g, case.params)
     ctx.load_state(case.state)
+    # every Poisson solve of every arm also reaches max|div u| <= 1e-10 after
+    # the projection (the metric's gate), not only its relative residual
+    ctx.set_divergence_gate(1e-10)
     pmode = api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64
     ctx.set_pressure_mode(pmode)
-    guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED}[a.guess]
+    guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED,
+             "project": api.GUESS_PROJECT}[a.guess]
     net = None
     if guess == api.GUESS_LEARNED:
         net = LN.attach(ctx, params)
         ctx.set_guess_stages(a.guess_stages)
+        ctx.set_guess_galerkin(a.galerkin)
     elif guess != api.GUESS_PREVIOUS:
         ctx.set_pressure_guess(guess)
     fp64_rate = api.measure_fp64_rate()
@@ -385,6 +392,7 @@ def main():
     assert divmax <= 1e-10, "divergence gate failed: %g" % divmax
     # ---- the arms side by side: one step of each in turn, cmp_steps rounds --
     arms = [("mixed_previous_guess", api.PMODE_MIXED, api.GUESS_PREVIOUS, None),
+            ("mixed_projection_guess", api.PMODE_MIXED, api.GUESS_PROJECT, 3),
             ("plain_fp64", api.PMODE_FP64, api.GUESS_PREVIOUS, None)]
     if guess == api.GUESS_LEARNED:
         arms.insert(0, ("learned_mixed", api.PMODE_MIXED, api.GUESS_LEARNED, a.guess_stages))
@@ -463,6 +471,7 @@ def main():
                              "frac_of_bf16_peak": flops / (net_ms / 1e3) / 1e12 / bf16_peak()[0],
                              "bf16_peak_source": bf16_peak()[1],
                              "guess_residual_ratio": ctx.pressure_guess_ratio()})
+    gate_n = ctx.divergence_gate_count()
     ctx.close()
     if net is not None:
         net.close()
@@ -509,6 +518,8 @@ def main():
                            "pressure": "%s MG-CG (FP64 CG, %s V-cycles), rtol 1e-10" % (
                                a.pmode, "FP32" if a.pmode == "mixed" else "FP64"),
                            "learned_warm_start": a.guess == "learned", "pressure_guess": a.guess,
+                           "guess_galerkin": bool(a.galerkin) if a.guess == "learned" else None,
+                           "divergence_gate": 1e-10,
                            "l2": "inputs larger than L2: each FP64 field is %.0f MB" % (npts * 8 / 1e6),
                            "parallelism": "replicas" if dist.world > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
@@ -516,6 +527,7 @@ def main():
                 "mixed_previous_guess": cmp.get("mixed_previous_guess"), "learned": learned_info,
                 "geometry_setup": geom, "poisson_alone": poisson, "parity": parity,
                 "solver": {"p_iters": [s["p_iters"] for s in stats], "vel_iters": stats[-1]["vel_iters"],
+                           "gate_tightened": gate_n,
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}
         print(json.dumps(line))
     dist.close()

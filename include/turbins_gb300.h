@@ -150,9 +150,25 @@ int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 #define TURB_GUESS_PREVIOUS 0
 #define TURB_GUESS_EXTRAPOLATE 1
 #define TURB_GUESS_LEARNED 2
+/* no reference counterpart: the energy-norm best guess in the span of the
+ * previous guess and this RK stage's last two solutions (a Galerkin fit over
+ * earlier solutions, after Fischer's projection method for successive
+ * right-hand sides) */
+#define TURB_GUESS_PROJECT 3
 int turb_set_pressure_guess(turb_ctx *ctx, int mode);
 /* RK stages whose pressure solve tries the extrapolated / learned candidate:
  * bit 0 the first stage, bit 1 the second (default 3, both) */
+/* max_div > 0: every Poisson solve, after reaching its relative residual,
+ * also iterates until dt * max|b - A phi| (the largest divergence the
+ * projection with phi leaves, dt of the last turb_Pressure_set_RHS) is at
+ * most max_div; 0 (default) turns the gate off.  The count is how often a
+ * solve had to go on. */
+int turb_set_divergence_gate(turb_ctx *ctx, double max_div);
+int turb_divergence_gate_count(turb_ctx *ctx, long long *tightened);
+/* 1: the learned candidate also goes through the Galerkin fit with this
+ * stage's last two solutions (TURB_GUESS_PROJECT's span plus the network's
+ * direction); the guard then compares the fit's residual */
+int turb_set_guess_galerkin(turb_ctx *ctx, int on);
 int turb_set_guess_stages(turb_ctx *ctx, int mask);
 int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);
 /* geometric mean over the tried candidates of |r(candidate)| / |r(previous)|

@@ -86,6 +86,10 @@ class _Stats(C.Structure):
 
 
 def _ptr(a, t=_dp):
+    """pointer to a C-contiguous array (a strided view would be read as if
+    it were contiguous, so it is refused)"""
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("oracle arrays must be C-contiguous")
     return a.ctypes.data_as(t)
 
 

@@ -90,3 +90,25 @@ def test_learned_guess_trains_and_gains(mods):
     p0, p1 = ref["phi"] - ref["phi"].mean(), got["phi"] - got["phi"].mean()
     assert np.abs(p1 - p0).max() <= 1e-7 * np.abs(p0).max()
     net.close()
+
+
+def test_projection_guess_keeps_the_answer(mods):
+    """The Galerkin fit over the stage's last two solutions (no network):
+    fields after 12 steps as with the previous-pressure guess, to the
+    solvers' tolerance, in no more PCG iterations."""
+    A, N = mods
+    case = _case()
+    ctx = A.Context(case.grid, case.params)
+    ctx.load_state(case.state)
+    for _ in range(20):
+        ctx.step(case.dt)
+    state = ctx.state()
+    ctx.close()
+    ref, it_prev, _, _, _ = _run(A, case, state, 12, case.dt, A.GUESS_PREVIOUS)
+    got, it_proj, tried, taken, ratio = _run(A, case, state, 12, case.dt, A.GUESS_PROJECT)
+    print("PCG iterations per step: previous %s  projection %s  (taken %d/%d, initial residual x%.3f)"
+          % (it_prev, it_proj, taken, tried, ratio))
+    assert tried > 0 and sum(it_proj) <= sum(it_prev)
+    for k in ("u", "v", "w"):
+        scale = max(np.abs(ref[k]).max(), 1e-30)
+        assert np.abs(got[k] - ref[k]).max() <= 1e-7 * scale, k

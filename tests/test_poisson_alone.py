@@ -33,6 +33,7 @@ def test_fourier_velocity_properties():
     b = W.fourier_velocity(g, 3)
     c = W.fourier_velocity(g, 4)
     for q in "uvw":
+        assert a[q].flags["C_CONTIGUOUS"]
         assert np.array_equal(a[q], b[q])                       # seeded
         assert not np.array_equal(a[q], c[q])
         assert np.all(a[q][g.status[q] == W.BOUNDARY] == 0.0)   # impermeable walls

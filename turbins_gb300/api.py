@@ -25,7 +25,7 @@ F_UBC, F_VBC, F_WBC, F_CONV_U, F_CONV_V, F_CONV_W, F_B_U, F_B_V, F_B_W, F_CTOT, 
 F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
 PMODE_FP64, PMODE_MIXED = 0, 1
 HMODE_FP64, HMODE_MIXED = 0, 1
-GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
+GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED, GUESS_PROJECT = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed", 6: "scratch limit", 7: "restart file I/O", 8: "restart file mismatch"}
@@ -273,6 +273,17 @@ class Context:
 
     def set_pressure_guess(self, mode):
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
+
+    def set_divergence_gate(self, max_div=1e-10):
+        _check(self.lib.turb_set_divergence_gate(self.ctx, C.c_double(max_div)), "set_divergence_gate")
+
+    def divergence_gate_count(self):
+        n = C.c_longlong()
+        _check(self.lib.turb_divergence_gate_count(self.ctx, C.byref(n)), "divergence_gate_count")
+        return n.value
+
+    def set_guess_galerkin(self, on=True):
+        _check(self.lib.turb_set_guess_galerkin(self.ctx, 1 if on else 0), "set_guess_galerkin")
 
     def set_guess_stages(self, mask):
         _check(self.lib.turb_set_guess_stages(self.ctx, int(mask)), "set_guess_stages")

@@ -252,9 +252,116 @@ __global__ void k_copy(long long n, const double *__restrict__ a, double *__rest
         b[c] = a[c];
 }
 
+// Galerkin fit of the initial guess (projection onto earlier solutions):
+// direction m is d_m = y_m - x0 with S-image s_m = w_m - bw + r1 when w_m is
+// the right-hand side y_m was solved for (S y_m = w_m to that solve's
+// tolerance), or s_m = r1 - w_m when w_m is the computed residual of a
+// candidate y_m.  Per block: G[a][b] = d_a . s_b and g[a] = d_a . r1, value
+// v = a * GAL_MAX + b (g at GAL_MAX * GAL_MAX + a) in part[v * GAL_NP + block].
+constexpr int GAL_NP = 512;
+__global__ void __launch_bounds__(BS) k_gal_dots(long long n, GalDirs dd, const double *__restrict__ x0,
+                                                 const double *__restrict__ r1, const double *__restrict__ bw,
+                                                 double *__restrict__ part)
+{
+    double G[GAL_MAX][GAL_MAX] = {}, gv[GAL_MAX] = {};
+    const int nd = dd.nd;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        double xc = x0[c], rc = r1[c], sb = rc - bw[c];
+        double d[GAL_MAX], sv[GAL_MAX];
+#pragma unroll
+        for (int m = 0; m < GAL_MAX; m++) {
+            if (m < nd) {
+                d[m] = dd.y[m][c] - xc;
+                sv[m] = dd.resid[m] ? rc - dd.w[m][c] : dd.w[m][c] + sb;
+            } else {
+                d[m] = 0.0;
+                sv[m] = 0.0;
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < GAL_MAX; a++) {
+            gv[a] = fma(d[a], rc, gv[a]);
+#pragma unroll
+            for (int b = 0; b < GAL_MAX; b++) G[a][b] = fma(d[a], sv[b], G[a][b]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < GAL_MAX; a++) {
+#pragma unroll
+        for (int b = 0; b < GAL_MAX; b++) block_store(G[a][b], part + (long long)(a * GAL_MAX + b) * GAL_NP + blockIdx.x);
+        block_store(gv[a], part + (long long)(GAL_MAX * GAL_MAX + a) * GAL_NP + blockIdx.x);
+    }
+}
+
+// x = x0 + sum_m alpha_m (y_m - x0)
+__global__ void k_gal_update(long long n, GalDirs dd, GalCoef al, const double *__restrict__ x0, double *__restrict__ x)
+{
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        double xc = x0[c], v = xc;
+        for (int m = 0; m < dd.nd; m++) v = fma(al.a[m], dd.y[m][c] - xc, v);
+        x[c] = v;
+    }
+}
+
+// largest |r_c| / (dx_i dy_j dz_k): the unweighted residual b - A phi of the
+// volume-weighted system, whose maximum times dt is the largest divergence
+// the projection with this phi leaves; per block, then the block maxima
+__global__ void k_rmax(MgDevLevel L, const double *__restrict__ r, double *__restrict__ part)
+{
+    double m = 0.0;
+    long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        int i = (int)(c % L.nx), j = (int)((c / L.nx) % L.ny), k = (int)(c / ((long long)L.nx * L.ny));
+        double v = fabs(r[c]) / (L.dxd[i] * L.dyd[j] * L.dzd[k]);
+        m = turb_nanmax(m, v);
+    }
+    __shared__ double sm[BS / 32];
+    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < BS / 32 ? sm[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) part[blockIdx.x] = m;
+    }
+}
+
+__global__ void k_max_parts(const double *__restrict__ part, int n, double *__restrict__ dst)
+{
+    double m = 0.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) m = turb_nanmax(m, part[t]);
+    __shared__ double sm[32];
+    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (int)(blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *dst = m;
+    }
+}
+
 long long ncell(const MgDevLevel &L) { return (long long)L.nx * L.ny * L.nz; }
 
 }  // namespace
+
+void pcg_rmax(cudaStream_t s, const MgDevLevel &L0, const double *r, double *part, double *dst)
+{
+    k_rmax<<<GAL_NP, BS, 0, s>>>(L0, r, part);
+    k_max_parts<<<1, 1024, 0, s>>>(part, GAL_NP, dst);
+}
+
+void pcg_gal_dots(cudaStream_t s, long long n, const GalDirs &dd, const double *x0, const double *r1,
+                  const double *bw, double *part, double *dst)
+{
+    k_gal_dots<<<GAL_NP, BS, 0, s>>>(n, dd, x0, r1, bw, part);
+    k_reduce<<<1, 1024, 0, s>>>(part, GAL_MAX * GAL_MAX + GAL_MAX, GAL_NP, dst);
+}
+
+void pcg_gal_update(cudaStream_t s, long long n, const GalDirs &dd, const GalCoef &al, const double *x0, double *x)
+{
+    k_gal_update<<<NP, BS, 0, s>>>(n, dd, al, x0, x);
+}
 
 int pcg_nparts() { return NP; }
 

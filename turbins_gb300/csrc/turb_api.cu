@@ -168,6 +168,11 @@ struct turb_ctx {
     int guess_stages = 3;   // RK stages (bit 0: first, bit 1: second) that try the candidate guess
     int stage = 0;
     double *ph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    double *pw[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // the right-hand sides W b of ph
+    int galerkin = 0;   // the learned candidate goes through the Galerkin fit with the history
+    double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
+    double p_dt = 0.0;           // dt of the last Pressure_set_RHS
+    long long gate_tightened = 0;
     int nh[2] = {0, 0};
     int guess_taken = 0, guess_tried = 0;
     double guess_logsum = 0.0;   // sum of log(|r candidate| / |r previous|)
@@ -1195,9 +1200,30 @@ int turb_field_download(turb_ctx *c, int field, double *h)
 
 int turb_set_pressure_guess(turb_ctx *c, int mode)
 {
-    if (!c || mode < TURB_GUESS_PREVIOUS || mode > TURB_GUESS_LEARNED) return TURB_ERR_ARG;
+    if (!c || mode < TURB_GUESS_PREVIOUS || mode > TURB_GUESS_PROJECT) return TURB_ERR_ARG;
     if (mode == TURB_GUESS_LEARNED && !c->net) return TURB_ERR_ARG;
     c->guess_mode = mode;
+    return TURB_OK;
+}
+
+int turb_set_divergence_gate(turb_ctx *c, double max_div)
+{
+    if (!c || !(max_div >= 0.0)) return TURB_ERR_ARG;
+    c->div_gate = max_div;
+    return TURB_OK;
+}
+
+int turb_divergence_gate_count(turb_ctx *c, long long *tightened)
+{
+    if (!c || !tightened) return TURB_ERR_ARG;
+    *tightened = c->gate_tightened;
+    return TURB_OK;
+}
+
+int turb_set_guess_galerkin(turb_ctx *c, int on)
+{
+    if (!c || (on != 0 && on != 1)) return TURB_ERR_ARG;
+    c->galerkin = on;
     return TURB_OK;
 }
 
@@ -2316,10 +2342,94 @@ int turb_helmholtz_apply(turb_ctx *c, char which, int ic, double dt, int fx, int
 int turb_Pressure_set_RHS(turb_ctx *c, double dt)
 {
     if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
+    c->p_dt = dt;
     launch_pressure_rhs(c->s, c->d, c->st[3], c->pcx, c->pcy, c->pcz, 1.0 / dt, c->ob, c->fld[TURB_F_U],
                         c->fld[TURB_F_V], c->fld[TURB_F_W], c->fld[TURB_F_PB]);
     c->launches += 1;
     return check_launch(c);
+}
+
+// Galerkin fit of the initial guess of stage st (projection onto earlier
+// solutions, after Fischer's method for successive right-hand sides): over
+// x0 + span{p1 - x0, p2 - x0 [, candidate - x0]}, with x0 the current guess
+// (px, residual pr), p1 / p2 this stage's last two solutions (S p_m = W b_m
+// to their tolerance) and the network candidate (pz, computed residual pq),
+// the coefficients minimise the S-norm of the error: (D^T S D) a = D^T r.
+// Directions whose pivot is negligible are dropped.  The fit goes to pp,
+// its true residual to pro; *nr_out = |pro| (0 when no fit was made).
+static int galerkin_guess(turb_ctx *c, int st, int with_net, double *nr_out)
+{
+    const MgDevLevel &L0 = c->H64.lev[0];
+    long long n0 = (long long)L0.nx * L0.ny * L0.nz;
+    cudaStream_t s = c->s;
+    GalDirs dd;
+    dd.nd = 0;
+    for (int m = 0; m < 2; m++) {
+        dd.y[dd.nd] = c->ph[st][m];
+        dd.w[dd.nd] = c->pw[st][m];
+        dd.resid[dd.nd] = 0;
+        dd.nd++;
+    }
+    if (with_net) {
+        dd.y[dd.nd] = c->pz;
+        dd.w[dd.nd] = c->pq;
+        dd.resid[dd.nd] = 1;
+        dd.nd++;
+    }
+    *nr_out = 0.0;
+    pcg_gal_dots(s, n0, dd, c->px, c->pr, c->pbw, c->part, c->dscal);
+    const int nv = GAL_MAX * GAL_MAX + GAL_MAX;
+    TURB_CHECK(cudaMemcpyAsync(c->hscal, c->dscal, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+    TURB_CHECK(cudaStreamSynchronize(s));
+    c->launches += 2;
+    double G[GAL_MAX][GAL_MAX], g[GAL_MAX];
+    int n = dd.nd;
+    for (int a = 0; a < n; a++) {
+        g[a] = c->hscal[GAL_MAX * GAL_MAX + a];
+        for (int b = 0; b < n; b++)
+            G[a][b] = 0.5 * (c->hscal[a * GAL_MAX + b] + c->hscal[b * GAL_MAX + a]);   // S is symmetric
+    }
+    // Cholesky with pivots below 1e-12 of the largest diagonal dropped
+    double dmax = 0.0;
+    for (int a = 0; a < n; a++) dmax = std::max(dmax, G[a][a]);
+    if (!(dmax > 0.0) || !std::isfinite(dmax)) return TURB_OK;
+    double L[GAL_MAX][GAL_MAX] = {}, y[GAL_MAX] = {}, al[GAL_MAX] = {};
+    int keep[GAL_MAX] = {};
+    for (int a = 0; a < n; a++) {
+        double d = G[a][a];
+        for (int k = 0; k < a; k++) if (keep[k]) d -= L[a][k] * L[a][k];
+        if (!(d > 1e-12 * dmax)) continue;
+        keep[a] = 1;
+        L[a][a] = std::sqrt(d);
+        for (int b = a + 1; b < n; b++) {
+            double t = G[b][a];
+            for (int k = 0; k < a; k++) if (keep[k]) t -= L[b][k] * L[a][k];
+            L[b][a] = t / L[a][a];
+        }
+    }
+    for (int a = 0; a < n; a++) {
+        if (!keep[a]) continue;
+        double t = g[a];
+        for (int k = 0; k < a; k++) if (keep[k]) t -= L[a][k] * y[k];
+        y[a] = t / L[a][a];
+    }
+    for (int a = n - 1; a >= 0; a--) {
+        if (!keep[a]) continue;
+        double t = y[a];
+        for (int k = a + 1; k < n; k++) if (keep[k]) t -= L[k][a] * al[k];
+        al[a] = t / L[a][a];
+    }
+    GalCoef co;
+    for (int a = 0; a < GAL_MAX; a++) co.a[a] = a < n && keep[a] && std::isfinite(al[a]) ? al[a] : 0.0;
+    pcg_gal_update(s, n0, dd, co, c->px, c->pp);
+    pcg_resid(s, L0, c->pbw, c->pp, c->pro, c->part);
+    pcg_reduce(s, c->part, 1, c->dscal, pcg_stencil_parts(L0));
+    TURB_CHECK(cudaMemcpyAsync(c->hscal, c->dscal, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TURB_CHECK(cudaStreamSynchronize(s));
+    c->launches += 3;
+    double nr = std::sqrt(c->hscal[0]);
+    *nr_out = std::isfinite(nr) ? nr : 0.0;
+    return TURB_OK;
 }
 
 int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
@@ -2351,6 +2461,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     }
     if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2 && ((c->guess_stages >> st) & 1)) {
         int ok = 0, ph = -1;
+        double nrc = 0.0;
         if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
             pcg_lincomb(s, n0, 2.0, c->ph[st][0], -1.0, c->ph[st][1], c->pz);
             c->launches += 1;
@@ -2370,8 +2481,24 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             c->launches += 2;
             TURB_CHECK(cudaMemcpyAsync(c->hscal + 2, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
             TURB_CHECK(cudaStreamSynchronize(s));
-            double nrc = std::sqrt(c->hscal[2]);
+            nrc = std::sqrt(c->hscal[2]);
             if (ph >= 0) prof_end(c, ph, NET_GUESS_LAUNCHES + 2);
+        }
+        // Galerkin fit over the earlier solutions of this stage (and the
+        // network candidate): the energy-norm best guess in their span
+        if ((c->guess_mode == TURB_GUESS_PROJECT || (c->guess_mode == TURB_GUESS_LEARNED && c->galerkin && ok)) &&
+            c->pw[st][1]) {
+            double ng = 0.0;
+            int rc = galerkin_guess(c, st, ok && c->guess_mode == TURB_GUESS_LEARNED, &ng);
+            if (rc) return rc;
+            if (ng > 0.0 && (!ok || ng < nrc)) {   // the fit is in pp / pro
+                std::swap(c->pz, c->pp);
+                std::swap(c->pq, c->pro);
+                nrc = ng;
+                ok = 1;
+            }
+        }
+        if (ok) {
             c->guess_tried++;
             if (nr > 0.0 && nrc > 0.0 && std::isfinite(nrc)) c->guess_logsum += std::log(nrc / nr);
             if (nrc < nr) {
@@ -2398,7 +2525,21 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             TURB_CHECK(cudaMemcpyAsync(c->hscal + 1, dsc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
             TURB_CHECK(cudaStreamSynchronize(s));
             nr = std::sqrt(c->hscal[1]);
-            if (nr <= tol) break;
+            if (nr <= tol) {
+                if (!(c->div_gate > 0.0)) break;
+                // the divergence the projection with this phi leaves is dt
+                // times the unweighted residual b - A phi = r / (dx dy dz)
+                pcg_rmax(s, L0, c->pr, c->part, c->dscal);
+                TURB_CHECK(cudaMemcpyAsync(c->hscal + 3, c->dscal, sizeof(double), cudaMemcpyDeviceToHost, s));
+                TURB_CHECK(cudaStreamSynchronize(s));
+                c->launches += 2;
+                double dmax = c->p_dt * c->hscal[3];
+                if (dmax <= c->div_gate) break;
+                if (!std::isfinite(dmax)) { status = TURB_ERR_NAN; break; }
+                // relative residual met, divergence not: tighten in proportion
+                tol = nr * std::min(0.5, 0.5 * c->div_gate / dmax);
+                c->gate_tightened++;
+            }
             if (it >= c->prm.p_maxit) { status = TURB_ERR_NOT_CONVERGED; break; }
             restart = 1;
         }
@@ -2469,6 +2610,16 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         }
         std::swap(c->ph[st][0], c->ph[st][1]);
         pcg_copy(s, n0, c->px, c->ph[st][0]);
+        {   // their right-hand sides, for the Galerkin fit
+            if (!c->pw[st][0]) {
+                c->pw[st][0] = c->mem.alloc<double>(n0);
+                c->pw[st][1] = c->mem.alloc<double>(n0);
+                if (c->mem.err != cudaSuccess) return TURB_ERR_ALLOC;
+            }
+            std::swap(c->pw[st][0], c->pw[st][1]);
+            pcg_copy(s, n0, c->pbw, c->pw[st][0]);
+            c->launches += 1;
+        }
         c->launches += 1;
         c->nh[st] = std::min(c->nh[st] + 1, 2);
     }

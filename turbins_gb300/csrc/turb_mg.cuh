@@ -75,3 +75,23 @@ void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b
 void pcg_copy(cudaStream_t s, long long n, const double *a, double *b);
 int pcg_nparts();
 void pcg_lincomb(cudaStream_t s, long long n, double a, const double *x, double b, const double *y, double *out);
+
+// Galerkin fit of the initial guess (k_pcg.cu): up to GAL_MAX candidate
+// solutions y_m, each with w_m = the right-hand side it solved (resid 0) or
+// its computed residual (resid 1)
+#define GAL_MAX 3
+struct GalDirs {
+    const double *y[GAL_MAX];
+    const double *w[GAL_MAX];
+    int resid[GAL_MAX];
+    int nd;
+};
+struct GalCoef {
+    double a[GAL_MAX];
+};
+// dst[a * GAL_MAX + b] = d_a . s_b, dst[GAL_MAX^2 + a] = d_a . r1 (part: >= 12 * 512 doubles)
+void pcg_gal_dots(cudaStream_t s, long long n, const GalDirs &dd, const double *x0, const double *r1,
+                  const double *bw, double *part, double *dst);
+void pcg_gal_update(cudaStream_t s, long long n, const GalDirs &dd, const GalCoef &al, const double *x0, double *x);
+// *dst = max_c |r_c| / (dx dy dz)_c on level 0 (part: >= 512 doubles)
+void pcg_rmax(cudaStream_t s, const MgDevLevel &L0, const double *r, double *part, double *dst);

@@ -473,7 +473,7 @@ def fourier_velocity(g, seed, kmax=8, slope=-5.0 / 3.0):
         t1 = cz @ ex                                                    # [kz, ky, NX]
         t2 = np.einsum("jb,abi->aji", ey.T, t1)                         # [kz, NY, NX]
         n = len(ks)
-        f = (ez @ t2.reshape(n, -1)).real.reshape(g.shape)
+        f = np.ascontiguousarray((ez @ t2.reshape(n, -1)).real.reshape(g.shape))
         f[g.status[q] == BOUNDARY] = 0.0
         out[q] = f
     return out
