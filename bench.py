@@ -390,6 +390,41 @@ def main():
     value = dist.world * nc * a.steps / (ms_max / 1e3) / 1e6
     divmax = max(max(s["div_max"]) for s in stats)
     assert divmax <= 1e-10, "divergence gate failed: %g" % divmax
+    # ---- end to end through the C ABI with host buffers ---------------------
+    e2e = None
+    if not a.no_e2e:
+        keys = [("u", api.F_U), ("v", api.F_V), ("w", api.F_W), ("phi", api.F_PHI), ("dpx", api.F_DPX),
+                ("dpy", api.F_DPY), ("dpz", api.F_DPZ)] + [("c%d" % i, api.F_C0 + i) for i in range(case.params.nconc)]
+        # the step's inputs and outputs in page-locked host memory
+        host = {}
+        for (k, f), buf in zip(keys, pinned):
+            host[k] = buf
+            ctx.download_many([(f, host[k])])
+        ne = max(1, min(a.steps, 3))
+        pairs = [(f, host[k]) for k, f in keys]
+        # one untimed round first
+        ctx.upload_many(pairs)
+        ctx.step(dt)
+        ctx.download_many(pairs)
+        dist.barrier()
+        t0 = time.perf_counter()
+        tu = ts = td = 0.0
+        for _ in range(ne):
+            t1 = time.perf_counter()
+            ctx.upload_many(pairs)
+            t2 = time.perf_counter()
+            ctx.step(dt)
+            ctx.synchronize()
+            t3 = time.perf_counter()
+            ctx.download_many(pairs)
+            t4 = time.perf_counter()
+            tu, ts, td = tu + t2 - t1, ts + t3 - t2, td + t4 - t3
+        ctx.synchronize()
+        te = dist.allmax(time.perf_counter() - t0)
+        nbytes = sum(arr.nbytes for arr in host.values())
+        e2e = {"value": dist.world * nc * ne / te / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": ne,
+               "ms_per_step": {"upload": 1e3 * tu / ne, "step": 1e3 * ts / ne, "download": 1e3 * td / ne}}
     # ---- the arms side by side: one step of each in turn, cmp_steps rounds --
     arms = [("mixed_previous_guess", api.PMODE_MIXED, api.GUESS_PREVIOUS, None),
             ("mixed_projection_guess", api.PMODE_MIXED, api.GUESS_PROJECT, 3),
@@ -414,41 +449,6 @@ def main():
         ctx.set_pressure_guess(guess)
         if guess == api.GUESS_LEARNED:
             ctx.set_guess_stages(a.guess_stages)
-    # ---- end to end through the C ABI with host buffers ---------------------
-    e2e = None
-    if not a.no_e2e:
-        keys = [("u", api.F_U), ("v", api.F_V), ("w", api.F_W), ("phi", api.F_PHI), ("dpx", api.F_DPX),
-                ("dpy", api.F_DPY), ("dpz", api.F_DPZ)] + [("c%d" % i, api.F_C0 + i) for i in range(case.params.nconc)]
-        # the step's inputs and outputs in page-locked host memory
-        host = {}
-        for (k, f), buf in zip(keys, pinned):
-            host[k] = buf
-            ctx.download_many([(f, host[k])])
-        ne = max(1, min(a.steps, 3))
-        pairs = [(f, host[k]) for k, f in keys]
-        # one untimed round first (the arms above switched modes)
-        ctx.upload_many(pairs)
-        ctx.step(dt)
-        ctx.download_many(pairs)
-        dist.barrier()
-        t0 = time.perf_counter()
-        tu = ts = td = 0.0
-        for _ in range(ne):
-            t1 = time.perf_counter()
-            ctx.upload_many(pairs)
-            t2 = time.perf_counter()
-            ctx.step(dt)
-            ctx.synchronize()
-            t3 = time.perf_counter()
-            ctx.download_many(pairs)
-            t4 = time.perf_counter()
-            tu, ts, td = tu + t2 - t1, ts + t3 - t2, td + t4 - t3
-        ctx.synchronize()
-        te = dist.allmax(time.perf_counter() - t0)
-        nbytes = sum(arr.nbytes for arr in host.values())
-        e2e = {"value": dist.world * nc * ne / te / 1e6, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "steps": ne,
-               "ms_per_step": {"upload": 1e3 * tu / ne, "step": 1e3 * ts / ne, "download": 1e3 * td / ne}}
     # ---- roofline: every group, and the dominant one -------------------------
     peak, peak_src = hbm_peak()
     groups = group_table(prof, pbytes, peak, fp64_rate, npts, nc)
