@@ -456,3 +456,26 @@ def test_divergence_gate(api, oracle_mod, name, mk):
     assert ungated > 1e-10 and ctx.divergence_gate_count() >= 1
     assert gated <= 1e-10 and rr <= case.params.p_rtol
     ctx.close()
+
+
+@pytest.mark.parametrize("name,mk", [("bump", lambda: _cases.bump_small()), ("multi", lambda: _cases.multi_small()),
+                                     ("bump_64", lambda: _cases.bump_small(64, 40, 24))])
+def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):
+    """The kernel variants that hide latency (FP32 Jacobi and red-black
+    sweeps marching along k through shared-memory plane tiles, ENO y / z
+    lines walked in segments) give the same bits as the one-point-per-thread
+    kernels: two full steps (every convection pass and every Helmholtz and
+    Poisson solve) with either."""
+    case = mk()
+    s = _cases.random_state(case, seed=13)
+    out = []
+    for marching in (False, True):
+        ctx = api.Context(case.grid, case.params)
+        ctx.set_sweep_kernels(marching)
+        ctx.load_state(s)
+        for _ in range(2):
+            ctx.step(case.dt)
+        out.append(ctx.state())
+        ctx.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k

@@ -274,6 +274,9 @@ class Context:
     def set_pressure_guess(self, mode):
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
+    def set_sweep_kernels(self, marching=True):
+        _check(self.lib.turb_set_sweep_kernels(self.ctx, 1 if marching else 0), "set_sweep_kernels")
+
     def set_divergence_gate(self, max_div=1e-10):
         _check(self.lib.turb_set_divergence_gate(self.ctx, C.c_double(max_div)), "set_divergence_gate")
 

@@ -10,6 +10,8 @@
 // Every divided difference is an IEEE division on the same operands as the
 // reference, and all sums/products are rounded one by one (no FMA), so the
 // stencil choices and fluxes are bit-identical to the reference's C.
+#include <algorithm>
+
 #include "turb_internal.cuh"
 #include "turb_kernels.cuh"
 #include "turb_div.cuh"
@@ -149,33 +151,41 @@ __global__ void k_eno_x(Dims d, EnoTab T, const double *__restrict__ q, AdvSrc a
     }
 }
 
-// y / z pass: one thread per line, sliding window along the line
+// y / z pass: one thread per segment of a line (blockIdx.z of nseg), a
+// sliding window along it.  A segment starts its window afresh from the
+// buffer entries before it, so every divided difference is formed from the
+// same operands as in one walk of the whole line and the results are the same
+// bits; the segments multiply the threads in flight, which hide the latency
+// of the line walk.
 template <int R>
 __global__ void k_eno_yz(Dims d, int dir, EnoTab T, const double *__restrict__ q, AdvSrc adv, int t1a,
-                         int t1b, int t2a, int first, double *__restrict__ conv)
+                         int t1b, int t2a, int first, int seglen, double *__restrict__ conv)
 {
     int i = t1a + blockIdx.x * blockDim.x + threadIdx.x;
     if (i > t1b) return;
     int o2 = t2a + blockIdx.y;   // k for the y pass, j for the z pass
+    const int cs = R + blockIdx.z * seglen, ce = min(cs + seglen, T.nb - R);
+    if (cs >= ce) return;
     long long stride = dir == 1 ? d.PX : d.plane;
     long long base = dir == 1 ? d.at(i, 0, o2) : d.at(i, o2, 0);
     double qf = q[base + (long long)T.s0 * stride], ql = q[base + (long long)T.e0 * stride];
     const int W = 2 * R + 1;
+    const int b0 = cs - R;       // buffer index of the window's first entry
     double w0[7], w1[6], w2[5], w3[4];
-    // window for c = R
+    // window for c = cs
 #pragma unroll
-    for (int t = 0; t < W; t++) w0[t] = d0_at(T, q, base, stride, t, qf, ql);
+    for (int t = 0; t < W; t++) w0[t] = d0_at(T, q, base, stride, b0 + t, qf, ql);
 #pragma unroll
-    for (int t = 0; t < 2 * R; t++) w1[t] = dd(T, sb(w0[t + 1], w0[t]), T.h1, T.rh1, T.rl1, t, 1);
+    for (int t = 0; t < 2 * R; t++) w1[t] = dd(T, sb(w0[t + 1], w0[t]), T.h1, T.rh1, T.rl1, b0 + t, 1);
     if (R > 1) {
 #pragma unroll
-        for (int t = 0; t < 2 * R - 1; t++) w2[t] = dd(T, sb(w1[t + 1], w1[t]), T.h2, T.rh2, T.rl2, t + 1, 2);
+        for (int t = 0; t < 2 * R - 1; t++) w2[t] = dd(T, sb(w1[t + 1], w1[t]), T.h2, T.rh2, T.rl2, b0 + t + 1, 2);
     }
     if (R > 2) {
 #pragma unroll
-        for (int t = 0; t < 2 * R - 2; t++) w3[t] = dd(T, sb(w2[t + 1], w2[t]), T.h3, T.rh3, T.rl3, t + 1, 4);
+        for (int t = 0; t < 2 * R - 2; t++) w3[t] = dd(T, sb(w2[t + 1], w2[t]), T.h3, T.rh3, T.rl3, b0 + t + 1, 4);
     }
-    for (int c = R; c < T.nb - R; c++) {
+    for (int c = cs; c < ce; c++) {
         int m = c - R + T.s0;
         long long p = base + (long long)m * stride;
         int jj = dir == 1 ? m : o2, kk = dir == 1 ? o2 : m;
@@ -185,7 +195,7 @@ __global__ void k_eno_yz(Dims d, int dir, EnoTab T, const double *__restrict__ q
                                R > 1 ? w2[R2 + 2] : 0.0, R > 2 ? w3[0] : 0.0, R > 2 ? w3[1] : 0.0,
                                R > 2 ? w3[2] : 0.0, R > 2 ? w3[3] : 0.0, T.g2 + 2 * c, T.g3 + 3 * c);
         conv[p] = first ? o : ad(conv[p], o);
-        if (c + 1 < T.nb - R) {
+        if (c + 1 < ce) {
             // slide: new D0[c+1+R], D1[c+R], D2[c+R], D3[c+R-1]
 #pragma unroll
             for (int t = 0; t < W - 1; t++) w0[t] = w0[t + 1];
@@ -244,8 +254,10 @@ __global__ void k_eno_line(int order, int n, const double *__restrict__ D0, cons
 
 }  // namespace
 
+// segments: per y / z line, 0 = about 64 nodes per segment, 1 = each line
+// walked by one thread
 void launch_eno_pass(cudaStream_t s, const Dims &d, int dir, const EnoTab &tab, const double *q, AdvSrc adv,
-                     int t1a, int t1b, int t2a, int t2b, int first, double *conv)
+                     int t1a, int t1b, int t2a, int t2b, int first, double *conv, int segments)
 {
     int n1 = t1b - t1a + 1, n2 = t2b - t2a + 1;
     if (n1 <= 0 || n2 <= 0) return;
@@ -256,10 +268,14 @@ void launch_eno_pass(cudaStream_t s, const Dims &d, int dir, const EnoTab &tab, 
         else if (tab.r == 2) k_eno_x<2><<<g, 128, sh, s>>>(d, tab, q, adv, t1a, t2a, first, conv);
         else k_eno_x<3><<<g, 128, sh, s>>>(d, tab, q, adv, t1a, t2a, first, conv);
     } else {
-        dim3 g((n1 + 63) / 64, n2);
-        if (tab.r == 1) k_eno_yz<1><<<g, 64, 0, s>>>(d, dir, tab, q, adv, t1a, t1b, t2a, first, conv);
-        else if (tab.r == 2) k_eno_yz<2><<<g, 64, 0, s>>>(d, dir, tab, q, adv, t1a, t1b, t2a, first, conv);
-        else k_eno_yz<3><<<g, 64, 0, s>>>(d, dir, tab, q, adv, t1a, t1b, t2a, first, conv);
+        // segments of about 64 nodes per line (at least one)
+        const int ncen = tab.nb - 2 * tab.r;
+        const int nseg = segments > 0 ? segments : std::max(1, (ncen + 32) / 64);
+        const int seglen = (ncen + nseg - 1) / nseg;
+        dim3 g((n1 + 63) / 64, n2, nseg);
+        if (tab.r == 1) k_eno_yz<1><<<g, 64, 0, s>>>(d, dir, tab, q, adv, t1a, t1b, t2a, first, seglen, conv);
+        else if (tab.r == 2) k_eno_yz<2><<<g, 64, 0, s>>>(d, dir, tab, q, adv, t1a, t1b, t2a, first, seglen, conv);
+        else k_eno_yz<3><<<g, 64, 0, s>>>(d, dir, tab, q, adv, t1a, t1b, t2a, first, seglen, conv);
     }
 }
 

@@ -188,6 +188,107 @@ __global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__
     *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
+// The half sweep of k_rbgs4 marching along k (not the first, zero-initial
+// one): a block of 32 x 8 threads owns 128 cells of its colour in each of 8
+// rows of every plane of a chunk of jz planes.  The other colour's plane k
+// (with a halo row above and below and a halo column either side) is a
+// shared-memory tile; its planes k-1 and k+1 at the thread's own cells stay
+// in registers, loaded one plane ahead.  Each cell's arithmetic is k_rbgs4's,
+// operation for operation, so the results are the same bits.
+constexpr int RTX = 4 * 32 + 2;
+__global__ void __launch_bounds__(256, 3) k_rbgs4z(MgDevLevel Ld, int color, int jz, const float *__restrict__ b,
+                                                   const float *__restrict__ invd, float *__restrict__ x)
+{
+    __shared__ float tile[8 + 2][RTX];
+    const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int q4 = blockIdx.x * 32 + tx, j = blockIdx.y * 8 + ty;
+    const int k0 = blockIdx.z * jz, k1 = min(k0 + jz, nz);
+    const bool act = j < ny && 4 * q4 < hx;
+    const int half = (int)(((long long)nx * ny * nz) >> 1), hxy = hx * ny;
+    const float *oth = x + (size_t)(1 - color) * half;
+    const float *bc = b + (size_t)color * half, *dc = invd + (size_t)color * half;
+    float *xc = x + (size_t)color * half;
+    const int mj = j * hx + 4 * q4;                    // plane offset of the thread's cells
+    const int jh = ty == 0 ? j - 1 : (ty == 7 ? j + 1 : -1);
+    const bool hrow = act && jh >= 0 && jh < ny;       // edge rows also load a halo row
+    const int mh = jh * hx + 4 * q4;
+    const bool hl = act && tx == 0 && q4 > 0, hr = act && tx == 31 && 4 * q4 + 4 < hx;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto ld = [&](const float *a, int off, int k) -> float4 {
+        return (act && k >= 0 && k < nz) ? *reinterpret_cast<const float4 *>(a + k * hxy + off) : z4;
+    };
+    const float dyj = act ? Ld.dyf[j] : 0.f;
+    const float ryj = act ? Ld.rfyf[j] : 0.f, ryj1 = act ? Ld.rfyf[j + 1] : 0.f;
+    float4 ob = ld(oth, mj, k0 - 1), oc = ld(oth, mj, k0), of = ld(oth, mj, k0 + 1);
+    float4 bb = ld(bc, mj, k0), dd = ld(dc, mj, k0);
+    float4 hc = (hrow && k0 < nz) ? ld(oth, mh, k0) : z4;
+    float xl = (hl && k0 < nz) ? oth[k0 * hxy + mj - 1] : 0.f, xr = (hr && k0 < nz) ? oth[k0 * hxy + mj + 4] : 0.f;
+    for (int k = k0; k < k1; k++) {
+        float *row = &tile[ty + 1][1 + 4 * tx];
+        row[0] = oc.x; row[1] = oc.y; row[2] = oc.z; row[3] = oc.w;
+        if (hrow) {
+            float *h = &tile[ty == 0 ? 0 : 9][1 + 4 * tx];
+            h[0] = hc.x; h[1] = hc.y; h[2] = hc.z; h[3] = hc.w;
+        }
+        if (hl) tile[ty + 1][0] = xl;
+        if (hr) tile[ty + 1][RTX - 1] = xr;
+        __syncthreads();
+        const int kn = k + 1;
+        const float4 of2 = ld(oth, mj, kn + 1), bn = ld(bc, mj, kn), dn = ld(dc, mj, kn);
+        const float4 hn = (hrow && kn < nz) ? ld(oth, mh, kn) : z4;
+        const float xln = (hl && kn < nz) ? oth[kn * hxy + mj - 1] : 0.f;
+        const float xrn = (hr && kn < nz) ? oth[kn * hxy + mj + 4] : 0.f;
+        if (act) {
+            const int p = (color + j + k) & 1;
+            const float cv[4] = {oc.x, oc.y, oc.z, oc.w};
+            // the fifth x-neighbour: left of the group (p = 0) or right of it (p = 1)
+            float ex = 0.0f;
+            if (p == 0) { if (q4 > 0) ex = tile[ty + 1][4 * tx]; }
+            else { if (4 * q4 + 4 < hx) ex = tile[ty + 1][4 * tx + 5]; }
+            float jmv[4], jpv[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                jmv[e] = j > 0 ? tile[ty][1 + 4 * tx + e] : 0.f;
+                jpv[e] = j < ny - 1 ? tile[ty + 2][1 + 4 * tx + e] : 0.f;
+            }
+            const float4 km = k > 0 ? ob : z4, kp = k < nz - 1 ? of : z4;
+            const float kmv[4] = {km.x, km.y, km.z, km.w}, kpv[4] = {kp.x, kp.y, kp.z, kp.w};
+            const float bv[4] = {bb.x, bb.y, bb.z, bb.w}, dv[4] = {dd.x, dd.y, dd.z, dd.w};
+            const float dzk = Ld.dzf[k];
+            const float dyz = rmul(dyj, dzk);
+            const float rzk = Ld.rfzf[k], rzk1 = Ld.rfzf[k + 1];
+            float out[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int i = 2 * (4 * q4 + e) + p;
+                const float xlv = p == 0 ? (e == 0 ? ex : cv[e - 1]) : cv[e];
+                const float xrv = p == 0 ? cv[e] : (e == 3 ? ex : cv[e + 1]);
+                const float dxi = Ld.dxf[i];
+                const float dxz = rmul(dxi, dzk), dxy = rmul(dxi, dyj);
+                float o = 0.0f, f;
+                if (i > 0) { f = rmul(dyz, Ld.rfxf[i]); o = rfma(f, xlv, o); }
+                if (i < nx - 1) { f = rmul(dyz, Ld.rfxf[i + 1]); o = rfma(f, xrv, o); }
+                if (j > 0) { f = rmul(dxz, ryj); o = rfma(f, jmv[e], o); }
+                if (j < ny - 1) { f = rmul(dxz, ryj1); o = rfma(f, jpv[e], o); }
+                if (k > 0) { f = rmul(dxy, rzk); o = rfma(f, kmv[e], o); }
+                if (k < nz - 1) { f = rmul(dxy, rzk1); o = rfma(f, kpv[e], o); }
+                out[e] = rmul(radd(bv[e], o), dv[e]);
+            }
+            *reinterpret_cast<float4 *>(xc + k * hxy + mj) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+        __syncthreads();
+        ob = oc;
+        oc = of;
+        of = of2;
+        bb = bn;
+        dd = dn;
+        hc = hn;
+        xl = xln;
+        xr = xrn;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void resid_cell(const LevelT<T> &L, const T *__restrict__ b, const T *__restrict__ x,
                                            T *__restrict__ r, int i, int j, int k)
@@ -561,12 +662,27 @@ void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd)
 // One V-cycle from level l: input b[l], output x[l] (x starts at zero).
 // one red-black half sweep of level L: the vectorised kernel where the
 // level is colour-split FP32 with nx a multiple of 8
+// marching: half sweeps after the first of a cycle march along k (k_rbgs4z)
+// on the levels large enough to fill the GPU with them
 template <typename T>
-void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, const T *b, const T *invd, T *x)
+void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, const T *b, const T *invd, T *x,
+             int marching)
 {
     if constexpr (sizeof(T) == 4) {
         if (L.split && L.nx % 8 == 0) {
             dim3 g4((unsigned)((L.nx / 8 + 31) / 32), (unsigned)((L.ny + 7) / 8), (unsigned)L.nz);
+            if (marching && !zero_init) {
+                // planes per block: the most (up to 16) that still gives two
+                // waves of three blocks on every SM
+                long long bxy = (long long)g4.x * g4.y;
+                int jz = 16;
+                while (jz > 2 && bxy * ((L.nz + jz - 1) / jz) < 2 * 3 * 152) jz >>= 1;
+                if (bxy * ((L.nz + jz - 1) / jz) >= 152) {
+                    dim3 gz(g4.x, g4.y, (unsigned)((L.nz + jz - 1) / jz));
+                    k_rbgs4z<<<gz, B38, 0, s>>>(L, color, jz, b, invd, x);
+                    return;
+                }
+            }
             k_rbgs4<<<g4, B38, 0, s>>>(L, color, zero_init, b, invd, x);
             return;
         }
@@ -616,8 +732,8 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
     for (int it = 0; it < npre; it++) {
         // the first colour-0 half sweep takes x = 0 (it reads no neighbours);
         // every colour-1 point is then rewritten from colour-0 values only
-        rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l]);
-        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l]);
+        rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l], H.marching);
+        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching);
     }
     resid_lev<T>(s, L, H.b[l], H.x[l], H.r[l]);
     const MgDevLevel &C = H.lev[l + 1];
@@ -635,8 +751,8 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
         k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
     }
     for (int it = 0; it < npost; it++) {
-        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l]);
-        rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l]);
+        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching);
+        rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l], H.marching);
     }
 }
 

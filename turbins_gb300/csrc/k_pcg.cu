@@ -305,24 +305,35 @@ __global__ void k_gal_update(long long n, GalDirs dd, GalCoef al, const double *
 
 // largest |r_c| / (dx_i dy_j dz_k): the unweighted residual b - A phi of the
 // volume-weighted system, whose maximum times dt is the largest divergence
-// the projection with this phi leaves; per block, then the block maxima
+// the projection with this phi leaves.  3-D launch as k_apply (KC planes per
+// thread); 1/(dx dy) once per thread and 1/dz once per plane of a block, so a
+// cell costs two multiplies.  Per block maxima into part (NaN kept).
 __global__ void k_rmax(MgDevLevel L, const double *__restrict__ r, double *__restrict__ part)
 {
-    double m = 0.0;
-    long long n = (long long)L.nx * L.ny * L.nz;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        int i = (int)(c % L.nx), j = (int)((c / L.nx) % L.ny), k = (int)(c / ((long long)L.nx * L.ny));
-        double v = fabs(r[c]) / (L.dxd[i] * L.dyd[j] * L.dzd[k]);
-        m = turb_nanmax(m, v);
-    }
-    __shared__ double sm[BS / 32];
-    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    __shared__ double izs[KC];
+    int t = threadIdx.y * blockDim.x + threadIdx.x;
+    if (t < KC && blockIdx.z * KC + t < L.nz) izs[t] = 1.0 / L.dzd[blockIdx.z * KC + t];
     __syncthreads();
-    if (threadIdx.x < 32) {
-        m = threadIdx.x < BS / 32 ? sm[threadIdx.x] : 0.0;
+    double m = 0.0;
+    if (i < L.nx && j < L.ny) {
+        double ixy = 1.0 / (L.dxd[i] * L.dyd[j]);
+        for (int kk = 0; kk < KC; kk++) {
+            int k = blockIdx.z * KC + kk;
+            if (k >= L.nz) break;
+            long long c = ((long long)k * L.ny + j) * L.nx + i;
+            m = turb_nanmax(m, fabs(r[c]) * ixy * izs[kk]);
+        }
+    }
+    __shared__ double sm[32];
+    int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((lt & 31) == 0) sm[lt >> 5] = m;
+    __syncthreads();
+    if (lt < 32) {
+        m = lt < (nt >> 5) ? sm[lt] : 0.0;
         for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0) part[blockIdx.x] = m;
+        if (lt == 0) part[blk3()] = m;
     }
 }
 
@@ -345,11 +356,6 @@ long long ncell(const MgDevLevel &L) { return (long long)L.nx * L.ny * L.nz; }
 
 }  // namespace
 
-void pcg_rmax(cudaStream_t s, const MgDevLevel &L0, const double *r, double *part, double *dst)
-{
-    k_rmax<<<GAL_NP, BS, 0, s>>>(L0, r, part);
-    k_max_parts<<<1, 1024, 0, s>>>(part, GAL_NP, dst);
-}
 
 void pcg_gal_dots(cudaStream_t s, long long n, const GalDirs &dd, const double *x0, const double *r1,
                   const double *bw, double *part, double *dst)
@@ -373,6 +379,12 @@ int pcg_stencil_parts(const MgDevLevel &L)
 {
     dim3 g = g3k(L);
     return (int)(g.x * g.y * g.z);
+}
+
+void pcg_rmax(cudaStream_t s, const MgDevLevel &L0, const double *r, double *part, double *dst)
+{
+    k_rmax<<<g3k(L0), dim3(32, 8), 0, s>>>(L0, r, part);
+    k_max_parts<<<1, 1024, 0, s>>>(part, pcg_stencil_parts(L0), dst);
 }
 
 void pcg_gather(cudaStream_t s, const Dims &d, const MgDevLevel &L0, const double *phi_da, const double *pb_da,

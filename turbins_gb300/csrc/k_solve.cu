@@ -307,6 +307,125 @@ __global__ void k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st
     }
 }
 
+// The same sweep (not the first one) marching along k: a block of 32 x 8
+// threads owns a tile of 128 x 8 points of every plane of a chunk of JZ
+// planes.  Each thread keeps its four points of planes k-1, k, k+1 in
+// registers (e of plane k+1 is loaded while plane k is computed); the x and
+// y neighbours come from the plane-k tile in shared memory, whose halo rows
+// j-1, j+8 and columns are loaded by the edge threads.  e is read from
+// memory about once per sweep instead of once per neighbour, and every
+// point's arithmetic and neighbour substitutions are k_helm_jac32v's, so the
+// results are the same bits.
+constexpr int JZ = 16;                 // planes per block
+constexpr int JTX = 4 * HBX + 2;       // tile row: 128 points and two halo columns
+__global__ void __launch_bounds__(HBX *HBY, 3) k_helm_jac32z(Dims d, HelmTabF h, const uint8_t *__restrict__ st,
+                                                          float a_dt, const float *__restrict__ r,
+                                                          const float *__restrict__ e, float *__restrict__ en)
+{
+    __shared__ float tile[HBY + 2][JTX];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = 4 * (blockIdx.x * HBX + tx), j = blockIdx.y * HBY + ty;
+    const int k0 = blockIdx.z * JZ, k1 = min(k0 + JZ, d.NZ);
+    const bool act = i0 < d.NX && j < d.NY;
+    const int nvalid = act ? min(4, d.NX - i0) : 0;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float apxv[4] = {}, awv[4] = {}, aev[4] = {};
+    float apyj = 0.f, asj = 0.f, anj = 0.f;
+    if (act) {
+        const float4 apx = *reinterpret_cast<const float4 *>(h.apx + i0);
+        const float4 aw = *reinterpret_cast<const float4 *>(h.aw + i0);
+        const float4 ae = *reinterpret_cast<const float4 *>(h.ae + i0);
+        apxv[0] = apx.x; apxv[1] = apx.y; apxv[2] = apx.z; apxv[3] = apx.w;
+        awv[0] = aw.x; awv[1] = aw.y; awv[2] = aw.z; awv[3] = aw.w;
+        aev[0] = ae.x; aev[1] = ae.y; aev[2] = ae.z; aev[3] = ae.w;
+        apyj = h.apy[j]; asj = h.as[j]; anj = h.an[j];
+    }
+    const long long pj = act ? d.at(i0, j, 0) : 0;
+    // the edge threads also load a halo row (j-1 for the first row of the
+    // block, j+1 for the last) and a halo column (left / right of the tile)
+    const int jh = ty == 0 ? j - 1 : (ty == HBY - 1 ? j + 1 : -1);
+    const bool hrow = act && jh >= 0 && jh < d.NY;
+    const long long ph = hrow ? d.at(i0, jh, 0) : 0;
+    const bool hl = act && tx == 0 && i0 > 0, hr_ = act && tx == HBX - 1 && i0 + 4 < d.NX;
+    auto in_k = [&](int k) { return act && k >= 0 && k < d.NZ; };
+    auto ld4 = [&](const float *a, long long base, int k) -> float4 {
+        return in_k(k) ? *reinterpret_cast<const float4 *>(a + base + (long long)k * d.plane) : z4;
+    };
+    // plane k0 and the planes around it; the rest is loaded one plane ahead
+    float4 eb = ld4(e, pj, k0 - 1), ec = ld4(e, pj, k0), ef = ld4(e, pj, k0 + 1);
+    float4 rc = ld4(r, pj, k0);
+    uchar4 sc = in_k(k0) ? *reinterpret_cast<const uchar4 *>(st + pj + (long long)k0 * d.plane) : make_uchar4(0, 0, 0, 0);
+    float4 hc = (hrow && k0 < d.NZ) ? ld4(e, ph, k0) : z4;
+    float xlc = hl ? e[pj + (long long)k0 * d.plane - 1] : 0.f, xrc = hr_ ? e[pj + (long long)k0 * d.plane + 4] : 0.f;
+    for (int k = k0; k < k1; k++) {
+        const float ev[4] = {ec.x, ec.y, ec.z, ec.w};
+        float *row = &tile[ty + 1][1 + 4 * tx];
+        row[0] = ev[0]; row[1] = ev[1]; row[2] = ev[2]; row[3] = ev[3];
+        if (hrow) {
+            float *hrw = &tile[ty == 0 ? 0 : HBY + 1][1 + 4 * tx];
+            hrw[0] = hc.x; hrw[1] = hc.y; hrw[2] = hc.z; hrw[3] = hc.w;
+        }
+        if (hl) tile[ty + 1][0] = xlc;
+        if (hr_) tile[ty + 1][JTX - 1] = xrc;
+        __syncthreads();
+        // the next plane's loads, in flight while this plane is computed
+        const int kn = k + 1;
+        const float4 ef2 = ld4(e, pj, kn + 1), rn = ld4(r, pj, kn);
+        const uchar4 sn = in_k(kn) ? *reinterpret_cast<const uchar4 *>(st + pj + (long long)kn * d.plane)
+                                   : make_uchar4(0, 0, 0, 0);
+        const float4 hn = (hrow && kn < d.NZ) ? ld4(e, ph, kn) : z4;
+        const float xln = (hl && kn < d.NZ) ? e[pj + (long long)kn * d.plane - 1] : 0.f;
+        const float xrn = (hr_ && kn < d.NZ) ? e[pj + (long long)kn * d.plane + 4] : 0.f;
+        if (act) {
+            const long long p = pj + (long long)k * d.plane;
+            const int sv[4] = {sc.x, sc.y, sc.z, sc.w};
+            const float rv[4] = {rc.x, rc.y, rc.z, rc.w};
+            const float apzk = h.apz[k], abk = h.ab[k], afk = h.af[k];
+            const float xw = i0 > 0 ? tile[ty + 1][4 * tx] : ev[0];
+            const float xe = i0 + 4 < d.NX ? tile[ty + 1][4 * tx + 5] : ev[3];
+            float sv_[4], nv_[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                sv_[t] = j > 0 ? tile[ty][1 + 4 * tx + t] : ev[t];
+                nv_[t] = j < d.NY - 1 ? tile[ty + 2][1 + 4 * tx + t] : ev[t];
+            }
+            const float4 b_ = k > 0 ? eb : ec, f_ = k < d.NZ - 1 ? ef : ec;
+            const float bv_[4] = {b_.x, b_.y, b_.z, b_.w}, fv_[4] = {f_.x, f_.y, f_.z, f_.w};
+            float out[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const bool stn = is_stencil(h.q, sv[t]);
+                const float dg = stn ? __fadd_rn(__fadd_rn(__fadd_rn(apxv[t], apyj), apzk), a_dt)
+                                     : __fadd_rn(h.ap_solid, a_dt);
+                float acc = __fmul_rn(dg, ev[t]);
+                if (stn) {
+                    acc = __fmaf_rn(awv[t], t == 0 ? xw : ev[t - 1], acc);
+                    acc = __fmaf_rn(aev[t], t == 3 ? xe : ev[t + 1], acc);
+                    acc = __fmaf_rn(asj, sv_[t], acc);
+                    acc = __fmaf_rn(anj, nv_[t], acc);
+                    acc = __fmaf_rn(abk, bv_[t], acc);
+                    acc = __fmaf_rn(afk, fv_[t], acc);
+                }
+                out[t] = __fmaf_rn(__fadd_rn(rv[t], -acc), __frcp_rn(dg), ev[t]);
+            }
+            if (nvalid == 4) {
+                *reinterpret_cast<float4 *>(en + p) = make_float4(out[0], out[1], out[2], out[3]);
+            } else {
+                for (int t = 0; t < nvalid; t++) en[p + t] = out[t];
+            }
+        }
+        __syncthreads();
+        eb = ec;
+        ec = ef;
+        ef = ef2;
+        rc = rn;
+        sc = sn;
+        hc = hn;
+        xlc = xln;
+        xrc = xrn;
+    }
+}
+
 __global__ void k_helm_jac32(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
                              const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
                              int first)
@@ -419,11 +538,19 @@ void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const 
     if (ib.n > 0) k_ib_resid64<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, b, x, rf, part + nparts);
 }
 
+// marching 1: the FP32 Jacobi sweeps after the first march along k through
+// shared-memory plane tiles (k_helm_jac32z); 0: k_helm_jac32v throughout
 void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
-                       const float *r, const float *e, float *en, const IbDevF &ib, int first)
+                       const float *r, const float *e, float *en, const IbDevF &ib, int first, int marching)
 {
     dim3 g((unsigned)((d.NX + 4 * HBX - 1) / (4 * HBX)), (unsigned)((d.NY + HBY - 1) / HBY),
            (unsigned)((d.NZ + KCJ - 1) / KCJ));
-    k_helm_jac32v<<<g, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
+    if (!first && marching) {
+        dim3 gz((unsigned)((d.NX + 4 * HBX - 1) / (4 * HBX)), (unsigned)((d.NY + HBY - 1) / HBY),
+                (unsigned)((d.NZ + JZ - 1) / JZ));
+        k_helm_jac32z<<<gz, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en);
+    } else {
+        k_helm_jac32v<<<g, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
+    }
     if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
 }

@@ -53,7 +53,7 @@ struct AdvSrc {
     int pNY = 0, nx = 0;
 };
 void launch_eno_pass(cudaStream_t s, const Dims &d, int dir, const EnoTab &tab, const double *q, AdvSrc adv,
-                     int t1a, int t1b, int t2a, int t2b, int first, double *conv);
+                     int t1a, int t1b, int t2a, int t2b, int first, double *conv, int segments = 0);
 int launch_eno_line(int order, int n, const double *D0, const double *P, const double *V, double *out,
                     cudaStream_t s);
 
@@ -69,7 +69,7 @@ void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const 
                          const double *b, const double *x, float *rf, const IbDev &ib, double *part,
                          long long nparts);
 void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const uint8_t *st, float a_dt,
-                       const float *r, const float *e, float *en, const IbDevF &ib, int first);
+                       const float *r, const float *e, float *en, const IbDevF &ib, int first, int marching);
 void launch_sum_final(cudaStream_t s, long long nparts, const double *part, double *out);
 void launch_norm2(cudaStream_t s, long long n, const double *x, double *part, long long nparts, double *out);
 long long norm_parts();

@@ -39,6 +39,8 @@ struct MgHier {
     // from this level on (-1: never) the V-cycle runs as one single-block
     // kernel (k_vcycle_tail); it must leave at most MG_TAIL_MAXLEV levels
     int tail_from = -1;
+    // 1: FP32 half sweeps after the first of a cycle march along k (k_rbgs4z)
+    int marching = 1;
 };
 
 template <typename T>
@@ -93,5 +95,5 @@ struct GalCoef {
 void pcg_gal_dots(cudaStream_t s, long long n, const GalDirs &dd, const double *x0, const double *r1,
                   const double *bw, double *part, double *dst);
 void pcg_gal_update(cudaStream_t s, long long n, const GalDirs &dd, const GalCoef &al, const double *x0, double *x);
-// *dst = max_c |r_c| / (dx dy dz)_c on level 0 (part: >= 512 doubles)
+// *dst = max_c |r_c| / (dx dy dz)_c on level 0 (part: >= pcg_stencil_parts(L0) doubles)
 void pcg_rmax(cudaStream_t s, const MgDevLevel &L0, const double *r, double *part, double *dst);
