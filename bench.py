@@ -55,6 +55,8 @@ def parse():
                     help="learned guess: fit the network candidate together with the stage's last two solutions")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--kv", type=int, default=None,
+                    help="kernel variants (turb_set_sweep_kernels flags; default: the library's)")
     ap.add_argument("--analytic-geometry", action="store_true",
                     help="keep the analytic-sdf immersed geometry instead of the reference construction")
     ap.add_argument("--cmp-steps", type=int, default=5,
@@ -351,6 +353,8 @@ def main():
     # every Poisson solve of every arm also reaches max|div u| <= 1e-10 after
     # the projection (the metric's gate), not only its relative residual
     ctx.set_divergence_gate(1e-10)
+    if a.kv is not None:
+        ctx.set_sweep_kernels(a.kv)
     pmode = api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64
     ctx.set_pressure_mode(pmode)
     guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED,

@@ -158,12 +158,15 @@ int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 int turb_set_pressure_guess(turb_ctx *ctx, int mode);
 /* RK stages whose pressure solve tries the extrapolated / learned candidate:
  * bit 0 the first stage, bit 1 the second (default 3, both) */
-/* 1 (default): the FP32 Helmholtz Jacobi sweeps and the FP32 red-black
- * half sweeps march along k through shared-memory plane tiles, and every
- * y / z ENO line is walked in segments of about 64 nodes by separate
- * threads; 0: one point (four cells) per thread and one thread per ENO line.
- * Both give the same bits. */
-int turb_set_sweep_kernels(turb_ctx *ctx, int marching);
+/* kernel variants, all giving the same bits: TURB_KV_MARCHING, the FP32
+ * Helmholtz Jacobi sweeps and FP32 red-black half sweeps march along k
+ * through shared-memory plane tiles (else one point, four cells, per thread);
+ * TURB_KV_ENO_SEGMENTS, every y / z ENO line is walked in segments of about
+ * 64 nodes by separate threads (else one thread per line).  Default:
+ * TURB_KV_ENO_SEGMENTS (measured fastest on GB300 at 512x256x256). */
+#define TURB_KV_MARCHING 1
+#define TURB_KV_ENO_SEGMENTS 2
+int turb_set_sweep_kernels(turb_ctx *ctx, int variants);
 /* max_div > 0: every Poisson solve, after reaching its relative residual,
  * also iterates until dt * max|b - A phi| (the largest divergence the
  * projection with phi leaves, dt of the last turb_Pressure_set_RHS) is at

@@ -469,9 +469,9 @@ def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):
     case = mk()
     s = _cases.random_state(case, seed=13)
     out = []
-    for marching in (False, True):
+    for variants in (0, api.KV_MARCHING | api.KV_ENO_SEGMENTS):
         ctx = api.Context(case.grid, case.params)
-        ctx.set_sweep_kernels(marching)
+        ctx.set_sweep_kernels(variants)
         ctx.load_state(s)
         for _ in range(2):
             ctx.step(case.dt)

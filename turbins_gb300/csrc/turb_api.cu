@@ -170,7 +170,9 @@ struct turb_ctx {
     double *ph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     double *pw[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // the right-hand sides W b of ph
     int galerkin = 0;   // the learned candidate goes through the Galerkin fit with the history
-    int marching = 1;   // sweep kernels that march along k through shared-memory plane tiles
+    // kernel variants (TURB_KV_*): FP32 sweeps marching along k through
+    // shared-memory plane tiles, ENO y / z lines walked in segments
+    int kvariant = TURB_KV_ENO_SEGMENTS;
     double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
     double p_dt = 0.0;           // dt of the last Pressure_set_RHS
     long long gate_tightened = 0;
@@ -1207,18 +1209,18 @@ int turb_set_pressure_guess(turb_ctx *c, int mode)
     return TURB_OK;
 }
 
-int turb_set_sweep_kernels(turb_ctx *c, int marching)
+int turb_set_sweep_kernels(turb_ctx *c, int variants)
 {
-    if (!c || (marching != 0 && marching != 1)) return TURB_ERR_ARG;
-    if (c->marching != marching) {   // captured sweep graphs hold the old kernels
+    if (!c || variants < 0 || variants > (TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS)) return TURB_ERR_ARG;
+    if ((c->kvariant ^ variants) & TURB_KV_MARCHING) {   // captured sweep graphs hold the old kernels
         for (auto &g : c->g_inner)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto &g : c->g_mg)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
-    c->marching = marching;
-    c->H64.marching = marching;
-    c->H32.marching = marching;
+    c->kvariant = variants;
+    c->H64.marching = (variants & TURB_KV_MARCHING) ? 1 : 0;
+    c->H32.marching = c->H64.marching;
     return TURB_OK;
 }
 
@@ -2129,11 +2131,11 @@ int turb_Velocity_convective_terms(turb_ctx *c, char which)
     cudaMemsetAsync(conv, 0, d.n * 8, c->s);
     const double npts = (double)d.NX * d.NY * d.NZ;
     int h = prof_begin(c, TURB_PROF_ENO_X);
-    launch_eno_pass(c->s, d, 0, c->eno[q][0], self, ax, j0, ny - 1, k0, nz - 1, 1, conv, c->marching ? 0 : 1);
+    launch_eno_pass(c->s, d, 0, c->eno[q][0], self, ax, j0, ny - 1, k0, nz - 1, 1, conv, (c->kvariant & TURB_KV_ENO_SEGMENTS) ? 0 : 1);
     prof_end(c, h, 1, ENO_X_BYTES * npts);
     h = prof_begin(c, TURB_PROF_ENO_YZ);
-    launch_eno_pass(c->s, d, 1, c->eno[q][1], self, ay, i0, nx - 1, k0, nz - 1, 0, conv, c->marching ? 0 : 1);
-    launch_eno_pass(c->s, d, 2, c->eno[q][2], self, az, i0, nx - 1, j0, ny - 1, 0, conv, c->marching ? 0 : 1);
+    launch_eno_pass(c->s, d, 1, c->eno[q][1], self, ay, i0, nx - 1, k0, nz - 1, 0, conv, (c->kvariant & TURB_KV_ENO_SEGMENTS) ? 0 : 1);
+    launch_eno_pass(c->s, d, 2, c->eno[q][2], self, az, i0, nx - 1, j0, ny - 1, 0, conv, (c->kvariant & TURB_KV_ENO_SEGMENTS) ? 0 : 1);
     prof_end(c, h, 2, 2.0 * ENO_YZ_BYTES * npts);
     c->launches += 3;
     return check_launch(c);
@@ -2154,11 +2156,11 @@ int turb_Conc_convective_terms(turb_ctx *c, int ic)
     const double npts = (double)d.NX * d.NY * d.NZ;
     int h = prof_begin(c, TURB_PROF_ENO_X);
     launch_eno_pass(c->s, d, 0, c->ob.in || c->ob.out ? c->eno_cx[ic] : c->eno[3][0], cf, ax, 0, d.ny - 1, 0,
-                    d.nz - 1, 1, conv, c->marching ? 0 : 1);
+                    d.nz - 1, 1, conv, (c->kvariant & TURB_KV_ENO_SEGMENTS) ? 0 : 1);
     prof_end(c, h, 1, ENO_X_BYTES * npts);
     h = prof_begin(c, TURB_PROF_ENO_YZ);
-    launch_eno_pass(c->s, d, 1, c->eno_cy[ic], cf, ay, 0, d.nx - 1, 0, d.nz - 1, 0, conv, c->marching ? 0 : 1);
-    launch_eno_pass(c->s, d, 2, c->eno[3][2], cf, az, 0, d.nx - 1, 0, d.ny - 1, 0, conv, c->marching ? 0 : 1);
+    launch_eno_pass(c->s, d, 1, c->eno_cy[ic], cf, ay, 0, d.nx - 1, 0, d.nz - 1, 0, conv, (c->kvariant & TURB_KV_ENO_SEGMENTS) ? 0 : 1);
+    launch_eno_pass(c->s, d, 2, c->eno[3][2], cf, az, 0, d.nx - 1, 0, d.ny - 1, 0, conv, (c->kvariant & TURB_KV_ENO_SEGMENTS) ? 0 : 1);
     prof_end(c, h, 2, 2.0 * ENO_YZ_BYTES * npts);
     c->launches += 3;
     return check_launch(c);
@@ -2282,7 +2284,8 @@ static int helm_solve_mixed(turb_ctx *c, int q, int ic, int fx, int fb, double d
         auto sweeps = [&]() {
             float *ea = c->he0, *eb = c->he1;
             for (int t = 0; t < c->hinner; t++) {
-                launch_helm_jac32(c->s, d, hf, c->st[q], (float)a_dt, c->hrf, ea, eb, ibf, t == 0, c->marching);
+                launch_helm_jac32(c->s, d, hf, c->st[q], (float)a_dt, c->hrf, ea, eb, ibf, t == 0,
+                                  c->kvariant & TURB_KV_MARCHING);
                 std::swap(ea, eb);
             }
         };

@@ -40,7 +40,7 @@ struct MgHier {
     // kernel (k_vcycle_tail); it must leave at most MG_TAIL_MAXLEV levels
     int tail_from = -1;
     // 1: FP32 half sweeps after the first of a cycle march along k (k_rbgs4z)
-    int marching = 1;
+    int marching = 0;
 };
 
 template <typename T>

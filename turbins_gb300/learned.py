@@ -101,25 +101,39 @@ def train_default(case_fn, seeds=8, steps=250, iters=3000, lr=1e-3, w_residual=1
     return params, info
 
 
-def compare(case, params, steps, pmode=A.PMODE_MIXED):
-    """Per-step PCG iterations and pressure-solve time with the previous-pressure
-    guess and with the learned guess, from the same initial state."""
+ARMS = {"previous": (A.GUESS_PREVIOUS, False), "projection": (A.GUESS_PROJECT, False),
+        "learned": (A.GUESS_LEARNED, False), "learned_galerkin": (A.GUESS_LEARNED, True)}
+
+
+def compare(case, params, steps, pmode=A.PMODE_MIXED, arms=tuple(ARMS), div_gate=1e-10):
+    """Per-step PCG iterations and pressure-solve time of each guess from the
+    same initial state: the previous pressure, the Galerkin fit over the
+    stage's last two solutions, the network candidate, and the network
+    candidate fitted together with those solutions."""
     out = {}
-    for name in ("previous", "learned"):
+    for name in arms:
+        mode, gal = ARMS[name]
         ctx = A.Context(case.grid, case.params)
         ctx.load_state(case.state)
         ctx.set_pressure_mode(pmode)
-        net = attach(ctx, params) if name == "learned" else None
+        ctx.set_divergence_gate(div_gate)
+        net = attach(ctx, params) if mode == A.GUESS_LEARNED else None
+        ctx.set_pressure_guess(mode)
+        ctx.set_guess_galerkin(gal)
         for _ in range(2):
             ctx.step(case.dt)   # history for the guess
         A.profile_enable(ctx, True)
         its = []
+        A.event_record(ctx, 0)
         for _ in range(steps):
             st = ctx.step(case.dt)
             its.append(list(st["p_iters"]))
+        A.event_record(ctx, 1)
+        ms = A.event_elapsed(ctx, 0, 1)
         prof = A.profile_read(ctx)
         tried, taken = ctx.pressure_guess_stats()
         out[name] = dict(p_iters=its, mean_iters=float(np.mean(its)), residual_ratio=ctx.pressure_guess_ratio(),
+                         step_ms=ms / steps,
                          solve_ms_per_step=sum(prof[g][0] for g in ("mg", "pcg", "net")) / steps,
                          net_ms_per_step=prof["net"][0] / steps, guess_tried=tried, guess_taken=taken)
         if net is not None:
