@@ -267,11 +267,13 @@ def run_reference(a, dist):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-# FP64 pipe instructions (thread-level DADD / DMUL / DFMA) per point of one
-# launch, from ncu counters of the kernel (smsp__sass_thread_inst_executed_op_
-# {dadd,dmul,dfma}_pred_on.sum divided by the points of the launch); see
-# profiles/fp64_ops_multi_bump_256x128x128.md.  None: not measured.
-FP64_OPS = {"eno_yz": None, "jacobi": None, "pcg": None}
+# FP64-pipe instructions per DA point of one launch of the group's kernel:
+# ncu's sm__pipe_fp64_cycles_active share x launch duration x the DFMA rate
+# measured here, divided by the launch's points, on one launch at 256x128x128
+# (profiles/fp64_pipe_multi_bump_256x128x128.md); it counts the compares and
+# moves the FP64 pipe executes besides DADD / DMUL / DFMA.  The jacobi group's
+# kernel is the FP64 Helmholtz residual (mixed defect correction).
+FP64_OPS = {"eno_yz": 21.4, "eno_x": 15.0, "jacobi": 12.1}
 
 
 def step_arm(ctx, api, dt, mode, guess, guess_stages=None):
@@ -299,9 +301,8 @@ def group_table(prof, pbytes, peak_hbm, fp64_rate, npts, ncell):
             row["hbm_frac"] = row["gbs"] / peak_hbm
         ops = FP64_OPS.get(g_)
         if ops and ms > 0 and fp64_rate:
-            pts = ncell if g_ == "pcg" else npts
-            units = nl / (2 if g_ == "eno_yz" else 1)
-            row["fp64_frac"] = ops * pts * units / (ms / 1e3) / fp64_rate
+            # every launch of these groups is one pass over the DA points
+            row["fp64_frac"] = ops * npts * nl / (ms / 1e3) / fp64_rate
         out[g_] = row
     return out
 

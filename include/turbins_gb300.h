@@ -162,10 +162,14 @@ int turb_set_pressure_guess(turb_ctx *ctx, int mode);
  * Helmholtz Jacobi sweeps and FP32 red-black half sweeps march along k
  * through shared-memory plane tiles (else one point, four cells, per thread);
  * TURB_KV_ENO_SEGMENTS, every y / z ENO line is walked in segments of about
- * 64 nodes by separate threads (else one thread per line).  Default:
+ * 64 nodes by separate threads (else one thread per line); TURB_KV_PDL,
+ * the V-cycle's kernels are launched with programmatic dependent launch, so
+ * that each may be scheduled while the one before it drains (else plain
+ * stream order).  Default:
  * TURB_KV_ENO_SEGMENTS (measured fastest on GB300 at 512x256x256). */
 #define TURB_KV_MARCHING 1
 #define TURB_KV_ENO_SEGMENTS 2
+#define TURB_KV_PDL 4   /* V-cycle kernels with programmatic dependent launch */
 int turb_set_sweep_kernels(turb_ctx *ctx, int variants);
 /* max_div > 0: every Poisson solve, after reaching its relative residual,
  * also iterates until dt * max|b - A phi| (the largest divergence the
@@ -176,7 +180,9 @@ int turb_set_divergence_gate(turb_ctx *ctx, double max_div);
 int turb_divergence_gate_count(turb_ctx *ctx, long long *tightened);
 /* 1: the learned candidate also goes through the Galerkin fit with this
  * stage's last two solutions (TURB_GUESS_PROJECT's span plus the network's
- * direction); the guard then compares the fit's residual */
+ * direction).  A fit is kept when it lowers the residual in the S^-1 norm
+ * (equivalently the S-norm of the error, the norm CG minimises); a network
+ * candidate alone when it lowers the residual's 2-norm. */
 int turb_set_guess_galerkin(turb_ctx *ctx, int on);
 int turb_set_guess_stages(turb_ctx *ctx, int mask);
 int turb_pressure_guess_stats(turb_ctx *ctx, int *tried, int *taken);

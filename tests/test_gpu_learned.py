@@ -25,13 +25,14 @@ def _case():
     return c
 
 
-def _run(A, case, state, steps, dt, guess, net=None):
+def _run(A, case, state, steps, dt, guess, net=None, galerkin=False):
     ctx = A.Context(case.grid, case.params)
     ctx.load_state(state)
     if net is not None:
         from turbins_gb300 import net as N
         N.set_learned_net(ctx, net)
     ctx.set_pressure_guess(guess)
+    ctx.set_guess_galerkin(galerkin)
     iters = []
     for _ in range(steps):
         st = ctx.step(dt)
@@ -75,18 +76,22 @@ def test_learned_guess_trains_and_gains(mods):
 
     ref, it_prev, _, _, _ = _run(A, case, state, 12, dt, A.GUESS_PREVIOUS)
     got, it_learn, tried, taken, ratio = _run(A, case, state, 12, dt, A.GUESS_LEARNED, net)
-    print("PCG iterations per step: previous %s  learned %s  (guess taken %d/%d, initial residual x%.3f)"
-          % (it_prev, it_learn, taken, tried, ratio))
+    got_g, it_gal, tried_g, taken_g, ratio_g = _run(A, case, state, 12, dt, A.GUESS_LEARNED, net, galerkin=True)
+    print("PCG iterations per step: previous %s  learned %s  (guess taken %d/%d, initial residual x%.3f)  "
+          "learned + Galerkin fit %s (taken %d/%d, x%.3f)"
+          % (it_prev, it_learn, taken, tried, ratio, it_gal, taken_g, tried_g, ratio_g))
     # what the network gains: a lower initial residual on every solve it is
-    # tried on; at rtol 1e-10 with a V-cycle per iteration (about 7x residual
-    # reduction each) that is worth at most about one iteration, so the
-    # iteration count must simply not grow
+    # tried on, and no more iterations than the previous pressure; fitted
+    # together with the stage's last two solutions (the energy-norm best
+    # guess in their span), fewer iterations in total
     assert tried > 0 and taken == tried and ratio < 0.6
-    assert sum(it_learn) <= sum(it_prev) + len(it_prev) // 4
+    assert sum(it_learn) <= sum(it_prev)
+    assert tried_g > 0 and sum(it_gal) < sum(it_prev)
     # the guess changes the iteration count, not the converged answer
     for k in ("u", "v", "w"):
         scale = max(np.abs(ref[k]).max(), 1e-30)
         assert np.abs(got[k] - ref[k]).max() <= 1e-7 * scale, k
+        assert np.abs(got_g[k] - ref[k]).max() <= 1e-7 * scale, k
     p0, p1 = ref["phi"] - ref["phi"].mean(), got["phi"] - got["phi"].mean()
     assert np.abs(p1 - p0).max() <= 1e-7 * np.abs(p0).max()
     net.close()

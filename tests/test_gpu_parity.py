@@ -463,13 +463,14 @@ def test_divergence_gate(api, oracle_mod, name, mk):
 def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):
     """The kernel variants that hide latency (FP32 Jacobi and red-black
     sweeps marching along k through shared-memory plane tiles, ENO y / z
-    lines walked in segments) give the same bits as the one-point-per-thread
-    kernels: two full steps (every convection pass and every Helmholtz and
-    Poisson solve) with either."""
+    lines walked in segments, V-cycle kernels with programmatic dependent
+    launch) give the same bits as the one-point-per-thread kernels in plain
+    stream order: two full steps (every convection pass and every Helmholtz
+    and Poisson solve) with either."""
     case = mk()
     s = _cases.random_state(case, seed=13)
     out = []
-    for variants in (0, api.KV_MARCHING | api.KV_ENO_SEGMENTS):
+    for variants in (0, api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL):
         ctx = api.Context(case.grid, case.params)
         ctx.set_sweep_kernels(variants)
         ctx.load_state(s)

@@ -26,7 +26,7 @@ F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
 PMODE_FP64, PMODE_MIXED = 0, 1
 HMODE_FP64, HMODE_MIXED = 0, 1
 GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED, GUESS_PROJECT = 0, 1, 2, 3
-KV_MARCHING, KV_ENO_SEGMENTS = 1, 2
+KV_MARCHING, KV_ENO_SEGMENTS, KV_PDL = 1, 2, 4
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed", 6: "scratch limit", 7: "restart file I/O", 8: "restart file mismatch"}
@@ -276,7 +276,7 @@ class Context:
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
     def set_sweep_kernels(self, variants=KV_ENO_SEGMENTS):
-        """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS); all give the same bits"""
+        """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL); all give the same bits"""
         _check(self.lib.turb_set_sweep_kernels(self.ctx, int(variants)), "set_sweep_kernels")
 
     def set_divergence_gate(self, max_div=1e-10):

@@ -121,6 +121,8 @@ template <typename T>
 __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restrict__ b, const T *__restrict__ invd,
                        T *__restrict__ x)
 {
+    pdl_trigger();
+    pdl_wait();
     LevelT<T> L = lev_of<T>(Ld);
     int i2 = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (j >= L.ny) return;
@@ -137,6 +139,8 @@ __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restr
 __global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__restrict__ b,
                         const float *__restrict__ invd, float *__restrict__ x)
 {
+    pdl_trigger();
+    pdl_wait();
     const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
     int q4 = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (j >= ny || 4 * q4 >= hx) return;
@@ -199,6 +203,8 @@ constexpr int RTX = 4 * 32 + 2;
 __global__ void __launch_bounds__(256, 3) k_rbgs4z(MgDevLevel Ld, int color, int jz, const float *__restrict__ b,
                                                    const float *__restrict__ invd, float *__restrict__ x)
 {
+    pdl_trigger();
+    pdl_wait();
     __shared__ float tile[8 + 2][RTX];
     const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -303,6 +309,8 @@ __device__ __forceinline__ void resid_cell(const LevelT<T> &L, const T *__restri
 template <typename T>
 __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r)
 {
+    pdl_trigger();
+    pdl_wait();
     LevelT<T> L = lev_of<T>(Ld);
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (i >= L.nx || j >= L.ny) return;
@@ -316,6 +324,8 @@ __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restr
 // natural order the restriction reads.  Per cell the arithmetic is s_row's.
 __global__ void k_resid8(MgDevLevel Ld, const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ r)
 {
+    pdl_trigger();
+    pdl_wait();
     const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
     int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (j >= ny || 4 * q >= hx) return;
@@ -439,6 +449,8 @@ __device__ __forceinline__ void prolong_cell(const MgDevLevel &Lf, const MgDevLe
 template <typename T>
 __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ rf, T *__restrict__ bc)
 {
+    pdl_trigger();
+    pdl_wait();
     int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
     if (I >= Lc.nx || J >= Lc.ny) return;
     restrict_cell<T>(Lf, Lc, rf, bc, I, J, K);
@@ -447,6 +459,8 @@ __global__ void k_restrict(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ r
 template <typename T>
 __global__ void k_prolong(MgDevLevel Lf, MgDevLevel Lc, const T *__restrict__ xc, T *__restrict__ xf)
 {
+    pdl_trigger();
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (i >= Lf.nx || j >= Lf.ny) return;
     prolong_cell<T>(Lf, Lc, xc, xf, i, j, k);
@@ -489,6 +503,8 @@ __device__ __forceinline__ void st8(const MgDevLevel &L, float *a, int i0, int j
 // storage order
 __global__ void k_restrict_yz8(MgDevLevel Lf, MgDevLevel Lc, const float *__restrict__ rf, float *__restrict__ bc)
 {
+    pdl_trigger();
+    pdl_wait();
     const int q = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
     if (8 * q >= Lc.nx || J >= Lc.ny) return;
     const int i0 = 8 * q;
@@ -513,6 +529,8 @@ __global__ void k_restrict_yz8(MgDevLevel Lf, MgDevLevel Lc, const float *__rest
 // prolongation where x is not coarsened, eight cells of a fine row per thread
 __global__ void k_prolong_yz8(MgDevLevel Lf, MgDevLevel Lc, const float *__restrict__ xc, float *__restrict__ xf)
 {
+    pdl_trigger();
+    pdl_wait();
     const int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (8 * q >= Lf.nx || j >= Lf.ny) return;
     const int i0 = 8 * q;
@@ -551,6 +569,8 @@ __device__ __forceinline__ void coarse_row(int n, const double *__restrict__ ain
 template <typename T>
 __global__ void k_coarse(int n, const double *__restrict__ ainv, const T *__restrict__ b, T *__restrict__ x)
 {
+    pdl_trigger();
+    pdl_wait();
     int r = threadIdx.x;
     if (r >= n) return;
     coarse_row<T>(n, ainv, b, x, r);
@@ -591,6 +611,8 @@ __device__ void tail_half(const MgDevLevel &Ld, int color, int zero_init, const 
 template <typename T>
 __global__ void __launch_bounds__(TAIL_THREADS) k_vcycle_tail(const TailArgs<T> a)
 {
+    pdl_trigger();
+    pdl_wait();
     const int last = a.nlev - 1;
     for (int l = 0; l < last; l++) {
         const MgDevLevel &Ld = a.L[l];
@@ -641,6 +663,8 @@ __global__ void k_to_float_lev(MgDevLevel L, const double *__restrict__ a, float
 }
 __global__ void k_to_double_lev(MgDevLevel L, const float *__restrict__ a, double *__restrict__ b)
 {
+    pdl_trigger();
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     if (i >= L.nx || j >= L.ny) return;
     long long c = ((long long)k * L.ny + j) * L.nx + i;
@@ -648,6 +672,29 @@ __global__ void k_to_double_lev(MgDevLevel L, const float *__restrict__ a, doubl
 }
 
 inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+// a V-cycle kernel launch; pdl: with the programmatic stream serialisation
+// attribute (the kernels start with pdl_trigger / pdl_wait), so that a small
+// level's launches overlap the drain of the kernel before them
+template <typename... P, typename... A>
+void launch_k(int pdl, void (*k)(P...), dim3 g, dim3 b, cudaStream_t s, A... args)
+{
+    if (!pdl) {
+        k<<<g, b, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
 inline dim3 g3(int nx, int ny, int nz) { return dim3((unsigned)((nx + 31) / 32), (unsigned)((ny + 7) / 8), (unsigned)nz); }
 const dim3 B38(32, 8, 1);
 
@@ -666,7 +713,7 @@ void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd)
 // on the levels large enough to fill the GPU with them
 template <typename T>
 void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, const T *b, const T *invd, T *x,
-             int marching)
+             int marching, int pdl)
 {
     if constexpr (sizeof(T) == 4) {
         if (L.split && L.nx % 8 == 0) {
@@ -679,28 +726,28 @@ void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, cons
                 while (jz > 2 && bxy * ((L.nz + jz - 1) / jz) < 2 * 3 * 152) jz >>= 1;
                 if (bxy * ((L.nz + jz - 1) / jz) >= 152) {
                     dim3 gz(g4.x, g4.y, (unsigned)((L.nz + jz - 1) / jz));
-                    k_rbgs4z<<<gz, B38, 0, s>>>(L, color, jz, b, invd, x);
+                    launch_k(pdl, k_rbgs4z, gz, B38, s, L, color, jz, b, invd, x);
                     return;
                 }
             }
-            k_rbgs4<<<g4, B38, 0, s>>>(L, color, zero_init, b, invd, x);
+            launch_k(pdl, k_rbgs4, g4, B38, s, L, color, zero_init, b, invd, x);
             return;
         }
     }
-    k_rbgs<T><<<g3((L.nx + 1) >> 1, L.ny, L.nz), B38, 0, s>>>(L, color, zero_init, b, invd, x);
+    launch_k(pdl, k_rbgs<T>, g3((L.nx + 1) >> 1, L.ny, L.nz), B38, s, L, color, zero_init, b, invd, x);
 }
 
 template <typename T>
-void resid_lev(cudaStream_t s, const MgDevLevel &L, const T *b, const T *x, T *r)
+void resid_lev(cudaStream_t s, const MgDevLevel &L, const T *b, const T *x, T *r, int pdl)
 {
     if constexpr (sizeof(T) == 4) {
         if (L.split && L.nx % 8 == 0) {
             dim3 g8((unsigned)((L.nx / 8 + 31) / 32), (unsigned)((L.ny + 7) / 8), (unsigned)L.nz);
-            k_resid8<<<g8, B38, 0, s>>>(L, b, x, r);
+            launch_k(pdl, k_resid8, g8, B38, s, L, b, x, r);
             return;
         }
     }
-    k_resid<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, b, x, r);
+    launch_k(pdl, k_resid<T>, g3(L.nx, L.ny, L.nz), B38, s, L, b, x, r);
 }
 
 template <typename T>
@@ -722,37 +769,37 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
             a.post[t] = post[l + t];
         }
         a.coarse_inv = H.coarse_inv;
-        k_vcycle_tail<T><<<1, TAIL_THREADS, 0, s>>>(a);
+        launch_k(H.pdl, k_vcycle_tail<T>, dim3(1), dim3(TAIL_THREADS), s, a);
         return;
     }
     if (l == H.nl - 1) {
-        k_coarse<T><<<1, 64, 0, s>>>((int)n, H.coarse_inv, H.b[l], H.x[l]);
+        launch_k(H.pdl, k_coarse<T>, dim3(1), dim3(64), s, (int)n, H.coarse_inv, H.b[l], H.x[l]);
         return;
     }
     for (int it = 0; it < npre; it++) {
         // the first colour-0 half sweep takes x = 0 (it reads no neighbours);
         // every colour-1 point is then rewritten from colour-0 values only
-        rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l], H.marching);
-        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching);
+        rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
+        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
     }
-    resid_lev<T>(s, L, H.b[l], H.x[l], H.r[l]);
+    resid_lev<T>(s, L, H.b[l], H.x[l], H.r[l], H.pdl);
     const MgDevLevel &C = H.lev[l + 1];
     bool yz8 = false;
     if constexpr (sizeof(T) == 4) yz8 = L.cx == 0 && L.nx % 8 == 0 && C.nx == L.nx;
     if (yz8) {
         if constexpr (sizeof(T) == 4) {
-            k_restrict_yz8<<<g3((C.nx / 8 + 31) / 32 * 32, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
+            launch_k(H.pdl, k_restrict_yz8, g3((C.nx / 8 + 31) / 32 * 32, C.ny, C.nz), B38, s, L, C, H.r[l], H.b[l + 1]);
             mg_vcycle<T>(s, H, l + 1, pre, post);
-            k_prolong_yz8<<<g3((L.nx / 8 + 31) / 32 * 32, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+            launch_k(H.pdl, k_prolong_yz8, g3((L.nx / 8 + 31) / 32 * 32, L.ny, L.nz), B38, s, L, C, H.x[l + 1], H.x[l]);
         }
     } else {
-        k_restrict<T><<<g3(C.nx, C.ny, C.nz), B38, 0, s>>>(L, C, H.r[l], H.b[l + 1]);
+        launch_k(H.pdl, k_restrict<T>, g3(C.nx, C.ny, C.nz), B38, s, L, C, H.r[l], H.b[l + 1]);
         mg_vcycle<T>(s, H, l + 1, pre, post);
-        k_prolong<T><<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, C, H.x[l + 1], H.x[l]);
+        launch_k(H.pdl, k_prolong<T>, g3(L.nx, L.ny, L.nz), B38, s, L, C, H.x[l + 1], H.x[l]);
     }
     for (int it = 0; it < npost; it++) {
-        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching);
-        rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l], H.marching);
+        rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
+        rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
     }
 }
 
@@ -760,9 +807,9 @@ void mg_to_float(cudaStream_t s, const MgDevLevel &L, const double *a, float *b)
 {
     k_to_float_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
-void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b)
+void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b, int pdl)
 {
-    k_to_double_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
+    launch_k(pdl, k_to_double_lev, g3(L.nx, L.ny, L.nz), B38, s, L, a, b);
 }
 
 // Algorithmic bytes of one V-cycle from level l (each array a kernel reads

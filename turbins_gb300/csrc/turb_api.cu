@@ -1211,8 +1211,8 @@ int turb_set_pressure_guess(turb_ctx *c, int mode)
 
 int turb_set_sweep_kernels(turb_ctx *c, int variants)
 {
-    if (!c || variants < 0 || variants > (TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS)) return TURB_ERR_ARG;
-    if ((c->kvariant ^ variants) & TURB_KV_MARCHING) {   // captured sweep graphs hold the old kernels
+    if (!c || variants < 0 || variants > (TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS | TURB_KV_PDL)) return TURB_ERR_ARG;
+    if ((c->kvariant ^ variants) & (TURB_KV_MARCHING | TURB_KV_PDL)) {   // captured graphs hold the old launches
         for (auto &g : c->g_inner)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto &g : c->g_mg)
@@ -1221,6 +1221,8 @@ int turb_set_sweep_kernels(turb_ctx *c, int variants)
     c->kvariant = variants;
     c->H64.marching = (variants & TURB_KV_MARCHING) ? 1 : 0;
     c->H32.marching = c->H64.marching;
+    c->H64.pdl = (variants & TURB_KV_PDL) ? 1 : 0;
+    c->H32.pdl = c->H64.pdl;
     return TURB_OK;
 }
 
@@ -2375,8 +2377,11 @@ int turb_Pressure_set_RHS(turb_ctx *c, double dt)
 // to their tolerance) and the network candidate (pz, computed residual pq),
 // the coefficients minimise the S-norm of the error: (D^T S D) a = D^T r.
 // Directions whose pivot is negligible are dropped.  The fit goes to pp,
-// its true residual to pro; *nr_out = |pro| (0 when no fit was made).
-static int galerkin_guess(turb_ctx *c, int st, int with_net, double *nr_out)
+// its true residual to pro; *nr_out = |pro| (0 when no fit was made) and
+// *de_out = -a^T g / 2, the change of the energy 1/2 x^T S x - x^T W b from
+// x0 to the fit (< 0: a smaller S-norm of the error, equivalently a smaller
+// S^-1-norm of the residual, the norm CG minimises).
+static int galerkin_guess(turb_ctx *c, int st, int with_net, double *nr_out, double *de_out)
 {
     const MgDevLevel &L0 = c->H64.lev[0];
     long long n0 = (long long)L0.nx * L0.ny * L0.nz;
@@ -2396,6 +2401,7 @@ static int galerkin_guess(turb_ctx *c, int st, int with_net, double *nr_out)
         dd.nd++;
     }
     *nr_out = 0.0;
+    *de_out = 0.0;
     pcg_gal_dots(s, n0, dd, c->px, c->pr, c->pbw, c->part, c->dscal);
     const int nv = GAL_MAX * GAL_MAX + GAL_MAX;
     TURB_CHECK(cudaMemcpyAsync(c->hscal, c->dscal, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -2439,7 +2445,12 @@ static int galerkin_guess(turb_ctx *c, int st, int with_net, double *nr_out)
         al[a] = t / L[a][a];
     }
     GalCoef co;
-    for (int a = 0; a < GAL_MAX; a++) co.a[a] = a < n && keep[a] && std::isfinite(al[a]) ? al[a] : 0.0;
+    double de = 0.0;
+    for (int a = 0; a < GAL_MAX; a++) {
+        co.a[a] = a < n && keep[a] && std::isfinite(al[a]) ? al[a] : 0.0;
+        if (a < n) de -= 0.5 * co.a[a] * g[a];
+    }
+    *de_out = de;
     pcg_gal_update(s, n0, dd, co, c->px, c->pp);
     pcg_resid(s, L0, c->pbw, c->pp, c->pro, c->part);
     pcg_reduce(s, c->part, 1, c->dscal, pcg_stencil_parts(L0));
@@ -2479,7 +2490,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         c->launches += 5;
     }
     if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2 && ((c->guess_stages >> st) & 1)) {
-        int ok = 0, ph = -1;
+        int ok = 0, ph = -1, fitted = 0;
         double nrc = 0.0;
         if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
             pcg_lincomb(s, n0, 2.0, c->ph[st][0], -1.0, c->ph[st][1], c->pz);
@@ -2507,10 +2518,14 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         // network candidate): the energy-norm best guess in their span
         if ((c->guess_mode == TURB_GUESS_PROJECT || (c->guess_mode == TURB_GUESS_LEARNED && c->galerkin && ok)) &&
             c->pw[st][1]) {
-            double ng = 0.0;
-            int rc = galerkin_guess(c, st, ok && c->guess_mode == TURB_GUESS_LEARNED, &ng);
+            double ng = 0.0, de = 0.0;
+            int rc = galerkin_guess(c, st, ok && c->guess_mode == TURB_GUESS_LEARNED, &ng, &de);
             if (rc) return rc;
-            if (ng > 0.0 && (!ok || ng < nrc)) {   // the fit is in pp / pro
+            // the fit minimises the S-norm of the error over a span that holds
+            // x0 and the network candidate: it is kept whenever it lowers the
+            // residual in the S^-1 norm (de < 0), the norm CG reduces
+            fitted = ng > 0.0 && de < 0.0;
+            if (fitted) {   // the fit is in pp / pro
                 std::swap(c->pz, c->pp);
                 std::swap(c->pq, c->pro);
                 nrc = ng;
@@ -2520,7 +2535,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         if (ok) {
             c->guess_tried++;
             if (nr > 0.0 && nrc > 0.0 && std::isfinite(nrc)) c->guess_logsum += std::log(nrc / nr);
-            if (nrc < nr) {
+            if (fitted || nrc < nr) {
                 pcg_copy(s, n0, c->pz, c->px);
                 pcg_copy(s, n0, c->pq, c->pr);
                 c->launches += 2;
@@ -2569,7 +2584,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
             } else {
                 mg_to_float(s, c->H32.lev[0], c->pr, c->H32.b[0]);
                 mg_vcycle<float>(s, c->H32, 0, npre, npost);
-                mg_to_double(s, c->H32.lev[0], c->H32.x[0], c->pz);
+                mg_to_double(s, c->H32.lev[0], c->H32.x[0], c->pz, c->H32.pdl);
             }
         };
         auto cgstep = [&](int rs) {

@@ -134,6 +134,15 @@ __device__ __forceinline__ double turb_nanmax(double a, double b)
     return (a != a || a > b) ? a : b;
 }
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream serialisation attribute may be scheduled while the kernel before it
+// on the stream drains; pdl_wait (before its first global-memory access)
+// holds it until that kernel has completed and its writes are visible, and
+// pdl_trigger lets the kernel after it be scheduled early.  In a kernel
+// launched without the attribute both return at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 #define TURB_CHECK(x)                                                          \
     do {                                                                       \
         cudaError_t e_ = (x);                                                  \

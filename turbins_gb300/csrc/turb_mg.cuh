@@ -41,6 +41,8 @@ struct MgHier {
     int tail_from = -1;
     // 1: FP32 half sweeps after the first of a cycle march along k (k_rbgs4z)
     int marching = 0;
+    // 1: the V-cycle's kernels after its first use programmatic dependent launch
+    int pdl = 0;
 };
 
 template <typename T>
@@ -73,7 +75,7 @@ void pcg_to_float(cudaStream_t s, long long n, const double *a, float *b);
 void pcg_to_double(cudaStream_t s, long long n, const float *a, double *b);
 // the same into / out of a level's storage order (colour-split or not)
 void mg_to_float(cudaStream_t s, const MgDevLevel &L, const double *a, float *b);
-void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b);
+void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b, int pdl = 0);
 void pcg_copy(cudaStream_t s, long long n, const double *a, double *b);
 int pcg_nparts();
 void pcg_lincomb(cudaStream_t s, long long n, double a, const double *x, double b, const double *y, double *out);
