@@ -269,11 +269,21 @@ def run_reference(a, dist):
 # ---------------------------------------------------------------------------
 # FP64-pipe instructions per DA point of one launch of the group's kernel:
 # ncu's sm__pipe_fp64_cycles_active share x launch duration x the DFMA rate
-# measured here, divided by the launch's points, on one launch at 256x128x128
-# (profiles/fp64_pipe_multi_bump_256x128x128.md); it counts the compares and
-# moves the FP64 pipe executes besides DADD / DMUL / DFMA.  The jacobi group's
-# kernel is the FP64 Helmholtz residual (mixed defect correction).
-FP64_OPS = {"eno_yz": 21.4, "eno_x": 15.0, "jacobi": 12.1}
+# measured here, divided by the launch's points, on single launches at
+# 256x128x128 (profiles/fp64_pipe_multi_bump_256x128x128.md); this counts the
+# compares and moves the FP64 pipe executes besides DADD / DMUL / DFMA.  A
+# pass advected by a bilinear transpose of another velocity costs 21.4
+# (y / z) or 21.8 (x) per point, a self-advected one 15.0; a step's passes
+# mix them 4:6 (y / z) and 2:3 (x).  The jacobi group's kernel is the FP64
+# Helmholtz residual.
+FP64_OPS = {"eno_yz": 17.6, "eno_x": 17.7, "jacobi": 12.1}
+
+# DRAM bytes of one V-cycle of the mixed method at 512x256x256 (all its
+# kernels, dram__bytes_read.sum + dram__bytes_write.sum, one ncu pass;
+# profiles/vcycle_dram_multi_bump_512x256x256.md): 7.18 GB over its 198
+# launches, against 8.42 GB of algorithmic bytes (the coarse levels stay in
+# L2).  Per launch, as the roofline's traffic of the mg group.
+MG_TRAFFIC_PER_LAUNCH = 7.18e9 / 198
 
 
 def step_arm(ctx, api, dt, mode, guess, guess_stages=None):
@@ -462,7 +472,9 @@ def main():
     roof = {"bound": "tensor" if dom == "net" else "hbm", "kernel_group": dom,
             "achieved": d.get("gbs"), "peak": peak, "unit": "GB/s", "frac": d.get("hbm_frac"),
             "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_src,
-            "traffic": None, "algorithmic_bytes_per_launch": pbytes.get(dom, 0.0) / max(d["launches"], 1),
+            "traffic": MG_TRAFFIC_PER_LAUNCH if dom == "mg" and (a.nx, a.ny, a.nz) == (512, 256, 256) else None,
+            "traffic_source": "ncu dram bytes of one V-cycle at 512x256x256, per launch" if dom == "mg" else None,
+            "algorithmic_bytes_per_launch": pbytes.get(dom, 0.0) / max(d["launches"], 1),
             "ms_per_launch": d["ms"] / max(d["launches"], 1), "launches": d["launches"],
             "fp64_rate_dfma_per_s": fp64_rate, "groups": groups}
     if learned_info is not None and prof["net"][1]:

@@ -165,8 +165,8 @@ int turb_set_pressure_guess(turb_ctx *ctx, int mode);
  * 64 nodes by separate threads (else one thread per line); TURB_KV_PDL,
  * the V-cycle's kernels are launched with programmatic dependent launch, so
  * that each may be scheduled while the one before it drains (else plain
- * stream order).  Default:
- * TURB_KV_ENO_SEGMENTS (measured fastest on GB300 at 512x256x256). */
+ * stream order).  Default: TURB_KV_ENO_SEGMENTS | TURB_KV_PDL (measured
+ * fastest on GB300 at 512x256x256). */
 #define TURB_KV_MARCHING 1
 #define TURB_KV_ENO_SEGMENTS 2
 #define TURB_KV_PDL 4   /* V-cycle kernels with programmatic dependent launch */

@@ -275,7 +275,7 @@ class Context:
     def set_pressure_guess(self, mode):
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
-    def set_sweep_kernels(self, variants=KV_ENO_SEGMENTS):
+    def set_sweep_kernels(self, variants=KV_ENO_SEGMENTS | KV_PDL):
         """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL); all give the same bits"""
         _check(self.lib.turb_set_sweep_kernels(self.ctx, int(variants)), "set_sweep_kernels")
 

@@ -172,7 +172,7 @@ struct turb_ctx {
     int galerkin = 0;   // the learned candidate goes through the Galerkin fit with the history
     // kernel variants (TURB_KV_*): FP32 sweeps marching along k through
     // shared-memory plane tiles, ENO y / z lines walked in segments
-    int kvariant = TURB_KV_ENO_SEGMENTS;
+    int kvariant = TURB_KV_ENO_SEGMENTS | TURB_KV_PDL;
     double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
     double p_dt = 0.0;           // dt of the last Pressure_set_RHS
     long long gate_tightened = 0;

@@ -41,8 +41,8 @@ struct MgHier {
     int tail_from = -1;
     // 1: FP32 half sweeps after the first of a cycle march along k (k_rbgs4z)
     int marching = 0;
-    // 1: the V-cycle's kernels after its first use programmatic dependent launch
-    int pdl = 0;
+    // 1: the V-cycle's kernels use programmatic dependent launch
+    int pdl = 1;
 };
 
 template <typename T>
