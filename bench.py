@@ -14,8 +14,9 @@ one rank per GPU, and reports the aggregate over ranks.  ``value`` is the
 device-timed throughput with all fields resident in HBM; ``e2e`` is the same
 step driven through the C ABI with the state copied host->device before and
 device->host after every step.  The reference arm times the CPU oracle port
-of the same step on a bounded sample of the workload, one process per host
-core (the reference parallelises only over MPI ranks).
+of the same step on the whole grid, split into one x-slab per host core,
+each stepped in its own process (the reference parallelises only over MPI
+ranks), for at most about 4 minutes of timed steps.
 """
 from __future__ import annotations
 
