@@ -165,11 +165,16 @@ int turb_set_pressure_guess(turb_ctx *ctx, int mode);
  * 64 nodes by separate threads (else one thread per line); TURB_KV_PDL,
  * the V-cycle's kernels are launched with programmatic dependent launch, so
  * that each may be scheduled while the one before it drains (else plain
- * stream order).  Default: TURB_KV_ENO_SEGMENTS | TURB_KV_PDL (measured
- * fastest on GB300 at 512x256x256). */
+ * stream order); TURB_KV_CLUSTER_VCYCLE, the V-cycle from the first level
+ * of at most turb_set_mg_cluster cells down runs as one launch of one
+ * thread-block cluster (16 blocks of 1024 threads, or 8 where 16 do not fit),
+ * its phases separated by the hardware cluster barrier.  Default:
+ * TURB_KV_ENO_SEGMENTS | TURB_KV_PDL (measured fastest on GB300 at
+ * 512x256x256). */
 #define TURB_KV_MARCHING 1
 #define TURB_KV_ENO_SEGMENTS 2
 #define TURB_KV_PDL 4   /* V-cycle kernels with programmatic dependent launch */
+#define TURB_KV_CLUSTER_VCYCLE 8   /* coarse V-cycle levels in one thread-block cluster */
 int turb_set_sweep_kernels(turb_ctx *ctx, int variants);
 /* max_div > 0: every Poisson solve, after reaching its relative residual,
  * also iterates until dt * max|b - A phi| (the largest divergence the
@@ -201,6 +206,11 @@ int turb_set_mg_coarse_sweeps(turb_ctx *ctx, int from_level, int npre, int npost
  * 4096; 0: never) down to the coarsest and back runs as one single-block
  * kernel instead of a launch per half sweep; results are bit-identical */
 int turb_set_mg_tail(turb_ctx *ctx, long long max_cells);
+/* with TURB_KV_CLUSTER_VCYCLE, the V-cycle from the first level of at most
+ * max_cells cells (default 131072; 0: never) runs as one thread-block
+ * cluster launch, the levels from the single-block tail's on in block 0 of
+ * it; results are bit-identical */
+int turb_set_mg_cluster(turb_ctx *ctx, long long max_cells);
 /* storage order of the FP32 multigrid levels: 1 (default) colour-split (red
  * and black cells in separate halves, dense half sweeps), 0 natural.  The
  * arithmetic is the same, so results are bit-identical either way. */

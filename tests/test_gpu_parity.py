@@ -470,7 +470,8 @@ def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):
     case = mk()
     s = _cases.random_state(case, seed=13)
     out = []
-    for variants in (0, api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL):
+    for variants in (0, api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL,
+                     api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL | api.KV_CLUSTER_VCYCLE):
         ctx = api.Context(case.grid, case.params)
         ctx.set_sweep_kernels(variants)
         ctx.load_state(s)
@@ -478,5 +479,36 @@ def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):
             ctx.step(case.dt)
         out.append(ctx.state())
         ctx.close()
-    for k in out[0]:
-        assert np.array_equal(out[0][k], out[1][k]), k
+    for o in out[1:]:
+        for k in out[0]:
+            assert np.array_equal(out[0][k], o[k]), k
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("cells,tail", [(1 << 17, 4096), (1 << 20, 4096), (1 << 17, 0)])
+def test_cluster_vcycle_is_bit_identical(api, mode, cells, tail):
+    """The one-cluster V-cycle (every level from the first of at most `cells`
+    cells in one thread-block cluster launch, phases separated by the
+    cluster barrier; the single-block tail's levels in block 0 of it, or
+    every level cluster-wide when the tail is off) gives the same Poisson
+    iterates as a launch per half sweep, in either pressure mode, on a
+    256x128x128 grid whose finest levels still run as separate launches."""
+    from turbins_gb300 import workload as W
+    case = W.poisson_case(256, 128, 128, (16.0, 2.0, 2.0), 1.5)
+    vel = W.fourier_velocity(case.grid, 3)
+    out = []
+    for variants in (api.KV_ENO_SEGMENTS | api.KV_PDL, api.KV_ENO_SEGMENTS | api.KV_PDL | api.KV_CLUSTER_VCYCLE):
+        ctx = api.Context(case.grid, case.params)
+        ctx.set_sweep_kernels(variants)
+        ctx.set_mg_cluster(cells)
+        ctx.set_mg_tail(tail)
+        ctx.set_pressure_mode(api.PMODE_FP64 if mode == "fp64" else api.PMODE_MIXED)
+        for f, k in ((api.F_U, "u"), (api.F_V, "v"), (api.F_W, "w")):
+            ctx.upload(f, vel[k])
+        ctx.upload(api.F_PHI, np.zeros(case.grid.shape))
+        ctx.Pressure_set_RHS(1.0)
+        it, rr = ctx.Pressure_solve()
+        out.append((it, rr, ctx.download(api.F_PHI)))
+        ctx.close()
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])

@@ -26,7 +26,7 @@ F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
 PMODE_FP64, PMODE_MIXED = 0, 1
 HMODE_FP64, HMODE_MIXED = 0, 1
 GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED, GUESS_PROJECT = 0, 1, 2, 3
-KV_MARCHING, KV_ENO_SEGMENTS, KV_PDL = 1, 2, 4
+KV_MARCHING, KV_ENO_SEGMENTS, KV_PDL, KV_CLUSTER_VCYCLE = 1, 2, 4, 8
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed", 6: "scratch limit", 7: "restart file I/O", 8: "restart file mismatch"}
@@ -276,7 +276,7 @@ class Context:
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
     def set_sweep_kernels(self, variants=KV_ENO_SEGMENTS | KV_PDL):
-        """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL); all give the same bits"""
+        """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL | KV_CLUSTER_VCYCLE); all give the same bits"""
         _check(self.lib.turb_set_sweep_kernels(self.ctx, int(variants)), "set_sweep_kernels")
 
     def set_divergence_gate(self, max_div=1e-10):
@@ -304,6 +304,10 @@ class Context:
     def set_mg_tail(self, max_cells):
         """turb_set_mg_tail: single-block V-cycle below max_cells cells (0: off)"""
         _check(self.lib.turb_set_mg_tail(self.ctx, C.c_longlong(int(max_cells))), "set_mg_tail")
+
+    def set_mg_cluster(self, max_cells):
+        """turb_set_mg_cluster: one-cluster V-cycle below max_cells cells (0: off), with KV_CLUSTER_VCYCLE"""
+        _check(self.lib.turb_set_mg_cluster(self.ctx, C.c_longlong(int(max_cells))), "set_mg_cluster")
 
     def set_mg_coarse_sweeps(self, from_level, npre, npost):
         """turb_set_mg_coarse_sweeps: levels >= from_level use npre / npost"""

@@ -653,6 +653,122 @@ __global__ void __launch_bounds__(TAIL_THREADS) k_vcycle_tail(const TailArgs<T> 
     }
 }
 
+// The V-cycle from level l0 down and back in one launch of one thread-block
+// cluster (CLUSTER_CTAS blocks on as many SMs): the first ncl levels are
+// swept by every block of the cluster, phases separated by the hardware
+// cluster barrier (release / acquire at cluster scope, so the global-memory
+// writes of one phase are seen by every block in the next); the levels below
+// by block 0 alone with block barriers (the single-block tail above) while
+// the other blocks wait at the next cluster barrier.  Every cell's
+// operations are those of the per-launch kernels (rb_cell, resid_cell,
+// restrict_cell, prolong_cell), so the iterates are the same bits.  Every
+// block passes the same sequence of cluster barriers.
+constexpr int CLUSTER_THREADS = TAIL_THREADS;
+
+template <typename T>
+struct ClusterArgs {
+    int nlev, ncl;
+    MgDevLevel L[MG_CLUSTER_MAXLEV];
+    T *x[MG_CLUSTER_MAXLEV], *b[MG_CLUSTER_MAXLEV], *r[MG_CLUSTER_MAXLEV];
+    const T *invd[MG_CLUSTER_MAXLEV];
+    int pre[MG_CLUSTER_MAXLEV], post[MG_CLUSTER_MAXLEV];
+    const double *coarse_inv;
+};
+
+__device__ __forceinline__ void cluster_barrier()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <typename T>
+__device__ void cluster_half(const MgDevLevel &Ld, int color, int zero_init, const T *b, const T *invd, T *x)
+{
+    LevelT<T> L = lev_of<T>(Ld);
+    const int hx = (L.nx + 1) >> 1;
+    const int n2 = hx * L.ny * L.nz;
+    for (int t = blockIdx.x * CLUSTER_THREADS + threadIdx.x; t < n2; t += gridDim.x * CLUSTER_THREADS) {
+        const int i2 = t % hx, q = t / hx;
+        const int j = q % L.ny, k = q / L.ny;
+        const int i = 2 * i2 + ((j + k + color) & 1);
+        if (i < L.nx) rb_cell<T>(L, zero_init, b, invd, x, i, j, k);
+    }
+    cluster_barrier();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CLUSTER_THREADS) k_vcycle_cluster(const ClusterArgs<T> a)
+{
+    pdl_trigger();
+    pdl_wait();
+    const int last = a.nlev - 1, ncl = min(a.ncl, last);
+    const int gstride = gridDim.x * CLUSTER_THREADS, g0 = blockIdx.x * CLUSTER_THREADS + threadIdx.x;
+    for (int l = 0; l < ncl; l++) {
+        const MgDevLevel &Ld = a.L[l];
+        for (int it = 0; it < a.pre[l]; it++) {
+            cluster_half<T>(Ld, 0, it == 0, a.b[l], a.invd[l], a.x[l]);
+            cluster_half<T>(Ld, 1, 0, a.b[l], a.invd[l], a.x[l]);
+        }
+        LevelT<T> L = lev_of<T>(Ld);
+        const int n = L.nx * L.ny * L.nz;
+        for (int c = g0; c < n; c += gstride)
+            resid_cell<T>(L, a.b[l], a.x[l], a.r[l], c % L.nx, (c / L.nx) % L.ny, c / (L.nx * L.ny));
+        cluster_barrier();
+        const MgDevLevel &C = a.L[l + 1];
+        const int nc = C.nx * C.ny * C.nz;
+        for (int c = g0; c < nc; c += gstride)
+            restrict_cell<T>(Ld, C, a.r[l], a.b[l + 1], c % C.nx, (c / C.nx) % C.ny, c / (C.nx * C.ny));
+        cluster_barrier();
+    }
+    if (blockIdx.x == 0) {   // the small levels: block 0 alone
+        for (int l = ncl; l < last; l++) {
+            const MgDevLevel &Ld = a.L[l];
+            for (int it = 0; it < a.pre[l]; it++) {
+                tail_half<T>(Ld, 0, it == 0, a.b[l], a.invd[l], a.x[l]);
+                tail_half<T>(Ld, 1, 0, a.b[l], a.invd[l], a.x[l]);
+            }
+            LevelT<T> L = lev_of<T>(Ld);
+            const int n = L.nx * L.ny * L.nz;
+            for (int c = threadIdx.x; c < n; c += CLUSTER_THREADS)
+                resid_cell<T>(L, a.b[l], a.x[l], a.r[l], c % L.nx, (c / L.nx) % L.ny, c / (L.nx * L.ny));
+            __syncthreads();
+            const MgDevLevel &C = a.L[l + 1];
+            const int nc = C.nx * C.ny * C.nz;
+            for (int c = threadIdx.x; c < nc; c += CLUSTER_THREADS)
+                restrict_cell<T>(Ld, C, a.r[l], a.b[l + 1], c % C.nx, (c / C.nx) % C.ny, c / (C.nx * C.ny));
+            __syncthreads();
+        }
+        {
+            const MgDevLevel &C = a.L[last];
+            const int n = C.nx * C.ny * C.nz;
+            for (int r = threadIdx.x; r < n; r += CLUSTER_THREADS) coarse_row<T>(n, a.coarse_inv, a.b[last], a.x[last], r);
+            __syncthreads();
+        }
+        for (int l = last - 1; l >= ncl; l--) {
+            const MgDevLevel &Ld = a.L[l], &C = a.L[l + 1];
+            const int n = Ld.nx * Ld.ny * Ld.nz;
+            for (int c = threadIdx.x; c < n; c += CLUSTER_THREADS)
+                prolong_cell<T>(Ld, C, a.x[l + 1], a.x[l], c % Ld.nx, (c / Ld.nx) % Ld.ny, c / (Ld.nx * Ld.ny));
+            __syncthreads();
+            for (int it = 0; it < a.post[l]; it++) {
+                tail_half<T>(Ld, 1, 0, a.b[l], a.invd[l], a.x[l]);
+                tail_half<T>(Ld, 0, 0, a.b[l], a.invd[l], a.x[l]);
+            }
+        }
+    }
+    cluster_barrier();
+    for (int l = ncl - 1; l >= 0; l--) {
+        const MgDevLevel &Ld = a.L[l], &C = a.L[l + 1];
+        const int n = Ld.nx * Ld.ny * Ld.nz;
+        for (int c = g0; c < n; c += gstride)
+            prolong_cell<T>(Ld, C, a.x[l + 1], a.x[l], c % Ld.nx, (c / Ld.nx) % Ld.ny, c / (Ld.nx * Ld.ny));
+        cluster_barrier();
+        for (int it = 0; it < a.post[l]; it++) {
+            cluster_half<T>(Ld, 1, 0, a.b[l], a.invd[l], a.x[l]);
+            cluster_half<T>(Ld, 0, 0, a.b[l], a.invd[l], a.x[l]);
+        }
+    }
+}
+
 // FP64 <-> FP32 between the natural order and a level's storage order
 __global__ void k_to_float_lev(MgDevLevel L, const double *__restrict__ a, float *__restrict__ b)
 {
@@ -772,6 +888,38 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
         launch_k(H.pdl, k_vcycle_tail<T>, dim3(1), dim3(TAIL_THREADS), s, a);
         return;
     }
+    if (H.cluster_from >= 0 && l == H.cluster_from && H.nl - l <= MG_CLUSTER_MAXLEV && l < H.nl - 1 &&
+        H.cluster_ctas > 0) {
+        ClusterArgs<T> a;
+        a.nlev = H.nl - l;
+        // the levels above the single-block tail (or all but the coarsest)
+        a.ncl = (H.tail_from > l) ? H.tail_from - l : a.nlev - 1;
+        for (int t = 0; t < a.nlev; t++) {
+            a.L[t] = H.lev[l + t];
+            a.x[t] = H.x[l + t];
+            a.b[t] = H.b[l + t];
+            a.r[t] = H.r[l + t];
+            a.invd[t] = H.invd[l + t];
+            a.pre[t] = pre[l + t];
+            a.post[t] = post[l + t];
+        }
+        a.coarse_inv = H.coarse_inv;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)H.cluster_ctas);
+        cfg.blockDim = dim3(CLUSTER_THREADS);
+        cfg.stream = s;
+        cudaLaunchAttribute at[2];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)H.cluster_ctas;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = H.pdl ? 2 : 1;
+        cudaLaunchKernelEx(&cfg, k_vcycle_cluster<T>, a);
+        return;
+    }
     if (l == H.nl - 1) {
         launch_k(H.pdl, k_coarse<T>, dim3(1), dim3(64), s, (int)n, H.coarse_inv, H.b[l], H.x[l]);
         return;
@@ -849,17 +997,47 @@ double mg_vcycle_bytes(const MgHier<T> &H, int l, const int *pre, const int *pos
 template double mg_vcycle_bytes<double>(const MgHier<double> &, int, const int *, const int *);
 template double mg_vcycle_bytes<float>(const MgHier<float> &, int, const int *, const int *);
 
-int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from)
+int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from, int cluster_from)
 {
     // per non-coarsest level: 2*pre + resid + restrict + prolong + 2*post;
-    // coarsest: 1; the fused tail from tail_from on: 1
+    // coarsest: 1; the fused tail from tail_from on: 1; the one-cluster
+    // V-cycle from cluster_from on: 1
     int n = 1;
     for (int l = 0; l < nl - 1; l++) {
+        if (cluster_from >= 0 && l == cluster_from && nl - l <= MG_CLUSTER_MAXLEV) return n;
         if (tail_from >= 0 && l == tail_from && nl - l <= MG_TAIL_MAXLEV) return n;
         n += 2 * pre[l] + 3 + 2 * post[l];
     }
     return n;
 }
+
+// blocks of the one-cluster V-cycle: 16 if a cluster of 16 such blocks can
+// be resident (a non-portable cluster size), else 8, else 0 (not used)
+template <typename T>
+int mg_cluster_ctas()
+{
+    if (cudaFuncSetAttribute(k_vcycle_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+    }
+    for (int ctas = 16; ctas >= 8; ctas /= 2) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)ctas);
+        cfg.blockDim = dim3(CLUSTER_THREADS);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)ctas;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, k_vcycle_cluster<T>, &cfg) == cudaSuccess && nc >= 1) return ctas;
+        cudaGetLastError();
+    }
+    return 0;
+}
+template int mg_cluster_ctas<float>();
+template int mg_cluster_ctas<double>();
 
 template void mg_setup_invdiag<double>(cudaStream_t, const MgDevLevel &, double *);
 template void mg_setup_invdiag<float>(cudaStream_t, const MgDevLevel &, float *);

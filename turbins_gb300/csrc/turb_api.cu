@@ -173,6 +173,7 @@ struct turb_ctx {
     // kernel variants (TURB_KV_*): FP32 sweeps marching along k through
     // shared-memory plane tiles, ENO y / z lines walked in segments
     int kvariant = TURB_KV_ENO_SEGMENTS | TURB_KV_PDL;
+    long long mg_cluster_cells = 1 << 17;   // TURB_KV_CLUSTER_VCYCLE from the first level of at most this many cells
     double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
     double p_dt = 0.0;           // dt of the last Pressure_set_RHS
     long long gate_tightened = 0;
@@ -687,6 +688,24 @@ Xfer1D mk_xfer(DevBuf &m, const std::vector<double> &Df, const std::vector<doubl
     return t;
 }
 
+
+// With TURB_KV_CLUSTER_VCYCLE, the first level of at most mg_cluster_cells
+// cells (and at most MG_CLUSTER_MAXLEV levels from it to the coarsest) runs
+// the rest of the V-cycle as one launch of one thread-block cluster, if the
+// device can hold such a cluster.
+static void set_cluster_from(turb_ctx *c)
+{
+    int from = -1;
+    if ((c->kvariant & TURB_KV_CLUSTER_VCYCLE) && c->H32.cluster_ctas > 0 && c->H64.cluster_ctas > 0)
+        for (int l = 0; l + 1 < c->H32.nl && c->mg_cluster_cells > 0; l++) {
+            const MgDevLevel &m = c->H32.lev[l];
+            if ((long long)m.nx * m.ny * m.nz <= c->mg_cluster_cells && c->H32.nl - l <= MG_CLUSTER_MAXLEV) {
+                from = l;
+                break;
+            }
+        }
+    c->H32.cluster_from = c->H64.cluster_from = from;
+}
 int build_mg(turb_ctx *c)
 {
     std::vector<HostLev> L = mg_host(c);
@@ -802,6 +821,9 @@ int build_mg(turb_ctx *c)
             break;
         }
     }
+    c->H64.cluster_ctas = mg_cluster_ctas<double>();
+    c->H32.cluster_ctas = mg_cluster_ctas<float>();
+    set_cluster_from(c);
     return c->mem.err == cudaSuccess ? TURB_OK : TURB_ERR_ALLOC;
 }
 
@@ -1211,8 +1233,9 @@ int turb_set_pressure_guess(turb_ctx *c, int mode)
 
 int turb_set_sweep_kernels(turb_ctx *c, int variants)
 {
-    if (!c || variants < 0 || variants > (TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS | TURB_KV_PDL)) return TURB_ERR_ARG;
-    if ((c->kvariant ^ variants) & (TURB_KV_MARCHING | TURB_KV_PDL)) {   // captured graphs hold the old launches
+    if (!c || variants < 0 || variants > (TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS | TURB_KV_PDL | TURB_KV_CLUSTER_VCYCLE))
+        return TURB_ERR_ARG;
+    if ((c->kvariant ^ variants) & (TURB_KV_MARCHING | TURB_KV_PDL | TURB_KV_CLUSTER_VCYCLE)) {   // captured graphs hold the old launches
         for (auto &g : c->g_inner)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto &g : c->g_mg)
@@ -1223,6 +1246,7 @@ int turb_set_sweep_kernels(turb_ctx *c, int variants)
     c->H32.marching = c->H64.marching;
     c->H64.pdl = (variants & TURB_KV_PDL) ? 1 : 0;
     c->H32.pdl = c->H64.pdl;
+    set_cluster_from(c);
     return TURB_OK;
 }
 
@@ -1597,6 +1621,16 @@ static void set_tail(turb_ctx *c, long long max_cells)
     c->H32.tail_from = c->H64.tail_from = from;
     for (int m = 0; m < 2; m++)
         if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+}
+
+int turb_set_mg_cluster(turb_ctx *c, long long max_cells)
+{
+    if (!c || max_cells < 0) return TURB_ERR_ARG;
+    c->mg_cluster_cells = max_cells;
+    set_cluster_from(c);
+    for (int m = 0; m < 2; m++)
+        if (c->g_mg[m]) { cudaGraphExecDestroy(c->g_mg[m]); c->g_mg[m] = nullptr; }
+    return TURB_OK;
 }
 
 int turb_set_mg_tail(turb_ctx *c, long long max_cells)
@@ -2548,8 +2582,8 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     int it = 0, restart = 1, status = TURB_OK;
     const int pmi = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
     const int *npre = c->mg_pre[pmi], *npost = c->mg_post[pmi];
-    int vl = pmi == 0 ? mg_vcycle_launches(c->H64.nl, npre, npost, c->H64.tail_from)
-                      : mg_vcycle_launches(c->H32.nl, npre, npost, c->H32.tail_from);
+    int vl = pmi == 0 ? mg_vcycle_launches(c->H64.nl, npre, npost, c->H64.tail_from, c->H64.cluster_from)
+                      : mg_vcycle_launches(c->H32.nl, npre, npost, c->H32.tail_from, c->H32.cluster_from);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
         if (nr <= tol || it >= c->prm.p_maxit) {

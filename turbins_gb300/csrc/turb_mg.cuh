@@ -4,6 +4,7 @@
 
 #define TURB_MG_MAXLEV 24
 #define MG_TAIL_MAXLEV 6   // levels a fused single-block V-cycle tail may hold
+#define MG_CLUSTER_MAXLEV 8   // levels a one-cluster V-cycle launch may hold
 
 // 1-D transfer tables between a level and the next coarser one along one
 // direction: prolongation weights per fine index (two coarse cells) and the
@@ -43,6 +44,10 @@ struct MgHier {
     int marching = 0;
     // 1: the V-cycle's kernels use programmatic dependent launch
     int pdl = 1;
+    // from this level on (-1: never) the V-cycle runs as one launch of one
+    // thread-block cluster of cluster_ctas blocks (k_vcycle_cluster)
+    int cluster_from = -1;
+    int cluster_ctas = 0;
 };
 
 template <typename T>
@@ -50,7 +55,9 @@ void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd);
 template <typename T>
 // level l smooths with pre[l] / post[l] red-black sweeps
 void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const int *post);
-int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from);
+int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from, int cluster_from = -1);
+template <typename T>
+int mg_cluster_ctas();
 template <typename T>
 double mg_vcycle_bytes(const MgHier<T> &H, int l, const int *pre, const int *post);
 
