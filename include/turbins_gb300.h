@@ -133,13 +133,17 @@ int turb_destroy(turb_ctx *ctx);
 int turb_field_upload(turb_ctx *ctx, int field, const double *host_da);
 int turb_field_download(turb_ctx *ctx, int field, double *host_da);
 /* n fields in one call (host[t] <-> fields[t]); the call returns when every
- * copy has completed.  Page-locked arrays (turb_host_alloc or
- * turb_host_register, whole array) are read / written in place by the layout
- * kernel; pageable ones move as one contiguous copy per field through a
+ * copy has completed.  Each field moves as one contiguous copy through a
  * device staging buffer, the copy of one field overlapping the layout
- * conversion of the one before. */
+ * conversion of the one before; from page-locked arrays (turb_host_alloc or
+ * turb_host_register, whole array) the copies run asynchronously on the copy
+ * engines.  With TURB_HOST_COPY_KERNEL page-locked arrays are instead read /
+ * written in place by the layout kernel across the host link. */
 int turb_fields_upload(turb_ctx *ctx, int n, const int *fields, const double *const *host_da);
 int turb_fields_download(turb_ctx *ctx, int n, const int *fields, double *const *host_da);
+#define TURB_HOST_COPY_DMA 0      /* default */
+#define TURB_HOST_COPY_KERNEL 1
+int turb_set_host_copy(turb_ctx *ctx, int mode);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 /* Initial guess of the Poisson solve.  PREVIOUS: the last solution (the
  * reference's nonzero initial guess, Solver.c:84).  EXTRAPOLATE: 2 p1 - p2 from
@@ -168,13 +172,19 @@ int turb_set_pressure_guess(turb_ctx *ctx, int mode);
  * stream order); TURB_KV_CLUSTER_VCYCLE, the V-cycle from the first level
  * of at most turb_set_mg_cluster cells down runs as one launch of one
  * thread-block cluster (16 blocks of 1024 threads, or 8 where 16 do not fit),
- * its phases separated by the hardware cluster barrier.  Default:
+ * its phases separated by the hardware cluster barrier; TURB_KV_SWEEP_PAIRS,
+ * the finest FP32 level (colour-split, nx a multiple of 64, ny of 32)
+ * applies its red-black sweeps two at a time in one pass over memory: z
+ * planes staged in shared memory by TMA, a wavefront of four half sweeps
+ * along z over overlapped 64 x 32 tiles, the result in a second x array.
+ * Default:
  * TURB_KV_ENO_SEGMENTS | TURB_KV_PDL (measured fastest on GB300 at
  * 512x256x256). */
 #define TURB_KV_MARCHING 1
 #define TURB_KV_ENO_SEGMENTS 2
 #define TURB_KV_PDL 4   /* V-cycle kernels with programmatic dependent launch */
 #define TURB_KV_CLUSTER_VCYCLE 8   /* coarse V-cycle levels in one thread-block cluster */
+#define TURB_KV_SWEEP_PAIRS 16    /* finest FP32 level: two sweeps per pass */
 int turb_set_sweep_kernels(turb_ctx *ctx, int variants);
 /* max_div > 0: every Poisson solve, after reaching its relative residual,
  * also iterates until dt * max|b - A phi| (the largest divergence the

@@ -461,17 +461,19 @@ def test_divergence_gate(api, oracle_mod, name, mk):
 @pytest.mark.parametrize("name,mk", [("bump", lambda: _cases.bump_small()), ("multi", lambda: _cases.multi_small()),
                                      ("bump_64", lambda: _cases.bump_small(64, 40, 24))])
 def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):
-    """The kernel variants that hide latency (FP32 Jacobi and red-black
-    sweeps marching along k through shared-memory plane tiles, ENO y / z
-    lines walked in segments, V-cycle kernels with programmatic dependent
-    launch) give the same bits as the one-point-per-thread kernels in plain
+    """The kernel variants that hide latency or traffic (FP32 Jacobi and
+    red-black sweeps marching along k through shared-memory plane tiles, ENO
+    y / z lines walked in segments, V-cycle kernels with programmatic
+    dependent launch, the coarse levels in one cluster launch, the finest
+    level's sweeps two per pass on the 64x32x16 case) give the same bits as the one-point-per-thread kernels in plain
     stream order: two full steps (every convection pass and every Helmholtz
     and Poisson solve) with either."""
     case = mk()
     s = _cases.random_state(case, seed=13)
     out = []
     for variants in (0, api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL,
-                     api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL | api.KV_CLUSTER_VCYCLE):
+                     api.KV_MARCHING | api.KV_ENO_SEGMENTS | api.KV_PDL | api.KV_CLUSTER_VCYCLE,
+                     api.KV_ENO_SEGMENTS | api.KV_PDL | api.KV_SWEEP_PAIRS):
         ctx = api.Context(case.grid, case.params)
         ctx.set_sweep_kernels(variants)
         ctx.load_state(s)
@@ -512,3 +514,36 @@ def test_cluster_vcycle_is_bit_identical(api, mode, cells, tail):
         ctx.close()
     assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
     assert np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("shape,lengths,q", [((256, 128, 128), (16.0, 2.0, 2.0), 1.5),
+                                             ((128, 64, 64), (1.0, 1.0, 1.0), None),
+                                             ((64, 64, 40), (4.0, 2.0, 2.0), 1.5)])
+def test_sweep_pairs_are_bit_identical(api, shape, lengths, q):
+    """The finest FP32 level's two-sweeps-per-pass smoother (TMA-staged z
+    planes, a wavefront of four half sweeps over overlapped tiles, ping-pong
+    x) gives the same Poisson iterates, residual and pressure as four launches
+    of one half sweep each: on a y-stretched 256x128x128 grid (blocks whose
+    plane ranges cross tiles), a uniform 128x64x64 grid, and a 64x64x40 grid
+    (a few planes per block, two tile rows)."""
+    from turbins_gb300 import workload as W
+    case = W.poisson_case(*shape, lengths, q)
+    vel = W.fourier_velocity(case.grid, 5)
+    out = []
+    for variants in (api.KV_ENO_SEGMENTS | api.KV_PDL, api.KV_ENO_SEGMENTS | api.KV_PDL | api.KV_SWEEP_PAIRS):
+        ctx = api.Context(case.grid, case.params)
+        ctx.set_sweep_kernels(variants)
+        ctx.set_pressure_mode(api.PMODE_MIXED)
+        for f, k in ((api.F_U, "u"), (api.F_V, "v"), (api.F_W, "w")):
+            ctx.upload(f, vel[k])
+        rec = []
+        ctx.upload(api.F_PHI, np.zeros(case.grid.shape))
+        for rhs_dt in (1.0, 0.5):   # a cold start (zero guess), then a warm one
+            ctx.Pressure_set_RHS(rhs_dt)
+            it, rr = ctx.Pressure_solve()
+            rec.append((it, rr, ctx.download(api.F_PHI)))
+        out.append(rec)
+        ctx.close()
+    for a, b in zip(out[0], out[1]):
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(a[2], b[2])

@@ -26,7 +26,8 @@ F_C0, F_CCONV0, F_CB0, F_VP0 = 32, 40, 48, 56
 PMODE_FP64, PMODE_MIXED = 0, 1
 HMODE_FP64, HMODE_MIXED = 0, 1
 GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED, GUESS_PROJECT = 0, 1, 2, 3
-KV_MARCHING, KV_ENO_SEGMENTS, KV_PDL, KV_CLUSTER_VCYCLE = 1, 2, 4, 8
+KV_MARCHING, KV_ENO_SEGMENTS, KV_PDL, KV_CLUSTER_VCYCLE, KV_SWEEP_PAIRS = 1, 2, 4, 8, 16
+HOST_COPY_DMA, HOST_COPY_KERNEL = 0, 1
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed", 6: "scratch limit", 7: "restart file I/O", 8: "restart file mismatch"}
@@ -234,6 +235,12 @@ class Context:
         _check(self.lib.turb_field_download(self.ctx, field, _ptr(a)), "download")
         return a
 
+    def set_host_copy(self, mode):
+        """turb_set_host_copy: HOST_COPY_DMA (staged copies on the copy
+        engines) or HOST_COPY_KERNEL (the layout kernel reads / writes
+        page-locked host arrays in place)"""
+        _check(self.lib.turb_set_host_copy(self.ctx, int(mode)), "set_host_copy")
+
     def upload_many(self, pairs):
         """turb_fields_upload: [(field, array), ...] in one overlapped call;
         the arrays must be C-contiguous float64 of the grid's shape"""
@@ -276,7 +283,7 @@ class Context:
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
     def set_sweep_kernels(self, variants=KV_ENO_SEGMENTS | KV_PDL):
-        """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL | KV_CLUSTER_VCYCLE); all give the same bits"""
+        """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL | KV_CLUSTER_VCYCLE | KV_SWEEP_PAIRS); all give the same bits"""
         _check(self.lib.turb_set_sweep_kernels(self.ctx, int(variants)), "set_sweep_kernels")
 
     def set_divergence_gate(self, max_div=1e-10):

@@ -924,7 +924,18 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
         launch_k(H.pdl, k_coarse<T>, dim3(1), dim3(64), s, (int)n, H.coarse_inv, H.b[l], H.x[l]);
         return;
     }
-    for (int it = 0; it < npre; it++) {
+    // level 0 in FP32: sweeps in pairs, one pass each (an even number of
+    // passes, so that x ends in its own array), the rest one half sweep each
+    int pre_done = 0, post_done = 0;
+    if constexpr (sizeof(T) == 4) {
+        if (l == 0 && H.tb) {
+            const int np = (npre / 4) * 2, nq = (npost / 4) * 2;
+            for (int f = 0; f < np; f++) mg_tb_sweeps(s, *H.tb, f & 1, 0, f == 0, H.pdl);
+            pre_done = 2 * np;
+            post_done = 2 * nq;
+        }
+    }
+    for (int it = pre_done; it < npre; it++) {
         // the first colour-0 half sweep takes x = 0 (it reads no neighbours);
         // every colour-1 point is then rewritten from colour-0 values only
         rb_half<T>(s, L, 0, it == 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
@@ -945,7 +956,10 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
         mg_vcycle<T>(s, H, l + 1, pre, post);
         launch_k(H.pdl, k_prolong<T>, g3(L.nx, L.ny, L.nz), B38, s, L, C, H.x[l + 1], H.x[l]);
     }
-    for (int it = 0; it < npost; it++) {
+    if constexpr (sizeof(T) == 4) {
+        for (int f = 0; f < post_done / 2; f++) mg_tb_sweeps(s, *H.tb, f & 1, 1, 0, H.pdl);
+    }
+    for (int it = post_done; it < npost; it++) {
         rb_half<T>(s, L, 1, 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
         rb_half<T>(s, L, 0, 0, H.b[l], H.invd[l], H.x[l], H.marching, H.pdl);
     }
@@ -986,7 +1000,17 @@ double mg_vcycle_bytes(const MgHier<T> &H, int l, const int *pre, const int *pos
         const MgDevLevel &C = H.lev[l + 1];
         double nc = (double)C.nx * C.ny * C.nz;
         int halves = 2 * pre[l] + 2 * post[l];
-        total += (halves > 0 ? 1.5 * e * n : 0.0) + (halves > 1 ? (halves - 1) * 2.0 * e * n : 0.0);
+        if (l == 0 && H.tb && sizeof(T) == 4) {
+            // a pass of two sweeps reads b, 1/diag and one colour of x and
+            // writes x (the first of a cycle reads no x)
+            const int np = (pre[l] / 4) * 2, nq = (post[l] / 4) * 2;
+            total += np > 0 ? 3.0 * e * n + (np - 1) * 3.5 * e * n : 0.0;
+            total += nq * 3.5 * e * n;
+            halves -= 4 * (np + nq);
+            total += halves * 2.0 * e * n;   // the remaining half sweeps (none of them the first)
+        } else {
+            total += (halves > 0 ? 1.5 * e * n : 0.0) + (halves > 1 ? (halves - 1) * 2.0 * e * n : 0.0);
+        }
         total += 3.0 * e * n;                 // residual
         total += e * n + e * nc;              // restriction
         total += e * nc + 2.0 * e * n;        // prolongation
@@ -997,16 +1021,18 @@ double mg_vcycle_bytes(const MgHier<T> &H, int l, const int *pre, const int *pos
 template double mg_vcycle_bytes<double>(const MgHier<double> &, int, const int *, const int *);
 template double mg_vcycle_bytes<float>(const MgHier<float> &, int, const int *, const int *);
 
-int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from, int cluster_from)
+int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from, int cluster_from, int tb0)
 {
     // per non-coarsest level: 2*pre + resid + restrict + prolong + 2*post;
     // coarsest: 1; the fused tail from tail_from on: 1; the one-cluster
-    // V-cycle from cluster_from on: 1
+    // V-cycle from cluster_from on: 1; level 0 with sweep pairs (tb0): one
+    // launch per pair of sweeps in place of four
     int n = 1;
     for (int l = 0; l < nl - 1; l++) {
         if (cluster_from >= 0 && l == cluster_from && nl - l <= MG_CLUSTER_MAXLEV) return n;
         if (tail_from >= 0 && l == tail_from && nl - l <= MG_TAIL_MAXLEV) return n;
         n += 2 * pre[l] + 3 + 2 * post[l];
+        if (l == 0 && tb0) n -= 3 * ((pre[l] / 4) * 2 + (post[l] / 4) * 2);
     }
     return n;
 }

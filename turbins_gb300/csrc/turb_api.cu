@@ -174,6 +174,11 @@ struct turb_ctx {
     // shared-memory plane tiles, ENO y / z lines walked in segments
     int kvariant = TURB_KV_ENO_SEGMENTS | TURB_KV_PDL;
     long long mg_cluster_cells = 1 << 17;   // TURB_KV_CLUSTER_VCYCLE from the first level of at most this many cells
+    // TURB_KV_SWEEP_PAIRS: the finest FP32 level's two-sweeps-per-pass smoother
+    RbTbPlan tbplan;
+    int host_copy = TURB_HOST_COPY_DMA;   // how page-locked host arrays move (turb_set_host_copy)
+    float *tb_x1 = nullptr;   // its second x array (ping-pong)
+    int *tb_err = nullptr;    // set by a block whose copy wait timed out
     double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
     double p_dt = 0.0;           // dt of the last Pressure_set_RHS
     long long gate_tightened = 0;
@@ -205,7 +210,7 @@ struct turb_ctx {
     // host transfers: two contiguous device staging buffers of one DA field,
     // a copy stream and the events that hand a buffer between the streams
     double *xfer[2] = {nullptr, nullptr};
-    cudaStream_t cs = nullptr;
+    cudaStream_t cs = nullptr, cs2 = nullptr;   // copy streams of the staged host copies (even / odd fields)
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_freed[2] = {nullptr, nullptr};
     // ghost-cell stencils made by turb_geometry (one allocation per quantity)
     GeomIb gib[4];
@@ -706,6 +711,30 @@ static void set_cluster_from(turb_ctx *c)
         }
     c->H32.cluster_from = c->H64.cluster_from = from;
 }
+
+// With TURB_KV_SWEEP_PAIRS, the finest FP32 level smooths two sweeps per
+// pass (k_rbgs_tb) where its shape allows (colour-split, nx a multiple of 64,
+// ny of 32); the second x array is allocated on first use.
+static void set_tb(turb_ctx *c)
+{
+    c->H32.tb = nullptr;
+    if (!(c->kvariant & TURB_KV_SWEEP_PAIRS) || c->H32.nl < 2) return;
+    const MgDevLevel &L0 = c->H32.lev[0];
+    if (!L0.split || L0.nx % 64 != 0 || L0.ny % 32 != 0) return;
+    if (!c->tb_x1) {
+        c->tb_x1 = c->mem.alloc<float>((size_t)L0.nx * L0.ny * L0.nz);
+        c->tb_err = c->mem.alloc<int>(1);
+        if (c->mem.err != cudaSuccess) {
+            c->mem.err = cudaSuccess;
+            cudaGetLastError();
+            return;
+        }
+    }
+    if (!c->tbplan.ok && mg_tb_plan(&c->tbplan, L0, c->H32.x[0], c->tb_x1, c->H32.b[0], c->H32.invd[0], c->tb_err))
+        return;
+    c->tbplan.lev = L0;
+    c->H32.tb = &c->tbplan;
+}
 int build_mg(turb_ctx *c)
 {
     std::vector<HostLev> L = mg_host(c);
@@ -824,6 +853,7 @@ int build_mg(turb_ctx *c)
     c->H64.cluster_ctas = mg_cluster_ctas<double>();
     c->H32.cluster_ctas = mg_cluster_ctas<float>();
     set_cluster_from(c);
+    set_tb(c);
     return c->mem.err == cudaSuccess ? TURB_OK : TURB_ERR_ALLOC;
 }
 
@@ -1101,6 +1131,7 @@ int turb_destroy(turb_ctx *c)
         if (c->ev_freed[t]) cudaEventDestroy(c->ev_freed[t]);
     }
     if (c->cs) cudaStreamDestroy(c->cs);
+    if (c->cs2) cudaStreamDestroy(c->cs2);
     cudaStreamDestroy(c->s);
     delete c;
     return TURB_OK;
@@ -1120,6 +1151,7 @@ static int stage_setup(turb_ctx *c)
     if (c->xfer[0]) return TURB_OK;
     size_t b = sizeof(double) * (size_t)c->d.NX * c->d.NY * c->d.NZ;
     TURB_CHECK(cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking));
+    TURB_CHECK(cudaStreamCreateWithFlags(&c->cs2, cudaStreamNonBlocking));
     for (int t = 0; t < 2; t++) {
         TURB_CHECK(cudaEventCreateWithFlags(&c->ev_copied[t], cudaEventDisableTiming));
         TURB_CHECK(cudaEventCreateWithFlags(&c->ev_freed[t], cudaEventDisableTiming));
@@ -1128,13 +1160,14 @@ static int stage_setup(turb_ctx *c)
     return TURB_OK;
 }
 
-// Host <-> device for several fields.  Page-locked host arrays are read or
-// written in place by the layout kernel (its loads / stores cross the host
-// link).  Pageable ones move as one contiguous copy per field on the copy
-// stream into / out of one of two staging buffers, and the kernel on the
-// context's stream converts between the contiguous and the pitched layout,
-// so the copy of one field overlaps the conversion of the one before.
-// Returns when everything has landed.
+// Host <-> device for several fields.  Every field moves as one contiguous
+// copy on the copy stream into / out of one of two staging buffers, and the
+// kernel on the context's stream converts between the contiguous and the
+// pitched layout, so the copy of one field overlaps the conversion of the
+// one before (for page-locked arrays the copies run on the copy engines at
+// the host link's rate).  With TURB_HOST_COPY_KERNEL, page-locked host
+// arrays are instead read or written in place by the layout kernel (its
+// loads / stores cross the host link).  Returns when everything has landed.
 // the device address of page-locked host memory (cudaMallocHost or
 // registered), or null for pageable memory
 static const void *host_device_ptr(const void *h)
@@ -1152,8 +1185,9 @@ int turb_fields_upload(turb_ctx *c, int n, const int *fields, const double *cons
     if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
     for (int t = 0; t < n; t++)
         if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
-    // page-locked arrays: the layout kernel reads them over the host link
-    bool direct = true;
+    // page-locked arrays with TURB_HOST_COPY_KERNEL: the layout kernel reads
+    // them over the host link
+    bool direct = c->host_copy == TURB_HOST_COPY_KERNEL;
     for (int t = 0; t < n && direct; t++) direct = host_device_ptr(host[t]) != nullptr;
     if (direct) {
         for (int t = 0; t < n; t++)
@@ -1170,9 +1204,10 @@ int turb_fields_upload(turb_ctx *c, int n, const int *fields, const double *cons
     TURB_CHECK(cudaEventRecord(c->ev_freed[1], c->s));
     for (int t = 0; t < n; t++) {
         int u = t & 1;
-        TURB_CHECK(cudaStreamWaitEvent(c->cs, c->ev_freed[u], 0));
-        TURB_CHECK(cudaMemcpyAsync(c->xfer[u], host[t], b, cudaMemcpyHostToDevice, c->cs));
-        TURB_CHECK(cudaEventRecord(c->ev_copied[u], c->cs));
+        cudaStream_t cp = u ? c->cs2 : c->cs;   // two copies in flight, on two copy engines
+        TURB_CHECK(cudaStreamWaitEvent(cp, c->ev_freed[u], 0));
+        TURB_CHECK(cudaMemcpyAsync(c->xfer[u], host[t], b, cudaMemcpyHostToDevice, cp));
+        TURB_CHECK(cudaEventRecord(c->ev_copied[u], cp));
         TURB_CHECK(cudaStreamWaitEvent(c->s, c->ev_copied[u], 0));
         launch_da_pitch(c->s, d, c->xfer[u], field_ptr(c, fields[t]), 1);
         TURB_CHECK(cudaEventRecord(c->ev_freed[u], c->s));
@@ -1186,7 +1221,7 @@ int turb_fields_download(turb_ctx *c, int n, const int *fields, double *const *h
     if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
     for (int t = 0; t < n; t++)
         if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
-    bool direct = true;
+    bool direct = c->host_copy == TURB_HOST_COPY_KERNEL;
     for (int t = 0; t < n && direct; t++) direct = host_device_ptr(host[t]) != nullptr;
     if (direct) {
         for (int t = 0; t < n; t++)
@@ -1199,17 +1234,26 @@ int turb_fields_download(turb_ctx *c, int n, const int *fields, double *const *h
     const Dims &d = c->d;
     size_t b = sizeof(double) * (size_t)d.NX * d.NY * d.NZ;
     TURB_CHECK(cudaEventRecord(c->ev_freed[0], c->cs));
-    TURB_CHECK(cudaEventRecord(c->ev_freed[1], c->cs));
+    TURB_CHECK(cudaEventRecord(c->ev_freed[1], c->cs2));
     for (int t = 0; t < n; t++) {
         int u = t & 1;
         TURB_CHECK(cudaStreamWaitEvent(c->s, c->ev_freed[u], 0));
         launch_da_pitch(c->s, d, field_ptr(c, fields[t]), c->xfer[u], 0);
         TURB_CHECK(cudaEventRecord(c->ev_copied[u], c->s));
-        TURB_CHECK(cudaStreamWaitEvent(c->cs, c->ev_copied[u], 0));
-        TURB_CHECK(cudaMemcpyAsync(host[t], c->xfer[u], b, cudaMemcpyDeviceToHost, c->cs));
-        TURB_CHECK(cudaEventRecord(c->ev_freed[u], c->cs));
+        cudaStream_t cp = u ? c->cs2 : c->cs;
+        TURB_CHECK(cudaStreamWaitEvent(cp, c->ev_copied[u], 0));
+        TURB_CHECK(cudaMemcpyAsync(host[t], c->xfer[u], b, cudaMemcpyDeviceToHost, cp));
+        TURB_CHECK(cudaEventRecord(c->ev_freed[u], cp));
     }
     TURB_CHECK(cudaStreamSynchronize(c->cs));
+    TURB_CHECK(cudaStreamSynchronize(c->cs2));
+    return TURB_OK;
+}
+
+int turb_set_host_copy(turb_ctx *c, int mode)
+{
+    if (!c || (mode != TURB_HOST_COPY_DMA && mode != TURB_HOST_COPY_KERNEL)) return TURB_ERR_ARG;
+    c->host_copy = mode;
     return TURB_OK;
 }
 
@@ -1233,9 +1277,9 @@ int turb_set_pressure_guess(turb_ctx *c, int mode)
 
 int turb_set_sweep_kernels(turb_ctx *c, int variants)
 {
-    if (!c || variants < 0 || variants > (TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS | TURB_KV_PDL | TURB_KV_CLUSTER_VCYCLE))
-        return TURB_ERR_ARG;
-    if ((c->kvariant ^ variants) & (TURB_KV_MARCHING | TURB_KV_PDL | TURB_KV_CLUSTER_VCYCLE)) {   // captured graphs hold the old launches
+    const int all = TURB_KV_MARCHING | TURB_KV_ENO_SEGMENTS | TURB_KV_PDL | TURB_KV_CLUSTER_VCYCLE | TURB_KV_SWEEP_PAIRS;
+    if (!c || variants < 0 || variants > all) return TURB_ERR_ARG;
+    if ((c->kvariant ^ variants) & (all & ~TURB_KV_ENO_SEGMENTS)) {   // captured graphs hold the old launches
         for (auto &g : c->g_inner)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto &g : c->g_mg)
@@ -1247,6 +1291,7 @@ int turb_set_sweep_kernels(turb_ctx *c, int variants)
     c->H64.pdl = (variants & TURB_KV_PDL) ? 1 : 0;
     c->H32.pdl = c->H64.pdl;
     set_cluster_from(c);
+    set_tb(c);
     return TURB_OK;
 }
 
@@ -1649,6 +1694,7 @@ int turb_set_mg_split(turb_ctx *c, int on)
         m.split = c->mg_split && (m.nx % 2 == 0) && l + 1 < c->H32.nl;
         mg_setup_invdiag<float>(c->s, m, c->H32.invd[l]);
     }
+    set_tb(c);
     if (c->g_mg[1]) { cudaGraphExecDestroy(c->g_mg[1]); c->g_mg[1] = nullptr; }
     return check_launch(c);
 }
@@ -2582,8 +2628,8 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
     int it = 0, restart = 1, status = TURB_OK;
     const int pmi = c->pmode == TURB_PMODE_FP64 ? 0 : 1;
     const int *npre = c->mg_pre[pmi], *npost = c->mg_post[pmi];
-    int vl = pmi == 0 ? mg_vcycle_launches(c->H64.nl, npre, npost, c->H64.tail_from, c->H64.cluster_from)
-                      : mg_vcycle_launches(c->H32.nl, npre, npost, c->H32.tail_from, c->H32.cluster_from);
+    int vl = pmi == 0 ? mg_vcycle_launches(c->H64.nl, npre, npost, c->H64.tail_from, c->H64.cluster_from, 0)
+                      : mg_vcycle_launches(c->H32.nl, npre, npost, c->H32.tail_from, c->H32.cluster_from, c->H32.tb ? 1 : 0);
     for (;;) {
         if (!std::isfinite(nr)) { status = TURB_ERR_NAN; break; }
         if (nr <= tol || it >= c->prm.p_maxit) {
@@ -2661,6 +2707,16 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         nr = std::sqrt(c->hscal[1]);
         restart = 0;
         it++;
+    }
+    if (pmi == 1 && c->H32.tb) {   // a copy wait of the two-sweep smoother that timed out
+        TURB_CHECK(cudaMemcpyAsync(c->hscal + 15, c->tb_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        TURB_CHECK(cudaStreamSynchronize(s));
+        int bad = 0;
+        std::memcpy(&bad, c->hscal + 15, sizeof(int));
+        if (bad) {
+            TURB_CHECK(cudaMemsetAsync(c->tb_err, 0, sizeof(int), s));
+            return turb_set_cuda_error(cudaErrorLaunchTimeout, __FILE__, __LINE__);
+        }
     }
     pcg_scatter(s, d, L0, c->px, c->fld[TURB_F_PHI]);
     c->launches += 1;

@@ -1,5 +1,7 @@
 // turb_mg.cuh -- multigrid hierarchy descriptors (device pointers).
 #pragma once
+#include <cuda.h>
+
 #include "turb_internal.cuh"
 
 #define TURB_MG_MAXLEV 24
@@ -31,6 +33,21 @@ struct MgDevLevel {
     int split = 0;
 };
 
+// the finest FP32 level's two-sweeps-per-pass smoother (k_rbtb.cu): TMA
+// maps of x (both ping-pong arrays), b and 1/diag, and the launch shape
+struct RbTbPlan {
+    CUtensorMap mx[2];
+    MgDevLevel lev;
+    const float *b = nullptr, *invd = nullptr;
+    float *xo[2];
+    int tiles_x = 0, ntiles = 0, grid = 0;
+    int *err = nullptr;
+    int ok = 0;
+};
+int mg_tb_plan(RbTbPlan *p, const MgDevLevel &L0, float *x0, float *x1, const float *b0, const float *invd0, int *err);
+void mg_tb_sweeps(cudaStream_t s, const RbTbPlan &p, int in, int c0, int zero_init, int pdl);
+size_t mg_tb_smem();
+
 template <typename T>
 struct MgHier {
     int nl;
@@ -48,6 +65,8 @@ struct MgHier {
     // thread-block cluster of cluster_ctas blocks (k_vcycle_cluster)
     int cluster_from = -1;
     int cluster_ctas = 0;
+    // level 0 (FP32 only): pairs of sweeps in one pass each (k_rbgs_tb), when set
+    const RbTbPlan *tb = nullptr;
 };
 
 template <typename T>
@@ -55,7 +74,7 @@ void mg_setup_invdiag(cudaStream_t s, const MgDevLevel &L, T *invd);
 template <typename T>
 // level l smooths with pre[l] / post[l] red-black sweeps
 void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const int *post);
-int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from, int cluster_from = -1);
+int mg_vcycle_launches(int nl, const int *pre, const int *post, int tail_from, int cluster_from = -1, int tb0 = 0);
 template <typename T>
 int mg_cluster_ctas();
 template <typename T>
