@@ -132,64 +132,77 @@ __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restr
 }
 
 // The same half sweep on colour-split FP32 storage, four cells of one row per
-// thread (nx a multiple of 8): the cells' own b and invd, their x-neighbours
-// (other colour, indices m-1+p .. m+p for row parity p) and the j+-1 / k+-1
-// neighbours are float4 loads, indices are 32-bit, and the row constants are
-// loaded once.  The arithmetic per cell is s_row's, operation for operation.
+// thread (nx a multiple of 8) in each of two planes k0, k0+1: the cells' own
+// b and invd, their x-neighbours (other colour, indices m-1+p .. m+p for row
+// parity p) and the j+-1 / k+-1 neighbours are float4 loads, the x metric
+// tables come as float4 from their parity-split copies (dxp / rlp / rrp),
+// indices are 32-bit, and the row constants are loaded once.  The arithmetic
+// per cell is s_row's, operation for operation.
+constexpr int RB4_PLANES = 2;
 __global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__restrict__ b,
                         const float *__restrict__ invd, float *__restrict__ x)
 {
     pdl_trigger();
     pdl_wait();
     const int nx = Ld.nx, ny = Ld.ny, nz = Ld.nz, hx = nx >> 1;
-    int q4 = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const int q4 = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (j >= ny || 4 * q4 >= hx) return;
     const int half = (int)(((long long)nx * ny * nz) >> 1), hxy = hx * ny;
-    const int p = (color + j + k) & 1;
-    const int rowm = (k * ny + j) * hx, m0 = rowm + 4 * q4;
-    const float4 bb = *reinterpret_cast<const float4 *>(b + (size_t)color * half + m0);
-    const float4 dd = *reinterpret_cast<const float4 *>(invd + (size_t)color * half + m0);
-    float4 res;
-    if (zero_init) {
-        res = make_float4(rmul(bb.x, dd.x), rmul(bb.y, dd.y), rmul(bb.z, dd.z), rmul(bb.w, dd.w));
-        *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) = res;
-        return;
-    }
-    const float *oth = x + (size_t)(1 - color) * half;
-    const float4 c4 = *reinterpret_cast<const float4 *>(oth + m0);
-    float ex = 0.0f;   // the fifth x-neighbour: left of the group (p = 0) or right of it (p = 1)
-    if (p == 0) { if (q4 > 0) ex = oth[m0 - 1]; }
-    else { if (4 * q4 + 4 < hx) ex = oth[m0 + 4]; }
-    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 jm = j > 0 ? *reinterpret_cast<const float4 *>(oth + m0 - hx) : zero4;
-    const float4 jp = j < ny - 1 ? *reinterpret_cast<const float4 *>(oth + m0 + hx) : zero4;
-    const float4 km = k > 0 ? *reinterpret_cast<const float4 *>(oth + m0 - hxy) : zero4;
-    const float4 kp = k < nz - 1 ? *reinterpret_cast<const float4 *>(oth + m0 + hxy) : zero4;
-    const float dyj = Ld.dyf[j], dzk = Ld.dzf[k];
-    const float dyz = rmul(dyj, dzk);
-    const float ryj = Ld.rfyf[j], ryj1 = Ld.rfyf[j + 1], rzk = Ld.rfzf[k], rzk1 = Ld.rfzf[k + 1];
-    const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
-    const float bv[4] = {bb.x, bb.y, bb.z, bb.w}, dv[4] = {dd.x, dd.y, dd.z, dd.w};
-    const float jmv[4] = {jm.x, jm.y, jm.z, jm.w}, jpv[4] = {jp.x, jp.y, jp.z, jp.w};
-    const float kmv[4] = {km.x, km.y, km.z, km.w}, kpv[4] = {kp.x, kp.y, kp.z, kp.w};
-    float out[4];
+    const float dyj = Ld.dyf[j], ryj = Ld.rfyf[j], ryj1 = Ld.rfyf[j + 1];
 #pragma unroll
-    for (int e = 0; e < 4; e++) {
-        const int i = 2 * (4 * q4 + e) + p;
-        const float xl = p == 0 ? (e == 0 ? ex : cv[e - 1]) : cv[e];
-        const float xr = p == 0 ? cv[e] : (e == 3 ? ex : cv[e + 1]);
-        const float dxi = Ld.dxf[i];
-        const float dxz = rmul(dxi, dzk), dxy = rmul(dxi, dyj);
-        float o = 0.0f, f;
-        if (i > 0) { f = rmul(dyz, Ld.rfxf[i]); o = rfma(f, xl, o); }
-        if (i < nx - 1) { f = rmul(dyz, Ld.rfxf[i + 1]); o = rfma(f, xr, o); }
-        if (j > 0) { f = rmul(dxz, ryj); o = rfma(f, jmv[e], o); }
-        if (j < ny - 1) { f = rmul(dxz, ryj1); o = rfma(f, jpv[e], o); }
-        if (k > 0) { f = rmul(dxy, rzk); o = rfma(f, kmv[e], o); }
-        if (k < nz - 1) { f = rmul(dxy, rzk1); o = rfma(f, kpv[e], o); }
-        out[e] = rmul(radd(bv[e], o), dv[e]);
+    for (int g = 0; g < RB4_PLANES; g++) {
+        const int k = blockIdx.z * RB4_PLANES + g;
+        if (k >= nz) break;
+        const int p = (color + j + k) & 1;
+        const int m0 = (k * ny + j) * hx + 4 * q4;
+        const float4 bb = *reinterpret_cast<const float4 *>(b + (size_t)color * half + m0);
+        const float4 dd = *reinterpret_cast<const float4 *>(invd + (size_t)color * half + m0);
+        if (zero_init) {
+            *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) =
+                make_float4(rmul(bb.x, dd.x), rmul(bb.y, dd.y), rmul(bb.z, dd.z), rmul(bb.w, dd.w));
+            continue;
+        }
+        const float *oth = x + (size_t)(1 - color) * half;
+        const float4 c4 = *reinterpret_cast<const float4 *>(oth + m0);
+        float ex = 0.0f;   // the fifth x-neighbour: left of the group (p = 0) or right of it (p = 1)
+        if (p == 0) { if (q4 > 0) ex = oth[m0 - 1]; }
+        else { if (4 * q4 + 4 < hx) ex = oth[m0 + 4]; }
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 jm = j > 0 ? *reinterpret_cast<const float4 *>(oth + m0 - hx) : zero4;
+        const float4 jp = j < ny - 1 ? *reinterpret_cast<const float4 *>(oth + m0 + hx) : zero4;
+        const float4 km = k > 0 ? *reinterpret_cast<const float4 *>(oth + m0 - hxy) : zero4;
+        const float4 kp = k < nz - 1 ? *reinterpret_cast<const float4 *>(oth + m0 + hxy) : zero4;
+        const float4 dx4 = *reinterpret_cast<const float4 *>(Ld.dxpf + p * hx + 4 * q4);
+        const float4 rl4 = *reinterpret_cast<const float4 *>(Ld.rlpf + p * hx + 4 * q4);
+        const float4 rr4 = *reinterpret_cast<const float4 *>(Ld.rrpf + p * hx + 4 * q4);
+        const float dzk = Ld.dzf[k];
+        const float dyz = rmul(dyj, dzk);
+        const float rzk = Ld.rfzf[k], rzk1 = Ld.rfzf[k + 1];
+        const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+        const float bv[4] = {bb.x, bb.y, bb.z, bb.w}, dv[4] = {dd.x, dd.y, dd.z, dd.w};
+        const float jmv[4] = {jm.x, jm.y, jm.z, jm.w}, jpv[4] = {jp.x, jp.y, jp.z, jp.w};
+        const float kmv[4] = {km.x, km.y, km.z, km.w}, kpv[4] = {kp.x, kp.y, kp.z, kp.w};
+        const float dxv[4] = {dx4.x, dx4.y, dx4.z, dx4.w};
+        const float rlv[4] = {rl4.x, rl4.y, rl4.z, rl4.w}, rrv[4] = {rr4.x, rr4.y, rr4.z, rr4.w};
+        float out[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int i = 2 * (4 * q4 + e) + p;
+            const float xl = p == 0 ? (e == 0 ? ex : cv[e - 1]) : cv[e];
+            const float xr = p == 0 ? cv[e] : (e == 3 ? ex : cv[e + 1]);
+            const float dxi = dxv[e];
+            const float dxz = rmul(dxi, dzk), dxy = rmul(dxi, dyj);
+            float o = 0.0f, f;
+            if (i > 0) { f = rmul(dyz, rlv[e]); o = rfma(f, xl, o); }
+            if (i < nx - 1) { f = rmul(dyz, rrv[e]); o = rfma(f, xr, o); }
+            if (j > 0) { f = rmul(dxz, ryj); o = rfma(f, jmv[e], o); }
+            if (j < ny - 1) { f = rmul(dxz, ryj1); o = rfma(f, jpv[e], o); }
+            if (k > 0) { f = rmul(dxy, rzk); o = rfma(f, kmv[e], o); }
+            if (k < nz - 1) { f = rmul(dxy, rzk1); o = rfma(f, kpv[e], o); }
+            out[e] = rmul(radd(bv[e], o), dv[e]);
+        }
+        *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) = make_float4(out[0], out[1], out[2], out[3]);
     }
-    *reinterpret_cast<float4 *>(x + (size_t)color * half + m0) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
 // The half sweep of k_rbgs4 marching along k (not the first, zero-initial
@@ -337,6 +350,9 @@ __global__ void k_resid8(MgDevLevel Ld, const float *__restrict__ b, const float
     auto inter = [](float4 a, float4 b, float (&v)[8]) {   // cells 2e from a, 2e+1 from b
         v[0] = a.x; v[1] = b.x; v[2] = a.y; v[3] = b.y; v[4] = a.z; v[5] = b.z; v[6] = a.w; v[7] = b.w;
     };
+    auto inter4 = [](float4 a, float4 b, float *v) {   // a then b
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    };
     float xc[8], bc[8], xjm[8], xjp[8], xkm[8], xkp[8];
     inter(ld4(h0 + m0), ld4(h1 + m0), xc);
     inter(ld4(b + (size_t)c0 * half + m0), ld4(b + (size_t)(c0 ^ 1) * half + m0), bc);
@@ -352,16 +368,21 @@ __global__ void k_resid8(MgDevLevel Ld, const float *__restrict__ b, const float
     const float dyj = Ld.dyf[j], dzk = Ld.dzf[k];
     const float dyz = rmul(dyj, dzk);
     const float ryj = Ld.rfyf[j], ryj1 = Ld.rfyf[j + 1], rzk = Ld.rfzf[k], rzk1 = Ld.rfzf[k + 1];
+    // the x tables of cells i0 .. i0+7 (and face i0+8) as float4 loads
+    float dxv[8], rxv[9];
+    inter4(ld4(Ld.dxf + i0), ld4(Ld.dxf + i0 + 4), dxv);
+    inter4(ld4(Ld.rfxf + i0), ld4(Ld.rfxf + i0 + 4), rxv);
+    rxv[8] = Ld.rfxf[i0 + 8];
     float out[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) {
         const int i = i0 + e;
-        const float dxi = Ld.dxf[i];
+        const float dxi = dxv[e];
         const float dxz = rmul(dxi, dzk), dxy = rmul(dxi, dyj);
         const float xw = e == 0 ? xl : xc[e - 1], xe = e == 7 ? xr : xc[e + 1];
         float o = 0.0f, d = 0.0f, f;
-        if (i > 0) { f = rmul(dyz, Ld.rfxf[i]); d = radd(d, f); o = rfma(f, xw, o); }
-        if (i < nx - 1) { f = rmul(dyz, Ld.rfxf[i + 1]); d = radd(d, f); o = rfma(f, xe, o); }
+        if (i > 0) { f = rmul(dyz, rxv[e]); d = radd(d, f); o = rfma(f, xw, o); }
+        if (i < nx - 1) { f = rmul(dyz, rxv[e + 1]); d = radd(d, f); o = rfma(f, xe, o); }
         if (j > 0) { f = rmul(dxz, ryj); d = radd(d, f); o = rfma(f, xjm[e], o); }
         if (j < ny - 1) { f = rmul(dxz, ryj1); d = radd(d, f); o = rfma(f, xjp[e], o); }
         if (k > 0) { f = rmul(dxy, rzk); d = radd(d, f); o = rfma(f, xkm[e], o); }
@@ -846,7 +867,8 @@ void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, cons
                     return;
                 }
             }
-            launch_k(pdl, k_rbgs4, g4, B38, s, L, color, zero_init, b, invd, x);
+            dim3 g4p(g4.x, g4.y, (unsigned)((L.nz + RB4_PLANES - 1) / RB4_PLANES));
+            launch_k(pdl, k_rbgs4, g4p, B38, s, L, color, zero_init, b, invd, x);
             return;
         }
     }

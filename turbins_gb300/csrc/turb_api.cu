@@ -764,6 +764,18 @@ int build_mg(turb_ctx *c)
         m.rfxd = c->mem.upload(rf[0]); m.rfyd = c->mem.upload(rf[1]); m.rfzd = c->mem.upload(rf[2]);
         m.dxf = c->mem.upload(Df[0]); m.dyf = c->mem.upload(Df[1]); m.dzf = c->mem.upload(Df[2]);
         m.rfxf = c->mem.upload(rff[0]); m.rfyf = c->mem.upload(rff[1]); m.rfzf = c->mem.upload(rff[2]);
+        if (h.nx % 2 == 0) {   // parity-split copies of the x tables (k_rbgs4)
+            const int hx = h.nx / 2;
+            std::vector<float> dxp(h.nx), rlp(h.nx), rrp(h.nx);
+            for (int par = 0; par < 2; par++)
+                for (int q = 0; q < hx; q++) {
+                    const int i = 2 * q + par;
+                    dxp[par * hx + q] = Df[0][i];
+                    rlp[par * hx + q] = rff[0][i];
+                    rrp[par * hx + q] = i + 1 < (int)rff[0].size() ? rff[0][i + 1] : 0.0f;
+                }
+            m.dxpf = c->mem.upload(dxp); m.rlpf = c->mem.upload(rlp); m.rrpf = c->mem.upload(rrp);
+        }
         c->H64.lev[l] = m;
         // FP32 levels store x, b, invd colour-split where nx is even (not on
         // the coarsest level, which the dense inverse reads in natural order)

@@ -26,6 +26,10 @@ struct MgDevLevel {
     Xfer1D tx, ty, tz;                                // transfer to the next level
     const double *dxd, *dyd, *dzd, *rfxd, *rfyd, *rfzd;
     const float *dxf, *dyf, *dzf, *rfxf, *rfyf, *rfzf;
+    // the x tables split by parity for 4-cell float4 reads (nx even): entry
+    // par * nx/2 + m is cell i = 2m + par: dx[i], 1/f of its left face
+    // (rfx[i]) and of its right face (rfx[i+1])
+    const float *dxpf = nullptr, *rlpf = nullptr, *rrpf = nullptr;
     double pin;
     // colour-split storage (x, b, invd; not r): with nx even, cell c of colour
     // (i+j+k)&1 lives at colour*(n/2) + c/2, so a red-black half sweep reads
