@@ -335,7 +335,8 @@ __global__ void k_resid(MgDevLevel Ld, const T *__restrict__ b, const T *__restr
 // live at index m0+e of colour halves c0 = (j+k)&1 and c0^1, so every x and
 // b access is a float4 (two scalars for the row ends); r is written in the
 // natural order the restriction reads.  Per cell the arithmetic is s_row's.
-__global__ void k_resid8(MgDevLevel Ld, const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ r)
+__global__ void __launch_bounds__(256, 4) k_resid8(MgDevLevel Ld, const float *__restrict__ b, const float *__restrict__ x,
+                                                   float *__restrict__ r)
 {
     pdl_trigger();
     pdl_wait();
@@ -808,6 +809,53 @@ __global__ void k_to_double_lev(MgDevLevel L, const float *__restrict__ a, doubl
     b[c] = (double)a[lev_at(L, c, i, j, k)];
 }
 
+// the same, eight cells of a row per thread (nx a multiple of 8): FP64 as
+// double2, FP32 as one float4 per colour (colour-split) or two (natural)
+__global__ void k_to_float_lev8(MgDevLevel L, const double *__restrict__ a, float *__restrict__ b)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (8 * q >= L.nx || j >= L.ny) return;
+    const long long c0 = ((long long)k * L.ny + j) * L.nx + 8 * q;
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const double2 d2 = *reinterpret_cast<const double2 *>(a + c0 + 2 * t);
+        v[2 * t] = (float)d2.x;
+        v[2 * t + 1] = (float)d2.y;
+    }
+    if (L.split) {
+        const long long half = ((long long)L.nx * L.ny * L.nz) >> 1;
+        const int ce = (j + k) & 1;   // colour of the even cells
+        *reinterpret_cast<float4 *>(b + ce * half + (c0 >> 1)) = make_float4(v[0], v[2], v[4], v[6]);
+        *reinterpret_cast<float4 *>(b + (1 - ce) * half + (c0 >> 1)) = make_float4(v[1], v[3], v[5], v[7]);
+    } else {
+        *reinterpret_cast<float4 *>(b + c0) = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4 *>(b + c0 + 4) = make_float4(v[4], v[5], v[6], v[7]);
+    }
+}
+__global__ void k_to_double_lev8(MgDevLevel L, const float *__restrict__ a, double *__restrict__ b)
+{
+    pdl_trigger();
+    pdl_wait();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    if (8 * q >= L.nx || j >= L.ny) return;
+    const long long c0 = ((long long)k * L.ny + j) * L.nx + 8 * q;
+    float v[8];
+    if (L.split) {
+        const long long half = ((long long)L.nx * L.ny * L.nz) >> 1;
+        const int ce = (j + k) & 1;
+        const float4 e4 = *reinterpret_cast<const float4 *>(a + ce * half + (c0 >> 1));
+        const float4 o4 = *reinterpret_cast<const float4 *>(a + (1 - ce) * half + (c0 >> 1));
+        v[0] = e4.x; v[1] = o4.x; v[2] = e4.y; v[3] = o4.y; v[4] = e4.z; v[5] = o4.z; v[6] = e4.w; v[7] = o4.w;
+    } else {
+        const float4 l4 = *reinterpret_cast<const float4 *>(a + c0), h4 = *reinterpret_cast<const float4 *>(a + c0 + 4);
+        v[0] = l4.x; v[1] = l4.y; v[2] = l4.z; v[3] = l4.w; v[4] = h4.x; v[5] = h4.y; v[6] = h4.z; v[7] = h4.w;
+    }
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+        *reinterpret_cast<double2 *>(b + c0 + 2 * t) = make_double2((double)v[2 * t], (double)v[2 * t + 1]);
+}
+
 inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 // a V-cycle kernel launch; pdl: with the programmatic stream serialisation
@@ -989,11 +1037,17 @@ void mg_vcycle(cudaStream_t s, const MgHier<T> &H, int l, const int *pre, const 
 
 void mg_to_float(cudaStream_t s, const MgDevLevel &L, const double *a, float *b)
 {
-    k_to_float_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
+    if (L.nx % 8 == 0)
+        k_to_float_lev8<<<g3(L.nx / 8, L.ny, L.nz), B38, 0, s>>>(L, a, b);
+    else
+        k_to_float_lev<<<g3(L.nx, L.ny, L.nz), B38, 0, s>>>(L, a, b);
 }
 void mg_to_double(cudaStream_t s, const MgDevLevel &L, const float *a, double *b, int pdl)
 {
-    launch_k(pdl, k_to_double_lev, g3(L.nx, L.ny, L.nz), B38, s, L, a, b);
+    if (L.nx % 8 == 0)
+        launch_k(pdl, k_to_double_lev8, g3(L.nx / 8, L.ny, L.nz), B38, s, L, a, b);
+    else
+        launch_k(pdl, k_to_double_lev, g3(L.nx, L.ny, L.nz), B38, s, L, a, b);
 }
 
 // Algorithmic bytes of one V-cycle from level l (each array a kernel reads

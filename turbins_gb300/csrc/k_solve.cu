@@ -240,7 +240,9 @@ __global__ void k_ib_resid64(IbDev ib, const double *__restrict__ b, const doubl
 // 16-byte (4-byte for status) loads, the x tables are padded to the pitch.
 // Immersed points get a placeholder that k_ib_jac32 overwrites; pad columns
 // (i >= NX) are not written.
-__global__ void k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
+// four blocks of 32 x 8 per SM (64 registers): measured 17 % faster at
+// 513x257x257 than the three that 76 registers allow
+__global__ void __launch_bounds__(HBX *HBY, 4) k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
                               const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
                               int first)
 {
