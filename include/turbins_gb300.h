@@ -133,16 +133,19 @@ int turb_destroy(turb_ctx *ctx);
 int turb_field_upload(turb_ctx *ctx, int field, const double *host_da);
 int turb_field_download(turb_ctx *ctx, int field, double *host_da);
 /* n fields in one call (host[t] <-> fields[t]); the call returns when every
- * copy has completed.  Each field moves as one contiguous copy through a
+ * copy has completed.  A field moves either as one contiguous copy through a
  * device staging buffer, the copy of one field overlapping the layout
- * conversion of the one before; from page-locked arrays (turb_host_alloc or
- * turb_host_register, whole array) the copies run asynchronously on the copy
- * engines.  With TURB_HOST_COPY_KERNEL page-locked arrays are instead read /
- * written in place by the layout kernel across the host link. */
+ * conversion of the one before (from page-locked arrays -- turb_host_alloc
+ * or turb_host_register, whole array -- on the copy engines), or, for a
+ * page-locked array, by the layout kernel reading / writing it in place
+ * across the host link.  TURB_HOST_COPY_AUTO (default): page-locked uploads
+ * by the copy engines, page-locked downloads by the kernel; _DMA / _KERNEL:
+ * one way for both directions.  Pageable arrays always go through staging. */
 int turb_fields_upload(turb_ctx *ctx, int n, const int *fields, const double *const *host_da);
 int turb_fields_download(turb_ctx *ctx, int n, const int *fields, double *const *host_da);
-#define TURB_HOST_COPY_DMA 0      /* default */
-#define TURB_HOST_COPY_KERNEL 1
+#define TURB_HOST_COPY_AUTO 0
+#define TURB_HOST_COPY_DMA 1
+#define TURB_HOST_COPY_KERNEL 2
 int turb_set_host_copy(turb_ctx *ctx, int mode);
 int turb_set_pressure_mode(turb_ctx *ctx, int mode);
 /* Initial guess of the Poisson solve.  PREVIOUS: the last solution (the
