@@ -37,12 +37,12 @@ __device__ __forceinline__ double block_max(double m)
 {
     __shared__ double sm[32];
     int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    m = turb_warp_maxbits(m);
     if ((lt & 31) == 0) sm[lt >> 5] = m;
     __syncthreads();
     if (lt < 32) {
         m = (lt < (nt >> 5)) ? sm[lt] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        m = turb_warp_maxbits(m);
     }
     return m;
 }
@@ -72,7 +72,7 @@ __global__ void k_div_noalloc(int NX, int NY, int NZ, long long PX, const double
                 dc = fabs(ad(ad(dudx, dvdy), dwdz));
             }
             div[p] = dc;
-            m = turb_nanmax(m, dc);
+            m = turb_maxbits(m, dc);
         }
     m = block_max(m);
     if (threadIdx.x == 0 && threadIdx.y == 0)
@@ -82,7 +82,7 @@ __global__ void k_div_noalloc(int NX, int NY, int NZ, long long PX, const double
 __global__ void k_max_noalloc(int nparts, double *__restrict__ part)
 {
     double m = 0.0;
-    for (int t = threadIdx.x; t < nparts; t += blockDim.x) m = turb_nanmax(m, part[t]);
+    for (int t = threadIdx.x; t < nparts; t += blockDim.x) m = turb_maxbits(m, part[t]);
     m = block_max(m);
     if (threadIdx.x == 0) part[TURB_NOALLOC_MAX_BLOCKS] = m;
 }

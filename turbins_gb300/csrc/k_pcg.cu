@@ -322,17 +322,17 @@ __global__ void k_rmax(MgDevLevel L, const double *__restrict__ r, double *__res
             int k = blockIdx.z * KC + kk;
             if (k >= L.nz) break;
             long long c = ((long long)k * L.ny + j) * L.nx + i;
-            m = turb_nanmax(m, fabs(r[c]) * ixy * izs[kk]);
+            m = turb_maxbits(m, fabs(r[c]) * ixy * izs[kk]);
         }
     }
     __shared__ double sm[32];
     int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    m = turb_warp_maxbits(m);
     if ((lt & 31) == 0) sm[lt >> 5] = m;
     __syncthreads();
     if (lt < 32) {
         m = lt < (nt >> 5) ? sm[lt] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        m = turb_warp_maxbits(m);
         if (lt == 0) part[blk3()] = m;
     }
 }
@@ -340,14 +340,14 @@ __global__ void k_rmax(MgDevLevel L, const double *__restrict__ r, double *__res
 __global__ void k_max_parts(const double *__restrict__ part, int n, double *__restrict__ dst)
 {
     double m = 0.0;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) m = turb_nanmax(m, part[t]);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) m = turb_maxbits(m, part[t]);
     __shared__ double sm[32];
-    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    m = turb_warp_maxbits(m);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x < 32) {
         m = threadIdx.x < (int)(blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        m = turb_warp_maxbits(m);
         if (threadIdx.x == 0) *dst = m;
     }
 }

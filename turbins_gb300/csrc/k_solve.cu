@@ -187,6 +187,7 @@ __global__ void k_helm_resid64(Dims d, HelmTab h, const uint8_t *__restrict__ st
     }
     __syncthreads();
     double r2 = 0.0;
+    pdl_trigger();   // the immersed rows' kernel (disjoint points) may start at once
     if (i < d.NX && j < d.NY) {
         const double axy = h.apx[i] + h.apy[j];
         for (int kk = 0; kk < KC; kk++) {
@@ -233,19 +234,21 @@ __global__ void k_ib_resid64(IbDev ib, const double *__restrict__ b, const doubl
     }
     double bs = block_sum(r2);
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
+    pdl_wait();   // as in k_ib_jac32: end after the stencil residual
 }
 
 // inner FP32 Jacobi sweep on A e = r (first sweep from e = 0), four points
 // of a row per thread: e, r, status and the j+-1 / k+-1 neighbours are
 // 16-byte (4-byte for status) loads, the x tables are padded to the pitch.
-// Immersed points get a placeholder that k_ib_jac32 overwrites; pad columns
-// (i >= NX) are not written.
+// Immersed points are left to k_ib_jac32 (not written here, so the two
+// kernels may overlap); pad columns (i >= NX) are not written.
 // four blocks of 32 x 8 per SM (64 registers): measured 17 % faster at
 // 513x257x257 than the three that 76 registers allow
 __global__ void __launch_bounds__(HBX *HBY, 4) k_helm_jac32v(Dims d, HelmTabF h, const uint8_t *__restrict__ st, float a_dt,
                               const float *__restrict__ r, const float *__restrict__ e, float *__restrict__ en,
                               int first)
 {
+    pdl_trigger();   // the immersed rows' kernel may start at once
     const int i0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x), j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i0 >= d.NX || j >= d.NY) return;
     const float4 apx = *reinterpret_cast<const float4 *>(h.apx + i0);
@@ -301,10 +304,12 @@ __global__ void __launch_bounds__(HBX *HBY, 4) k_helm_jac32v(Dims d, HelmTabF h,
                 out[t] = __fmaf_rn(__fadd_rn(rv[t], -acc), __frcp_rn(dg), ev[t]);
             }
         }
-        if (nvalid == 4) {
+        const bool ib4 = sv[0] == T_IMMERSED || sv[1] == T_IMMERSED || sv[2] == T_IMMERSED || sv[3] == T_IMMERSED;
+        if (nvalid == 4 && !ib4) {
             *reinterpret_cast<float4 *>(en + p) = make_float4(out[0], out[1], out[2], out[3]);
         } else {
-            for (int t = 0; t < nvalid; t++) en[p + t] = out[t];
+            for (int t = 0; t < nvalid; t++)
+                if (sv[t] != T_IMMERSED) en[p + t] = out[t];
         }
     }
 }
@@ -462,14 +467,22 @@ __global__ void k_ib_jac32(IbDevF ib, const float *__restrict__ r, const float *
                            float *__restrict__ en, int first)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ib.n) return;
-    long long im = ib.im[t];
-    float inv = __frcp_rn(ib.diag[t]);
-    if (first) { en[im] = r[im] * inv; return; }
-    float acc = ib.diag[t] * e[im];
-    int c = ib.cnt[t];
-    for (int g = 0; g < c; g++) acc += ib.val[t * 8 + g] * e[ib.col[t * 8 + g]];
-    en[im] = fmaf(r[im] - acc, inv, e[im]);
+    if (t < ib.n) {
+        long long im = ib.im[t];
+        float inv = __frcp_rn(ib.diag[t]);
+        if (first) {
+            en[im] = r[im] * inv;
+        } else {
+            float acc = ib.diag[t] * e[im];
+            int c = ib.cnt[t];
+            for (int g = 0; g < c; g++) acc += ib.val[t * 8 + g] * e[ib.col[t * 8 + g]];
+            en[im] = fmaf(r[im] - acc, inv, e[im]);
+        }
+    }
+    // launched as a programmatic dependent of the stencil sweep (which
+    // writes the other points of en): end only after it has completed, so
+    // that the kernels after this one see both
+    pdl_wait();
 }
 
 inline dim3 hgrid(const Dims &d)
@@ -532,12 +545,31 @@ void launch_add_corr(cudaStream_t s, long long n, const double *x, const float *
     k_add_corr<<<1216, 256, 0, s>>>(n, x, e, xn);
 }
 
+// a launch with the programmatic stream serialisation attribute: the kernel
+// may start while the one before it on the stream runs (the immersed rows'
+// kernels are written for that: they read nothing the stencil kernel writes,
+// write only immersed points, and end with pdl_wait)
+template <typename... P, typename... A>
+static void launch_pdl(void (*k)(P...), dim3 g, dim3 b, cudaStream_t s, A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 void launch_helm_resid64(cudaStream_t s, const Dims &d, const HelmTab &h, const uint8_t *st, double a_dt,
                          const double *b, const double *x, float *rf, const IbDev &ib, double *part,
                          long long nparts)
 {
     k_helm_resid64<<<hgrid(d), dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, b, x, rf, part);
-    if (ib.n > 0) k_ib_resid64<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, b, x, rf, part + nparts);
+    if (ib.n > 0) launch_pdl(k_ib_resid64, dim3((ib.n + 255) / 256), dim3(256), s, ib, b, x, rf, part + nparts);
 }
 
 // marching 1: the FP32 Jacobi sweeps after the first march along k through
@@ -551,8 +583,11 @@ void launch_helm_jac32(cudaStream_t s, const Dims &d, const HelmTabF &h, const u
         dim3 gz((unsigned)((d.NX + 4 * HBX - 1) / (4 * HBX)), (unsigned)((d.NY + HBY - 1) / HBY),
                 (unsigned)((d.NZ + JZ - 1) / JZ));
         k_helm_jac32z<<<gz, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en);
-    } else {
-        k_helm_jac32v<<<g, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
+        // k_helm_jac32z writes placeholders at immersed points: the immersed
+        // rows go after it in plain stream order
+        if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
+        return;
     }
-    if (ib.n > 0) k_ib_jac32<<<(ib.n + 255) / 256, 256, 0, s>>>(ib, r, e, en, first);
+    k_helm_jac32v<<<g, dim3(HBX, HBY), 0, s>>>(d, h, st, a_dt, r, e, en, first);
+    if (ib.n > 0) launch_pdl(k_ib_jac32, dim3((ib.n + 255) / 256), dim3(256), s, ib, r, e, en, first);
 }

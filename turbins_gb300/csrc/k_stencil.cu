@@ -242,12 +242,12 @@ __global__ void k_divergence(Dims d, const uint8_t *__restrict__ st, const doubl
     __shared__ double sm[32];
     int lt = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     double m = dc;
-    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    m = turb_warp_maxbits(m);
     if ((lt & 31) == 0) sm[lt >> 5] = m;
     __syncthreads();
     if (lt < 32) {
         m = (lt < (nt >> 5)) ? sm[lt] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        m = turb_warp_maxbits(m);
         if (lt == 0) part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = m;
     }
 }
@@ -255,14 +255,14 @@ __global__ void k_divergence(Dims d, const uint8_t *__restrict__ st, const doubl
 __global__ void k_max_final(long long nparts, const double *__restrict__ part, double *__restrict__ out)
 {
     double m = 0.0;
-    for (long long t = threadIdx.x; t < nparts; t += blockDim.x) m = turb_nanmax(m, part[t]);
+    for (long long t = threadIdx.x; t < nparts; t += blockDim.x) m = turb_maxbits(m, part[t]);
     __shared__ double sm[32];
-    for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    m = turb_warp_maxbits(m);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x < 32) {
         m = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = turb_nanmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        m = turb_warp_maxbits(m);
         if (threadIdx.x == 0) *out = m;
     }
 }

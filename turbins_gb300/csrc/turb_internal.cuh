@@ -127,11 +127,28 @@ struct MgLevel {
     double pin;                     // corner east-face coefficient
 };
 
-// Maximum of two non-negative values that keeps a NaN: fmax drops a NaN
-// operand, which would let a non-finite field pass a divergence gate.
-__device__ __forceinline__ double turb_nanmax(double a, double b)
+// Maximum of two values whose magnitude is all that can appear (fabs results
+// and products of non-negative factors: non-negative numbers, +inf, NaN) that
+// keeps a NaN -- fmax drops a NaN operand, which would let a non-finite field
+// pass a divergence gate.  It compares the bit patterns on the integer pipe,
+// which leaves the FP64 pipe to the stencil arithmetic: for such values the
+// order of the patterns as unsigned integers is the numeric order, and every
+// NaN pattern (either sign) lies above +inf.
+__device__ __forceinline__ double turb_maxbits(double a, double b)
 {
-    return (a != a || a > b) ? a : b;
+    const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+    return __longlong_as_double((long long)(x > y ? x : y));
+}
+// turb_maxbits over the 32 lanes of a warp (every lane gets the result)
+__device__ __forceinline__ double turb_warp_maxbits(double v)
+{
+    unsigned long long m = (unsigned long long)__double_as_longlong(v);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    return __longlong_as_double((long long)m);
 }
 
 // Programmatic dependent launch.  A kernel launched with the programmatic
