@@ -132,14 +132,17 @@ __global__ void k_rbgs(MgDevLevel Ld, int color, int zero_init, const T *__restr
 }
 
 // The same half sweep on colour-split FP32 storage, four cells of one row per
-// thread (nx a multiple of 8) in each of two planes k0, k0+1: the cells' own
+// thread (nx a multiple of 8) in each of `planes` planes (2 on the large
+// levels, 1 on the small ones, whose launches are latency-bound and need
+// every thread they can get): the cells' own
 // b and invd, their x-neighbours (other colour, indices m-1+p .. m+p for row
 // parity p) and the j+-1 / k+-1 neighbours are float4 loads, the x metric
 // tables come as float4 from their parity-split copies (dxp / rlp / rrp),
 // indices are 32-bit, and the row constants are loaded once.  The arithmetic
 // per cell is s_row's, operation for operation.
-constexpr int RB4_PLANES = 2;
-__global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__restrict__ b,
+constexpr int RB4_PLANES = 2;                    // planes per thread on the large levels
+constexpr long long RB4_PLANES_CELLS = 1ll << 22;   // levels of at least this many cells
+__global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, int planes, const float *__restrict__ b,
                         const float *__restrict__ invd, float *__restrict__ x)
 {
     pdl_trigger();
@@ -151,8 +154,8 @@ __global__ void k_rbgs4(MgDevLevel Ld, int color, int zero_init, const float *__
     const float dyj = Ld.dyf[j], ryj = Ld.rfyf[j], ryj1 = Ld.rfyf[j + 1];
 #pragma unroll
     for (int g = 0; g < RB4_PLANES; g++) {
-        const int k = blockIdx.z * RB4_PLANES + g;
-        if (k >= nz) break;
+        const int k = blockIdx.z * planes + g;
+        if (g >= planes || k >= nz) break;
         const int p = (color + j + k) & 1;
         const int m0 = (k * ny + j) * hx + 4 * q4;
         const float4 bb = *reinterpret_cast<const float4 *>(b + (size_t)color * half + m0);
@@ -915,8 +918,9 @@ void rb_half(cudaStream_t s, const MgDevLevel &L, int color, int zero_init, cons
                     return;
                 }
             }
-            dim3 g4p(g4.x, g4.y, (unsigned)((L.nz + RB4_PLANES - 1) / RB4_PLANES));
-            launch_k(pdl, k_rbgs4, g4p, B38, s, L, color, zero_init, b, invd, x);
+            const int planes = (long long)L.nx * L.ny * L.nz >= RB4_PLANES_CELLS ? RB4_PLANES : 1;
+            dim3 g4p(g4.x, g4.y, (unsigned)((L.nz + planes - 1) / planes));
+            launch_k(pdl, k_rbgs4, g4p, B38, s, L, color, zero_init, planes, b, invd, x);
             return;
         }
     }
