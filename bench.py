@@ -58,8 +58,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--kv", type=int, default=None,
                     help="kernel variants (turb_set_sweep_kernels flags; default: the library's)")
-    ap.add_argument("--host-copy", default=None, choices=["auto", "dma", "kernel"],
+    ap.add_argument("--host-copy", default=None, choices=["dma", "kernel"],
                     help="how page-locked host arrays move in the e2e leg (turb_set_host_copy; default: the library's)")
+    ap.add_argument("--mg-sweeps", default=None,
+                    help="red-black sweeps (pre = post) of the mixed V-cycle: finest,next,coarser (e.g. 4,5,12)")
     ap.add_argument("--mg-cluster", type=int, default=None,
                     help="one-cluster V-cycle from the first level of at most this many cells (turb_set_mg_cluster)")
     ap.add_argument("--analytic-geometry", action="store_true",
@@ -423,9 +425,14 @@ def main():
         ctx.set_sweep_kernels(a.kv)
     if a.mg_cluster is not None:
         ctx.set_mg_cluster(a.mg_cluster)
+    if a.mg_sweeps is not None:
+        s0, s1, s2 = (int(v) for v in a.mg_sweeps.split(","))
+        ctx.set_pressure_mode(api.PMODE_MIXED)
+        ctx.set_mg_sweeps(s0, s0)
+        ctx.set_mg_coarse_sweeps(1, s1, s1)
+        ctx.set_mg_coarse_sweeps(2, s2, s2)
     if a.host_copy is not None:
-        ctx.set_host_copy({"auto": api.HOST_COPY_AUTO, "dma": api.HOST_COPY_DMA,
-                           "kernel": api.HOST_COPY_KERNEL}[a.host_copy])
+        ctx.set_host_copy(api.HOST_COPY_DMA if a.host_copy == "dma" else api.HOST_COPY_KERNEL)
     pmode = api.PMODE_MIXED if a.pmode == "mixed" else api.PMODE_FP64
     ctx.set_pressure_mode(pmode)
     guess = {"previous": api.GUESS_PREVIOUS, "extrapolate": api.GUESS_EXTRAPOLATE, "learned": api.GUESS_LEARNED,

@@ -138,12 +138,11 @@ int turb_field_download(turb_ctx *ctx, int field, double *host_da);
  * conversion of the one before (from page-locked arrays -- turb_host_alloc
  * or turb_host_register, whole array -- on the copy engines), or, for a
  * page-locked array, by the layout kernel reading / writing it in place
- * across the host link.  TURB_HOST_COPY_AUTO (default): page-locked uploads
- * by the copy engines, page-locked downloads by the kernel; _DMA / _KERNEL:
- * one way for both directions.  Pageable arrays always go through staging. */
+ * across the host link.  TURB_HOST_COPY_KERNEL (default): page-locked
+ * arrays by the kernel; TURB_HOST_COPY_DMA: through staging on the copy
+ * engines.  Pageable arrays always go through staging. */
 int turb_fields_upload(turb_ctx *ctx, int n, const int *fields, const double *const *host_da);
 int turb_fields_download(turb_ctx *ctx, int n, const int *fields, double *const *host_da);
-#define TURB_HOST_COPY_AUTO 0
 #define TURB_HOST_COPY_DMA 1
 #define TURB_HOST_COPY_KERNEL 2
 int turb_set_host_copy(turb_ctx *ctx, int mode);

@@ -1,8 +1,8 @@
 """Host <-> device transfers (turb_fields_upload / turb_fields_download and
 the single-field calls built on them): every field round-trips bit for bit,
-with pinned and pageable host arrays, in each host-copy mode (copy engines
-through staging, the layout kernel across the host link, or the default
-mix), for field counts that use both staging buffers more than once."""
+with pinned and pageable host arrays, in both host-copy modes (copy engines
+through staging, or the layout kernel across the host link), for field
+counts that use both staging buffers more than once."""
 import numpy as np
 import pytest
 
@@ -19,13 +19,13 @@ def api():
     return A
 
 
-@pytest.mark.parametrize("mode", ["auto", "dma", "kernel"])
+@pytest.mark.parametrize("mode", ["dma", "kernel"])
 @pytest.mark.parametrize("pinned", ["pageable", "registered", "driver"])
 def test_fields_round_trip(api, pinned, mode):
     case = _cases.bump_small(24, 12, 8)
     g = case.grid
     ctx = api.Context(g, case.params)
-    ctx.set_host_copy({"auto": api.HOST_COPY_AUTO, "dma": api.HOST_COPY_DMA, "kernel": api.HOST_COPY_KERNEL}[mode])
+    ctx.set_host_copy(api.HOST_COPY_DMA if mode == "dma" else api.HOST_COPY_KERNEL)
     rng = np.random.Generator(np.random.PCG64(5))
     fields = [api.F_U, api.F_V, api.F_W, api.F_PHI, api.F_DPX, api.F_DPY, api.F_DPZ, api.F_C0]
     src = [np.ascontiguousarray(rng.standard_normal(g.shape)) for _ in fields]

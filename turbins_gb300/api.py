@@ -27,7 +27,7 @@ PMODE_FP64, PMODE_MIXED = 0, 1
 HMODE_FP64, HMODE_MIXED = 0, 1
 GUESS_PREVIOUS, GUESS_EXTRAPOLATE, GUESS_LEARNED, GUESS_PROJECT = 0, 1, 2, 3
 KV_MARCHING, KV_ENO_SEGMENTS, KV_PDL, KV_CLUSTER_VCYCLE, KV_SWEEP_PAIRS = 1, 2, 4, 8, 16
-HOST_COPY_AUTO, HOST_COPY_DMA, HOST_COPY_KERNEL = 0, 1, 2
+HOST_COPY_DMA, HOST_COPY_KERNEL = 1, 2
 
 STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "non-finite residual",
           5: "device allocation failed", 6: "scratch limit", 7: "restart file I/O", 8: "restart file mismatch"}
@@ -236,10 +236,9 @@ class Context:
         return a
 
     def set_host_copy(self, mode):
-        """turb_set_host_copy: HOST_COPY_AUTO (uploads on the copy engines,
-        downloads by the layout kernel), HOST_COPY_DMA (staged copies on the
-        copy engines both ways) or HOST_COPY_KERNEL (the layout kernel reads
-        / writes page-locked host arrays in place both ways)"""
+        """turb_set_host_copy: HOST_COPY_KERNEL (default: the layout kernel
+        reads / writes page-locked host arrays in place) or HOST_COPY_DMA
+        (staged copies on the copy engines)"""
         _check(self.lib.turb_set_host_copy(self.ctx, int(mode)), "set_host_copy")
 
     def upload_many(self, pairs):

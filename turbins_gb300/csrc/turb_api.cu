@@ -176,7 +176,7 @@ struct turb_ctx {
     long long mg_cluster_cells = 1 << 17;   // TURB_KV_CLUSTER_VCYCLE from the first level of at most this many cells
     // TURB_KV_SWEEP_PAIRS: the finest FP32 level's two-sweeps-per-pass smoother
     RbTbPlan tbplan;
-    int host_copy = TURB_HOST_COPY_AUTO;   // how page-locked host arrays move (turb_set_host_copy)
+    int host_copy = TURB_HOST_COPY_KERNEL;   // how page-locked host arrays move (turb_set_host_copy)
     float *tb_x1 = nullptr;   // its second x array (ping-pong)
     int *tb_err = nullptr;    // set by a block whose copy wait timed out
     double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
@@ -1179,10 +1179,11 @@ static int stage_setup(turb_ctx *c)
 // (for page-locked arrays the copies run on the copy engines at the host
 // link's rate); or, for page-locked arrays, the layout kernel reads or
 // writes the host array in place (its loads / stores cross the host link).
-// TURB_HOST_COPY_AUTO uploads through the copy engines and downloads by the
-// kernel: on GB300 the device-to-host copies of the copy engines ran at 190
-// GB/s in some runs and at a quarter of that in others, the kernel's stores
-// at a steady 170 GB/s.  Returns when everything has landed.
+// TURB_HOST_COPY_KERNEL (default) takes the second way for page-locked
+// arrays: on GB300 the copy engines' transfers issued after a long step ran
+// at 190-210 GB/s in some runs and at a quarter of that in others, in either
+// direction, while the kernel's loads and stores held a steady 170-200 GB/s.
+// Returns when everything has landed.
 // the device address of page-locked host memory (cudaMallocHost or
 // registered), or null for pageable memory
 static const void *host_device_ptr(const void *h)
@@ -1200,8 +1201,8 @@ int turb_fields_upload(turb_ctx *c, int n, const int *fields, const double *cons
     if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
     for (int t = 0; t < n; t++)
         if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
-    // page-locked arrays with TURB_HOST_COPY_KERNEL: the layout kernel reads
-    // them over the host link
+    // page-locked arrays with TURB_HOST_COPY_KERNEL (default): the layout
+    // kernel reads them over the host link
     bool direct = c->host_copy == TURB_HOST_COPY_KERNEL;
     for (int t = 0; t < n && direct; t++) direct = host_device_ptr(host[t]) != nullptr;
     if (direct) {
@@ -1236,9 +1237,9 @@ int turb_fields_download(turb_ctx *c, int n, const int *fields, double *const *h
     if (!c || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
     for (int t = 0; t < n; t++)
         if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
-    // page-locked arrays with TURB_HOST_COPY_KERNEL or _AUTO: the layout
+    // page-locked arrays with TURB_HOST_COPY_KERNEL (default): the layout
     // kernel writes them over the host link
-    bool direct = c->host_copy != TURB_HOST_COPY_DMA;
+    bool direct = c->host_copy == TURB_HOST_COPY_KERNEL;
     for (int t = 0; t < n && direct; t++) direct = host_device_ptr(host[t]) != nullptr;
     if (direct) {
         for (int t = 0; t < n; t++)
@@ -1269,7 +1270,7 @@ int turb_fields_download(turb_ctx *c, int n, const int *fields, double *const *h
 
 int turb_set_host_copy(turb_ctx *c, int mode)
 {
-    if (!c || mode < TURB_HOST_COPY_AUTO || mode > TURB_HOST_COPY_KERNEL) return TURB_ERR_ARG;
+    if (!c || (mode != TURB_HOST_COPY_DMA && mode != TURB_HOST_COPY_KERNEL)) return TURB_ERR_ARG;
     c->host_copy = mode;
     return TURB_OK;
 }
