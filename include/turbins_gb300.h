@@ -312,6 +312,18 @@ int turb_velocity_divergence_noalloc(int nx, int ny, int nz, long long pitch, co
 
 /* one TVD-RK2 step of the restated driver (the absent main loop) */
 int turb_step(turb_ctx *ctx, double dt, turb_step_stats *stats);
+/* turb_fields_upload, turb_step, turb_fields_download of the same n fields
+ * and host arrays in one call, for a driver that moves the state every step:
+ * the same results, with the copies of the fields the step reads late
+ * (the concentrations after the velocity convective terms when no open face
+ * sets them, dpx, dpy, dpz at the velocity RHS, phi at the Poisson solve)
+ * overlapping the step's first kernels, and the downloads of the
+ * concentrations (final after the second stage's concentration solve) and
+ * of dpx, dpy, dpz, phi its last ones (page-locked arrays with
+ * TURB_HOST_COPY_KERNEL; otherwise the three calls in turn).
+ * Returns when every copy has landed. */
+int turb_step_host(turb_ctx *ctx, double dt, int n, const int *fields, double *const *host_da,
+                   turb_step_stats *stats);
 
 /* ---- measurement ---------------------------------------------------------
  * CUDA-event timing per kernel group on the context stream (enable resets the

@@ -56,3 +56,43 @@ def test_fields_round_trip(api, pinned, mode):
             for a in src + dst:
                 api.host_unregister(a)
         ctx.close()
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_host_matches_separate_calls(api, pinned):
+    """turb_step_host (the state uploaded, one step, downloaded into the same
+    arrays, the late fields' copies overlapping the step) gives the same bits
+    and the same solver statistics as turb_fields_upload, turb_step and
+    turb_fields_download in turn, for three steps of the immersed multi-bump
+    case; with pageable arrays it is those three calls."""
+    case = _cases.multi_small()
+    s = _cases.random_state(case, seed=3)
+    g = case.grid
+    fields = [api.F_U, api.F_V, api.F_W, api.F_PHI, api.F_DPX, api.F_DPY, api.F_DPZ] + \
+        [api.F_C0 + i for i in range(case.params.nconc)]
+    out, stats = [], []
+    for fused in (False, True):
+        ctx = api.Context(g, case.params)
+        try:
+            ctx.load_state(s)
+            bufs = [api.host_empty(g.shape) if pinned else np.zeros(g.shape) for _ in fields]
+            pairs = list(zip(fields, bufs))
+            ctx.download_many(pairs)
+            st = []
+            for _ in range(3):
+                if fused:
+                    st.append(ctx.step_host(case.dt, pairs))
+                else:
+                    ctx.upload_many(pairs)
+                    st.append(ctx.step(case.dt))
+                    ctx.download_many(pairs)
+            out.append([b.copy() for b in bufs])
+            stats.append(st)
+        finally:
+            ctx.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    for a, b in zip(stats[0], stats[1]):
+        for k in a:
+            if k != "kernel_launches":
+                assert a[k] == b[k], k

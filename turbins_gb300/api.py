@@ -569,6 +569,18 @@ class Context:
         _check(self.lib.turb_step(self.ctx, C.c_double(dt), C.byref(st)), "turb_step")
         return st.as_dict(self.params.nconc)
 
+    def step_host(self, dt, pairs):
+        """turb_step_host: upload [(field, array), ...], one step, download
+        into the same arrays, with the late fields' copies overlapped"""
+        n = len(pairs)
+        f = (C.c_int * n)(*[int(fi) for fi, _ in pairs])
+        for _, a in pairs:
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.grid.npts
+        h = (C.c_void_p * n)(*[a.ctypes.data for _, a in pairs])
+        st = StepStats()
+        _check(self.lib.turb_step_host(self.ctx, C.c_double(dt), n, f, h, C.byref(st)), "turb_step_host")
+        return st.as_dict(self.params.nconc)
+
 
 def ENO_compute_convective_terms(order, D0, P, V):
     """ENO.c:103-245 on one host line, computed on the GPU."""

@@ -211,6 +211,12 @@ struct turb_ctx {
     // a copy stream and the events that hand a buffer between the streams
     double *xfer[2] = {nullptr, nullptr};
     cudaStream_t cs = nullptr, cs2 = nullptr;   // copy streams of the staged host copies (even / odd fields)
+    // turb_step_host: the stream that moves the late fields, its events and
+    // the step's hooks (set only during that call)
+    cudaStream_t ios = nullptr;
+    // start, dp in, phi in, dp / phi out, c in, c out
+    cudaEvent_t io_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    struct StepIo *io = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_freed[2] = {nullptr, nullptr};
     // ghost-cell stencils made by turb_geometry (one allocation per quantity)
     GeomIb gib[4];
@@ -1143,6 +1149,9 @@ int turb_destroy(turb_ctx *c)
         if (c->ev_freed[t]) cudaEventDestroy(c->ev_freed[t]);
     }
     if (c->cs) cudaStreamDestroy(c->cs);
+    if (c->ios) cudaStreamDestroy(c->ios);
+    for (auto &e : c->io_ev)
+        if (e) cudaEventDestroy(e);
     if (c->cs2) cudaStreamDestroy(c->cs2);
     cudaStreamDestroy(c->s);
     delete c;
@@ -1156,6 +1165,7 @@ static double *field_ptr(turb_ctx *c, int f)
 }
 
 void launch_da_pitch(cudaStream_t s, const Dims &d, const double *src, double *dst, int to_pitched);
+void launch_da_pitch_lean(cudaStream_t s, const Dims &d, const double *src, double *dst, int to_pitched);
 
 // transfer staging, made on first use
 static int stage_setup(turb_ctx *c)
@@ -2942,7 +2952,91 @@ int turb_host_free(void *p)
         if (rc_ != TURB_OK) return rc_;  \
     } while (0)
 
+// turb_step_host: the fields the step reads late (the concentrations after
+// the velocity convective terms, dpx, dpy, dpz at the velocity RHS, phi at
+// the Poisson solve) are uploaded on a second stream while the step's first
+// kernels run; the concentrations are downloaded on it once their RK average
+// (right after the second stage's concentration solve) has written them,
+// while the pressure solve runs, and dpx, dpy, dpz and phi once the second
+// stage's projection has written them, while the last divergence check and
+// the velocities' RK average run.  The step waits for them through these
+// hooks; the copies beside the step use a kernel on a few SMs.
+struct StepIo {
+    std::vector<char> late;      // per field of the call: dpx, dpy, dpz, phi
+    std::vector<char> conc;      // per field: c_i, moved with the late ones (no open boundaries)
+    bool dp_wait = false, phi_wait = false, c_wait = false, out_started = false, c_out_started = false;
+    int n = 0;
+    const int *fields = nullptr;
+    double *const *host = nullptr;
+};
+
+static bool late_field(int f)
+{
+    return f == TURB_F_DPX || f == TURB_F_DPY || f == TURB_F_DPZ || f == TURB_F_PHI;
+}
+
+static void step_io_before_rhs(turb_ctx *c)
+{
+    if (c->io->dp_wait) {
+        cudaStreamWaitEvent(c->s, c->io_ev[1], 0);
+        c->io->dp_wait = false;
+    }
+}
+
+static void step_io_before_conc(turb_ctx *c)
+{
+    if (c->io->c_wait) {
+        cudaStreamWaitEvent(c->s, c->io_ev[4], 0);
+        c->io->c_wait = false;
+    }
+}
+
+static void step_io_before_poisson(turb_ctx *c)
+{
+    if (c->io->phi_wait) {
+        cudaStreamWaitEvent(c->s, c->io_ev[2], 0);
+        c->io->phi_wait = false;
+    }
+}
+
+static int step_io_after_conc_average(turb_ctx *c)
+{
+    StepIo &io = *c->io;
+    bool any = false;
+    for (int t = 0; t < io.n; t++) any = any || io.conc[t];
+    if (!any) return TURB_OK;
+    TURB_CHECK(cudaEventRecord(c->io_ev[0], c->s));   // the concentrations are final
+    TURB_CHECK(cudaStreamWaitEvent(c->ios, c->io_ev[0], 0));
+    for (int t = 0; t < io.n; t++)
+        if (io.conc[t])
+            launch_da_pitch_lean(c->ios, c->d, field_ptr(c, io.fields[t]), (double *)host_device_ptr(io.host[t]), 0);
+    TURB_CHECK(cudaEventRecord(c->io_ev[5], c->ios));
+    io.c_out_started = true;
+    return check_launch(c);
+}
+
+static int step_io_after_projection(turb_ctx *c)
+{
+    StepIo &io = *c->io;
+    TURB_CHECK(cudaEventRecord(c->io_ev[0], c->s));   // dpx, dpy, dpz, phi are final
+    TURB_CHECK(cudaStreamWaitEvent(c->ios, c->io_ev[0], 0));
+    for (int t = 0; t < io.n; t++)
+        if (io.late[t])
+            launch_da_pitch_lean(c->ios, c->d, field_ptr(c, io.fields[t]), (double *)host_device_ptr(io.host[t]), 0);
+    TURB_CHECK(cudaEventRecord(c->io_ev[3], c->ios));
+    io.out_started = true;
+    return check_launch(c);
+}
+
+static int step_impl(turb_ctx *c, double dt, turb_step_stats *st);
+
 int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
+{
+    if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
+    return step_impl(c, dt, st);
+}
+
+static int step_impl(turb_ctx *c, double dt, turb_step_stats *st)
 {
     if (!c || !(dt > 0.0)) return TURB_ERR_ARG;
     turb_step_stats local;
@@ -2957,16 +3051,24 @@ int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
         for (int ic = 0; ic < c->prm.nconc; ic++) STEP_TRY(turb_Inflow_conc_profile(c, ic, c->time));
     }
     if (c->ob.out) STEP_TRY(turb_store_old_outflow(c));
-    STEP_TRY(turb_store_old_data(c));
+    // the old data of the velocities now, of the concentrations once the
+    // velocity convective terms are queued (nothing reads the concentrations
+    // before that, so a host copy of them can still be in flight)
+    for (int q = 0; q < 3; q++) STEP_TRY(turb_store_old_field(c, TURB_F_U + q));
     for (int stage = 0; stage < 2; stage++) {
         c->stage = stage;
         if (c->ob.out) STEP_TRY(turb_Outflow_impose_convective_boundary(c, dt));
         STEP_TRY(turb_Velocity_cell_center(c));
-        if (c->prm.nconc > 1) STEP_TRY(turb_Conc_compute_total_concentration(c));
         STEP_TRY(turb_Velocity_convective_terms(c, 'u'));
         STEP_TRY(turb_Velocity_convective_terms(c, 'v'));
         STEP_TRY(turb_Velocity_convective_terms(c, 'w'));
+        if (stage == 0) {
+            if (c->io) step_io_before_conc(c);
+            for (int ic = 0; ic < c->prm.nconc; ic++) STEP_TRY(turb_store_old_field(c, TURB_F_C0 + ic));
+        }
+        if (c->prm.nconc > 1) STEP_TRY(turb_Conc_compute_total_concentration(c));
         for (int ic = 0; ic < c->prm.nconc; ic++) STEP_TRY(turb_Conc_convective_terms(c, ic));
+        if (c->io) step_io_before_rhs(c);
         STEP_TRY(turb_Velocity_set_RHS(c, 'u', dt));
         STEP_TRY(turb_Velocity_set_RHS(c, 'v', dt));
         STEP_TRY(turb_Velocity_set_RHS(c, 'w', dt));
@@ -2977,16 +3079,102 @@ int turb_step(turb_ctx *c, double dt, turb_step_stats *st)
             STEP_TRY(turb_Conc_set_RHS(c, ic, dt));
             STEP_TRY(turb_Conc_solve(c, ic, dt, &st->conc_iters[ic][stage]));
         }
+        if (stage == 1) {   // the concentrations are final: their RK average now (nothing after reads them)
+            for (int ic = 0; ic < c->prm.nconc; ic++) STEP_TRY(turb_rk_average_field(c, TURB_F_C0 + ic, 0.5, 0.5));
+            if (c->io) STEP_TRY(step_io_after_conc_average(c));
+        }
         STEP_TRY(turb_Pressure_set_RHS(c, dt));
+        if (c->io) step_io_before_poisson(c);
         STEP_TRY(turb_Pressure_solve(c, &st->p_iters[stage], &st->p_relres[stage]));
         STEP_TRY(turb_Pressure_project_velocity(c, dt));
+        if (c->io && stage == 1) STEP_TRY(step_io_after_projection(c));
         STEP_TRY(turb_Pressure_compute_velocity_divergence(c, &st->div_max[stage]));
     }
-    STEP_TRY(turb_rk_average(c, 0.5, 0.5));
+    for (int q = 0; q < 3; q++) STEP_TRY(turb_rk_average_field(c, TURB_F_U + q, 0.5, 0.5));
     if (c->ob.out) STEP_TRY(turb_rk_average_outflow(c, 0.5, 0.5));
     if (c->deposit_on) STEP_TRY(turb_deposit_integrate(c, dt));
     c->time += dt;
     st->kernel_launches = (int)(c->launches - l0);
+    return TURB_OK;
+}
+
+int turb_step_host(turb_ctx *c, double dt, int n, const int *fields, double *const *host, turb_step_stats *st)
+{
+    if (!c || !(dt > 0.0) || n < 0 || (n > 0 && (!fields || !host))) return TURB_ERR_ARG;
+    bool direct = c->host_copy == TURB_HOST_COPY_KERNEL;
+    for (int t = 0; t < n; t++) {
+        if (!field_ptr(c, fields[t]) || !host[t]) return TURB_ERR_ARG;
+        direct = direct && host_device_ptr(host[t]) != nullptr;
+    }
+    if (!direct) {   // the calls it stands for, one after the other
+        int rc = turb_fields_upload(c, n, fields, host);
+        if (rc) return rc;
+        rc = step_impl(c, dt, st);
+        if (rc) return rc;
+        return turb_fields_download(c, n, fields, host);
+    }
+    if (!c->ios) TURB_CHECK(cudaStreamCreateWithFlags(&c->ios, cudaStreamNonBlocking));
+    for (auto &e : c->io_ev)
+        if (!e) TURB_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    StepIo io;
+    io.n = n;
+    io.fields = fields;
+    io.host = host;
+    io.late.resize(n);
+    io.conc.resize(n);
+    // the open faces set concentrations at the step's start and average
+    // the outflow planes at its end: then the concentrations move with u, v, w
+    const bool open = c->ob.in || c->ob.out;
+    for (int t = 0; t < n; t++) {
+        io.late[t] = late_field(fields[t]) ? 1 : 0;
+        io.conc[t] = (!open && fields[t] >= TURB_F_C0 && fields[t] < TURB_F_C0 + c->prm.nconc) ? 1 : 0;
+    }
+    for (int t = 0; t < n; t++)
+        if (!io.late[t] && !io.conc[t])
+            launch_da_pitch(c->s, c->d, (const double *)host_device_ptr(host[t]), field_ptr(c, fields[t]), 1);
+    // the late copies start when the early ones have landed (they share the
+    // host link, and the step waits for the early ones) and after the work
+    // already on the context's stream, which may still use the fields
+    TURB_CHECK(cudaEventRecord(c->io_ev[0], c->s));
+    TURB_CHECK(cudaStreamWaitEvent(c->ios, c->io_ev[0], 0));
+    // in the order the step reads them: c_i, then dpx, dpy, dpz, then phi
+    for (int pass = 0; pass < 3; pass++) {
+        bool any = false;
+        for (int t = 0; t < n; t++) {
+            if (!io.late[t] && !io.conc[t]) continue;
+            const int kind = io.late[t] ? (fields[t] == TURB_F_PHI ? 2 : 1) : 0;
+            if (kind != pass) continue;
+            launch_da_pitch_lean(c->ios, c->d, (const double *)host_device_ptr(host[t]), field_ptr(c, fields[t]), 1);
+            any = true;
+        }
+        if (any) {
+            TURB_CHECK(cudaEventRecord(c->io_ev[pass == 0 ? 4 : pass], c->ios));
+            (pass == 0 ? io.c_wait : pass == 1 ? io.dp_wait : io.phi_wait) = true;
+        }
+    }
+    int rc = check_launch(c);
+    if (rc) return rc;
+    c->io = &io;
+    rc = step_impl(c, dt, st);
+    c->io = nullptr;
+    if (rc) {
+        cudaStreamSynchronize(c->ios);
+        return rc;
+    }
+    // a stage that returned early never waited: the context's stream waits now
+    if (io.c_wait) TURB_CHECK(cudaStreamWaitEvent(c->s, c->io_ev[4], 0));
+    if (io.dp_wait) TURB_CHECK(cudaStreamWaitEvent(c->s, c->io_ev[1], 0));
+    if (io.phi_wait) TURB_CHECK(cudaStreamWaitEvent(c->s, c->io_ev[2], 0));
+    for (int t = 0; t < n; t++) {
+        const bool done = (io.late[t] && io.out_started) || (io.conc[t] && io.c_out_started);
+        if (!done) launch_da_pitch(c->s, c->d, field_ptr(c, fields[t]), (double *)host_device_ptr(host[t]), 0);
+    }
+    if (io.out_started) TURB_CHECK(cudaStreamWaitEvent(c->s, c->io_ev[3], 0));
+    if (io.c_out_started) TURB_CHECK(cudaStreamWaitEvent(c->s, c->io_ev[5], 0));
+    rc = check_launch(c);
+    if (rc) return rc;
+    TURB_CHECK(cudaStreamSynchronize(c->s));
+    TURB_CHECK(cudaStreamSynchronize(c->ios));
     return TURB_OK;
 }
 
@@ -3040,6 +3228,40 @@ __global__ void k_da_pitch(Dims d, const double *__restrict__ src, double *__res
     long long c = ((long long)k * d.NY + j) * d.NX + i, p = d.at(i, j, k);
     if (to_pitched) dst[p] = src[c];
     else dst[c] = src[p];
+}
+
+// The same conversion from a few SMs only, for copies that run beside the
+// step's kernels: a grid-stride loop over the DA array, four elements in
+// flight per thread (the host link's latency wants many loads in flight, the
+// step wants its SMs)
+constexpr int DA_LEAN_BLOCKS = 16, DA_LEAN_THREADS = 1024;
+__global__ void __launch_bounds__(DA_LEAN_THREADS) k_da_pitch_lean(Dims d, const double *__restrict__ src,
+                                                                  double *__restrict__ dst, int to_pitched)
+{
+    const long long n = (long long)d.NX * d.NY * d.NZ;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long c0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; c0 < n; c0 += 4 * stride) {
+        double v[4];
+        long long at[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long c = c0 + u * stride;
+            if (c < n) {
+                const long long row = c / d.NX;
+                const long long p = row * d.PX + (c - row * d.NX);
+                at[u] = to_pitched ? p : c;
+                v[u] = src[to_pitched ? c : p];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (c0 + u * stride < n) dst[at[u]] = v[u];
+    }
+}
+
+void launch_da_pitch_lean(cudaStream_t s, const Dims &d, const double *src, double *dst, int to_pitched)
+{
+    k_da_pitch_lean<<<DA_LEAN_BLOCKS, DA_LEAN_THREADS, 0, s>>>(d, src, dst, to_pitched);
 }
 
 void launch_da_pitch(cudaStream_t s, const Dims &d, const double *src, double *dst, int to_pitched)
