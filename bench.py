@@ -472,9 +472,18 @@ def main():
     value = dist.world * nc * a.steps / (ms_max / 1e3) / 1e6
     divmax = max(max(s["div_max"]) for s in stats)
     assert divmax <= 1e-10, "divergence gate failed: %g" % divmax
+    # The later legs start again from the initial state: on this bed the
+    # reference's immersed-boundary stencils let a spanwise-velocity mode grow
+    # from about step 25 at 512x256x256 (the oracle shows the same growth on
+    # the same stencils), so every timed leg stays within the first 20 steps.
+    def restart():
+        ctx.load_state(case.state)
+        ctx.reset_pressure_history()
+
     # ---- end to end through the C ABI with host buffers ---------------------
     e2e = None
     if not a.no_e2e:
+        restart()
         keys = [("u", api.F_U), ("v", api.F_V), ("w", api.F_W), ("phi", api.F_PHI), ("dpx", api.F_DPX),
                 ("dpy", api.F_DPY), ("dpz", api.F_DPZ)] + [("c%d" % i, api.F_C0 + i) for i in range(case.params.nconc)]
         # the step's inputs and outputs in page-locked host memory
@@ -523,13 +532,26 @@ def main():
         arms.insert(0, ("learned_mixed", api.PMODE_MIXED, api.GUESS_LEARNED, a.guess_stages))
     cmp = {}
     if a.cmp_steps > 0:
+        restart()
         for nm, md, gs, stg in arms:            # each arm once untimed (graphs of its mode)
             step_arm(ctx, api, dt, md, gs, stg)
+        restart()                               # the rounds then cover steps 1-20
         rec = {nm: [] for nm, _, _, _ in arms}
-        for _ in range(a.cmp_steps):
+        failed = {}
+        for rnd in range(a.cmp_steps):
             for nm, md, gs, stg in arms:
-                rec[nm].append(step_arm(ctx, api, dt, md, gs, stg))
+                if nm in failed:
+                    continue
+                try:
+                    rec[nm].append(step_arm(ctx, api, dt, md, gs, stg))
+                except api.TurbError as e:   # the arm stops; the others go on from the state it left
+                    failed[nm] = {"round": rnd, "error": str(e), "stats": getattr(e, "stats", None)}
+                    print("arm %s failed in round %d: %s %s" % (nm, rnd, e, failed[nm]["stats"]), file=sys.stderr)
+        for nm, info in failed.items():
+            cmp[nm] = {"failed": info, "steps": len(rec[nm])}
         for nm, lst in rec.items():
+            if nm in failed or not lst:
+                continue
             t = dist.allmax(sum(x[0] for x in lst))
             cmp[nm] = {"value": dist.world * nc * len(lst) / (t / 1e3) / 1e6, "ms_per_step": t / len(lst),
                        "steps": len(lst), "p_iters": [x[1]["p_iters"] for x in lst],
@@ -564,6 +586,7 @@ def main():
                              "bf16_peak_source": bf16_peak()[1],
                              "guess_residual_ratio": ctx.pressure_guess_ratio()})
     gate_n = ctx.divergence_gate_count()
+    gate_floor = ctx.divergence_gate_floor_count()
     ctx.close()
     if net is not None:
         net.close()
@@ -619,7 +642,7 @@ def main():
                 "mixed_previous_guess": cmp.get("mixed_previous_guess"), "learned": learned_info,
                 "geometry_setup": geom, "poisson_alone": poisson, "parity": parity,
                 "solver": {"p_iters": [s["p_iters"] for s in stats], "vel_iters": stats[-1]["vel_iters"],
-                           "gate_tightened": gate_n,
+                           "gate_tightened": gate_n, "gate_at_floor": gate_floor,
                            "conc_iters": stats[-1]["conc_iters"], "div_max": divmax}}
         print(json.dumps(line))
     dist.close()

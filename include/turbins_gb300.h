@@ -162,6 +162,10 @@ int turb_set_pressure_mode(turb_ctx *ctx, int mode);
  * right-hand sides) */
 #define TURB_GUESS_PROJECT 3
 int turb_set_pressure_guess(turb_ctx *ctx, int mode);
+/* forget the earlier solutions the extrapolated, projected and learned
+ * guesses start from (after fields were replaced from elsewhere, e.g. a
+ * state loaded again); the next solves of each stage rebuild it */
+int turb_reset_pressure_history(turb_ctx *ctx);
 /* RK stages whose pressure solve tries the extrapolated / learned candidate:
  * bit 0 the first stage, bit 1 the second (default 3, both) */
 /* kernel variants, all giving the same bits: TURB_KV_MARCHING, the FP32
@@ -191,10 +195,14 @@ int turb_set_sweep_kernels(turb_ctx *ctx, int variants);
 /* max_div > 0: every Poisson solve, after reaching its relative residual,
  * also iterates until dt * max|b - A phi| (the largest divergence the
  * projection with phi leaves, dt of the last turb_Pressure_set_RHS) is at
- * most max_div; 0 (default) turns the gate off.  The count is how often a
- * solve had to go on. */
+ * most max_div, or until the residual's 2-norm is at its round-off floor
+ * (64 DBL_EPSILON |b|: there the estimate sees the rounding of b - A phi
+ * divided by the smallest cell volumes, which no iteration removes); 0
+ * (default) turns the gate off.  The counts are how often a solve had to go
+ * on, and how often the gate let a solve go at the floor. */
 int turb_set_divergence_gate(turb_ctx *ctx, double max_div);
 int turb_divergence_gate_count(turb_ctx *ctx, long long *tightened);
+int turb_divergence_gate_floor_count(turb_ctx *ctx, long long *at_floor);
 /* 1: the learned candidate also goes through the Galerkin fit with this
  * stage's last two solutions (TURB_GUESS_PROJECT's span plus the network's
  * direction).  A fit is kept when it lowers the residual in the S^-1 norm

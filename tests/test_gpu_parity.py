@@ -458,6 +458,28 @@ def test_divergence_gate(api, oracle_mod, name, mk):
     ctx.close()
 
 
+@pytest.mark.parametrize("pmode", ["mixed", "fp64"])
+def test_divergence_gate_stops_at_round_off(api, oracle_mod, pmode):
+    """A gate no residual can meet (1e-30): the solve goes on down to the
+    round-off floor of its residual (64 DBL_EPSILON |b|) and returns there,
+    counted, instead of running into the iteration limit; the projected
+    velocity is as divergence-free as the floor allows."""
+    case = _cases.multi_small()
+    s = _cases.random_state(case, seed=11)
+    dt = case.dt
+    ctx, orc, _ = _pair(case, api, oracle_mod, s)
+    ctx.set_pressure_mode(api.PMODE_MIXED if pmode == "mixed" else api.PMODE_FP64)
+    ctx.set_divergence_gate(1e-30)
+    ctx.Pressure_set_RHS(dt)
+    it, rr = ctx.Pressure_solve()
+    ctx.Pressure_project_velocity(dt)
+    div = ctx.Pressure_compute_velocity_divergence()
+    assert ctx.divergence_gate_floor_count() == 1
+    assert it < case.params.p_maxit and rr <= 64 * np.finfo(np.float64).eps
+    assert div <= 1e-10
+    ctx.close()
+
+
 @pytest.mark.parametrize("name,mk", [("bump", lambda: _cases.bump_small()), ("multi", lambda: _cases.multi_small()),
                                      ("bump_64", lambda: _cases.bump_small(64, 40, 24))])
 def test_marching_sweeps_are_bit_identical(api, oracle_mod, name, mk):

@@ -282,6 +282,10 @@ class Context:
     def set_pressure_guess(self, mode):
         _check(self.lib.turb_set_pressure_guess(self.ctx, mode), "set_pressure_guess")
 
+    def reset_pressure_history(self):
+        """turb_reset_pressure_history: the guesses forget earlier solutions"""
+        _check(self.lib.turb_reset_pressure_history(self.ctx), "reset_pressure_history")
+
     def set_sweep_kernels(self, variants=KV_ENO_SEGMENTS | KV_PDL):
         """kernel variants (KV_MARCHING | KV_ENO_SEGMENTS | KV_PDL | KV_CLUSTER_VCYCLE | KV_SWEEP_PAIRS); all give the same bits"""
         _check(self.lib.turb_set_sweep_kernels(self.ctx, int(variants)), "set_sweep_kernels")
@@ -292,6 +296,12 @@ class Context:
     def divergence_gate_count(self):
         n = C.c_longlong()
         _check(self.lib.turb_divergence_gate_count(self.ctx, C.byref(n)), "divergence_gate_count")
+        return n.value
+
+    def divergence_gate_floor_count(self):
+        """solves the divergence gate let go at the residual's round-off floor"""
+        n = C.c_longlong()
+        _check(self.lib.turb_divergence_gate_floor_count(self.ctx, C.byref(n)), "divergence_gate_floor_count")
         return n.value
 
     def set_guess_galerkin(self, on=True):
@@ -565,8 +575,16 @@ class Context:
         _check(self.lib.turb_pressure_apply(self.ctx, fx, fy), "pressure_apply")
 
     def step(self, dt):
+        """one step; on a solver failure the TurbError carries the step's
+        statistics so far (iterations of every solve that ran) as .stats"""
         st = StepStats()
-        _check(self.lib.turb_step(self.ctx, C.c_double(dt), C.byref(st)), "turb_step")
+        rc = self.lib.turb_step(self.ctx, C.c_double(dt), C.byref(st))
+        if rc != 0:
+            try:
+                _check(rc, "turb_step")
+            except TurbError as e:
+                e.stats = st.as_dict(self.params.nconc)
+                raise
         return st.as_dict(self.params.nconc)
 
     def step_host(self, dt, pairs):

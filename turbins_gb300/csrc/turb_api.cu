@@ -4,6 +4,7 @@
 // grid-only quantities (with the reference's own expressions, so device
 // roundings match) and sequences launches on the context's stream.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -182,6 +183,7 @@ struct turb_ctx {
     double div_gate = 0.0;       // > 0: Poisson solves also reach dt * max|b - A phi| <= div_gate
     double p_dt = 0.0;           // dt of the last Pressure_set_RHS
     long long gate_tightened = 0;
+    long long gate_floor = 0;   // solves the gate let go at the residual's round-off floor
     int nh[2] = {0, 0};
     int guess_taken = 0, guess_tried = 0;
     double guess_logsum = 0.0;   // sum of log(|r candidate| / |r previous|)
@@ -1334,6 +1336,20 @@ int turb_divergence_gate_count(turb_ctx *c, long long *tightened)
 {
     if (!c || !tightened) return TURB_ERR_ARG;
     *tightened = c->gate_tightened;
+    return TURB_OK;
+}
+
+int turb_reset_pressure_history(turb_ctx *c)
+{
+    if (!c) return TURB_ERR_ARG;
+    c->nh[0] = c->nh[1] = 0;
+    return TURB_OK;
+}
+
+int turb_divergence_gate_floor_count(turb_ctx *c, long long *at_floor)
+{
+    if (!c || !at_floor) return TURB_ERR_ARG;
+    *at_floor = c->gate_floor;
     return TURB_OK;
 }
 
@@ -2678,8 +2694,18 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
                 double dmax = c->p_dt * c->hscal[3];
                 if (dmax <= c->div_gate) break;
                 if (!std::isfinite(dmax)) { status = TURB_ERR_NAN; break; }
-                // relative residual met, divergence not: tighten in proportion
-                tol = nr * std::min(0.5, 0.5 * c->div_gate / dmax);
+                // relative residual met, divergence not: tighten in
+                // proportion, down to the residual's round-off floor.  At the
+                // floor more iterations cannot lower r; what the estimate
+                // still sees is the rounding of b - A phi divided by the
+                // smallest cell volumes of a stretched grid, not divergence
+                // the projection would leave
+                const double floor = 64.0 * DBL_EPSILON * nb;
+                if (nr <= floor) {
+                    c->gate_floor++;
+                    break;
+                }
+                tol = std::max(floor, nr * std::min(0.5, 0.5 * c->div_gate / dmax));
                 c->gate_tightened++;
             }
             if (it >= c->prm.p_maxit) { status = TURB_ERR_NOT_CONVERGED; break; }
