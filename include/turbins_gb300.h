@@ -167,7 +167,9 @@ int turb_set_pressure_guess(turb_ctx *ctx, int mode);
  * state loaded again); the next solves of each stage rebuild it */
 int turb_reset_pressure_history(turb_ctx *ctx);
 /* RK stages whose pressure solve tries the extrapolated / learned candidate:
- * bit 0 the first stage, bit 1 the second (default 3, both) */
+ * bit 0 the first stage, bit 1 the second (default 3, both).  With the
+ * Galerkin fit on (turb_set_guess_galerkin), the learned mode's other stages
+ * take the fit over their earlier solutions alone (no network). */
 /* kernel variants, all giving the same bits: TURB_KV_MARCHING, the FP32
  * Helmholtz Jacobi sweeps and FP32 red-black half sweeps march along k
  * through shared-memory plane tiles (else one point, four cells, per thread);

@@ -117,3 +117,38 @@ def test_projection_guess_keeps_the_answer(mods):
     for k in ("u", "v", "w"):
         scale = max(np.abs(ref[k]).max(), 1e-30)
         assert np.abs(got[k] - ref[k]).max() <= 1e-7 * scale, k
+
+
+def test_learned_mode_without_network_stages_is_the_projection(mods):
+    """With the Galerkin fit on, the learned mode's stages that do not
+    evaluate the network take the fit over their earlier solutions alone:
+    with no network stage at all (guess stages 0) the run is the projection
+    guess's, bit for bit, iteration for iteration, and the network never
+    runs."""
+    A, N = mods
+    case = _case()
+    ctx = A.Context(case.grid, case.params)
+    ctx.load_state(case.state)
+    for _ in range(10):
+        ctx.step(case.dt)
+    state = ctx.state()
+    ctx.close()
+    proj, it_proj, _, _, _ = _run(A, case, state, 6, case.dt, A.GUESS_PROJECT)
+    nx, ny, nz = case.params.nx, case.params.ny, case.params.nz
+    net = N.Net(nx, ny, nz, train=False)
+    net.init_params(3)
+    ctx = A.Context(case.grid, case.params)
+    try:
+        ctx.load_state(state)
+        N.set_learned_net(ctx, net)
+        ctx.set_pressure_guess(A.GUESS_LEARNED)
+        ctx.set_guess_galerkin(True)
+        ctx.set_guess_stages(0)
+        it = [sum(ctx.step(case.dt)["p_iters"]) for _ in range(6)]
+        got = ctx.state()
+    finally:
+        ctx.close()
+        net.close()
+    assert it == it_proj
+    for k in proj:
+        assert np.array_equal(proj[k], got[k]), k

@@ -2613,10 +2613,17 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         if (rc) return rc;
         c->launches += 5;
     }
-    if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2 && ((c->guess_stages >> st) & 1)) {
+    // the stages that evaluate the candidate (guess_stages); with the
+    // Galerkin fit on, the learned mode fits the earlier solutions alone in
+    // the other stages
+    const bool cand_stage = (c->guess_stages >> st) & 1;
+    const bool fit_only = !cand_stage && c->guess_mode == TURB_GUESS_LEARNED && c->galerkin;
+    if (c->guess_mode != TURB_GUESS_PREVIOUS && c->nh[st] >= 2 && (cand_stage || fit_only)) {
         int ok = 0, ph = -1, fitted = 0;
         double nrc = 0.0;
-        if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
+        if (fit_only) {
+            // no candidate: the fit below over this stage's earlier solutions
+        } else if (c->guess_mode == TURB_GUESS_EXTRAPOLATE) {
             pcg_lincomb(s, n0, 2.0, c->ph[st][0], -1.0, c->ph[st][1], c->pz);
             c->launches += 1;
             ok = 1;
@@ -2640,7 +2647,7 @@ int turb_Pressure_solve(turb_ctx *c, int *iters, double *relres)
         }
         // Galerkin fit over the earlier solutions of this stage (and the
         // network candidate): the energy-norm best guess in their span
-        if ((c->guess_mode == TURB_GUESS_PROJECT || (c->guess_mode == TURB_GUESS_LEARNED && c->galerkin && ok)) &&
+        if ((c->guess_mode == TURB_GUESS_PROJECT || (c->guess_mode == TURB_GUESS_LEARNED && c->galerkin && (ok || fit_only))) &&
             c->pw[st][1]) {
             double ng = 0.0, de = 0.0;
             int rc = galerkin_guess(c, st, ok && c->guess_mode == TURB_GUESS_LEARNED, &ng, &de);
