@@ -11,9 +11,13 @@ Re=5000, dt=2.5e-4, every step checked to max|div u| <= 1e-10.
 
 N > 1 runs independent replicas (the step has no exchange between GPUs),
 one rank per GPU, and reports the aggregate over ranks.  ``value`` is the
-device-timed throughput with all fields resident in HBM; ``e2e`` is the same
-step driven through the C ABI with the state copied host->device before and
-device->host after every step.  The reference arm times the CPU oracle port
+device-timed throughput with all fields resident in HBM (steps 4-13); ``e2e``
+is the same step driven through the C ABI with the state copied host->device
+before and device->host after every step (turb_step_host), and the arms time
+the guess and precision methods in turn; both start again from the initial
+state, so that every timed step lies within the first 20 (on this bed the
+reference's immersed-boundary stencils let a spanwise-velocity mode grow from
+about step 25 at 512x256x256, in the oracle as on the GPU).  The reference arm times the CPU oracle port
 of the same step on the whole grid, split into one x-slab per host core,
 each stepped in its own process (the reference parallelises only over MPI
 ranks), for at most about 4 minutes of timed steps.
