@@ -366,16 +366,26 @@ int turb_host_unregister(void *ptr);
 int turb_host_alloc(size_t bytes, void **ptr);
 int turb_host_free(void *ptr);
 
-/* self-test: the ENO kernels' division by a grid spacing (two-term
- * reciprocal, one Markstein correction) against IEEE division on nsamples
- * operand pairs;
- * returns the number of bitwise mismatches (and one offending (a, h)) */
 /* FP64 FMA instructions per second of the current GPU (thread-level;
  * FLOP/s = 2x), measured with CUDA events on a DFMA-only kernel over every SM;
  * the denominator of the FP64-pipe fractions */
 int turb_measure_fp64_rate(double *dfma_per_s);
+/* self-test: the ENO kernels' division by a grid spacing (two-term
+ * reciprocal, one Markstein correction) against IEEE division on nsamples
+ * operand pairs;
+ * returns the number of bitwise mismatches (and one offending (a, h)) */
 int turb_selftest_division(long long nsamples, unsigned long long seed,
                            unsigned long long *mismatches, double *example);
+/* 1 when the two-term quotient RN(a y + RN(a yl)) (y = RN(1/h), yl its
+ * correction) rounds as a/h for every numerator a, so the ENO kernels divide
+ * by h with one multiply and one fused multiply-add; decided at set-up by
+ * trying the form on the few numerators whose quotient lies within its error
+ * of a midpoint between doubles.  Host only, needs no GPU. */
+int turb_division_two_term_exact(double h);
+/* self-test: for n caller-chosen pairs, the kernels' two-term quotient of
+ * a[t] / h[t] and the IEEE quotient, computed on the GPU */
+int turb_selftest_division_pairs(long long n, const double *a, const double *h,
+                                 double *q_two_term, double *q_ieee);
 
 /* ---- learned initial guess of the pressure solve ---------------------------
  * No reference counterpart: the reference starts each Poisson solve from the

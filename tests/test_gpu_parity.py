@@ -89,6 +89,36 @@ def test_division_selftest(api):
         assert bad == 0, (bad, ex)
 
 
+def test_two_term_division_on_device(api):
+    """The kernels' two-term quotient on the GPU equals the CPU's (libm fma)
+    on every pair, and the IEEE quotient wherever the set-up's check flags
+    the spacing; the pairs are the near-midpoint numerators (|k| <= 8) of
+    seeded spacings, where an unflagged spacing fails."""
+    import math
+    import random
+    from tests import _division as D
+    rng = random.Random(21)
+    a, h, flag = [], [], []
+    for _ in range(400):
+        hh = math.ldexp(rng.uniform(1.0, 2.0), rng.randint(-14, 3))
+        H, e = D.mantissa(hh)
+        f = api.division_two_term_exact(hh)
+        for A in D.near_midpoint(H, 8, 8) + [rng.randrange(1 << 52, 1 << 53) for _ in range(8)]:
+            for sh in (0, -300, 300):
+                for s in (1.0, -1.0):
+                    a.append(s * math.ldexp(A, e - 53 + sh))
+                    h.append(hh)
+                    flag.append(f)
+    a, h, flag = np.array(a), np.array(h), np.array(flag)
+    q2, qd = api.selftest_division_pairs(a, h)
+    host = np.array([D.two_term(x, y) for x, y in zip(a, h)])
+    bits = lambda x: x.view(np.int64)
+    assert np.array_equal(bits(q2), bits(host))
+    assert np.array_equal(bits(q2[flag]), bits(qd[flag]))
+    assert flag.any() and (~flag).any()
+    assert (q2[~flag] != qd[~flag]).any()
+
+
 @pytest.mark.parametrize("fastdiv", [1, 0])
 @pytest.mark.parametrize("name,mk", CASES)
 def test_convection_bitexact(api, oracle_mod, name, mk, fastdiv):

@@ -687,6 +687,26 @@ def selftest_division(nsamples, seed=1):
     return bad.value, (ex[0], ex[1])
 
 
+def division_two_term_exact(h):
+    """Whether the ENO kernels divide by spacing h with the two-term quotient
+    alone (turb_division_two_term_exact; host only)."""
+    f = load_library().turb_division_two_term_exact
+    f.argtypes = [C.c_double]
+    return bool(f(float(h)))
+
+
+def selftest_division_pairs(a, h):
+    """The kernels' two-term quotient and the IEEE quotient of a / h on the GPU."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    if a.shape != h.shape:
+        raise ValueError("a and h differ in shape")
+    q2, qd = np.empty_like(a), np.empty_like(a)
+    _check(load_library().turb_selftest_division_pairs(C.c_longlong(a.size), _ptr(a), _ptr(h), _ptr(q2), _ptr(qd)),
+           "selftest_division_pairs")
+    return q2, qd
+
+
 def measure_fp64_rate():
     """FP64 FMA instructions per second of the current GPU (turb_measure_fp64_rate)"""
     r = C.c_double()

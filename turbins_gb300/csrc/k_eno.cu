@@ -24,12 +24,16 @@ __device__ __forceinline__ double ml(double a, double b) { return __dmul_rn(a, b
 __device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
 
 // a / h[b] rounded to nearest: IEEE division or the reciprocal-based form;
-// for a power-of-two spacing (flag bit `bit` of T.p2[b]) one exact scaling
+// for a power-of-two spacing (flag bit `bit` of T.p2[b]) one exact scaling,
+// for a spacing whose two-term quotient is exact (bit `bit` << 3) that
+// quotient without the correction
 __device__ __forceinline__ double dd(const EnoTab &T, double a, const double *__restrict__ h,
                                      const double *__restrict__ rh, const double *__restrict__ rl, int b, int bit)
 {
     if (!T.fastdiv) return dv(a, h[b]);
-    if (T.p2[b] & bit) return __dmul_rn(a, rh[b]);
+    const int f = T.p2[b];
+    if (f & bit) return __dmul_rn(a, rh[b]);
+    if (f & (bit << 3)) return div_by_spacing_2t(a, h[b], rh[b], rl[b]);
     return div_by_spacing(a, h[b], rh[b], rl[b]);
 }
 

@@ -1,6 +1,9 @@
 // k_selftest.cu -- on-device self-tests of arithmetic building blocks.
 // turb_selftest_division compares div_by_spacing (turb_div.cuh) with the IEEE
-// division __ddiv_rn bit for bit on random and adversarial operands.
+// division __ddiv_rn bit for bit on random and adversarial operands;
+// turb_selftest_division_pairs returns the two-term quotient
+// (div_by_spacing_2t) and the IEEE quotient of caller-chosen pairs, and
+// turb_division_two_term_exact is the set-up's per-spacing check.
 #include <algorithm>
 #include <cstdint>
 #include "../../include/turbins_gb300.h"
@@ -80,7 +83,48 @@ __global__ void k_dfma_rate(int iters, double b, double c, double *out)
     if (s == 12345.678) out[0] = s;   // never true: keeps the chains live
 }
 
+// per pair: the kernels' two-term quotient (div_by_spacing_2t, with the
+// reciprocal and its correction formed here as the set-up forms them) and the
+// IEEE quotient
+__global__ void k_div_pairs(long long n, const double *__restrict__ a, const double *__restrict__ h,
+                            double *__restrict__ q2t, double *__restrict__ qd)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double y = __ddiv_rn(1.0, h[t]);
+        q2t[t] = div_by_spacing_2t(a[t], h[t], y, recip_low(h[t], y));
+        qd[t] = __ddiv_rn(a[t], h[t]);
+    }
+}
+
 }  // namespace
+
+extern "C" int turb_division_two_term_exact(double h)
+{
+    const double y = 1.0 / h;
+    return div_two_term_exact(h, y, recip_low(h, y)) ? 1 : 0;
+}
+
+extern "C" int turb_selftest_division_pairs(long long n, const double *a, const double *h, double *q_two_term,
+                                            double *q_ieee)
+{
+    if (n <= 0 || !a || !h || !q_two_term || !q_ieee) return TURB_ERR_ARG;
+    const size_t b = sizeof(double) * (size_t)n;
+    double *buf = nullptr;
+    TURB_CHECK(cudaMalloc(&buf, 4 * b));
+    double *da = buf, *dh = buf + n, *d2 = buf + 2 * n, *dd = buf + 3 * n;
+    cudaError_t e = cudaMemcpy(da, a, b, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dh, h, b, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const long long blocks = std::min<long long>((n + 255) / 256, 4096);
+        k_div_pairs<<<(unsigned)blocks, 256>>>(n, da, dh, d2, dd);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(q_two_term, d2, b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(q_ieee, dd, b, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return turb_set_cuda_error(e, __FILE__, __LINE__);
+    return TURB_OK;
+}
 
 // FP64 FMA instructions per second of this GPU (thread-level, so one DFMA of
 // one thread counts once; FLOP/s is twice this): a fixed number of DFMAs on

@@ -381,9 +381,16 @@ EnoTab mk_eno(DevBuf &m, int r, const std::vector<double> &pos, int s0, int e0, 
         int e;
         return h > 0.0 && std::isfinite(h) && std::frexp(h, &e) == 0.5;
     };
+    // other spacings whose two-term quotient alone rounds as the division
+    // for every numerator (div_two_term_exact, turb_div.cuh): bits 3-5
     std::vector<uint8_t> p2(nb, 0);
-    for (int b = 0; b < nb; b++)
-        p2[b] = (uint8_t)((pow2(h1[b]) ? 1 : 0) | (pow2(h2[b]) ? 2 : 0) | (pow2(h3[b]) ? 4 : 0));
+    for (int b = 0; b < nb; b++) {
+        int f = (pow2(h1[b]) ? 1 : 0) | (pow2(h2[b]) ? 2 : 0) | (pow2(h3[b]) ? 4 : 0);
+        if (!(f & 1) && div_two_term_exact(h1[b], r1[b], l1[b])) f |= 8;
+        if (!(f & 2) && div_two_term_exact(h2[b], r2[b], l2[b])) f |= 16;
+        if (!(f & 4) && div_two_term_exact(h3[b], r3[b], l3[b])) f |= 32;
+        p2[b] = (uint8_t)f;
+    }
     T.p2 = m.upload(p2);
     T.g2 = m.upload(g2);
     T.g3 = m.upload(g3);

@@ -80,7 +80,8 @@ struct EnoTab {
     const double *rl1, *rl2, *rl3;   // and its correction RN((1 - RN(1/h) h)/h)
     int fastdiv;         // 1: div_by_spacing (turb_div.cuh), 0: IEEE division
     const uint8_t *p2;   // per b: bit 0/1/2 set when h1/h2/h3 is a power of two, so that
-                         // a/h = a*RN(1/h) exactly (fastdiv only)
+                         // a/h = a*RN(1/h) exactly; bit 3/4/5 when the two-term
+                         // quotient alone is exact (div_two_term_exact; fastdiv only)
     int gsrc[6];         // ghost b<r: [0..r), ghost b>=nb-r: [3..3+r) by ex
     double gm[6];        // 0: zero, 1: m*q[s0], 2: m*q[e0], 3: glo[line], 4: ghi[line]
     const double *glo = nullptr, *ghi = nullptr;   // x lines at open faces: [NZ][NY] planes
