@@ -22,7 +22,10 @@ __device__ __forceinline__ double interp2(double q0, double q1, const Interp2 &T
     if (T.flat[t]) return q0;
     double a = sb(q1, q0), h = T.dx[t];
     int mode = T.div[t];
-    double m = mode == 1 ? ml(a, T.rdx[t]) : (mode == 2 ? div_by_spacing(a, h, T.rdx[t], T.rdxl[t]) : dv(a, h));
+    double m = mode == 1   ? ml(a, T.rdx[t])
+               : mode == 3 ? div_by_spacing_2t(a, h, T.rdx[t], T.rdxl[t])
+               : mode == 2 ? div_by_spacing(a, h, T.rdx[t], T.rdxl[t])
+                           : dv(a, h);
     return ad(ml(m, T.dq[t]), q0);
 }
 

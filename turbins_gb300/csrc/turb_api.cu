@@ -276,7 +276,7 @@ Interp2 mk_interp2(DevBuf &m, int n, const std::vector<double> &X0, const std::v
         if (h > 0.0 && std::isfinite(h) && std::frexp(h, &e) && e > -500 && e < 500) {
             rdx[t] = 1.0 / h;
             rdxl[t] = recip_low(h, rdx[t]);
-            dm[t] = std::frexp(h, &e) == 0.5 ? 1 : 2;
+            dm[t] = std::frexp(h, &e) == 0.5 ? 1 : (div_two_term_exact(h, rdx[t], rdxl[t]) ? 3 : 2);
         }
     }
     Interp2 o;

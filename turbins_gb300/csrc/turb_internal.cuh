@@ -52,7 +52,8 @@ struct Geo {
 // (x0, x1): dx = x1 - x0, dq = xq - x0, flat = |dx| < 1e-8; the division by
 // dx as div = 0: IEEE division, 1: one exact multiply by rdx = 1/dx (a power
 // of two), 2: the reciprocal-based correctly rounded division (turb_div.cuh,
-// rdxl its correction term).
+// rdxl its correction term), 3: its two-term quotient alone, for spacings
+// that pass div_two_term_exact.
 struct Interp2 {
     const double *dx, *dq, *rdx, *rdxl;
     const uint8_t *flat, *div;
