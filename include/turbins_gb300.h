@@ -243,8 +243,11 @@ int turb_set_mg_split(turb_ctx *ctx, int on);
 int turb_set_helmholtz_mode(turb_ctx *ctx, int mode, int inner_sweeps);
 /* ENO divided differences: 1 (default) divides by a grid spacing through its
  * precomputed two-term reciprocal and one correction step (FP64: 1 multiply +
- * 3 FMA, range tests on the integer pipe), 0 uses IEEE division; both round
- * to nearest, so the results are the same bits */
+ * 3 FMA, range tests on the integer pipe), without the correction (1
+ * multiply + 1 FMA) for the spacings the set-up proves it unneeded for
+ * (turb_division_two_term_exact), and by one exact multiply for
+ * power-of-two spacings; 0 uses IEEE division; all round to nearest, so the
+ * results are the same bits */
 int turb_set_eno_division(turb_ctx *ctx, int fast);
 int turb_synchronize(turb_ctx *ctx);
 const char *turb_status_string(int status);
