@@ -60,6 +60,13 @@ def main(nx=128, ny=64, nz=64):
     for name, mk in rows:
         a, b = _time(mk(orc)), _time(mk(ref))
         print("%-38s %9.2f %9.2f %7.2f" % (name, a, b, a / b))
+    # ENO_compute_convective_terms on one 256-node line (ENO-3), both called
+    # through the same kind of ctypes wrapper, so the call overhead is alike
+    P = np.cumsum(rng.uniform(0.5, 1.5, 262))
+    D0, V = rng.standard_normal(262), rng.standard_normal(262)
+    a = _time(lambda: [orc.eno_line(3, D0, P, V) for _ in range(1000)], 3)
+    b = _time(lambda: [ref.eno_line(3, D0, P, V) for _ in range(1000)], 3)
+    print("%-38s %9.4f %9.4f %7.2f" % ("ENO_compute_convective_terms (line)", a / 1000, b / 1000, a / b))
 
 
 if __name__ == "__main__":
