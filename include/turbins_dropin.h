@@ -37,6 +37,7 @@ typedef struct concentration Concentration; /* Include/DataTypes.h:101 */
 typedef struct parameters Parameters;       /* Include/DataTypes.h:249 */
 typedef struct eno_scheme ENO_Scheme;       /* Include/DataTypes.h:369 */
 typedef struct mac_grid MAC_grid;           /* Include/DataTypes.h:628 */
+typedef struct gvg_bag GVG_bag;             /* Include/DataTypes.h:645 */
 typedef struct _p_Vec *Vec;                 /* PETSc vector handle */
 
 /* ---- binding (no reference counterpart) -----------------------------------
@@ -60,6 +61,17 @@ int turb_dropin_download(MAC_grid *grid);
 int turb_dropin_status(void);
 /* forget every binding of grid (the context is the caller's) */
 int turb_dropin_unbind_grid(MAC_grid *grid);
+
+/* ---- the fused step (no reference routine: the reference ships no time-step
+ * driver) -------------------------------------------------------------------
+ * bag: the GVG_bag holding the grid's structs, bound to the grid.  One
+ * TVD-RK2 step of dt on the bound device state (turb_step: both stages of
+ * convection, Helmholtz solves, Poisson solve and projection, then the RK
+ * average); *status (if given) receives the library status, which is also
+ * returned (0: ok).  The layer never writes the bag: its time and iteration
+ * counters stay the host's. */
+int turb_dropin_bind_bag(GVG_bag *bag, MAC_grid *grid);
+int turb_dropin_step(GVG_bag *bag, double dt, int *status);
 
 /* ---- the reference's routines ---------------------------------------------
  * Include/Velocity.h */

@@ -90,6 +90,35 @@ def _build_driver(tmp):
     return so
 
 
+def test_dropin_step_refuses_unbound_keys(tmp_path):
+    """the fused step through a GVG_bag: a bag whose grid has no context, or
+    an unbound bag, is refused with TURB_ERR_ARG, which turb_dropin_status
+    reports once (CPU: no device call is reached)"""
+    lib = _lib()
+    libdir = os.path.dirname(lib)
+    prog = tmp_path / "bag.c"
+    prog.write_text(
+        '#include <stdio.h>\n#include "turbins_dropin.h"\n'
+        'int main(void) {\n'
+        '  static char bag_key, grid_key; GVG_bag *bag = (GVG_bag *)&bag_key;\n'
+        '  MAC_grid *grid = (MAC_grid *)&grid_key; int st = 12345;\n'
+        '  int a = turb_dropin_bind_bag(NULL, grid), b = turb_dropin_bind_bag(bag, grid);\n'
+        '  int c = turb_dropin_step(bag, 1e-3, &st), d = turb_dropin_status(), e = turb_dropin_status();\n'
+        '  int f = turb_dropin_step(NULL, 1e-3, NULL);\n'
+        '  printf("%d %d %d %d %d %d %d %d\\n", TURB_ERR_ARG, a, b, c, st, d, e, f);\n'
+        '  return 0;\n}\n')
+    exe = tmp_path / "bag"
+    subprocess.check_call(["gcc", "-O2", str(prog), os.path.join(SHIM, "shim.c"), "-I", SHIM,
+                           "-I", os.path.join(ROOT, "include"), "-o", str(exe), "-L", libdir, "-lturbdropin",
+                           "-lturbgpu", "-Wl,-rpath," + libdir, "-lm"])
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    err, a, b, c, st, d, e, f = map(int, r.stdout.split())
+    assert err != 0
+    assert (a, b, c, st, d, e, f) == (err, err, err, err, err, 0, err)
+    assert "turbins_dropin: turb_dropin_step" in r.stderr
+
+
 def test_driver_builds_without_reference(tmp_path):
     """the host step compiles and links against the layer with no reference
     header in sight (CPU: build only)"""

@@ -37,7 +37,7 @@ int VecGetSize(Vec v, int *n);
 #define MAXGRID 16
 #define MAXKEY 64
 
-enum { K_VEL = 1, K_CONC, K_PRES, K_ENO };
+enum { K_VEL = 1, K_CONC, K_PRES, K_ENO, K_BAG };
 
 typedef struct {
     const void *key;
@@ -219,6 +219,26 @@ static int transfer(MAC_grid *grid, int up)
 
 int turb_dropin_upload(MAC_grid *grid) { return transfer(grid, 1); }
 int turb_dropin_download(MAC_grid *grid) { return transfer(grid, 0); }
+
+/* ---- the fused step ------------------------------------------------------ */
+
+int turb_dropin_bind_bag(GVG_bag *bag, MAC_grid *grid)
+{
+    binding *b;
+    if (!bag || !ctx_of(grid)) return TURB_ERR_ARG;
+    if (!(b = slot(bag, K_BAG))) return TURB_ERR_ARG;
+    b->grid = grid;
+    return TURB_OK;
+}
+
+int turb_dropin_step(GVG_bag *bag, double dt, int *status)
+{
+    turb_ctx *c = lookup(bag, K_BAG, NULL, "turb_dropin_step");
+    int rc = c ? turb_step(c, dt, NULL) : TURB_ERR_ARG;
+    if (c) note(rc, "turb_dropin_step");
+    if (status) *status = rc;
+    return rc;
+}
 
 /* ---- Include/Velocity.h -------------------------------------------------- */
 
