@@ -59,12 +59,13 @@ __device__ __forceinline__ double div_by_spacing_2t(double a, double h, double y
 // itself), so it rounds as a/h unless a/h lies that close to a midpoint
 // N 2^-c between doubles (N odd; c = 53 for a/h in [1, 2), c = 54 in
 // [1/2, 1)), i.e. unless 2^c A - H N = k with |k| <= 1 (c = 53) or |k| <= 3
-// (c = 54); k = 0 is impossible (H N would be even).  For a given H each k
-// admits at most two N in range, from the congruence H N = -k (mod 2^c), so
-// the check tries the form on those few A and on nothing else.  This is the
-// condition of Brisebarre, Muller and Raina (IEEE Trans. Computers 53(8),
-// 2004) for their two-term algorithm, derived and checked here by the
-// enumeration; about 99 % of random spacings pass.  Host only.
+// (c = 54); k = 0 is impossible (2^c would divide H N, so H, as N is odd,
+// while 0 < H < 2^53).  For a given H each k admits at most two N in range,
+// from the congruence H N = -k (mod 2^c), so the check tries the form on
+// those few A and on nothing else.  The two-term algorithm is Brisebarre,
+// Muller and Raina's (IEEE Trans. Computers 53(8), 2004); this check is
+// derived from the bound above and was confirmed by exhaustive search at
+// reduced precision.  About 99 % of random spacings pass.  Host only.
 inline bool div_two_term_exact(double h, double y, double yl)
 {
     int e = 0;
